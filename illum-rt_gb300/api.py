@@ -1,0 +1,266 @@
+"""ctypes binding of the C-ABI (include/grt.h) and a Python mirror of the reference tracer.
+
+``BatchRayTracer`` mirrors ``wf::cuda::batch_rt`` (rt/cuda/base.h:403-429) as the wavefront
+steps use it: ``build`` a scene, ``use`` a ray-data object, ``compute_closest_hit`` /
+``compute_any_hit`` over all of its rays, and ``interprete`` the reference's script commands
+(``bvh type``, ``bvh max_tris`` from rt/cuda/base.cpp:134-153, ``raytracer`` from
+rt/cuda/platform.cpp:102-131). Every call goes through libgrt.so; there is no Python or CPU
+implementation of any traversal here. PyTorch is used only to hold device buffers.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import _libs
+
+GRT_OK = 0
+STATUS_NAMES = {0: "GRT_OK", 1: "GRT_ERR_INVALID_ARG", 2: "GRT_ERR_OOM", 3: "GRT_ERR_CUDA", 4: "GRT_ERR_TIMEOUT",
+                5: "GRT_ERR_BVH_TOO_DEEP", 6: "GRT_ERR_NOT_BUILT", 7: "GRT_ERR_TRAVERSAL",
+                8: "GRT_ERR_UNKNOWN_TRACER", 9: "GRT_ERR_NO_DEVICE"}
+SPLIT = {"om": 0, "sm": 1, "sah": 2}
+TRACERS = ("while-while", "persistent-while-while")
+
+
+class GRTError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+class BvhOpts(ctypes.Structure):
+    _fields_ = [("split", ctypes.c_int), ("max_tris_per_node", ctypes.c_int), ("number_of_planes", ctypes.c_int),
+                ("esc", ctypes.c_int)]
+
+
+class BvhStats(ctypes.Structure):
+    _fields_ = [("ref_nodes", ctypes.c_uint32), ("inner_nodes", ctypes.c_uint32), ("tri_records", ctypes.c_uint32),
+                ("depth", ctypes.c_uint32), ("device_bytes", ctypes.c_uint64), ("build_ms", ctypes.c_double),
+                ("flatten_ms", ctypes.c_double), ("upload_ms", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [("block_threads", ctypes.c_int), ("blocks_per_sm", ctypes.c_int), ("refill_threshold", ctypes.c_int),
+                ("refill_period", ctypes.c_int), ("stack_entries", ctypes.c_int)]
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("reserved", ctypes.c_uint32)]
+
+
+_lib = None
+P, U32, I, VP = ctypes.POINTER, ctypes.c_uint32, ctypes.c_int, ctypes.c_void_p
+
+_PROTOS = {
+    "grt_version": (I, []),
+    "grt_create": (I, [P(Config), P(VP)]),
+    "grt_destroy": (I, [VP]),
+    "grt_last_error": (ctypes.c_char_p, [VP]),
+    "grt_bvh_opts_default": (None, [P(BvhOpts)]),
+    "grt_build": (I, [VP, VP, U32, VP, U32, P(BvhOpts)]),
+    "grt_bvh_info": (I, [VP, P(BvhStats)]),
+    "grt_export_bvh": (I, [VP, VP, VP, P(U32)]),
+    "grt_host_bvh_build": (I, [VP, U32, VP, U32, P(BvhOpts), P(VP)]),
+    "grt_host_bvh_info": (I, [VP, P(BvhStats)]),
+    "grt_host_bvh_export": (I, [VP, VP, VP, P(U32)]),
+    "grt_host_bvh_free": (None, [VP]),
+    "grt_select_tracer": (I, [VP, ctypes.c_char_p]),
+    "grt_set_tuning": (I, [VP, P(Tuning)]),
+    "grt_get_tuning": (I, [VP, P(Tuning)]),
+    "grt_trace": (I, [VP, VP, VP, U32, I, VP]),
+    "grt_trace_host": (I, [VP, VP, VP, U32, I]),
+    "grt_check": (I, [VP, VP, U32]),
+}
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        path = os.path.join(_libs.LIB_DIR, "libgrt.so")
+        if not os.path.exists(path):
+            raise RuntimeError(f"{path} is missing: build it first (python -c 'import __graft_entry__ as g; g.build()')")
+        L = ctypes.CDLL(path)
+        for name, (res, args) in _PROTOS.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _ptr(a) -> int:
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return a.data_ptr()  # torch tensor
+
+
+def make_opts(split="sah", max_tris=4, planes=16, esc=True) -> BvhOpts:
+    return BvhOpts(SPLIT[split] if isinstance(split, str) else int(split), int(max_tris), int(planes), int(bool(esc)))
+
+
+class HostBVH:
+    """The product builder run on the host only (grt_host_bvh_*): reference-layout nodes."""
+
+    def __init__(self, vpos, tris, **opts):
+        v = np.ascontiguousarray(vpos, np.float32)
+        t = np.ascontiguousarray(tris, np.uint32)
+        h = VP()
+        o = make_opts(**opts)
+        st = lib().grt_host_bvh_build(_ptr(v), v.shape[0], _ptr(t), t.shape[0], ctypes.byref(o), ctypes.byref(h))
+        if st != GRT_OK:
+            raise GRTError(st, "host BVH build failed")
+        self.h = h
+        s = BvhStats()
+        lib().grt_host_bvh_info(self.h, ctypes.byref(s))
+        self.stats = s.as_dict()
+
+    def export(self):
+        nodes = np.zeros((self.stats["ref_nodes"], 14), np.uint32)
+        index = np.zeros(self.stats["tri_records"], np.uint32)
+        root = U32()
+        lib().grt_host_bvh_export(self.h, _ptr(nodes), _ptr(index), ctypes.byref(root))
+        return nodes, index, int(root.value)
+
+    def __del__(self):
+        try:
+            lib().grt_host_bvh_free(self.h)
+        except Exception:
+            pass
+
+
+class RayData:
+    """Device ray and hit buffers in the reference's CUDA layout (wf::cuda::raydata,
+    rt/cuda/base.h:328-351): rays float32 [n, 8], hits float32 [n, 4] (ref as uint32 bits)."""
+
+    def __init__(self, rays, hits=None):
+        import torch
+        self.rays = rays
+        self.hits = hits if hits is not None else torch.empty((rays.shape[0], 4), dtype=torch.float32,
+                                                              device=rays.device)
+
+    @property
+    def n(self) -> int:
+        return int(self.rays.shape[0])
+
+
+class BatchRayTracer:
+    """One traversal context on one GPU (a grt_ctx)."""
+
+    def __init__(self, device: int = 0):
+        cfg = Config(device, 0)
+        h = VP()
+        st = lib().grt_create(ctypes.byref(cfg), ctypes.byref(h))
+        if st != GRT_OK:
+            raise GRTError(st, "grt_create failed")
+        self.ctx = h
+        self.device = device
+        self.bvh_type = "sah"         # `bvh type`
+        self.bvh_max_tris_per_node = 4  # `bvh max_tris`
+        self.rd: RayData | None = None
+        self.tracer = TRACERS[0]
+
+    # -- helpers ------------------------------------------------------------------------
+    def _check(self, st: int):
+        if st != GRT_OK:
+            msg = lib().grt_last_error(self.ctx)
+            raise GRTError(st, msg.decode() if msg else "")
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            lib().grt_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- wf::batch_ray_tracer surface -----------------------------------------------------
+    def interprete(self, command: str) -> bool:
+        """Script commands of the CUDA tracer and platform; returns False for unknown ones."""
+        words = command.split()
+        if len(words) == 3 and words[:2] == ["bvh", "type"]:
+            if words[2] not in SPLIT:
+                raise ValueError('"bvh type" must be one of "sm", "om", "sah"')
+            self.bvh_type = words[2]
+            return True
+        if len(words) == 3 and words[:2] == ["bvh", "max_tris"]:
+            self.bvh_max_tris_per_node = int(words[2])
+            return True
+        if len(words) == 2 and words[0] == "raytracer":
+            self.select(words[1])
+            return True
+        return False
+
+    def select(self, name: str):
+        self._check(lib().grt_select_tracer(self.ctx, name.encode()))
+        self.tracer = name
+
+    def build(self, vpos, tris, split=None, max_tris=None, planes=16, esc=True) -> dict:
+        v = np.ascontiguousarray(vpos, np.float32)
+        t = np.ascontiguousarray(tris, np.uint32)
+        o = make_opts(split or self.bvh_type, max_tris or self.bvh_max_tris_per_node, planes, esc)
+        self._check(lib().grt_build(self.ctx, _ptr(v), v.shape[0], _ptr(t), t.shape[0], ctypes.byref(o)))
+        return self.info()
+
+    def use(self, rd: RayData):
+        self.rd = rd
+
+    def compute_closest_hit(self):
+        self._run(False)
+
+    def compute_any_hit(self):
+        self._run(True)
+
+    def _run(self, any_hit: bool):
+        import torch
+        if self.rd is None:
+            raise RuntimeError("use() a RayData first")
+        stream = torch.cuda.current_stream(self.rd.rays.device).cuda_stream
+        self.trace(self.rd.rays, self.rd.hits, any_hit, stream)
+        self.check(stream)  # the reference synchronises after every launch (rt/cuda/tracers.cu:67-68)
+
+    # -- direct access ------------------------------------------------------------------
+    def trace(self, rays, hits, any_hit=False, stream=None, n=None):
+        n = int(rays.shape[0]) if n is None else int(n)
+        self._check(lib().grt_trace(self.ctx, _ptr(rays), _ptr(hits), n, int(any_hit), VP(stream or 0)))
+
+    def check(self, stream=None, timeout_ms: int = 0):
+        self._check(lib().grt_check(self.ctx, VP(stream or 0), timeout_ms))
+
+    def trace_host(self, rays: np.ndarray, any_hit=False, hits: np.ndarray | None = None) -> np.ndarray:
+        r = np.ascontiguousarray(rays, np.float32)
+        out = hits if hits is not None else np.zeros((r.shape[0], 4), np.float32)
+        self._check(lib().grt_trace_host(self.ctx, _ptr(r), _ptr(out), r.shape[0], int(any_hit)))
+        return out
+
+    def info(self) -> dict:
+        s = BvhStats()
+        self._check(lib().grt_bvh_info(self.ctx, ctypes.byref(s)))
+        return s.as_dict()
+
+    def export_bvh(self):
+        info = self.info()
+        nodes = np.zeros((info["ref_nodes"], 14), np.uint32)
+        index = np.zeros(info["tri_records"], np.uint32)
+        root = U32()
+        self._check(lib().grt_export_bvh(self.ctx, _ptr(nodes), _ptr(index), ctypes.byref(root)))
+        return nodes, index, int(root.value)
+
+    def set_tuning(self, **kw):
+        t = Tuning()
+        self._check(lib().grt_get_tuning(self.ctx, ctypes.byref(t)))
+        for k, v in kw.items():
+            setattr(t, k, int(v))
+        self._check(lib().grt_set_tuning(self.ctx, ctypes.byref(t)))
+
+    def get_tuning(self) -> dict:
+        t = Tuning()
+        self._check(lib().grt_get_tuning(self.ctx, ctypes.byref(t)))
+        return {k: getattr(t, k) for k, _ in t._fields_}

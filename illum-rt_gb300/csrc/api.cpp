@@ -1,0 +1,420 @@
+// C-ABI of libgrt.so (include/grt.h): context, BVH build/upload, tracer selection, launches.
+//
+// This is the GB300 counterpart of wf::cuda::batch_rt (rt/cuda/base.h:403-429) and of the
+// CUDA platform's tracer registry (rt/cuda/platform.cpp:34-56, 102-131), reduced to plain
+// pointers, sizes and status codes.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/grt.h"
+#include "bvh_builder.hpp"
+#include "grt_internal.hpp"
+
+struct grt_ctx {
+    int device = 0;
+    int num_sms = 0;
+    std::string err;
+    bool built = false;
+    grt::ref_tree tree;
+    grt::dev_scene sc{};
+    void *d_nodes = nullptr, *d_recs = nullptr, *d_vpos = nullptr, *d_tris = nullptr;
+    uint32_t nv = 0, nt = 0, depth = 0;
+    grt_bvh_stats stats{};
+    int tracer = 0;  // 0 while-while, 1 persistent-while-while
+    grt_tuning tuning{};
+    unsigned *d_err = nullptr;      // error bits ORed in by kernels
+    unsigned *d_counter = nullptr;  // ray counter of the persistent kernel
+    void *d_stage = nullptr;        // grt_trace_host staging: rays then hits
+    size_t stage_bytes = 0;
+    cudaStream_t stream = nullptr;  // grt_trace_host stream
+};
+
+namespace {
+
+struct device_guard {
+    int prev = -1;
+    explicit device_guard(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~device_guard() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+grt_status fail(grt_ctx *c, grt_status s, const std::string &msg) {
+    if (c) c->err = msg;
+    return s;
+}
+
+grt_status cuda_fail(grt_ctx *c, cudaError_t e, const char *what) {
+    cudaGetLastError();  // clear a non-sticky error so the context stays usable
+    return fail(c, e == cudaErrorMemoryAllocation ? GRT_ERR_OOM : GRT_ERR_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+void free_scene(grt_ctx *c) {
+    for (void **p : {&c->d_nodes, &c->d_recs, &c->d_vpos, &c->d_tris}) {
+        if (*p) cudaFree(*p);
+        *p = nullptr;
+    }
+    c->built = false;
+}
+
+double ms_since(std::chrono::steady_clock::time_point t0) {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+const char *kTracerNames[] = {"while-while", "persistent-while-while"};
+
+grt::launch_params params_for(grt_ctx *c, bool any_hit) {
+    grt::launch_params lp{};
+    const grt_tuning &t = c->tuning;
+    lp.stack_entries = t.stack_entries > 0 ? t.stack_entries : (int)c->depth;
+    if (lp.stack_entries < (int)c->depth) lp.stack_entries = (int)c->depth;
+    lp.block_threads = t.block_threads > 0 ? t.block_threads : 128;
+    lp.refill_threshold = t.refill_threshold > 0 ? t.refill_threshold : 20;
+    lp.refill_period = t.refill_period > 0 ? t.refill_period : 4;
+    if (c->tracer == 1) {
+        int per_sm = t.blocks_per_sm > 0 ? t.blocks_per_sm
+                                         : grt::persistent_blocks_per_sm(lp.block_threads, lp.stack_entries, any_hit);
+        lp.grid_blocks = per_sm * c->num_sms;
+    }
+    return lp;
+}
+
+bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
+
+grt::build_opts to_build_opts(const grt_bvh_opts *opts) {
+    grt_bvh_opts o;
+    grt_bvh_opts_default(&o);
+    if (opts) o = *opts;
+    grt::build_opts bo;
+    bo.split = o.split;
+    bo.max_tris = o.max_tris_per_node;
+    bo.planes = o.number_of_planes;
+    bo.esc = o.esc != 0;
+    return bo;
+}
+
+void export_tree(const grt::ref_tree &tree, uint32_t *nodes14, uint32_t *index, uint32_t *root) {
+    if (nodes14) {
+        for (size_t i = 0; i < tree.nodes.size(); ++i) {
+            const grt::ref_node &n = tree.nodes[i];
+            uint32_t *o = nodes14 + 14 * i;
+            std::memcpy(o + 0, n.lmin, 12);
+            std::memcpy(o + 3, n.lmax, 12);
+            std::memcpy(o + 6, n.rmin, 12);
+            std::memcpy(o + 9, n.rmax, 12);
+            std::memcpy(o + 12, &n.link_l, 4);
+            std::memcpy(o + 13, &n.link_r, 4);
+        }
+    }
+    if (index) std::memcpy(index, tree.index.data(), tree.index.size() * 4);
+    if (root) *root = tree.root;
+}
+
+uint32_t tree_depth(const grt::ref_tree &tree) {
+    // an empty scene is one leaf of count 0, whose link_r = 0 reads as an inner node
+    if (tree.index.empty()) return 0;
+    uint32_t best = 0;
+    std::vector<std::pair<uint32_t, uint32_t>> st = {{tree.root, 0}};
+    while (!st.empty()) {
+        auto [n, d] = st.back();
+        st.pop_back();
+        if (d > best) best = d;
+        if (tree.nodes[n].inner()) {
+            st.push_back({(uint32_t)tree.nodes[n].link_l, d + 1});
+            st.push_back({(uint32_t)tree.nodes[n].link_r, d + 1});
+        }
+    }
+    return best;
+}
+
+}  // namespace
+
+extern "C" {
+
+int grt_version(void) { return GRT_VERSION_MAJOR * 1000 + GRT_VERSION_MINOR; }
+
+void grt_bvh_opts_default(grt_bvh_opts *o) {
+    if (!o) return;
+    o->split = GRT_SPLIT_SAH;
+    o->max_tris_per_node = 4;
+    o->number_of_planes = 16;
+    o->esc = 1;
+}
+
+grt_status grt_create(const grt_config *cfg, grt_ctx **out) {
+    if (!out) return GRT_ERR_INVALID_ARG;
+    *out = nullptr;
+    int dev = cfg ? cfg->device : 0;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || dev < 0 || dev >= count) {
+        cudaGetLastError();
+        return GRT_ERR_NO_DEVICE;
+    }
+    grt_ctx *c = new grt_ctx();
+    c->device = dev;
+    device_guard g(dev);
+    cudaError_t e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_err, 2 * sizeof(unsigned));
+    if (e == cudaSuccess) {
+        c->d_counter = c->d_err + 1;
+        e = cudaMemset(c->d_err, 0, 2 * sizeof(unsigned));
+    }
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        if (c->d_err) cudaFree(c->d_err);
+        delete c;
+        return e == cudaErrorMemoryAllocation ? GRT_ERR_OOM : GRT_ERR_CUDA;
+    }
+    *out = c;
+    return GRT_OK;
+}
+
+grt_status grt_destroy(grt_ctx *c) {
+    if (!c) return GRT_ERR_INVALID_ARG;
+    {
+        device_guard g(c->device);
+        free_scene(c);
+        if (c->d_stage) cudaFree(c->d_stage);
+        if (c->d_err) cudaFree(c->d_err);
+        if (c->stream) cudaStreamDestroy(c->stream);
+    }
+    delete c;
+    return GRT_OK;
+}
+
+const char *grt_last_error(const grt_ctx *c) { return c ? c->err.c_str() : "null context"; }
+
+grt_status grt_build(grt_ctx *c, const float *vpos4, uint32_t nv, const uint32_t *tris4, uint32_t nt,
+                     const grt_bvh_opts *opts) {
+    if (!c) return GRT_ERR_INVALID_ARG;
+    if ((nv && !vpos4) || (nt && !tris4)) return fail(c, GRT_ERR_INVALID_ARG, "null vertex or triangle array");
+    const grt::build_opts bo = to_build_opts(opts);
+    device_guard g(c->device);
+    free_scene(c);
+    c->stats = grt_bvh_stats{};
+
+    auto t0 = std::chrono::steady_clock::now();
+    std::string msg;
+    grt::ref_tree tree;
+    if (!grt::build_reference_bvh(vpos4, nv, tris4, nt, bo, tree, msg)) return fail(c, GRT_ERR_INVALID_ARG, msg);
+    c->stats.build_ms = ms_since(t0);
+
+    t0 = std::chrono::steady_clock::now();
+    grt::flat_bvh flat;
+    if (!grt::flatten_bvh(tree, vpos4, tris4, flat, msg)) return fail(c, GRT_ERR_INVALID_ARG, msg);
+    c->stats.flatten_ms = ms_since(t0);
+    if (flat.depth > (uint32_t)grt::kStackLarge)
+        return fail(c, GRT_ERR_BVH_TOO_DEEP,
+                    "BVH depth " + std::to_string(flat.depth) + " exceeds the largest traversal stack (" +
+                        std::to_string(grt::kStackLarge) + ")");
+    bool finite = true;
+    for (size_t i = 0; i < (size_t)nv && finite; ++i)
+        for (int k = 0; k < 3; ++k) finite = finite && std::isfinite(vpos4[4 * i + k]);
+
+    t0 = std::chrono::steady_clock::now();
+    const size_t nb = flat.nodes.size() * 4, rb = flat.records.size() * 4;
+    const size_t vb = (size_t)nv * 16, tb = (size_t)nt * 16;
+    cudaError_t e = cudaSuccess;
+    auto up = [&](void **dst, const void *src, size_t bytes) {
+        if (e != cudaSuccess || bytes == 0) return;
+        e = cudaMalloc(dst, bytes);
+        if (e == cudaSuccess) e = cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
+    };
+    up(&c->d_nodes, flat.nodes.data(), nb);
+    up(&c->d_recs, flat.records.data(), rb);
+    up(&c->d_vpos, vpos4, vb);
+    up(&c->d_tris, tris4, tb);
+    if (e != cudaSuccess) {
+        free_scene(c);
+        return cuda_fail(c, e, "uploading the BVH");
+    }
+    c->stats.upload_ms = ms_since(t0);
+
+    c->sc.nodes = (const float4 *)c->d_nodes;
+    c->sc.records = (const float4 *)c->d_recs;
+    c->sc.root = flat.root;
+    c->sc.empty = flat.empty ? 1 : 0;
+    c->sc.finite = finite ? 1 : 0;
+    c->nv = nv;
+    c->nt = nt;
+    c->depth = flat.depth;
+    c->stats.ref_nodes = (uint32_t)tree.nodes.size();
+    c->stats.inner_nodes = flat.inner;
+    c->stats.tri_records = (uint32_t)tree.index.size();
+    c->stats.depth = flat.depth;
+    c->stats.device_bytes = nb + rb + vb + tb;
+    c->tree = std::move(tree);
+    c->built = true;
+    return GRT_OK;
+}
+
+grt_status grt_bvh_info(grt_ctx *c, grt_bvh_stats *out) {
+    if (!c || !out) return GRT_ERR_INVALID_ARG;
+    if (!c->built) return fail(c, GRT_ERR_NOT_BUILT, "no scene has been built");
+    *out = c->stats;
+    return GRT_OK;
+}
+
+grt_status grt_export_bvh(grt_ctx *c, uint32_t *nodes14, uint32_t *index, uint32_t *root) {
+    if (!c) return GRT_ERR_INVALID_ARG;
+    if (!c->built) return fail(c, GRT_ERR_NOT_BUILT, "no scene has been built");
+    export_tree(c->tree, nodes14, index, root);
+    return GRT_OK;
+}
+
+struct grt_host_bvh {
+    grt::ref_tree tree;
+    grt_bvh_stats stats{};
+};
+
+grt_status grt_host_bvh_build(const float *vpos4, uint32_t nv, const uint32_t *tris4, uint32_t nt,
+                              const grt_bvh_opts *opts, grt_host_bvh **out) {
+    if (!out || (nv && !vpos4) || (nt && !tris4)) return GRT_ERR_INVALID_ARG;
+    *out = nullptr;
+    grt_host_bvh *h = new grt_host_bvh();
+    std::string msg;
+    auto t0 = std::chrono::steady_clock::now();
+    if (!grt::build_reference_bvh(vpos4, nv, tris4, nt, to_build_opts(opts), h->tree, msg)) {
+        delete h;
+        return GRT_ERR_INVALID_ARG;
+    }
+    h->stats.build_ms = ms_since(t0);
+    h->stats.ref_nodes = (uint32_t)h->tree.nodes.size();
+    h->stats.tri_records = (uint32_t)h->tree.index.size();
+    h->stats.depth = tree_depth(h->tree);
+    *out = h;
+    return GRT_OK;
+}
+
+grt_status grt_host_bvh_info(const grt_host_bvh *h, grt_bvh_stats *out) {
+    if (!h || !out) return GRT_ERR_INVALID_ARG;
+    *out = h->stats;
+    return GRT_OK;
+}
+
+grt_status grt_host_bvh_export(const grt_host_bvh *h, uint32_t *nodes14, uint32_t *index, uint32_t *root) {
+    if (!h) return GRT_ERR_INVALID_ARG;
+    export_tree(h->tree, nodes14, index, root);
+    return GRT_OK;
+}
+
+void grt_host_bvh_free(grt_host_bvh *h) { delete h; }
+
+grt_status grt_select_tracer(grt_ctx *c, const char *name) {
+    if (!c || !name) return GRT_ERR_INVALID_ARG;
+    std::string n(name);
+    if (n == "default") n = kTracerNames[0];
+    for (int i = 0; i < 2; ++i)
+        if (n == kTracerNames[i]) {
+            c->tracer = i;
+            return GRT_OK;
+        }
+    return fail(c, GRT_ERR_UNKNOWN_TRACER, "there is no tracer named '" + n + "'");
+}
+
+grt_status grt_set_tuning(grt_ctx *c, const grt_tuning *t) {
+    if (!c || !t) return GRT_ERR_INVALID_ARG;
+    if (t->block_threads < 0 || t->block_threads % 32 || t->block_threads > 256 || t->blocks_per_sm < 0 ||
+        t->refill_threshold < 0 || t->refill_threshold > 32 || t->refill_period < 0 || t->stack_entries < 0 ||
+        t->stack_entries > grt::kStackLarge)
+        return fail(c, GRT_ERR_INVALID_ARG, "tuning value out of range");
+    c->tuning = *t;
+    return GRT_OK;
+}
+
+grt_status grt_get_tuning(grt_ctx *c, grt_tuning *t) {
+    if (!c || !t) return GRT_ERR_INVALID_ARG;
+    *t = c->tuning;
+    return GRT_OK;
+}
+
+grt_status grt_trace(grt_ctx *c, const float *rays_dev, grt_hit *hits_dev, uint32_t n, int any_hit,
+                     grt_stream_t stream) {
+    if (!c) return GRT_ERR_INVALID_ARG;
+    if (!c->built) return fail(c, GRT_ERR_NOT_BUILT, "grt_trace before a successful grt_build");
+    if (n == 0) return GRT_OK;
+    if (n > (1u << 31)) return fail(c, GRT_ERR_INVALID_ARG, "more than 2^31 rays in one call");
+    if (!rays_dev || !hits_dev || !aligned16(rays_dev) || !aligned16(hits_dev))
+        return fail(c, GRT_ERR_INVALID_ARG, "ray and hit buffers must be non-null and 16-byte aligned");
+    device_guard g(c->device);
+    grt::launch_params lp = params_for(c, any_hit != 0);
+    cudaError_t e;
+    if (c->tracer == 1)
+        e = grt::launch_trace_persistent(c->sc, (const float4 *)rays_dev, hits_dev, n, any_hit != 0, lp, c->d_err,
+                                         c->d_counter, (cudaStream_t)stream);
+    else
+        e = grt::launch_trace_plain(c->sc, (const float4 *)rays_dev, hits_dev, n, any_hit != 0, lp, c->d_err,
+                                    (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "launching the traversal kernel");
+    return GRT_OK;
+}
+
+grt_status grt_check(grt_ctx *c, grt_stream_t stream, uint32_t timeout_ms) {
+    if (!c) return GRT_ERR_INVALID_ARG;
+    device_guard g(c->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        cudaError_t q = cudaStreamQuery(st);
+        if (q == cudaSuccess) break;
+        if (q != cudaErrorNotReady) return cuda_fail(c, q, "waiting for the stream");
+        if (timeout_ms && ms_since(t0) > timeout_ms)
+            return fail(c, GRT_ERR_TIMEOUT, "stream did not finish within " + std::to_string(timeout_ms) + " ms");
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+    unsigned bits = 0;
+    cudaError_t e = cudaMemcpy(&bits, c->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(c, e, "reading the kernel error word");
+    if (bits) {
+        cudaMemset(c->d_err, 0, sizeof(unsigned));
+        std::string m = "traversal kernel reported:";
+        if (bits & grt::ERR_STACK_OVERFLOW) m += " stack overflow";
+        if (bits & grt::ERR_STEP_LIMIT) m += " step limit";
+        return fail(c, GRT_ERR_TRAVERSAL, m);
+    }
+    return GRT_OK;
+}
+
+grt_status grt_trace_host(grt_ctx *c, const float *rays_host, grt_hit *hits_host, uint32_t n, int any_hit) {
+    if (!c) return GRT_ERR_INVALID_ARG;
+    if (!c->built) return fail(c, GRT_ERR_NOT_BUILT, "grt_trace_host before a successful grt_build");
+    if (n == 0) return GRT_OK;
+    if (!rays_host || !hits_host) return fail(c, GRT_ERR_INVALID_ARG, "null host buffer");
+    device_guard g(c->device);
+    const size_t rb = (size_t)n * 32, hb = (size_t)n * 16;
+    if (c->stage_bytes < rb + hb) {
+        if (c->d_stage) cudaFree(c->d_stage);
+        c->d_stage = nullptr;
+        c->stage_bytes = 0;
+        cudaError_t e = cudaMalloc(&c->d_stage, rb + hb);
+        if (e != cudaSuccess) return cuda_fail(c, e, "allocating staging buffers");
+        c->stage_bytes = rb + hb;
+    }
+    float *d_rays = (float *)c->d_stage;
+    grt_hit *d_hits = (grt_hit *)((char *)c->d_stage + rb);
+    cudaError_t e = cudaMemcpyAsync(d_rays, rays_host, rb, cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "copying rays to the device");
+    if (any_hit) {  // any-hit leaves beta/gamma as they were, like the reference
+        e = cudaMemcpyAsync(d_hits, hits_host, hb, cudaMemcpyHostToDevice, c->stream);
+        if (e != cudaSuccess) return cuda_fail(c, e, "copying hits to the device");
+    }
+    grt_status s = grt_trace(c, d_rays, d_hits, n, any_hit, (grt_stream_t)c->stream);
+    if (s != GRT_OK) return s;
+    e = cudaMemcpyAsync(hits_host, d_hits, hb, cudaMemcpyDeviceToHost, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "copying hits to the host");
+    return grt_check(c, (grt_stream_t)c->stream, 0);
+}
+
+}  // extern "C"

@@ -1,0 +1,50 @@
+// Internal interfaces between the C-ABI (api.cpp) and the kernels (*.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "../../include/grt.h"
+
+namespace grt {
+
+// Everything a traversal kernel needs about one scene; passed by value as a kernel argument.
+struct dev_scene {
+    const float4 *nodes;    // 4 float4 per inner node (layout in bvh_builder.hpp)
+    const float4 *records;  // 3 float4 per triangle record
+    int32_t root;           // child reference of the root
+    int32_t empty;          // 1: no triangles, every ray misses
+    int32_t finite;         // 1: every vertex coordinate is finite (enables the min/max slab test)
+    int32_t pad;
+};
+
+// Bits a kernel ORs into the context's error word.
+enum : unsigned { ERR_STACK_OVERFLOW = 1u, ERR_STEP_LIMIT = 2u };
+
+// Stack variants compiled into the library (entries per thread, shared memory).
+static const int kStackSmall = 32;
+static const int kStackLarge = 64;
+
+// Upper bound on traversal steps (inner nodes + leaves) of one ray. A DFS over a tree visits
+// each node at most once per ray, so a correct BVH never reaches it; it bounds the work of a
+// kernel given a corrupted tree.
+static const uint32_t kStepLimit = 1u << 26;
+
+struct launch_params {
+    int block_threads;
+    int grid_blocks;        // persistent kernels: total resident blocks
+    int refill_threshold;
+    int refill_period;
+    int stack_entries;
+};
+
+cudaError_t launch_trace_plain(const dev_scene &sc, const float4 *rays, grt_hit *hits, uint32_t n, bool any_hit,
+                               const launch_params &lp, unsigned *err, cudaStream_t stream);
+
+cudaError_t launch_trace_persistent(const dev_scene &sc, const float4 *rays, grt_hit *hits, uint32_t n, bool any_hit,
+                                    const launch_params &lp, unsigned *err, unsigned *counter, cudaStream_t stream);
+
+// Occupancy of the persistent kernel for a block size and stack variant (blocks per SM).
+int persistent_blocks_per_sm(int block_threads, int stack_entries, bool any_hit);
+
+}  // namespace grt

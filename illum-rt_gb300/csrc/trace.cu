@@ -1,0 +1,169 @@
+// Closest-hit / any-hit traversal kernels for sm_103a.
+//
+// Two tracers replace the reference's CUDA variants (rt/cuda/trace-kernels.cu):
+//   * k_trace_plain  — "while-while": one thread per ray, the wavefront baseline
+//     (the role of whilewhile_trace, rt/cuda/trace-kernels.cu:292-316);
+//   * k_trace_persistent — persistent warps that refill lanes whose ray finished from a global
+//     ray counter whenever fewer than `refill_threshold` lanes are still busy (the idea of
+//     dynamicwhilewhile_trace, rt/cuda/trace-kernels.cu:702-876, restructured so that every
+//     ballot is taken by all 32 lanes at a uniform point of the loop, and the counter is reset
+//     by the host before the launch instead of by the kernel's own threads).
+// Both walk the BVH with trav_step (traverse.cuh), so their results are identical to each
+// other and to the reference CPU tracer.
+#include "traverse.cuh"
+
+namespace grt {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+template <int STACK, bool ANY>
+__global__ void __launch_bounds__(256) k_trace_plain(const float4 *__restrict__ rays, grt_hit *__restrict__ hits,
+                                                     uint32_t n, dev_scene sc, unsigned *err) {
+    extern __shared__ int s_stack[];
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const ray_t r = load_ray(rays, i);
+    trav_t s;
+    trav_init(s, sc);
+    int *stk = s_stack + threadIdx.x;
+    const int stride = blockDim.x;
+    if (sc.finite && ray_is_plain(r)) {
+        while (!s.done) trav_step<STACK, ANY, true>(s, sc, r, stk, stride, err);
+    } else {
+        while (!s.done) trav_step<STACK, ANY, false>(s, sc, r, stk, stride, err);
+    }
+    store_hit<ANY>(hits, i, s);
+}
+
+template <int STACK, bool ANY>
+__global__ void __launch_bounds__(256) k_trace_persistent(const float4 *__restrict__ rays, grt_hit *__restrict__ hits,
+                                                          uint32_t n, dev_scene sc, unsigned *err,
+                                                          unsigned *counter, int refill_threshold, int refill_period) {
+    extern __shared__ int s_stack[];
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned lanes_below = (1u << lane) - 1u;
+    int *stk = s_stack + threadIdx.x;
+    const int stride = blockDim.x;
+    trav_t s;
+    ray_t r;
+    uint32_t idx = 0;
+    bool have = false, plain = false, exhausted = false;
+    for (;;) {
+        // refill the lanes without a ray (all 32 lanes arrive here together)
+        if (!exhausted) {
+            const unsigned need = __ballot_sync(kFull, !have);
+            if (need) {
+                const unsigned cnt = __popc(need);
+                unsigned base = 0;
+                if (lane == 0) base = atomicAdd(counter, cnt);
+                base = __shfl_sync(kFull, base, 0);
+                if (base + cnt >= n) exhausted = true;
+                if (!have) {
+                    const uint32_t my = base + __popc(need & lanes_below);
+                    if (my < n) {
+                        idx = my;
+                        r = load_ray(rays, my);
+                        trav_init(s, sc);
+                        plain = sc.finite && ray_is_plain(r);
+                        have = true;
+                        if (s.done) {  // empty scene
+                            store_hit<ANY>(hits, idx, s);
+                            have = false;
+                        }
+                    }
+                }
+            }
+        }
+        if (__ballot_sync(kFull, have) == 0) {
+            if (exhausted) break;
+            continue;
+        }
+        // traverse; every `refill_period` steps the warp counts its busy lanes
+        for (int it = 1;; ++it) {
+            if (have) {
+                if (plain)
+                    trav_step<STACK, ANY, true>(s, sc, r, stk, stride, err);
+                else
+                    trav_step<STACK, ANY, false>(s, sc, r, stk, stride, err);
+                if (s.done) {
+                    store_hit<ANY>(hits, idx, s);
+                    have = false;
+                }
+            }
+            if (it % refill_period == 0) {
+                const int busy = __popc(__ballot_sync(kFull, have));
+                if (busy == 0 || (!exhausted && busy < refill_threshold)) break;
+            }
+        }
+    }
+}
+
+template <int STACK, bool ANY>
+cudaError_t plain_launch(const dev_scene &sc, const float4 *rays, grt_hit *hits, uint32_t n, const launch_params &lp,
+                         unsigned *err, cudaStream_t st) {
+    const int bt = lp.block_threads;
+    const size_t smem = (size_t)STACK * bt * sizeof(int);
+    auto kern = k_trace_plain<STACK, ANY>;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    const uint32_t blocks = (n + bt - 1) / bt;
+    kern<<<blocks, bt, smem, st>>>(rays, hits, n, sc, err);
+    return cudaGetLastError();
+}
+
+template <int STACK, bool ANY>
+cudaError_t persistent_launch(const dev_scene &sc, const float4 *rays, grt_hit *hits, uint32_t n,
+                              const launch_params &lp, unsigned *err, unsigned *counter, cudaStream_t st) {
+    const int bt = lp.block_threads;
+    const size_t smem = (size_t)STACK * bt * sizeof(int);
+    auto kern = k_trace_persistent<STACK, ANY>;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
+    if (e != cudaSuccess) return e;
+    kern<<<lp.grid_blocks, bt, smem, st>>>(rays, hits, n, sc, err, counter, lp.refill_threshold, lp.refill_period);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_trace_plain(const dev_scene &sc, const float4 *rays, grt_hit *hits, uint32_t n, bool any_hit,
+                               const launch_params &lp, unsigned *err, cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    if (lp.stack_entries <= kStackSmall)
+        return any_hit ? plain_launch<kStackSmall, true>(sc, rays, hits, n, lp, err, stream)
+                       : plain_launch<kStackSmall, false>(sc, rays, hits, n, lp, err, stream);
+    return any_hit ? plain_launch<kStackLarge, true>(sc, rays, hits, n, lp, err, stream)
+                   : plain_launch<kStackLarge, false>(sc, rays, hits, n, lp, err, stream);
+}
+
+cudaError_t launch_trace_persistent(const dev_scene &sc, const float4 *rays, grt_hit *hits, uint32_t n, bool any_hit,
+                                    const launch_params &lp, unsigned *err, unsigned *counter, cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    if (lp.stack_entries <= kStackSmall)
+        return any_hit ? persistent_launch<kStackSmall, true>(sc, rays, hits, n, lp, err, counter, stream)
+                       : persistent_launch<kStackSmall, false>(sc, rays, hits, n, lp, err, counter, stream);
+    return any_hit ? persistent_launch<kStackLarge, true>(sc, rays, hits, n, lp, err, counter, stream)
+                   : persistent_launch<kStackLarge, false>(sc, rays, hits, n, lp, err, counter, stream);
+}
+
+int persistent_blocks_per_sm(int block_threads, int stack_entries, bool any_hit) {
+    int blocks = 0;
+    const bool small = stack_entries <= kStackSmall;
+    const size_t smem = (size_t)(small ? kStackSmall : kStackLarge) * block_threads * sizeof(int);
+    const void *fn = small ? (any_hit ? (const void *)k_trace_persistent<kStackSmall, true>
+                                      : (const void *)k_trace_persistent<kStackSmall, false>)
+                           : (any_hit ? (const void *)k_trace_persistent<kStackLarge, true>
+                                      : (const void *)k_trace_persistent<kStackLarge, false>);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, block_threads, smem) != cudaSuccess) return 1;
+    return blocks > 0 ? blocks : 1;
+}
+
+}  // namespace grt

@@ -1,0 +1,222 @@
+// Device-side traversal of the flattened BVH (layout in bvh_builder.hpp).
+//
+// Results are bit-identical to the reference CPU tracer (rt/cpu/bvh2.cpp:71-189) on the same
+// BVH and rays:
+//   * the slab test follows intersect4 (libgi/intersect.h:230-267) with the ray's [t_min, t_max]
+//     range and the same compare-and-select structure (so NaN cases come out the same);
+//   * the triangle test is the reference's Cramer/Shirley test (libgi/intersect.h:19-74) with
+//     every product, sum and quotient rounded exactly as written (__fmul_rn, __fadd_rn,
+//     __fdiv_rn; nothing is contracted into an FMA);
+//   * children are visited in the reference's order (near child first, ties to the right),
+//     boxes are culled against the closest hit when they are tested (not when popped), and a
+//     hit replaces the closest one only if strictly nearer, so the first of two equal hits wins.
+#pragma once
+#include <cfloat>
+#include <cstdint>
+
+#include "grt_internal.hpp"
+
+namespace grt {
+
+struct ray_t {
+    float ox, oy, oz, dx, dy, dz, ix, iy, iz, tmin, tmax;
+};
+
+struct hit_t {
+    float t, b, g;
+    uint32_t ref;
+};
+
+__device__ __forceinline__ ray_t load_ray(const float4 *__restrict__ rays, uint32_t i) {
+    const float4 a = __ldg(rays + 2 * (size_t)i), d = __ldg(rays + 2 * (size_t)i + 1);
+    ray_t r;
+    r.ox = a.x;
+    r.oy = a.y;
+    r.oz = a.z;
+    r.tmin = a.w;
+    r.dx = d.x;
+    r.dy = d.y;
+    r.dz = d.z;
+    r.tmax = d.w;
+    // ray::ray computes id = 1/d in IEEE float (libgi/rt.h:28)
+    r.ix = __fdiv_rn(1.0f, d.x);
+    r.iy = __fdiv_rn(1.0f, d.y);
+    r.iz = __fdiv_rn(1.0f, d.z);
+    return r;
+}
+
+__device__ __forceinline__ bool finite_nonzero(float x) { return isfinite(x) && x != 0.f; }
+
+// A ray is "plain" when no slab product (box - o) * (1/d) can be NaN: o finite and every
+// 1/d finite and non-zero. Then min/max instructions give exactly the reference's selects
+// (they differ only on NaN operands, and on the sign of zero, which no comparison sees).
+__device__ __forceinline__ bool ray_is_plain(const ray_t &r) {
+    return finite_nonzero(r.ix) && finite_nonzero(r.iy) && finite_nonzero(r.iz) && isfinite(r.ox) &&
+           isfinite(r.oy) && isfinite(r.oz);
+}
+
+template <bool PLAIN>
+__device__ __forceinline__ bool slab(float lx, float ly, float lz, float hx, float hy, float hz, const ray_t &r,
+                                     float &tnear) {
+    const float ax = __fmul_rn(__fsub_rn(lx, r.ox), r.ix), bx = __fmul_rn(__fsub_rn(hx, r.ox), r.ix);
+    const float ay = __fmul_rn(__fsub_rn(ly, r.oy), r.iy), by = __fmul_rn(__fsub_rn(hy, r.oy), r.iy);
+    const float az = __fmul_rn(__fsub_rn(lz, r.oz), r.iz), bz = __fmul_rn(__fsub_rn(hz, r.oz), r.iz);
+    float t1, t2;
+    if (PLAIN) {
+        t1 = fmaxf(fmaxf(fminf(ax, bx), fminf(ay, by)), fminf(az, bz));
+        t2 = fminf(fminf(fmaxf(ax, bx), fmaxf(ay, by)), fmaxf(az, bz));
+    } else {
+        const float t1x = (ax < bx) ? ax : bx, t2x = (bx < ax) ? ax : bx;
+        const float t1y = (ay < by) ? ay : by, t2y = (by < ay) ? ay : by;
+        const float t1z = (az < bz) ? az : bz, t2z = (bz < az) ? az : bz;
+        t1 = (t1x < t1y) ? t1y : t1x;
+        t1 = (t1z < t1) ? t1 : t1z;
+        t2 = (t2x < t2y) ? t2x : t2y;
+        t2 = (t2z < t2) ? t2z : t2;
+    }
+    tnear = t1;
+    return !(t1 > t2) && !(t2 < r.tmin) && !(t1 > r.tmax);
+}
+
+// Cramer's rule test of the reference (libgi/intersect.h:36-67) on a triangle record
+// (v0, v0 - v1, v0 - v2). The sign tests before the divisions only discard cases whose
+// quotients cannot pass the reference's `beta > 0` / `gamma > 0` (zero numerator, or
+// numerator and determinant of opposite sign), so the outcome is unchanged.
+__device__ __forceinline__ bool tri_test(const float4 &p0, const float4 &p1, const float4 &p2, const ray_t &r,
+                                         float &t_out, float &b_out, float &g_out) {
+    const float a = p1.x, b = p1.y, c = p1.z;
+    const float d = p2.x, e = p2.y, f = p2.z;
+    const float g = r.dx, h = r.dy, i = r.dz;
+    const float j = __fsub_rn(p0.x, r.ox), k = __fsub_rn(p0.y, r.oy), l = __fsub_rn(p0.z, r.oz);
+    float c1 = __fsub_rn(__fmul_rn(e, i), __fmul_rn(h, f));
+    float c2 = __fsub_rn(__fmul_rn(g, f), __fmul_rn(d, i));
+    float c3 = __fsub_rn(__fmul_rn(d, h), __fmul_rn(e, g));
+    const float M = __fadd_rn(__fadd_rn(__fmul_rn(a, c1), __fmul_rn(b, c2)), __fmul_rn(c, c3));
+    float beta = __fadd_rn(__fadd_rn(__fmul_rn(j, c1), __fmul_rn(k, c2)), __fmul_rn(l, c3));
+    if (beta == 0.f || ((__float_as_uint(beta) ^ __float_as_uint(M)) & 0x80000000u)) return false;
+    c1 = __fsub_rn(__fmul_rn(a, k), __fmul_rn(j, b));
+    c2 = __fsub_rn(__fmul_rn(j, c), __fmul_rn(a, l));
+    c3 = __fsub_rn(__fmul_rn(b, l), __fmul_rn(k, c));
+    float gamma = __fadd_rn(__fadd_rn(__fmul_rn(i, c1), __fmul_rn(h, c2)), __fmul_rn(g, c3));
+    if (gamma == 0.f || ((__float_as_uint(gamma) ^ __float_as_uint(M)) & 0x80000000u)) return false;
+    float tt = -__fadd_rn(__fadd_rn(__fmul_rn(f, c1), __fmul_rn(e, c2)), __fmul_rn(d, c3));
+    beta = __fdiv_rn(beta, M);
+    gamma = __fdiv_rn(gamma, M);
+    tt = __fdiv_rn(tt, M);
+    if (tt > r.tmin && tt < r.tmax && beta > 0.f && gamma > 0.f && __fadd_rn(beta, gamma) <= 1.f) {
+        t_out = tt;
+        b_out = beta;
+        g_out = gamma;
+        return true;
+    }
+    return false;
+}
+
+// Decoding of a leaf child reference: ~ref = (first << 4) | (count - 1).
+__device__ __forceinline__ void leaf_range(int32_t ref, uint32_t &first, uint32_t &count) {
+    const uint32_t v = ~(uint32_t)ref;
+    first = v >> 4;
+    count = (v & 15u) + 1u;
+}
+
+// Traversal state of one ray, kept in registers; the stack lives in shared memory at
+// stk[k * stride] for entry k.
+struct trav_t {
+    int32_t cur;   // node or leaf reference being processed
+    int32_t sp;    // entries on the stack
+    uint32_t steps;
+    bool done;
+    bool found;  // any-hit: an occluder was found
+    hit_t hit;
+};
+
+__device__ __forceinline__ void trav_init(trav_t &s, const dev_scene &sc) {
+    s.cur = sc.root;
+    s.sp = 0;
+    s.steps = 0;
+    s.done = sc.empty != 0;
+    s.found = false;
+    s.hit.t = FLT_MAX;
+    s.hit.b = 0.f;
+    s.hit.g = 0.f;
+    s.hit.ref = 0u;
+}
+
+// One traversal step: one inner node (two box tests) or one leaf (its triangle tests).
+// Mirrors one pop of the reference loop (rt/cpu/bvh2.cpp:82-127 / 147-182): the near child is
+// kept in `cur` instead of being pushed and popped straight back.
+template <int STACK, bool ANY, bool PLAIN>
+__device__ __forceinline__ void trav_step(trav_t &s, const dev_scene &sc, const ray_t &r, int *stk, int stride,
+                                          unsigned *err) {
+    if (++s.steps > kStepLimit) {
+        atomicOr(err, ERR_STEP_LIMIT);
+        s.done = true;
+        return;
+    }
+    if (s.cur >= 0) {
+        const float4 *np = sc.nodes + 4 * (size_t)s.cur;
+        const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3);
+        float dl, dr;
+        bool hl = slab<PLAIN>(n0.x, n0.y, n0.z, n1.x, n1.y, n1.z, r, dl);
+        bool hr = slab<PLAIN>(n2.x, n2.y, n2.z, n3.x, n3.y, n3.z, r, dr);
+        if (!ANY) {
+            hl = hl && dl < s.hit.t;
+            hr = hr && dr < s.hit.t;
+        }
+        const int32_t cl = __float_as_int(n0.w), cr = __float_as_int(n2.w);
+        if (hl && hr) {
+            const bool left_first = dl < dr;
+            if (s.sp >= STACK) {
+                atomicOr(err, ERR_STACK_OVERFLOW);
+                s.done = true;
+                return;
+            }
+            stk[s.sp * stride] = left_first ? cr : cl;
+            ++s.sp;
+            s.cur = left_first ? cl : cr;
+            return;
+        }
+        if (hl || hr) {
+            s.cur = hl ? cl : cr;
+            return;
+        }
+    } else {
+        uint32_t first, count;
+        leaf_range(s.cur, first, count);
+        const float4 *rp = sc.records + 3 * (size_t)first;
+        for (uint32_t k = 0; k < count; ++k) {
+            const float4 p0 = __ldg(rp + 3 * k), p1 = __ldg(rp + 3 * k + 1), p2 = __ldg(rp + 3 * k + 2);
+            float t, b, g;
+            if (tri_test(p0, p1, p2, r, t, b, g) && (ANY || t < s.hit.t)) {
+                s.hit.t = t;
+                s.hit.b = b;
+                s.hit.g = g;
+                s.hit.ref = __float_as_uint(p0.w);
+                if (ANY) {
+                    s.found = true;
+                    s.done = true;
+                    return;
+                }
+            }
+        }
+    }
+    if (s.sp == 0) {
+        s.done = true;
+        return;
+    }
+    --s.sp;
+    s.cur = stk[s.sp * stride];
+}
+
+// Writes one result in the reference's encodings (see include/grt.h).
+template <bool ANY>
+__device__ __forceinline__ void store_hit(grt_hit *hits, uint32_t i, const trav_t &s) {
+    if (ANY) {
+        hits[i].t = s.found ? 4294967296.0f : FLT_MAX;
+        hits[i].ref = s.found ? 0xFFFFFFFFu : 0u;
+    } else {
+        reinterpret_cast<float4 *>(hits)[i] = make_float4(s.hit.t, s.hit.b, s.hit.g, __uint_as_float(s.hit.ref));
+    }
+}
+
+}  // namespace grt

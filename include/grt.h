@@ -1,0 +1,173 @@
+/*
+ * grt.h — C-ABI of the GB300 batch ray-traversal library (libgrt.so).
+ *
+ * The library replaces the CUDA batch tracers of RTGI (lwolf98/illum-rt). In the reference a
+ * wavefront algorithm calls a pluggable `wf::batch_ray_tracer` (libgi/wavefront-rt.h:145-149)
+ * whose CUDA specialisation `wf::cuda::batch_rt` (rt/cuda/base.h:403-429) builds a BVH on the
+ * host (rt/cuda/base.cpp:88-117) and launches traversal kernels over device ray buffers
+ * (rt/cuda/tracers.cu:57-294). This header exposes the same operations over plain pointers and
+ * sizes so that a thin adapter class can drop in for that path (INTEGRATION.md shows it).
+ *
+ * Data layouts are the reference's device layouts:
+ *   vertex positions : float4 per vertex (x, y, z, 1)              rt/cuda/base.cpp:57-66
+ *   triangles        : uint4 per triangle (a, b, c, material id)   rt/cuda/base.cpp:49-53
+ *   rays             : two float4 per ray, (o.xyz, t_min), (d.xyz, t_max)
+ *                                                                  rt/cuda/base.h:337, kernels.cu:52-60
+ *   hits             : grt_hit per ray, identical to wf::cuda::tri_is (rt/cuda/base.h:32-41)
+ *
+ * Results: closest hits are those of the reference CPU tracer binary_bvh_tracer::closest_hit
+ * (rt/cpu/bvh2.cpp:71-137) on the same BVH: same triangle, bit-identical t, beta, gamma (the
+ * ray/triangle test is the reference's Cramer test, libgi/intersect.h:19-74, evaluated with
+ * the same IEEE operations). A miss is t = FLT_MAX, ref = 0. Any-hit results use the CPU
+ * platform's encoding (rt/cpu/wavefront.cpp:60-70): occluded rays get ref = 0xFFFFFFFF and
+ * t = 4294967296.0f; the others t = FLT_MAX, ref = 0; beta and gamma are not written.
+ *
+ * Errors are status codes, never exceptions, and the library never resets the device
+ * (the reference's check_cuda_error calls cudaDeviceReset, rt/cuda/cuda-helpers.cpp:5-12).
+ * All launches are stream-ordered and asynchronous; grt_check() synchronises the stream and
+ * reports errors that kernels flagged (stack overflow, step limit). A context is not
+ * thread-safe; use one context per host thread.
+ */
+#ifndef GRT_H
+#define GRT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GRT_VERSION_MAJOR 1
+#define GRT_VERSION_MINOR 0
+
+/* A cudaStream_t. NULL means the legacy default stream. */
+typedef struct CUstream_st *grt_stream_t;
+typedef struct grt_ctx grt_ctx;
+
+typedef enum grt_status {
+    GRT_OK = 0,
+    GRT_ERR_INVALID_ARG = 1,    /* bad pointer, size or option */
+    GRT_ERR_OOM = 2,            /* device or pinned host allocation failed */
+    GRT_ERR_CUDA = 3,           /* a CUDA runtime call failed (message in grt_last_error) */
+    GRT_ERR_TIMEOUT = 4,        /* grt_check gave up waiting for the stream */
+    GRT_ERR_BVH_TOO_DEEP = 5,   /* the BVH needs a deeper stack than any kernel variant has */
+    GRT_ERR_NOT_BUILT = 6,      /* trace called before a successful build */
+    GRT_ERR_TRAVERSAL = 7,      /* a kernel flagged a stack overflow or hit its step limit */
+    GRT_ERR_UNKNOWN_TRACER = 8, /* grt_select_tracer: no tracer of that name */
+    GRT_ERR_NO_DEVICE = 9       /* no CUDA device of the requested ordinal */
+} grt_status;
+
+/* One hit record, 16 bytes, the layout of wf::cuda::tri_is (rt/cuda/base.h:32-41).
+ * `ref` is the index of the triangle in the triangle array given to grt_build. */
+typedef struct grt_hit {
+    float t, beta, gamma;
+    uint32_t ref;
+} grt_hit;
+
+typedef struct grt_config {
+    int device;         /* CUDA device ordinal */
+    uint32_t reserved;  /* must be 0 */
+} grt_config;
+
+/* BVH builder options: the `bvh type` / `bvh max_tris` commands of the CUDA tracer
+ * (rt/cuda/base.cpp:134-153). Defaults (grt_bvh_opts_default) are the reference's CUDA
+ * build: SAH with 16 planes, at most 4 triangles per leaf, early split clipping on. */
+enum { GRT_SPLIT_OM = 0, GRT_SPLIT_SM = 1, GRT_SPLIT_SAH = 2 };
+typedef struct grt_bvh_opts {
+    int split;             /* GRT_SPLIT_SAH, GRT_SPLIT_SM or GRT_SPLIT_OM */
+    int max_tris_per_node; /* 1..16 */
+    int number_of_planes;  /* SAH candidate planes, >= 1 */
+    int esc;               /* early split clipping, 0 or 1 */
+} grt_bvh_opts;
+
+typedef struct grt_bvh_stats {
+    uint32_t ref_nodes;     /* nodes of the reference layout (inner + leaf) */
+    uint32_t inner_nodes;   /* 64-byte device nodes */
+    uint32_t tri_records;   /* 48-byte device triangle records (ESC duplicates included) */
+    uint32_t depth;         /* edges from the root to the deepest leaf */
+    uint64_t device_bytes;  /* nodes + records + triangles + vertices held on the device */
+    double build_ms;        /* host SAH/ESC build */
+    double flatten_ms;      /* host flattening */
+    double upload_ms;       /* host-to-device copies */
+} grt_bvh_stats;
+
+/* Launch parameters picked by the autotuner (or by hand). Zero fields mean "default". */
+typedef struct grt_tuning {
+    int block_threads;     /* threads per block (multiple of 32) */
+    int blocks_per_sm;     /* persistent kernels: resident blocks per SM */
+    int refill_threshold;  /* persistent kernels: refill a warp when fewer lanes are active */
+    int refill_period;     /* persistent kernels: traversal steps between refill checks */
+    int stack_entries;     /* 0 = smallest variant that fits the BVH depth */
+} grt_tuning;
+
+/* ---- context ------------------------------------------------------------------------ */
+
+/* Version as major*1000 + minor. */
+int grt_version(void);
+
+/* Creates a context on config->device (NULL = device 0). */
+grt_status grt_create(const grt_config *config, grt_ctx **out);
+grt_status grt_destroy(grt_ctx *ctx);
+
+/* Message of the last error on this context ("" if none). Valid until the next call. */
+const char *grt_last_error(const grt_ctx *ctx);
+
+/* Fills opts with the reference CUDA defaults (SAH, 16 planes, 4 per leaf, ESC on). */
+void grt_bvh_opts_default(grt_bvh_opts *opts);
+
+/* ---- build (wf::cuda::batch_rt::build, rt/cuda/base.cpp:88-117) --------------------- */
+
+/* Builds the BVH of one scene from HOST arrays with the reference's CPU SAH/SM/OM builder
+ * and early split clipping (rt/cpu/bvh-ctor.h:96-503), flattens it into the device layout and
+ * uploads it. Replaces any previous scene of the context. opts may be NULL (defaults). */
+grt_status grt_build(grt_ctx *ctx, const float *vpos4, uint32_t nv, const uint32_t *tris4, uint32_t nt,
+                     const grt_bvh_opts *opts);
+
+grt_status grt_bvh_info(grt_ctx *ctx, grt_bvh_stats *out);
+
+/* Copies the BVH of the current scene in the reference's layout: `nodes14` receives
+ * stats.ref_nodes records of 14 words (box_l.min xyz, box_l.max xyz, box_r.min xyz,
+ * box_r.max xyz as float bits, link_l, link_r; bbvh_node, rt/cpu/bvh.h:42-52) and `index`
+ * receives stats.tri_records triangle ids (::bvh::index, rt/cpu/bvh.h:58-63). Either may be
+ * NULL. Used to check the builder against the reference. */
+grt_status grt_export_bvh(grt_ctx *ctx, uint32_t *nodes14, uint32_t *index, uint32_t *root);
+
+/* Host-only access to the builder (no device needed): builds the reference BVH and keeps it
+ * in host memory so that its nodes can be compared with the reference's. */
+typedef struct grt_host_bvh grt_host_bvh;
+grt_status grt_host_bvh_build(const float *vpos4, uint32_t nv, const uint32_t *tris4, uint32_t nt,
+                              const grt_bvh_opts *opts, grt_host_bvh **out);
+/* ref_nodes, tri_records and depth of the host BVH; build_ms of its construction. */
+grt_status grt_host_bvh_info(const grt_host_bvh *bvh, grt_bvh_stats *out);
+grt_status grt_host_bvh_export(const grt_host_bvh *bvh, uint32_t *nodes14, uint32_t *index, uint32_t *root);
+void grt_host_bvh_free(grt_host_bvh *bvh);
+
+/* ---- tracer selection (platform::select / `raytracer <name>`, rt/cuda/platform.cpp:102-131) */
+
+/* Names: "while-while" (default; one thread per ray), "persistent-while-while" (persistent
+ * warps with dynamic ray fetch, the tuned kernel). Unknown name: GRT_ERR_UNKNOWN_TRACER. */
+grt_status grt_select_tracer(grt_ctx *ctx, const char *name);
+grt_status grt_set_tuning(grt_ctx *ctx, const grt_tuning *tuning);
+grt_status grt_get_tuning(grt_ctx *ctx, grt_tuning *tuning);
+
+/* ---- trace (batch_rt::compute_closest_hit / compute_any_hit, rt/cuda/base.h:422-428) ---- */
+
+/* Traces n rays from DEVICE buffers: rays_dev holds 2n float4, hits_dev n grt_hit (16-byte
+ * aligned). Asynchronous on `stream`; call grt_check to wait and collect kernel errors. */
+grt_status grt_trace(grt_ctx *ctx, const float *rays_dev, grt_hit *hits_dev, uint32_t n, int any_hit,
+                     grt_stream_t stream);
+
+/* Same as grt_trace from HOST buffers: copies the rays in, traces, copies the hits out and
+ * waits. Uses context-owned device and pinned staging buffers. */
+grt_status grt_trace_host(grt_ctx *ctx, const float *rays_host, grt_hit *hits_host, uint32_t n, int any_hit);
+
+/* Waits for `stream` (at most timeout_ms milliseconds; 0 = no limit) and returns the first
+ * error flagged by a kernel since the previous check. */
+grt_status grt_check(grt_ctx *ctx, grt_stream_t stream, uint32_t timeout_ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GRT_H */

@@ -1,0 +1,640 @@
+// ORACLE — test infrastructure only. Never linked into, loaded by or called from the product.
+//
+// A CPU restatement of the reference's ray-traversal path (lwolf98/illum-rt, "RTGI"):
+//   * BVH construction: bvh_ctor::build + early split clipping + the OM / SM / SAH subdivision
+//     (rt/cpu/bvh-ctor.h:96-503), indexed triangle layout as the CUDA platform uses it
+//     (rt/cuda/base.cpp:88-117);
+//   * ray/box and ray/triangle tests (libgi/intersect.h:19-74, 230-267);
+//   * binary_bvh_tracer::closest_hit / any_hit (rt/cpu/bvh2.cpp:71-189);
+//   * the OpenMP batch loop of the CPU platform (rt/cpu/wavefront.cpp:53-70).
+// It is written in C++ rather than C because the reference's builder orders primitives with
+// std::sort, whose placement of equal keys is part of the result; calling the same library
+// routine with the same comparator reproduces it. Compiled with -ffp-contract=off so every
+// float operation rounds exactly as written, on x86-64 and aarch64 alike.
+//
+// Pinning: tests compare this restatement with the reference itself (oracle/_ref, built from
+// the reference sources by oracle/build_ref.sh where they are available) node for node, and
+// with golden fixtures generated from oracle/_ref (tests/golden/).
+//
+// One deliberate difference: the reference traversal keeps a fixed 25-entry stack
+// (rt/cpu/bvh2.cpp:76,145) and overflows it on trees deeper than 24. The restatement uses a
+// growable stack and reports the deepest stack it needed, so callers can flag rays on which
+// the reference itself would have had undefined behaviour.
+#include <algorithm>
+#include <atomic>
+#include <cfloat>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <omp.h>
+#include <vector>
+
+namespace orc {
+
+struct v3 {
+    float x, y, z;
+    float operator[](int k) const { return k == 0 ? x : (k == 1 ? y : z); }
+};
+
+// aabb with the reference's grow semantics (libgi/intersect.h:5-16, glm::min/max semantics:
+// min(x, y) = (y < x) ? y : x, max(x, y) = (x < y) ? y : x).
+struct box {
+    v3 lo{FLT_MAX, FLT_MAX, FLT_MAX}, hi{-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    void grow(const v3 &v) {
+        lo = {(lo.x < v.x) ? lo.x : v.x, (lo.y < v.y) ? lo.y : v.y, (lo.z < v.z) ? lo.z : v.z};
+        hi = {(v.x < hi.x) ? hi.x : v.x, (v.y < hi.y) ? hi.y : v.y, (v.z < hi.z) ? hi.z : v.z};
+    }
+    void grow(const box &o) {
+        lo = {(lo.x < o.lo.x) ? lo.x : o.lo.x, (lo.y < o.lo.y) ? lo.y : o.lo.y, (lo.z < o.lo.z) ? lo.z : o.lo.z};
+        hi = {(o.hi.x < hi.x) ? hi.x : o.hi.x, (o.hi.y < hi.y) ? hi.y : o.hi.y, (o.hi.z < hi.z) ? hi.z : o.hi.z};
+    }
+    v3 center() const { return {(lo.x + hi.x) * 0.5f, (lo.y + hi.y) * 0.5f, (lo.z + hi.z) * 0.5f}; }
+    v3 extent() const { return {hi.x - lo.x, hi.y - lo.y, hi.z - lo.z}; }
+};
+
+// surface area as written in bvh-ctor.h:121-124, 184-187, 387-390
+inline float area(const box &b) {
+    v3 e = b.extent();
+    return 2 * (e.x * e.y + e.x * e.z + e.y * e.z);
+}
+
+inline float fmax_ref(float a, float b) { return (a < b) ? b : a; }  // std::max
+inline int largest_axis(const v3 &e) {
+    float largest = fmax_ref(e.x, fmax_ref(e.y, e.z));
+    return largest == e.x ? 0 : (largest == e.y ? 1 : 2);
+}
+
+// bbvh_node (rt/cpu/bvh.h:42-52): a leaf has link_l = -offset, link_r = -count.
+struct node {
+    box l, r;
+    int32_t link_l = 0, link_r = 0;
+    bool inner() const { return link_r >= 0; }
+};
+
+struct prim {
+    box b;
+    uint32_t tri;
+};
+
+struct scene {
+    const float *v4;
+    const uint32_t *t4;
+    uint32_t nv, nt;
+    v3 vert(uint32_t i) const { return {v4[4 * i], v4[4 * i + 1], v4[4 * i + 2]}; }
+};
+
+struct builder {
+    const scene &sc;
+    int split_type;  // 0 om, 1 sm, 2 sah
+    int max_tris, planes;
+    bool esc;
+    std::vector<prim> prims;
+    std::vector<uint32_t> index;
+    std::vector<node> nodes;
+    bool failed = false;
+
+    builder(const scene &s, int type, int mt, int np, bool e) : sc(s), split_type(type), max_tris(mt), planes(np), esc(e) {}
+
+    float c(uint32_t pi, int axis) const { return prims[pi].b.center()[axis]; }
+    void sort_range(uint32_t start, uint32_t end, int axis) {
+        std::sort(index.data() + start, index.data() + end,
+                  [&](uint32_t a, uint32_t b) { return c(a, axis) < c(b, axis); });
+    }
+    box range_box(uint32_t start, uint32_t end) const {
+        box b;
+        for (uint32_t i = start; i < end; ++i) b.grow(prims[index[i]].b);
+        return b;
+    }
+    uint32_t make_leaf(uint32_t start, uint32_t end) {
+        uint32_t id = (uint32_t)nodes.size();
+        nodes.emplace_back();
+        nodes[id].link_l = -(int32_t)start;
+        nodes[id].link_r = -(int32_t)(end - start);
+        return id;
+    }
+
+    // Split of one polygon at the centre of its largest box axis until each part's box area is
+    // at most `thres` (the split() helper, rt/cpu/bvh-ctor.h:120-179).
+    void split_poly(const std::vector<v3> &poly, float thres, std::vector<box> &out) {
+        box b;
+        for (const v3 &v : poly) b.grow(v);
+        if (area(b) <= thres) {
+            out.push_back(b);
+            return;
+        }
+        int ax = largest_axis(b.extent());
+        float center = (b.hi[ax] + b.lo[ax]) * 0.5f;
+        int n = (int)poly.size();
+        bool last_left = poly[0][ax] < center;
+        int cross_first = -1, cross_second = -1;
+        for (int i = 0; i < n; ++i) {
+            bool left = poly[i][ax] < center;
+            if (left != last_left) {
+                if (cross_first == -1)
+                    cross_first = i - 1;
+                else
+                    cross_second = i - 1;
+            }
+            last_left = left;
+        }
+        if (cross_second == -1) cross_second = n - 1;
+        if (cross_first == -1) {  // unreachable for finite input (the reference asserts here)
+            out.push_back(b);
+            return;
+        }
+        auto ipoint = [&](int a) {
+            float delta = center - poly[a][ax];
+            int bb = a + 1 < n ? a + 1 : 0;
+            float s = delta / (poly[bb][ax] - poly[a][ax]);
+            return v3{poly[a].x + (poly[bb].x - poly[a].x) * s, poly[a].y + (poly[bb].y - poly[a].y) * s,
+                      poly[a].z + (poly[bb].z - poly[a].z) * s};
+        };
+        v3 c1 = ipoint(cross_first), c2 = ipoint(cross_second);
+        std::vector<v3> p1, p2;
+        for (int i = 0; i <= cross_first; ++i) p1.push_back(poly[i]);
+        p1.push_back(c1);
+        p2.push_back(c1);
+        for (int i = cross_first + 1; i <= cross_second; ++i) p2.push_back(poly[i]);
+        p2.push_back(c2);
+        p1.push_back(c2);
+        for (int i = cross_second + 1; i < n; ++i) p1.push_back(poly[i]);
+        auto same = [](const v3 &a, const v3 &b) { return a.x == b.x && a.y == b.y && a.z == b.z; };
+        p1.erase(std::unique(p1.begin(), p1.end(), same), p1.end());
+        p2.erase(std::unique(p2.begin(), p2.end(), same), p2.end());
+        split_poly(p1, thres, out);
+        split_poly(p2, thres, out);
+    }
+
+    // early_split_clipping (rt/cpu/bvh-ctor.h:181-226): threshold = area at the 90th percentile.
+    void early_split_clipping() {
+        std::vector<float> areas(prims.size());
+        for (size_t i = 0; i < prims.size(); ++i) areas[i] = area(prims[i].b);
+        size_t k = 9 * prims.size() / 10;
+        std::nth_element(areas.begin(), areas.begin() + k, areas.end());
+        float thres = areas[k];
+        uint32_t N = (uint32_t)prims.size();
+        std::vector<box> gen;
+        for (uint32_t i = 0; i < N; ++i) {
+            const uint32_t *t = sc.t4 + 4 * index[i];
+            std::vector<v3> poly = {sc.vert(t[0]), sc.vert(t[1]), sc.vert(t[2])};
+            gen.clear();
+            split_poly(poly, thres, gen);
+            prims[i] = {gen[0], i};
+            for (size_t j = 1; j < gen.size(); ++j) {
+                prims.push_back({gen[j], i});
+                index.push_back((uint32_t)prims.size() - 1);
+            }
+        }
+    }
+
+    // Object median (rt/cpu/bvh-ctor.h:251-300).
+    uint32_t subdivide_om(uint32_t start, uint32_t end) {
+        if (end - start <= (uint32_t)max_tris) return make_leaf(start, end);
+        box b = range_box(start, end);
+        sort_range(start, end, largest_axis(b.extent()));
+        uint32_t mid = start + (end - start) / 2;
+        uint32_t id = (uint32_t)nodes.size();
+        nodes.emplace_back();
+        uint32_t l = subdivide(start, mid);
+        uint32_t r = subdivide(mid, end);
+        nodes[id].link_l = (int32_t)l;
+        nodes[id].link_r = (int32_t)r;
+        nodes[id].l = range_box(start, mid);
+        nodes[id].r = range_box(mid, end);
+        return id;
+    }
+
+    // Partition of index[start, end) by center <= plane, as both the spatial-median and the SAH
+    // builders do it (rt/cpu/bvh-ctor.h:333-343, 427-440). Returns the resulting mid.
+    uint32_t partition(uint32_t start, uint32_t end, int ax, float plane) {
+        uint32_t mid = start;
+        uint32_t *L = index.data() + start, *R = index.data() + end - 1;
+        while (L < R) {
+            while (c(*L, ax) <= plane && L < R) {
+                ++L;
+                ++mid;
+            }
+            while (c(*R, ax) > plane && L < R) --R;
+            if (c(*L, ax) > c(*R, ax) && L < R) std::swap(*L, *R);
+        }
+        return mid;
+    }
+
+    // Spatial median (rt/cpu/bvh-ctor.h:302-369).
+    uint32_t subdivide_sm(uint32_t start, uint32_t end) {
+        if (end - start <= (uint32_t)max_tris) return make_leaf(start, end);
+        box b = range_box(start, end);
+        v3 e = b.extent();
+        int ax = largest_axis(e);
+        v3 half = {b.lo.x + e.x * 0.5f, b.lo.y + e.y * 0.5f, b.lo.z + e.z * 0.5f};
+        uint32_t mid = partition(start, end, ax, half[ax]);
+        if (mid == start || mid == end - 1) {
+            sort_range(start, end, ax);
+            mid = start + (end - start) / 2;
+        }
+        uint32_t id = (uint32_t)nodes.size();
+        nodes.emplace_back();
+        uint32_t l = subdivide(start, mid);
+        uint32_t r = subdivide(mid, end);
+        nodes[id].link_l = (int32_t)l;
+        nodes[id].link_r = (int32_t)r;
+        nodes[id].l = range_box(start, mid);
+        nodes[id].r = range_box(mid, end);
+        return id;
+    }
+
+    // SAH over `planes` uniform planes on the largest axis (rt/cpu/bvh-ctor.h:371-503).
+    uint32_t subdivide_sah(uint32_t start, uint32_t end) {
+        if (end - start <= (uint32_t)max_tris) return make_leaf(start, end);
+        box b = range_box(start, end);
+        float surf = area(b);
+        v3 e = b.extent();
+        int ax = largest_axis(e);
+        uint32_t mid = start;
+        box bl, br;
+        if (surf == 0) {
+            sort_range(start, end, ax);
+            mid = start + (end - start) / 2;
+            bl = range_box(start, mid);
+            br = range_box(mid, end);
+        } else {
+            float cost_l = FLT_MAX, cost_r = FLT_MAX;
+            bool use_om = true;
+            auto try_plane = [&](float plane) {
+                uint32_t cur = partition(start, end, ax, plane);
+                if (cur == start || cur == end - 1) {
+                    if (!use_om) return;
+                    sort_range(start, end, ax);
+                    cur = start + (end - start) / 2;
+                    use_om = false;
+                }
+                box cbl = range_box(start, cur), cbr = range_box(cur, end);
+                float cl = (area(cbl) / surf) * (float)(int)(cur - start);
+                float cr = (area(cbr) / surf) * (float)(int)(end - cur);
+                if (cl + cr < cost_l + cost_r) {
+                    bl = cbl;
+                    br = cbr;
+                    cost_l = cl;
+                    cost_r = cr;
+                    mid = cur;
+                }
+            };
+            int np = planes;
+            if ((int)(end - start) < np) np = (int)(end - start);
+            for (int i = 0; i < np; ++i) try_plane(b.lo[ax] + (float)(i + 1) * (e[ax] / (float)(np + 1)));
+            const float K_T = 1, K_I = 1;
+            if (max_tris > 1 && (K_I * (float)(int)(end - start)) < (K_T + K_I * (cost_l + cost_r)) &&
+                (int)(end - start) <= max_tris)
+                return make_leaf(start, end);  // unreachable: ranges this small returned above
+        }
+        if (mid == start || mid == end) {  // no split found; the reference would recurse forever
+            failed = true;
+            return make_leaf(start, end);
+        }
+        uint32_t id = (uint32_t)nodes.size();
+        nodes.emplace_back();
+        uint32_t l = subdivide(start, mid);
+        uint32_t r = subdivide(mid, end);
+        nodes[id].link_l = (int32_t)l;
+        nodes[id].link_r = (int32_t)r;
+        nodes[id].l = bl;
+        nodes[id].r = br;
+        return id;
+    }
+
+    uint32_t subdivide(uint32_t start, uint32_t end) {
+        if (failed) return make_leaf(start, end);
+        switch (split_type) {
+            case 0: return subdivide_om(start, end);
+            case 1: return subdivide_sm(start, end);
+            default: return subdivide_sah(start, end);
+        }
+    }
+
+    // bvh_ctor::build + commit_shuffled_triangles for the indexed layout (bvh-ctor.h:96-118, 239-248)
+    uint32_t build() {
+        prims.resize(sc.nt);
+        index.resize(sc.nt);
+        for (uint32_t i = 0; i < sc.nt; ++i) {
+            const uint32_t *t = sc.t4 + 4 * i;
+            box b;
+            b.grow(sc.vert(t[0]));
+            b.grow(sc.vert(t[1]));
+            b.grow(sc.vert(t[2]));
+            prims[i] = {b, i};
+            index[i] = i;
+        }
+        if (esc && sc.nt > 0) early_split_clipping();
+        uint32_t root = subdivide(0, (uint32_t)prims.size());
+        if (esc)
+            for (auto &x : index) x = prims[x].tri;
+        return root;
+    }
+};
+
+struct bvh {
+    scene sc;
+    std::vector<float> v4;
+    std::vector<uint32_t> t4;
+    uint32_t root = 0;
+    std::vector<node> nodes;
+    std::vector<uint32_t> index;
+    bool failed = false;
+};
+
+struct ray {
+    v3 o, d, id;
+    float tmin, tmax;
+};
+
+inline ray load_ray(const float *r) {
+    ray out;
+    out.o = {r[0], r[1], r[2]};
+    out.d = {r[4], r[5], r[6]};
+    out.id = {1.0f / r[4], 1.0f / r[5], 1.0f / r[6]};  // ray::ray (libgi/rt.h:28)
+    out.tmin = r[3];
+    out.tmax = r[7];
+    return out;
+}
+
+struct hit {
+    float t = FLT_MAX, beta = 0, gamma = 0;
+    uint32_t ref = 0;
+};
+
+// Cramer's rule ray/triangle test (libgi/intersect.h:19-74), same operation order.
+inline bool intersect_tri(const scene &sc, uint32_t tri, const ray &r, hit &info) {
+    const uint32_t *t = sc.t4 + 4 * tri;
+    v3 A = sc.vert(t[0]), B = sc.vert(t[1]), C = sc.vert(t[2]);
+    const float a = A.x - B.x, b = A.y - B.y, c = A.z - B.z;
+    const float d = A.x - C.x, e = A.y - C.y, f = A.z - C.z;
+    const float g = r.d.x, h = r.d.y, i = r.d.z;
+    const float j = A.x - r.o.x, k = A.y - r.o.y, l = A.z - r.o.z;
+    float common1 = e * i - h * f;
+    float common2 = g * f - d * i;
+    float common3 = d * h - e * g;
+    float M = a * common1 + b * common2 + c * common3;
+    float beta = j * common1 + k * common2 + l * common3;
+    common1 = a * k - j * b;
+    common2 = j * c - a * l;
+    common3 = b * l - k * c;
+    float gamma = i * common1 + h * common2 + g * common3;
+    float tt = -(f * common1 + e * common2 + d * common3);
+    beta /= M;
+    gamma /= M;
+    tt /= M;
+    if (tt > r.tmin && tt < r.tmax)
+        if (beta > 0 && gamma > 0 && beta + gamma <= 1) {
+            info.t = tt;
+            info.beta = beta;
+            info.gamma = gamma;
+            return true;
+        }
+    return false;
+}
+
+// Slab test intersect4 (libgi/intersect.h:230-267), same selects so NaN cases match too.
+inline bool intersect_box(const box &bx, const ray &r, float &is) {
+    float t1x_tmp = (bx.lo.x - r.o.x) * r.id.x;
+    float t2x_tmp = (bx.hi.x - r.o.x) * r.id.x;
+    float t1x = (t1x_tmp < t2x_tmp) ? t1x_tmp : t2x_tmp;
+    float t2x = (t2x_tmp < t1x_tmp) ? t1x_tmp : t2x_tmp;
+    float t1y_tmp = (bx.lo.y - r.o.y) * r.id.y;
+    float t2y_tmp = (bx.hi.y - r.o.y) * r.id.y;
+    float t1y = (t1y_tmp < t2y_tmp) ? t1y_tmp : t2y_tmp;
+    float t2y = (t2y_tmp < t1y_tmp) ? t1y_tmp : t2y_tmp;
+    float t1z_tmp = (bx.lo.z - r.o.z) * r.id.z;
+    float t2z_tmp = (bx.hi.z - r.o.z) * r.id.z;
+    float t1z = (t1z_tmp < t2z_tmp) ? t1z_tmp : t2z_tmp;
+    float t2z = (t2z_tmp < t1z_tmp) ? t1z_tmp : t2z_tmp;
+    float t1 = (t1x < t1y) ? t1y : t1x;
+    t1 = (t1z < t1) ? t1 : t1z;
+    float t2 = (t2x < t2y) ? t2x : t2y;
+    t2 = (t2z < t2) ? t2z : t2;
+    if (t1 > t2) return false;
+    if (t2 < r.tmin) return false;
+    if (t1 > r.tmax) return false;
+    is = t1;
+    return true;
+}
+
+struct counters {
+    uint32_t inner = 0, tris = 0, max_sp = 0;
+};
+
+// binary_bvh_tracer::closest_hit (rt/cpu/bvh2.cpp:71-137), non-alpha, indexed layout.
+inline hit closest_hit(const bvh &h, const ray &r, counters *cnt) {
+    hit closest, is;
+    uint32_t stack_local[64];
+    std::vector<uint32_t> stack_big;
+    uint32_t *stack = stack_local;
+    uint32_t cap = 64;
+    int32_t sp = 0;
+    stack[0] = h.root;
+    uint32_t max_sp = 0;
+    auto push = [&](uint32_t v) {
+        ++sp;
+        if ((uint32_t)sp >= cap) {
+            if (stack_big.empty()) stack_big.assign(stack_local, stack_local + cap);
+            stack_big.resize(cap * 2);
+            cap *= 2;
+            stack = stack_big.data();
+        }
+        stack[sp] = v;
+        if ((uint32_t)sp > max_sp) max_sp = sp;
+    };
+    uint32_t n_inner = 0, n_tri = 0;
+    while (sp >= 0) {
+        const node &n = h.nodes[stack[sp--]];
+        if (n.inner()) {
+            ++n_inner;
+            float dl, dr;
+            bool hl = intersect_box(n.l, r, dl) && dl < closest.t;
+            bool hr = intersect_box(n.r, r, dr) && dr < closest.t;
+            if (hl && hr) {
+                if (dl < dr) {
+                    push(n.link_r);
+                    push(n.link_l);
+                } else {
+                    push(n.link_l);
+                    push(n.link_r);
+                }
+            } else if (hl)
+                push(n.link_l);
+            else if (hr)
+                push(n.link_r);
+        } else {
+            int32_t off = -n.link_l, count = -n.link_r;
+            for (int32_t i = 0; i < count; ++i) {
+                uint32_t tri = h.index[off + i];
+                ++n_tri;
+                if (intersect_tri(h.sc, tri, r, is)) {
+                    if (is.t < closest.t) {
+                        closest = is;
+                        closest.ref = tri;
+                    }
+                }
+            }
+        }
+    }
+    if (cnt) *cnt = {n_inner, n_tri, max_sp};
+    return closest;
+}
+
+// binary_bvh_tracer::any_hit (rt/cpu/bvh2.cpp:139-189), non-alpha, indexed layout.
+inline bool any_hit(const bvh &h, const ray &r, counters *cnt) {
+    hit is;
+    std::vector<uint32_t> stack(64);
+    int32_t sp = 0;
+    stack[0] = h.root;
+    uint32_t max_sp = 0, n_inner = 0, n_tri = 0;
+    auto push = [&](uint32_t v) {
+        ++sp;
+        if ((size_t)sp >= stack.size()) stack.resize(stack.size() * 2);
+        stack[sp] = v;
+        if ((uint32_t)sp > max_sp) max_sp = sp;
+    };
+    bool result = false;
+    while (sp >= 0 && !result) {
+        const node &n = h.nodes[stack[sp--]];
+        if (n.inner()) {
+            ++n_inner;
+            float dl, dr;
+            bool hl = intersect_box(n.l, r, dl);
+            bool hr = intersect_box(n.r, r, dr);
+            if (hl && hr) {
+                if (dl < dr) {
+                    push(n.link_r);
+                    push(n.link_l);
+                } else {
+                    push(n.link_l);
+                    push(n.link_r);
+                }
+            } else if (hl)
+                push(n.link_l);
+            else if (hr)
+                push(n.link_r);
+        } else {
+            int32_t off = -n.link_l, count = -n.link_r;
+            for (int32_t i = 0; i < count; ++i) {
+                ++n_tri;
+                if (intersect_tri(h.sc, h.index[off + i], r, is)) {
+                    result = true;
+                    break;
+                }
+            }
+        }
+    }
+    if (cnt) *cnt = {n_inner, n_tri, max_sp};
+    return result;
+}
+
+inline void set_threads(int threads) {
+    if (threads > 0) omp_set_num_threads(threads);
+}
+
+}  // namespace orc
+
+using namespace orc;
+
+extern "C" {
+
+// Builds the reference BVH over a copy of the scene. split: 0 om, 1 sm, 2 sah.
+void *orc_build(const float *vpos4, uint32_t nv, const uint32_t *tris4, uint32_t nt, int esc, int split, int max_tris,
+                int planes) {
+    bvh *h = new bvh();
+    h->v4.assign(vpos4, vpos4 + 4 * (size_t)nv);
+    h->t4.assign(tris4, tris4 + 4 * (size_t)nt);
+    h->sc = {h->v4.data(), h->t4.data(), nv, nt};
+    builder b(h->sc, split, max_tris, planes, esc != 0);
+    h->root = b.build();
+    h->nodes.swap(b.nodes);
+    h->index.swap(b.index);
+    h->failed = b.failed;
+    return h;
+}
+
+int orc_failed(void *hp) { return ((bvh *)hp)->failed ? 1 : 0; }
+uint32_t orc_root(void *hp) { return ((bvh *)hp)->root; }
+uint32_t orc_num_nodes(void *hp) { return (uint32_t)((bvh *)hp)->nodes.size(); }
+uint32_t orc_num_index(void *hp) { return (uint32_t)((bvh *)hp)->index.size(); }
+
+// Same 14-word node layout as the reference harness: l.lo, l.hi, r.lo, r.hi, link_l, link_r.
+void orc_get_nodes(void *hp, uint32_t *out) {
+    const auto &nodes = ((bvh *)hp)->nodes;
+    for (size_t i = 0; i < nodes.size(); ++i) {
+        const node &n = nodes[i];
+        float f[12] = {n.l.lo.x, n.l.lo.y, n.l.lo.z, n.l.hi.x, n.l.hi.y, n.l.hi.z,
+                       n.r.lo.x, n.r.lo.y, n.r.lo.z, n.r.hi.x, n.r.hi.y, n.r.hi.z};
+        std::memcpy(out + 14 * i, f, sizeof(f));
+        std::memcpy(out + 14 * i + 12, &n.link_l, 4);
+        std::memcpy(out + 14 * i + 13, &n.link_r, 4);
+    }
+}
+
+void orc_get_index(void *hp, uint32_t *out) {
+    const auto &idx = ((bvh *)hp)->index;
+    std::memcpy(out, idx.data(), idx.size() * 4);
+}
+
+// Depth of the tree in edges from the root to the deepest leaf.
+uint32_t orc_depth(void *hp) {
+    bvh *h = (bvh *)hp;
+    std::vector<std::pair<uint32_t, uint32_t>> st = {{h->root, 0}};
+    uint32_t best = 0;
+    while (!st.empty()) {
+        auto [n, d] = st.back();
+        st.pop_back();
+        best = std::max(best, d);
+        if (h->nodes[n].inner()) {
+            st.push_back({(uint32_t)h->nodes[n].link_l, d + 1});
+            st.push_back({(uint32_t)h->nodes[n].link_r, d + 1});
+        }
+    }
+    return best;
+}
+
+// Closest hits for a batch (rt/cpu/wavefront.cpp:53-59): out4 = (t, beta, gamma, ref) per ray;
+// a miss is t = FLT_MAX, ref = 0 (beta, gamma written as 0). `counts` (optional) receives
+// (inner nodes visited, triangle tests, deepest stack index) per ray.
+void orc_closest(void *hp, const float *rays8, uint64_t n, float *out4, uint32_t *counts, int threads) {
+    bvh *h = (bvh *)hp;
+    set_threads(threads);
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+        counters c;
+        hit r = closest_hit(*h, load_ray(rays8 + 8 * i), counts ? &c : nullptr);
+        float *o = out4 + 4 * i;
+        o[0] = r.t;
+        o[1] = r.t != FLT_MAX ? r.beta : 0.f;
+        o[2] = r.t != FLT_MAX ? r.gamma : 0.f;
+        std::memcpy(o + 3, &r.ref, 4);
+        if (counts) {
+            counts[3 * i] = c.inner;
+            counts[3 * i + 1] = c.tris;
+            counts[3 * i + 2] = c.max_sp;
+        }
+    }
+}
+
+// Any-hit occlusion flags (rt/cpu/wavefront.cpp:60-70 reduced to the boolean).
+void orc_any(void *hp, const float *rays8, uint64_t n, uint8_t *occluded, uint32_t *counts, int threads) {
+    bvh *h = (bvh *)hp;
+    set_threads(threads);
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+        counters c;
+        occluded[i] = any_hit(*h, load_ray(rays8 + 8 * i), counts ? &c : nullptr) ? 1 : 0;
+        if (counts) {
+            counts[3 * i] = c.inner;
+            counts[3 * i + 1] = c.tris;
+            counts[3 * i + 2] = c.max_sp;
+        }
+    }
+}
+
+int orc_max_threads() { return omp_get_max_threads(); }
+
+void orc_free(void *hp) { delete (bvh *)hp; }
+
+}  // extern "C"

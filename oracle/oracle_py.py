@@ -1,0 +1,146 @@
+"""ctypes access to the oracle (oracle.cpp) and to the reference build (oracle/_ref).
+
+Test infrastructure only: the tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` import this module, as the checker. The product never does.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libref_bbvh.so")
+
+SPLIT = {"om": 0, "sm": 1, "sah": 2}
+_libs: dict[str, ctypes.CDLL] = {}
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _load(path: str, prefix: str) -> ctypes.CDLL:
+    if path in _libs:
+        return _libs[path]
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} missing: run oracle/build.py")
+    lib = ctypes.CDLL(path)
+    getattr(lib, prefix + "build").restype = ctypes.c_void_p
+    getattr(lib, prefix + "build").argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint32,
+                                               ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    for fn in ("root", "num_nodes", "num_index"):
+        getattr(lib, prefix + fn).restype = ctypes.c_uint32
+        getattr(lib, prefix + fn).argtypes = [ctypes.c_void_p]
+    for fn in ("get_nodes", "get_index", "free"):
+        getattr(lib, prefix + fn).argtypes = [ctypes.c_void_p] + ([ctypes.c_void_p] if fn != "free" else [])
+    _libs[path] = lib
+    return lib
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_SO)
+
+
+class _BVHBase:
+    prefix = ""
+
+    def __init__(self, lib, vpos, tris, esc=True, split="sah", max_tris=4, planes=16):
+        self.lib = lib
+        self._v = np.ascontiguousarray(vpos, np.float32)
+        self._t = np.ascontiguousarray(tris, np.uint32)
+        self.h = getattr(lib, self.prefix + "build")(_p(self._v), self._v.shape[0], _p(self._t), self._t.shape[0],
+                                                     int(esc), SPLIT[split], max_tris, planes)
+
+    def _fn(self, name):
+        return getattr(self.lib, self.prefix + name)
+
+    @property
+    def root(self) -> int:
+        return int(self._fn("root")(self.h))
+
+    def nodes(self) -> np.ndarray:
+        """uint32 [n, 14]: box_l.lo, box_l.hi, box_r.lo, box_r.hi (float bits), link_l, link_r."""
+        n = self._fn("num_nodes")(self.h)
+        out = np.zeros((n, 14), np.uint32)
+        self._fn("get_nodes")(self.h, _p(out))
+        return out
+
+    def index(self) -> np.ndarray:
+        n = self._fn("num_index")(self.h)
+        out = np.zeros(n, np.uint32)
+        self._fn("get_index")(self.h, _p(out))
+        return out
+
+    def __del__(self):
+        try:
+            self._fn("free")(ctypes.c_void_p(self.h))
+        except Exception:
+            pass
+
+
+class OracleBVH(_BVHBase):
+    """The oracle restatement: reference builder + bbvh traversal."""
+    prefix = "orc_"
+
+    def __init__(self, vpos, tris, **kw):
+        lib = _load(ORACLE_SO, "orc_")
+        lib.orc_depth.restype = ctypes.c_uint32
+        lib.orc_depth.argtypes = [ctypes.c_void_p]
+        lib.orc_closest.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p,
+                                    ctypes.c_void_p, ctypes.c_int]
+        lib.orc_any.argtypes = lib.orc_closest.argtypes
+        lib.orc_failed.argtypes = [ctypes.c_void_p]
+        super().__init__(lib, vpos, tris, **kw)
+        if lib.orc_failed(self.h):
+            raise RuntimeError("oracle BVH build found no split (non-finite input?)")
+
+    def depth(self) -> int:
+        return int(self.lib.orc_depth(self.h))
+
+    def closest(self, rays, threads=0, counts=False):
+        """Returns (hits float32[n,4] with ref in the last column as uint32 bits, counts|None)."""
+        rays = np.ascontiguousarray(rays, np.float32)
+        n = rays.shape[0]
+        out = np.zeros((n, 4), np.float32)
+        cnt = np.zeros((n, 3), np.uint32) if counts else None
+        self.lib.orc_closest(self.h, _p(rays), n, _p(out), _p(cnt) if counts else None, threads)
+        return out, cnt
+
+    def any(self, rays, threads=0, counts=False):
+        rays = np.ascontiguousarray(rays, np.float32)
+        n = rays.shape[0]
+        occ = np.zeros(n, np.uint8)
+        cnt = np.zeros((n, 3), np.uint32) if counts else None
+        self.lib.orc_any(self.h, _p(rays), n, _p(occ), _p(cnt) if counts else None, threads)
+        return occ, cnt
+
+
+class ReferenceBVH(_BVHBase):
+    """The reference's own binary_bvh_tracer, compiled from its sources into oracle/_ref."""
+    prefix = "ref_"
+
+    def __init__(self, vpos, tris, **kw):
+        lib = _load(REF_SO, "ref_")
+        lib.ref_closest.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_int]
+        lib.ref_any.argtypes = lib.ref_closest.argtypes
+        super().__init__(lib, vpos, tris, **kw)
+
+    def closest(self, rays, threads=0):
+        rays = np.ascontiguousarray(rays, np.float32)
+        out = np.zeros((rays.shape[0], 4), np.float32)
+        self.lib.ref_closest(self.h, _p(rays), rays.shape[0], _p(out), threads)
+        return out
+
+    def any(self, rays, threads=0):
+        rays = np.ascontiguousarray(rays, np.float32)
+        occ = np.zeros(rays.shape[0], np.uint8)
+        self.lib.ref_any(self.h, _p(rays), rays.shape[0], _p(occ), threads)
+        return occ
+
+
+def max_threads() -> int:
+    lib = _load(ORACLE_SO, "orc_")
+    return int(lib.orc_max_threads())
