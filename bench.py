@@ -1,0 +1,417 @@
+#!/usr/bin/env python3
+"""Benchmark: Mrays/s closest-hit (coherent + diffuse) on one GB300, tuned persistent vs plain.
+
+Workload (seeded synthetic scene, no external data): 256 UV spheres of 32x16 quads (262,144
+triangles), one step =
+  * 1024x1024 coherent primary rays, closest hit;
+  * 4,194,304 diffuse paths starting at the primary hits, cosine-weighted bounces, at most 5
+    bounce rays per path, Russian roulette (continue with p = 0.8) from bounce ray 3 on.
+`value` counts every closest-hit ray of the step (primary + bounce rays) per second with the
+inputs resident in HBM, using the tuned persistent kernels (persistent primary trace and the
+fused traverse+shade+regenerate loop replayed as a CUDA graph). The plain wavefront step (one
+thread per ray, one traversal kernel plus one shade kernel per bounce, also as a graph) is timed
+beside it. `e2e` runs the same step through the C-ABI from pinned host buffers with the host
+copies inside the timed region.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+Multi-GPU (torchrun): every rank runs an independent replica (the path does not shard across
+GPUs); value = all ranks' rays / the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mrays/s closest-hit (coherent+diffuse) on 1 GB300: tuned persistent vs plain wavefront"
+WORKLOAD = ("spheres-262144: 1024x1024 coherent primary closest-hit + 4,194,304 diffuse paths "
+            "(<=5 bounces, RR p=0.8 from bounce 3)")
+RES = 1024
+N_PATHS = 4 << 20
+LIGHT = (0.0, 15.0, 0.0)
+FLT_MAX = 3.4028234663852886e38
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.file.flush()
+        rows = []
+        with open(self.file.name) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.file.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_hbm_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def load_tuning(gpu_name: str) -> dict:
+    path = os.path.join(ROOT, "illum-rt_gb300", "tuning.json")
+    try:
+        with open(path) as f:
+            table = json.load(f)
+    except Exception:
+        return {}
+    for key in (f"{gpu_name}|spheres", "default|spheres"):
+        if key in table:
+            return table[key]
+    return {}
+
+
+def profile_traffic():
+    """DRAM bytes per launch of the fused kernel from the committed ncu summary, if any."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "k_pt_fused_spheres.json")) as f:
+            d = json.load(f)
+        return d
+    except Exception:
+        return None
+
+
+# ---- the GB300 arm --------------------------------------------------------------------------
+
+class Step:
+    """Device buffers and the two forms of one benchmark step on one GPU."""
+
+    def __init__(self, api, wl, device: int, tuning: dict):
+        import torch
+        self.torch = torch
+        self.api = api
+        sc, rays = wl.spheres_primary(res=RES)
+        self.n_primary = rays.shape[0]
+        self.rt = api.BatchRayTracer(device)
+        self.build_info = self.rt.build(sc.vpos, sc.tris, max_tris=tuning.get("max_tris", 4))
+        self.rt_plain = api.BatchRayTracer(device)  # the reference's CUDA defaults, untuned
+        self.rt_plain.build(sc.vpos, sc.tris)
+        self.rt_plain.select("while-while")
+        self.rt.select("persistent-while-while")
+        kw = {k: v for k, v in tuning.items() if k in ("block_threads", "blocks_per_sm", "refill_threshold",
+                                                         "refill_period", "stack_entries")}
+        if kw:
+            self.rt.set_tuning(**kw)
+        self.dev = torch.device("cuda", device)
+        self.h_rays = torch.from_numpy(rays).pin_memory()
+        self.rays = self.h_rays.to(self.dev)
+        self.hits = torch.zeros((self.n_primary, 4), device=self.dev)
+        self.results = torch.zeros((N_PATHS, 4), dtype=torch.int32, device=self.dev)
+        self.h_results = torch.zeros((N_PATHS, 4), dtype=torch.int32).pin_memory()
+        self.stream = torch.cuda.Stream(self.dev)
+        self.sp = self.stream.cuda_stream
+        self.p_fused = api.BatchRayTracer.pt_params(mode=api.PT_FUSED, use_graph=1)
+        self.p_plain = api.BatchRayTracer.pt_params(mode=api.PT_WAVEFRONT, use_graph=1)
+        self.flush_buf = torch.empty(512 << 20, dtype=torch.uint8, device=self.dev)  # > 129 MB of L2
+
+    def flush_l2(self):
+        with self.torch.cuda.stream(self.stream):
+            self.flush_buf.fill_(1)
+
+    def tuned(self, ev=None):
+        self.rt.trace(self.rays, self.hits, False, self.sp)
+        if ev is not None:
+            ev.record(self.stream)
+        self.rt.pathtrace(self.p_fused, self.rays, self.hits, N_PATHS, self.results, None, self.sp)
+
+    def plain(self):
+        self.rt_plain.trace(self.rays, self.hits, False, self.sp)
+        self.rt_plain.pathtrace(self.p_plain, self.rays, self.hits, N_PATHS, self.results, None, self.sp)
+
+    def e2e(self):
+        with self.torch.cuda.stream(self.stream):
+            self.rays.copy_(self.h_rays, non_blocking=True)
+            self.rt.trace(self.rays, self.hits, False, self.sp)
+            self.rt.pathtrace(self.p_fused, self.rays, self.hits, N_PATHS, self.results, None, self.sp)
+            self.h_results.copy_(self.results, non_blocking=True)
+
+    def rays_per_step(self) -> int:
+        self.plain()
+        self.rt_plain.check(self.sp)
+        bounces = int(self.results[:, 1].sum().item())
+        return self.n_primary + bounces
+
+    def algorithmic_bytes(self):
+        """(bytes per step of the pathtrace part, bytes of the primary part) from the counting
+        kernel: 32 B ray + 16 B hit + 64 B per inner node + 48 B per triangle test."""
+        torch = self.torch
+        cnt = torch.zeros(3, dtype=torch.int64, device=self.dev)
+        self.rt_plain.set_traversal_counters(cnt)
+        self.rt_plain.trace(self.rays, self.hits, False, self.sp)
+        self.rt_plain.check(self.sp)
+        prim = [int(x) for x in cnt.cpu()]
+        cnt.zero_()
+        p = self.api.BatchRayTracer.pt_params(mode=self.api.PT_WAVEFRONT)
+        self.rt_plain.pathtrace(p, self.rays, self.hits, N_PATHS, self.results, None, self.sp)
+        self.rt_plain.check(self.sp)
+        bounce = [int(x) for x in cnt.cpu()]
+        self.rt_plain.set_traversal_counters(None)
+        to_bytes = lambda c: 48 * c[0] + 64 * c[1] + 48 * c[2]
+        return to_bytes(bounce), to_bytes(prim), bounce, prim
+
+
+def time_steps(step: Step, fn, k: int, flush=True, split=False):
+    """Per-step device times (ms) with CUDA events on the step's stream, L2 flushed in between
+    (outside the events). With split=True also returns the pathtrace part of each step."""
+    torch = step.torch
+    totals, parts = [], []
+    for _ in range(k):
+        if flush:
+            step.flush_l2()
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(step.stream)
+        if split:
+            fn(e1)
+        else:
+            fn()
+        e2.record(step.stream)
+        e2.synchronize()
+        totals.append(e0.elapsed_time(e2))
+        if split:
+            parts.append(e1.elapsed_time(e2))
+    return totals, parts
+
+
+def cpu_baseline(rays_np, n_paths_sample: int, threads: int = 0):
+    """The oracle port of the reference CPU tracer (OpenMP over rays, all host threads) on a
+    bounded sample of the same workload: all primary rays plus n_paths_sample diffuse paths."""
+    import __graft_entry__ as ge
+    from illum_rt_gb300 import workloads as wl
+    orc = ge.load_oracle()
+    sc = wl.spheres()
+    o = orc.OracleBVH(sc.vpos, sc.tris)
+    o.closest(rays_np[:4096])  # warm-up
+    t0 = time.perf_counter()
+    hits, _ = o.closest(rays_np, threads=threads)
+    res, _ = o.pathtrace(rays_np, hits, n_paths_sample, threads=threads)
+    dt = time.perf_counter() - t0
+    n = rays_np.shape[0] + int(res[:, 1].sum())
+    return n / dt / 1e6, n, dt, orc.max_threads() if threads == 0 else threads
+
+
+def rays_in_results(step: Step) -> int:
+    return step.n_primary + int(step.results[:, 1].sum().item())
+
+
+def run_gb300(args):
+    import torch
+    import __graft_entry__ as ge
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    ge.load_package()
+    from illum_rt_gb300 import api, workloads as wl
+    gpu_name = torch.cuda.get_device_name(local)
+    tuning = load_tuning(gpu_name)
+    step = Step(api, wl, local, tuning)
+
+    # rays per step of each form (identical work: same paths, same bounces)
+    step.plain()
+    step.rt_plain.check(step.sp)
+    rays_plain = rays_in_results(step)
+    step.tuned()
+    step.rt.check(step.sp)
+    rays_tuned = rays_in_results(step)
+    pt_bytes, prim_bytes, bounce_cnt, prim_cnt = step.algorithmic_bytes()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    def max_over_ranks(x: float) -> float:
+        if world == 1:
+            return x
+        t = torch.tensor([x], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    # warm-up (graphs get captured here)
+    for _ in range(max(3, args.warmup)):
+        step.tuned()
+        step.plain()
+        step.e2e()
+    step.rt.check(step.sp)
+    step.rt_plain.check(step.sp)
+
+    clocks = ClockSampler(local)
+    barrier()
+    clocks.start()
+    tuned_ms, pt_ms = time_steps(step, step.tuned, args.steps, split=True)
+    barrier()
+    clk = clocks.stop()
+    plain_ms, _ = time_steps(step, step.plain, args.steps)
+    e2e_ms, _ = time_steps(step, step.e2e, args.steps)
+    barrier()
+    step.rt.check(step.sp)
+    step.rt_plain.check(step.sp)
+
+    t_tuned = max_over_ranks(sum(tuned_ms) / 1e3)
+    t_plain = max_over_ranks(sum(plain_ms) / 1e3)
+    t_e2e = max_over_ranks(sum(e2e_ms) / 1e3)
+    value = world * rays_tuned * args.steps / t_tuned / 1e6
+    plain_value = world * rays_plain * args.steps / t_plain / 1e6
+    e2e_value = world * rays_tuned * args.steps / t_e2e / 1e6
+
+    # roofline of the dominant kernel (the fused persistent loop): algorithmic bytes of all its
+    # bounce rays per launch / the pathtrace part of each timed step
+    peak, peak_kind = measured_hbm_peak()
+    pt_s = statistics.mean(pt_ms) / 1e3
+    achieved = pt_bytes / pt_s / 1e9
+    prof = profile_traffic()
+    traffic = prof.get("dram_bytes_per_launch") if prof else None
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": traffic,
+                "kernel": "k_pt_fused", "peak_source": peak_kind,
+                "bytes_per_launch": pt_bytes, "bounce_rays": bounce_cnt[0],
+                "inner_nodes_per_ray": round(bounce_cnt[1] / max(1, bounce_cnt[0]), 2),
+                "tri_tests_per_ray": round(bounce_cnt[2] / max(1, bounce_cnt[0]), 2),
+                "note": "B_ray = 32 + 16 + 64 n_node + 48 n_tri; the BVH (26 MB) stays L2-resident, "
+                        "so these bytes are mostly served from L2"}
+    line = {
+        "metric": METRIC, "value": round(value, 1), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(statistics.mean(tuned_ms), 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "triangles": 262144, "primary_rays": step.n_primary, "paths": N_PATHS,
+                   "rays_per_step": rays_tuned, "bvh": "SAH 16 planes, ESC, leaf<=%d" % tuning.get("max_tris", 4),
+                   "l2": "flushed between timed steps (512 MB write)", "parallelism": f"replicas x{world}",
+                   "tuning": tuning or "defaults"},
+        "plain_wavefront": {"value": round(plain_value, 1), "ms_per_step": round(statistics.mean(plain_ms), 4),
+                            "rays_per_step": rays_plain},
+        "speedup_vs_plain": round(value / plain_value, 3),
+        "e2e": {"value": round(e2e_value, 1), "unit": "Mrays/s", "ms_per_step": round(statistics.mean(e2e_ms), 4),
+                "h2d_bytes_per_step": int(step.n_primary * 32), "d2h_bytes_per_step": int(N_PATHS * 16)},
+        "gpu_launches": 5 * args.steps,
+        "roofline": roofline,
+        "clocks": clk,
+        "build_ms": round(step.build_info["build_ms"], 1),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        rays_np = step.h_rays.numpy()
+        v, n, dt, cores = cpu_baseline(rays_np, 1 << 20)
+        line["cpu_baseline"] = {"value": round(v, 2), "unit": "Mrays/s", "cores": cores, "kind": "port",
+                                "sample": f"1024x1024 primary rays + 1,048,576 diffuse paths ({n} rays, {dt:.2f} s)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+# ---- the reference arm: the reference's CPU tracer (oracle port) on the host cores ------------
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    import __graft_entry__ as ge
+    ge.load_package()
+    from illum_rt_gb300 import workloads as wl
+    orc = ge.load_oracle()
+    sc, rays = wl.spheres_primary(res=RES)
+    o = orc.OracleBVH(sc.vpos, sc.tris)
+    sample_rays = rays[: RES * RES // 4]  # every step: a quarter of the primary rays + 262,144 paths
+    hits_full, _ = o.closest(rays)
+    sample_paths = 1 << 18
+
+    def one():
+        t0 = time.perf_counter()
+        o.closest(sample_rays)
+        res, _ = o.pathtrace(rays, hits_full, sample_paths)
+        return sample_rays.shape[0] + int(res[:, 1].sum()), time.perf_counter() - t0
+
+    for _ in range(args.warmup):
+        one()
+    n_tot, t_tot, times = 0, 0.0, []
+    for _ in range(args.steps):
+        n, dt = one()
+        n_tot += n
+        t_tot += dt
+        times.append(dt)
+    value = n_tot / t_tot / 1e6
+    cores = orc.max_threads()
+    line = {"metric": METRIC, "value": round(value, 2), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(1e3 * t_tot / args.steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "impl": "reference",
+            "config": {"workload": WORKLOAD, "sample_per_step": "262,144 primary rays + 262,144 diffuse paths"},
+            "cpu_baseline": {"value": round(value, 2), "unit": "Mrays/s", "cores": cores, "kind": "port",
+                             "sample": "per step 262,144 primary rays + 262,144 diffuse paths, OpenMP over rays"},
+            "e2e": {"value": round(value, 2), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

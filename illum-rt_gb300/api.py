@@ -49,6 +49,14 @@ class Tuning(ctypes.Structure):
                 ("refill_period", ctypes.c_int), ("stack_entries", ctypes.c_int)]
 
 
+class PtParams(ctypes.Structure):
+    _fields_ = [("max_bounces", ctypes.c_uint32), ("rr_start", ctypes.c_uint32), ("rr_continue", ctypes.c_float),
+                ("eps", ctypes.c_float), ("seed", ctypes.c_uint64), ("mode", ctypes.c_int), ("use_graph", ctypes.c_int)]
+
+
+PT_WAVEFRONT, PT_FUSED = 0, 1
+
+
 class Config(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("reserved", ctypes.c_uint32)]
 
@@ -75,6 +83,12 @@ _PROTOS = {
     "grt_trace": (I, [VP, VP, VP, U32, I, VP]),
     "grt_trace_host": (I, [VP, VP, VP, U32, I]),
     "grt_check": (I, [VP, VP, U32]),
+    "grt_set_traversal_counters": (I, [VP, VP]),
+    "grt_compact_hits": (I, [VP, VP, U32, VP, VP, VP]),
+    "grt_shadow_rays": (I, [VP, VP, VP, U32, P(ctypes.c_float), ctypes.c_float, VP, VP, VP]),
+    "grt_set_materials": (I, [VP, VP, U32]),
+    "grt_pt_params_default": (None, [P(PtParams)]),
+    "grt_pathtrace": (I, [VP, P(PtParams), VP, VP, U32, U32, VP, VP, VP]),
 }
 
 
@@ -231,6 +245,10 @@ class BatchRayTracer:
         n = int(rays.shape[0]) if n is None else int(n)
         self._check(lib().grt_trace(self.ctx, _ptr(rays), _ptr(hits), n, int(any_hit), VP(stream or 0)))
 
+    def set_traversal_counters(self, counters=None):
+        """counters: a CUDA int64 tensor of 3 (rays, inner nodes, triangle tests) or None."""
+        self._check(lib().grt_set_traversal_counters(self.ctx, _ptr(counters) if counters is not None else None))
+
     def check(self, stream=None, timeout_ms: int = 0):
         self._check(lib().grt_check(self.ctx, VP(stream or 0), timeout_ms))
 
@@ -264,3 +282,30 @@ class BatchRayTracer:
         t = Tuning()
         self._check(lib().grt_get_tuning(self.ctx, ctypes.byref(t)))
         return {k: getattr(t, k) for k, _ in t._fields_}
+
+    # -- ray generation and path tracing -------------------------------------------------
+    def compact_hits(self, hits, indices, count, stream=None):
+        self._check(lib().grt_compact_hits(self.ctx, _ptr(hits), int(hits.shape[0]), _ptr(indices), _ptr(count),
+                                           VP(stream or 0)))
+
+    def shadow_rays(self, rays, hits, light, eps, out_rays, count, stream=None):
+        lt = (ctypes.c_float * 3)(*[float(x) for x in light])
+        self._check(lib().grt_shadow_rays(self.ctx, _ptr(rays), _ptr(hits), int(rays.shape[0]), lt,
+                                          ctypes.c_float(eps), _ptr(out_rays), _ptr(count), VP(stream or 0)))
+
+    def set_materials(self, albedo):
+        a = np.ascontiguousarray(albedo, np.float32)
+        self._check(lib().grt_set_materials(self.ctx, _ptr(a) if a.size else None, int(a.size)))
+
+    @staticmethod
+    def pt_params(**kw) -> PtParams:
+        p = PtParams()
+        lib().grt_pt_params_default(ctypes.byref(p))
+        for k, v in kw.items():
+            setattr(p, k, v)
+        return p
+
+    def pathtrace(self, params: PtParams, prim_rays, prim_hits, n_paths, results, bounce_hits=None, stream=None):
+        self._check(lib().grt_pathtrace(self.ctx, ctypes.byref(params), _ptr(prim_rays), _ptr(prim_hits),
+                                        int(prim_rays.shape[0]), int(n_paths), _ptr(results),
+                                        _ptr(bounce_hits) if bounce_hits is not None else None, VP(stream or 0)))

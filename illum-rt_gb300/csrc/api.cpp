@@ -13,132 +13,10 @@
 #include <thread>
 #include <vector>
 
-#include "../../include/grt.h"
-#include "bvh_builder.hpp"
-#include "grt_internal.hpp"
+#include "ctx.hpp"
+#include "pathtrace.hpp"
 
-struct grt_ctx {
-    int device = 0;
-    int num_sms = 0;
-    std::string err;
-    bool built = false;
-    grt::ref_tree tree;
-    grt::dev_scene sc{};
-    void *d_nodes = nullptr, *d_recs = nullptr, *d_vpos = nullptr, *d_tris = nullptr;
-    uint32_t nv = 0, nt = 0, depth = 0;
-    grt_bvh_stats stats{};
-    int tracer = 0;  // 0 while-while, 1 persistent-while-while
-    grt_tuning tuning{};
-    unsigned *d_err = nullptr;      // error bits ORed in by kernels
-    unsigned *d_counter = nullptr;  // ray counter of the persistent kernel
-    void *d_stage = nullptr;        // grt_trace_host staging: rays then hits
-    size_t stage_bytes = 0;
-    cudaStream_t stream = nullptr;  // grt_trace_host stream
-};
-
-namespace {
-
-struct device_guard {
-    int prev = -1;
-    explicit device_guard(int dev) {
-        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
-        if (prev != dev) cudaSetDevice(dev);
-    }
-    ~device_guard() {
-        if (prev >= 0) cudaSetDevice(prev);
-    }
-};
-
-grt_status fail(grt_ctx *c, grt_status s, const std::string &msg) {
-    if (c) c->err = msg;
-    return s;
-}
-
-grt_status cuda_fail(grt_ctx *c, cudaError_t e, const char *what) {
-    cudaGetLastError();  // clear a non-sticky error so the context stays usable
-    return fail(c, e == cudaErrorMemoryAllocation ? GRT_ERR_OOM : GRT_ERR_CUDA,
-                std::string(what) + ": " + cudaGetErrorString(e));
-}
-
-void free_scene(grt_ctx *c) {
-    for (void **p : {&c->d_nodes, &c->d_recs, &c->d_vpos, &c->d_tris}) {
-        if (*p) cudaFree(*p);
-        *p = nullptr;
-    }
-    c->built = false;
-}
-
-double ms_since(std::chrono::steady_clock::time_point t0) {
-    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-}
-
-const char *kTracerNames[] = {"while-while", "persistent-while-while"};
-
-grt::launch_params params_for(grt_ctx *c, bool any_hit) {
-    grt::launch_params lp{};
-    const grt_tuning &t = c->tuning;
-    lp.stack_entries = t.stack_entries > 0 ? t.stack_entries : (int)c->depth;
-    if (lp.stack_entries < (int)c->depth) lp.stack_entries = (int)c->depth;
-    lp.block_threads = t.block_threads > 0 ? t.block_threads : 128;
-    lp.refill_threshold = t.refill_threshold > 0 ? t.refill_threshold : 20;
-    lp.refill_period = t.refill_period > 0 ? t.refill_period : 4;
-    if (c->tracer == 1) {
-        int per_sm = t.blocks_per_sm > 0 ? t.blocks_per_sm
-                                         : grt::persistent_blocks_per_sm(lp.block_threads, lp.stack_entries, any_hit);
-        lp.grid_blocks = per_sm * c->num_sms;
-    }
-    return lp;
-}
-
-bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
-
-grt::build_opts to_build_opts(const grt_bvh_opts *opts) {
-    grt_bvh_opts o;
-    grt_bvh_opts_default(&o);
-    if (opts) o = *opts;
-    grt::build_opts bo;
-    bo.split = o.split;
-    bo.max_tris = o.max_tris_per_node;
-    bo.planes = o.number_of_planes;
-    bo.esc = o.esc != 0;
-    return bo;
-}
-
-void export_tree(const grt::ref_tree &tree, uint32_t *nodes14, uint32_t *index, uint32_t *root) {
-    if (nodes14) {
-        for (size_t i = 0; i < tree.nodes.size(); ++i) {
-            const grt::ref_node &n = tree.nodes[i];
-            uint32_t *o = nodes14 + 14 * i;
-            std::memcpy(o + 0, n.lmin, 12);
-            std::memcpy(o + 3, n.lmax, 12);
-            std::memcpy(o + 6, n.rmin, 12);
-            std::memcpy(o + 9, n.rmax, 12);
-            std::memcpy(o + 12, &n.link_l, 4);
-            std::memcpy(o + 13, &n.link_r, 4);
-        }
-    }
-    if (index) std::memcpy(index, tree.index.data(), tree.index.size() * 4);
-    if (root) *root = tree.root;
-}
-
-uint32_t tree_depth(const grt::ref_tree &tree) {
-    // an empty scene is one leaf of count 0, whose link_r = 0 reads as an inner node
-    if (tree.index.empty()) return 0;
-    uint32_t best = 0;
-    std::vector<std::pair<uint32_t, uint32_t>> st = {{tree.root, 0}};
-    while (!st.empty()) {
-        auto [n, d] = st.back();
-        st.pop_back();
-        if (d > best) best = d;
-        if (tree.nodes[n].inner()) {
-            st.push_back({(uint32_t)tree.nodes[n].link_l, d + 1});
-            st.push_back({(uint32_t)tree.nodes[n].link_r, d + 1});
-        }
-    }
-    return best;
-}
-
-}  // namespace
+using namespace grt;
 
 extern "C" {
 
@@ -171,6 +49,8 @@ grt_status grt_create(const grt_config *cfg, grt_ctx **out) {
         e = cudaMemset(c->d_err, 0, 2 * sizeof(unsigned));
     }
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = grt::prepare_trace_kernels();
+    if (e == cudaSuccess) e = grt::prepare_pt_kernels();
     if (e != cudaSuccess) {
         cudaGetLastError();
         if (c->d_err) cudaFree(c->d_err);
@@ -187,6 +67,9 @@ grt_status grt_destroy(grt_ctx *c) {
         device_guard g(c->device);
         free_scene(c);
         if (c->d_stage) cudaFree(c->d_stage);
+        if (c->d_scratch) cudaFree(c->d_scratch);
+        if (c->d_albedo) cudaFree(c->d_albedo);
+        if (c->pt_graph.exec) cudaGraphExecDestroy(c->pt_graph.exec);
         if (c->d_err) cudaFree(c->d_err);
         if (c->stream) cudaStreamDestroy(c->stream);
     }
@@ -203,6 +86,7 @@ grt_status grt_build(grt_ctx *c, const float *vpos4, uint32_t nv, const uint32_t
     const grt::build_opts bo = to_build_opts(opts);
     device_guard g(c->device);
     free_scene(c);
+    ++c->scene_generation;
     c->stats = grt_bvh_stats{};
 
     auto t0 = std::chrono::steady_clock::now();
@@ -358,6 +242,13 @@ grt_status grt_trace(grt_ctx *c, const float *rays_dev, grt_hit *hits_dev, uint3
         e = grt::launch_trace_plain(c->sc, (const float4 *)rays_dev, hits_dev, n, any_hit != 0, lp, c->d_err,
                                     (cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "launching the traversal kernel");
+    return GRT_OK;
+}
+
+grt_status grt_set_traversal_counters(grt_ctx *c, unsigned long long *counters_dev) {
+    if (!c) return GRT_ERR_INVALID_ARG;
+    if (((uintptr_t)counters_dev & 7u) != 0) return fail(c, GRT_ERR_INVALID_ARG, "counters must be 8-byte aligned");
+    c->d_trav_counters = counters_dev;
     return GRT_OK;
 }
 

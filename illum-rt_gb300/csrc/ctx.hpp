@@ -1,0 +1,149 @@
+// The context behind the C-ABI (struct grt_ctx) and helpers shared by the api*.cpp files.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/grt.h"
+#include "bvh_builder.hpp"
+#include "grt_internal.hpp"
+
+struct grt_ctx {
+    int device = 0;
+    int num_sms = 0;
+    std::string err;
+    bool built = false;
+    grt::ref_tree tree;
+    grt::dev_scene sc{};
+    void *d_nodes = nullptr, *d_recs = nullptr, *d_vpos = nullptr, *d_tris = nullptr;
+    uint32_t nv = 0, nt = 0, depth = 0;
+    grt_bvh_stats stats{};
+    int tracer = 0;  // 0 while-while, 1 persistent-while-while
+    grt_tuning tuning{};
+    unsigned *d_err = nullptr;      // error bits ORed in by kernels
+    unsigned *d_counter = nullptr;  // ray counter of the persistent kernel
+    void *d_stage = nullptr;        // grt_trace_host staging: rays then hits
+    size_t stage_bytes = 0;
+    cudaStream_t stream = nullptr;  // grt_trace_host stream
+    unsigned long long *d_trav_counters = nullptr;  // grt_set_traversal_counters (caller's memory)
+    uint64_t scene_generation = 0;  // bumped by every build (invalidates captured graphs)
+    // shading data of the path tracer
+    float *d_albedo = nullptr;
+    uint32_t n_albedo = 0;
+    // scratch arena of the path tracer and the ray-generation steps
+    void *d_scratch = nullptr;
+    size_t scratch_bytes = 0;
+    // captured path-tracing step, replayed while its key matches
+    struct graph_cache {
+        cudaGraphExec_t exec = nullptr;
+        std::vector<uint64_t> key;
+    } pt_graph;
+};
+
+namespace grt {
+
+struct device_guard {
+    int prev = -1;
+    explicit device_guard(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~device_guard() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+inline grt_status fail(grt_ctx *c, grt_status s, const std::string &msg) {
+    if (c) c->err = msg;
+    return s;
+}
+
+inline grt_status cuda_fail(grt_ctx *c, cudaError_t e, const char *what) {
+    cudaGetLastError();  // clear a non-sticky error so the context stays usable
+    return fail(c, e == cudaErrorMemoryAllocation ? GRT_ERR_OOM : GRT_ERR_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+inline void free_scene(grt_ctx *c) {
+    for (void **p : {&c->d_nodes, &c->d_recs, &c->d_vpos, &c->d_tris}) {
+        if (*p) cudaFree(*p);
+        *p = nullptr;
+    }
+    c->built = false;
+}
+
+inline double ms_since(std::chrono::steady_clock::time_point t0) {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+inline const char *kTracerNames[] = {"while-while", "persistent-while-while"};
+
+inline launch_params params_for(grt_ctx *c, bool any_hit) {
+    grt::launch_params lp{};
+    const grt_tuning &t = c->tuning;
+    lp.stack_entries = t.stack_entries > 0 ? t.stack_entries : (int)c->depth;
+    if (lp.stack_entries < (int)c->depth) lp.stack_entries = (int)c->depth;
+    lp.block_threads = t.block_threads > 0 ? t.block_threads : 128;
+    lp.refill_threshold = t.refill_threshold > 0 ? t.refill_threshold : 20;
+    lp.refill_period = t.refill_period > 0 ? t.refill_period : 4;
+    lp.counters = c->d_trav_counters;
+    if (c->tracer == 1) {
+        int per_sm = t.blocks_per_sm > 0 ? t.blocks_per_sm
+                                         : grt::persistent_blocks_per_sm(lp.block_threads, lp.stack_entries, any_hit);
+        lp.grid_blocks = per_sm * c->num_sms;
+    }
+    return lp;
+}
+
+inline bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
+
+inline build_opts to_build_opts(const grt_bvh_opts *opts) {
+    grt_bvh_opts o;
+    grt_bvh_opts_default(&o);
+    if (opts) o = *opts;
+    grt::build_opts bo;
+    bo.split = o.split;
+    bo.max_tris = o.max_tris_per_node;
+    bo.planes = o.number_of_planes;
+    bo.esc = o.esc != 0;
+    return bo;
+}
+
+inline void export_tree(const grt::ref_tree &tree, uint32_t *nodes14, uint32_t *index, uint32_t *root) {
+    if (nodes14) {
+        for (size_t i = 0; i < tree.nodes.size(); ++i) {
+            const grt::ref_node &n = tree.nodes[i];
+            uint32_t *o = nodes14 + 14 * i;
+            std::memcpy(o + 0, n.lmin, 12);
+            std::memcpy(o + 3, n.lmax, 12);
+            std::memcpy(o + 6, n.rmin, 12);
+            std::memcpy(o + 9, n.rmax, 12);
+            std::memcpy(o + 12, &n.link_l, 4);
+            std::memcpy(o + 13, &n.link_r, 4);
+        }
+    }
+    if (index) std::memcpy(index, tree.index.data(), tree.index.size() * 4);
+    if (root) *root = tree.root;
+}
+
+inline uint32_t tree_depth(const grt::ref_tree &tree) {
+    // an empty scene is one leaf of count 0, whose link_r = 0 reads as an inner node
+    if (tree.index.empty()) return 0;
+    uint32_t best = 0;
+    std::vector<std::pair<uint32_t, uint32_t>> st = {{tree.root, 0}};
+    while (!st.empty()) {
+        auto [n, d] = st.back();
+        st.pop_back();
+        if (d > best) best = d;
+        if (tree.nodes[n].inner()) {
+            st.push_back({(uint32_t)tree.nodes[n].link_l, d + 1});
+            st.push_back({(uint32_t)tree.nodes[n].link_r, d + 1});
+        }
+    }
+    return best;
+}
+
+}  // namespace grt

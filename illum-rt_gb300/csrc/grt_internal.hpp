@@ -36,13 +36,21 @@ struct launch_params {
     int refill_threshold;
     int refill_period;
     int stack_entries;
+    unsigned long long *counters;  // one-thread-per-ray kernel: rays, inner nodes, triangle tests (or null)
 };
 
+// `n_dev` (optional): the ray count is read on the device from *n_dev (at most n); the grid
+// still covers n rays.
 cudaError_t launch_trace_plain(const dev_scene &sc, const float4 *rays, grt_hit *hits, uint32_t n, bool any_hit,
-                               const launch_params &lp, unsigned *err, cudaStream_t stream);
+                               const launch_params &lp, unsigned *err, cudaStream_t stream,
+                               const uint32_t *n_dev = nullptr);
 
 cudaError_t launch_trace_persistent(const dev_scene &sc, const float4 *rays, grt_hit *hits, uint32_t n, bool any_hit,
                                     const launch_params &lp, unsigned *err, unsigned *counter, cudaStream_t stream);
+
+// Raises the dynamic shared-memory limit of every traversal kernel variant (once per device,
+// before any launch, so that launches need no attribute calls and can be captured).
+cudaError_t prepare_trace_kernels();
 
 // Occupancy of the persistent kernel for a block size and stack variant (blocks per SM).
 int persistent_blocks_per_sm(int block_threads, int stack_entries, bool any_hit);

@@ -1,0 +1,503 @@
+// Diffuse multi-bounce path tracing and shadow-ray setup on top of the traversal kernels.
+//
+// The reference wires a diffuse bounce as wavefront steps: find closest hits, then a
+// sampling kernel that turns every hit into the next ray (k::sample_cos_dir,
+// rt/cuda/bounce.cu:91-142), then find closest hits again. Two forms are implemented:
+//   * GRT_PT_WAVEFRONT — that structure, one thread per ray: per bounce a traversal kernel over
+//     the queue of live paths and a shade kernel that shades, applies Russian roulette,
+//     samples the next direction and appends the survivors to the next queue;
+//   * GRT_PT_FUSED — one persistent kernel in which a warp's lanes take paths from a global
+//     counter, and each lane traverses, shades and regenerates its path's rays in registers
+//     until the path ends, then takes the next path; lanes are refilled whenever too few of
+//     a warp's lanes are still busy.
+// Both produce the same per-path results: the math is shared (pt_math.cuh) and each path's
+// random stream depends only on its index.
+#include "pathtrace.hpp"
+#include "pt_math.cuh"
+#include "traverse.cuh"
+
+namespace grt {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kTile = 2048;  // elements per block in the stable compaction
+
+// ---- stable compaction of valid hits (pixel order is kept) ---------------------------------
+
+__device__ __forceinline__ bool hit_valid(const grt_hit *hits, uint32_t i) { return hits[i].t != FLT_MAX; }
+
+__global__ void k_count_valid(const grt_hit *__restrict__ hits, uint32_t n, uint32_t *block_counts) {
+    __shared__ uint32_t warp_sums[32];
+    const uint32_t base = blockIdx.x * kTile;
+    uint32_t c = 0;
+    for (uint32_t k = threadIdx.x; k < kTile; k += blockDim.x) {
+        const uint32_t i = base + k;
+        c += (i < n && hit_valid(hits, i)) ? 1u : 0u;
+    }
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(kFull, c, o);
+    if ((threadIdx.x & 31) == 0) warp_sums[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t s = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += warp_sums[w];
+        block_counts[blockIdx.x] = s;
+    }
+}
+
+// Exclusive scan of the block counts by one block; writes the total to *total.
+__global__ void k_scan_counts(uint32_t *counts, uint32_t nblocks, uint32_t *total) {
+    __shared__ uint32_t warp_sums[32];
+    __shared__ uint32_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (uint32_t base = 0; base < nblocks; base += blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        const uint32_t v = i < nblocks ? counts[i] : 0u;
+        uint32_t x = v;  // inclusive warp scan
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(kFull, x, o);
+            if ((threadIdx.x & 31) >= (unsigned)o) x += y;
+        }
+        if ((threadIdx.x & 31) == 31) warp_sums[threadIdx.x >> 5] = x;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            const uint32_t nw = blockDim.x >> 5;
+            uint32_t w = threadIdx.x < nw ? warp_sums[threadIdx.x] : 0u;
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(kFull, w, o);
+                if (threadIdx.x >= (unsigned)o) w += y;
+            }
+            if (threadIdx.x < nw) warp_sums[threadIdx.x] = w;  // inclusive warp prefix
+        }
+        __syncthreads();
+        const uint32_t wid = threadIdx.x >> 5;
+        const uint32_t excl = carry + (wid ? warp_sums[wid - 1] : 0u) + x - v;
+        if (i < nblocks) counts[i] = excl;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry = excl + v;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
+// Scatter pass: element i with a valid hit goes to out position offset(i). `emit(i, pos)`.
+template <typename Emit>
+__device__ void scatter_valid(const grt_hit *__restrict__ hits, uint32_t n, const uint32_t *block_offsets, Emit emit) {
+    __shared__ uint32_t warp_sums[32];
+    __shared__ uint32_t carry;
+    const uint32_t base = blockIdx.x * kTile;
+    if (threadIdx.x == 0) carry = block_offsets[blockIdx.x];
+    __syncthreads();
+    const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (uint32_t r = 0; r < kTile; r += blockDim.x) {
+        const uint32_t i = base + r + threadIdx.x;
+        const bool f = i < n && hit_valid(hits, i);
+        const unsigned b = __ballot_sync(kFull, f);
+        if (lane == 0) warp_sums[wid] = __popc(b);
+        __syncthreads();
+        uint32_t before = carry;
+        for (unsigned w = 0; w < wid; ++w) before += warp_sums[w];
+        if (f) emit(i, before + __popc(b & ((1u << lane) - 1u)));
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t s = 0;
+            for (unsigned w = 0; w < nw; ++w) s += warp_sums[w];
+            carry += s;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_scatter_indices(const grt_hit *__restrict__ hits, uint32_t n, const uint32_t *block_offsets,
+                                  uint32_t *out) {
+    scatter_valid(hits, n, block_offsets, [&](uint32_t i, uint32_t pos) { out[pos] = i; });
+}
+
+__device__ __forceinline__ pm::f3 vtx(const float4 *__restrict__ v, uint32_t i) {
+    const float4 p = __ldg(v + i);
+    return {p.x, p.y, p.z};
+}
+
+// Facing geometric normal of triangle `ref` for a ray travelling along d.
+__device__ __forceinline__ pm::f3 tri_normal(const pt_scene &ps, uint32_t ref, pm::f3 d, uint32_t &material) {
+    const uint4 t = __ldg(ps.tris + ref);
+    material = t.w;
+    return pm::facing_normal(vtx(ps.vpos, t.x), vtx(ps.vpos, t.y), vtx(ps.vpos, t.z), d);
+}
+
+__global__ void k_scatter_shadow(const grt_hit *__restrict__ hits, uint32_t n, const uint32_t *block_offsets,
+                                 const float4 *__restrict__ rays, pt_scene ps, float lx, float ly, float lz, float eps,
+                                 float4 *out) {
+    scatter_valid(hits, n, block_offsets, [&](uint32_t i, uint32_t pos) {
+        const float4 a = rays[2 * (size_t)i], b = rays[2 * (size_t)i + 1];
+        const pm::f3 o = {a.x, a.y, a.z}, d = {b.x, b.y, b.z};
+        uint32_t m;
+        const pm::f3 nrm = tri_normal(ps, hits[i].ref, d, m);
+        const pm::f3 p = pm::offset_hit_point(o, d, hits[i].t, nrm, eps);
+        const pm::f3 to = pm::sub3({lx, ly, lz}, p);
+        const float dist = pm::sqrt_rn(pm::dot3(to, to));
+        const pm::f3 dir = {pm::div(to.x, dist), pm::div(to.y, dist), pm::div(to.z, dist)};
+        out[2 * (size_t)pos] = make_float4(p.x, p.y, p.z, eps);
+        out[2 * (size_t)pos + 1] = make_float4(dir.x, dir.y, dir.z, pm::sub(dist, eps));
+    });
+}
+
+// ---- path state and the per-bounce logic shared by both forms -------------------------------
+
+struct path_t {
+    pm::pcg32 rng;
+    float thr;        // throughput
+    uint32_t digest;  // running digest of the path's hits
+    uint32_t bounce;  // index of the bounce ray currently traced (1-based)
+    uint32_t last_ref;
+};
+
+__device__ __forceinline__ float albedo_of(const pt_scene &ps, uint32_t material) {
+    return material < ps.n_albedo ? __ldg(ps.albedo + material) : 0.8f;
+}
+
+// First bounce ray of path p: from primary hit H[p mod |H|].
+__device__ __forceinline__ void path_start(const pt_scene &ps, const pt_params_dev &pp, uint32_t p,
+                                           const float4 *__restrict__ prim_rays, const grt_hit *__restrict__ prim_hits,
+                                           const uint32_t *__restrict__ hit_list, uint32_t n_list, path_t &st,
+                                           float4 &ro, float4 &rd) {
+    const uint32_t i = __ldg(hit_list + (p % n_list));
+    const float4 a = __ldg(prim_rays + 2 * (size_t)i), b = __ldg(prim_rays + 2 * (size_t)i + 1);
+    const float4 h = __ldg(reinterpret_cast<const float4 *>(prim_hits) + i);
+    const pm::f3 o = {a.x, a.y, a.z}, d = {b.x, b.y, b.z};
+    st.rng.set_sequence((uint64_t)pp.seed + p);
+    st.thr = 1.0f;
+    st.digest = pm::kDigestSeed;
+    st.bounce = 1;
+    st.last_ref = pm::kMissWord;
+    uint32_t m;
+    const pm::f3 n = tri_normal(ps, __float_as_uint(h.w), d, m);
+    const pm::f3 org = pm::offset_hit_point(o, d, h.x, n, pp.eps);
+    const float u0 = st.rng.uniform(), u1 = st.rng.uniform();
+    const pm::f3 dir = pm::align(pm::cosine_sample_hemisphere(u0, u1), n);
+    ro = make_float4(org.x, org.y, org.z, pp.eps);
+    rd = make_float4(dir.x, dir.y, dir.z, FLT_MAX);
+}
+
+// Consumes the closest hit of the current bounce ray (ro, rd). Returns true if the path goes
+// on, with (ro, rd) replaced by the next ray; otherwise fills `res`.
+__device__ __forceinline__ bool path_bounce(const pt_scene &ps, const pt_params_dev &pp, path_t &st, const hit_t &h,
+                                            float4 &ro, float4 &rd, grt_path_result &res) {
+    const pm::f3 o = {ro.x, ro.y, ro.z}, d = {rd.x, rd.y, rd.z};
+    if (h.t == FLT_MAX) {  // escaped: collects the sky
+        st.digest = pm::digest_word(st.digest, pm::kMissWord);
+        res = {pm::mul(st.thr, pm::sky(d)), st.bounce, st.last_ref, st.digest};
+        return false;
+    }
+    st.digest = pm::digest_word(pm::digest_word(st.digest, h.ref), __float_as_uint(h.t));
+    st.last_ref = h.ref;
+    uint32_t m;
+    const pm::f3 n = tri_normal(ps, h.ref, d, m);
+    st.thr = pm::mul(st.thr, albedo_of(ps, m));
+    if (st.bounce >= pp.max_bounces) {
+        res = {0.f, st.bounce, st.last_ref, st.digest};
+        return false;
+    }
+    if (st.bounce + 1 >= pp.rr_start) {  // Russian roulette before the next bounce
+        if (!(st.rng.uniform() < pp.rr_continue)) {
+            res = {0.f, st.bounce, st.last_ref, st.digest};
+            return false;
+        }
+        st.thr = pm::div(st.thr, pp.rr_continue);
+    }
+    const pm::f3 org = pm::offset_hit_point(o, d, h.t, n, pp.eps);
+    const float u0 = st.rng.uniform(), u1 = st.rng.uniform();
+    const pm::f3 dir = pm::align(pm::cosine_sample_hemisphere(u0, u1), n);
+    ro = make_float4(org.x, org.y, org.z, pp.eps);
+    rd = make_float4(dir.x, dir.y, dir.z, FLT_MAX);
+    ++st.bounce;
+    return true;
+}
+
+__device__ __forceinline__ void record_bounce(grt_hit *bounce_hits, const pt_params_dev &pp, uint32_t p,
+                                              uint32_t bounce, const hit_t &h) {
+    if (bounce_hits)
+        reinterpret_cast<float4 *>(bounce_hits)[(size_t)p * pp.max_bounces + (bounce - 1)] =
+            make_float4(h.t, h.b, h.g, __uint_as_float(h.ref));
+}
+
+__device__ __forceinline__ void clear_unused(grt_hit *bounce_hits, const pt_params_dev &pp, uint32_t p,
+                                             uint32_t traced) {
+    if (bounce_hits)
+        for (uint32_t k = traced; k < pp.max_bounces; ++k)
+            reinterpret_cast<float4 *>(bounce_hits)[(size_t)p * pp.max_bounces + k] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+__device__ __forceinline__ ray_t to_ray(const float4 &a, const float4 &d) {
+    ray_t r;
+    r.ox = a.x;
+    r.oy = a.y;
+    r.oz = a.z;
+    r.tmin = a.w;
+    r.dx = d.x;
+    r.dy = d.y;
+    r.dz = d.z;
+    r.tmax = d.w;
+    r.ix = __fdiv_rn(1.0f, d.x);
+    r.iy = __fdiv_rn(1.0f, d.y);
+    r.iz = __fdiv_rn(1.0f, d.z);
+    return r;
+}
+
+// ---- wavefront form -----------------------------------------------------------------------
+
+struct wf_state {
+    uint64_t rng_state, rng_inc;
+    float thr;
+    uint32_t digest, bounce, last_ref;
+};
+
+__global__ void k_wf_init(pt_scene ps, pt_params_dev pp, const float4 *__restrict__ prim_rays,
+                          const grt_hit *__restrict__ prim_hits, const uint32_t *__restrict__ hit_list,
+                          const uint32_t *__restrict__ n_list, uint32_t n_paths, wf_state *states, uint32_t *queue,
+                          float4 *rays, grt_path_result *results, uint32_t *n_queue) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p == 0) *n_queue = n_paths;
+    if (p >= n_paths) return;
+    path_t st;
+    float4 ro, rd;
+    const uint32_t nl = *n_list;
+    if (nl == 0) {  // no primary hit at all: every path is empty
+        results[p] = {0.f, 0u, pm::kMissWord, pm::kDigestSeed};
+        queue[p] = 0xFFFFFFFFu;
+        rays[2 * (size_t)p] = make_float4(0.f, 0.f, 0.f, 1.f);
+        rays[2 * (size_t)p + 1] = make_float4(0.f, 0.f, 1.f, -1.f);  // empty interval: misses
+        return;
+    }
+    path_start(ps, pp, p, prim_rays, prim_hits, hit_list, nl, st, ro, rd);
+    states[p] = {st.rng.state, st.rng.inc, st.thr, st.digest, st.bounce, st.last_ref};
+    queue[p] = p;
+    rays[2 * (size_t)p] = ro;
+    rays[2 * (size_t)p + 1] = rd;
+}
+
+__global__ void k_wf_shade(pt_scene ps, pt_params_dev pp, const uint32_t *__restrict__ n_in,
+                           const uint32_t *__restrict__ queue_in, const float4 *__restrict__ rays_in,
+                           const grt_hit *__restrict__ hits, wf_state *states, uint32_t *n_out, uint32_t *queue_out,
+                           float4 *rays_out, grt_path_result *results, grt_hit *bounce_hits) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = *n_in;
+    bool go_on = false;
+    uint32_t p = 0;
+    float4 ro, rd;
+    if (k < n) {
+        p = queue_in[k];
+        if (p != 0xFFFFFFFFu) {
+            wf_state w = states[p];
+            path_t st;
+            st.rng.state = w.rng_state;
+            st.rng.inc = w.rng_inc;
+            st.thr = w.thr;
+            st.digest = w.digest;
+            st.bounce = w.bounce;
+            st.last_ref = w.last_ref;
+            ro = rays_in[2 * (size_t)k];
+            rd = rays_in[2 * (size_t)k + 1];
+            const float4 hv = reinterpret_cast<const float4 *>(hits)[k];
+            hit_t h = {hv.x, hv.y, hv.z, __float_as_uint(hv.w)};
+            record_bounce(bounce_hits, pp, p, st.bounce, h);
+            grt_path_result res;
+            go_on = path_bounce(ps, pp, st, h, ro, rd, res);
+            if (go_on) {
+                states[p] = {st.rng.state, st.rng.inc, st.thr, st.digest, st.bounce, st.last_ref};
+            } else {
+                results[p] = res;
+                clear_unused(bounce_hits, pp, p, st.bounce);
+            }
+        }
+    }
+    // warp-aggregated append to the next queue
+    const unsigned m = __ballot_sync(kFull, go_on);
+    if (m == 0) return;
+    const unsigned lane = threadIdx.x & 31;
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(n_out, __popc(m));
+    base = __shfl_sync(kFull, base, 0);
+    if (go_on) {
+        const uint32_t slot = base + __popc(m & ((1u << lane) - 1u));
+        queue_out[slot] = p;
+        rays_out[2 * (size_t)slot] = ro;
+        rays_out[2 * (size_t)slot + 1] = rd;
+    }
+}
+
+// ---- fused persistent form ----------------------------------------------------------------
+
+template <int STACK>
+__global__ void __launch_bounds__(256) k_pt_fused(dev_scene sc, pt_scene ps, pt_params_dev pp,
+                                                  const float4 *__restrict__ prim_rays,
+                                                  const grt_hit *__restrict__ prim_hits,
+                                                  const uint32_t *__restrict__ hit_list,
+                                                  const uint32_t *__restrict__ n_list, uint32_t n_paths,
+                                                  grt_path_result *results, grt_hit *bounce_hits, unsigned *err,
+                                                  unsigned *counter, int refill_threshold, int refill_period) {
+    extern __shared__ int s_stack[];
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned lanes_below = (1u << lane) - 1u;
+    int *stk = s_stack + threadIdx.x;
+    const int stride = blockDim.x;
+    const uint32_t nl = *n_list;
+    trav_t s;
+    ray_t r;
+    path_t st;
+    float4 ro, rd;
+    uint32_t p = 0;
+    bool have = false, plain = false, exhausted = false;
+    for (;;) {
+        if (!exhausted) {
+            const unsigned need = __ballot_sync(kFull, !have);
+            if (need) {
+                const unsigned cnt = __popc(need);
+                unsigned base = 0;
+                if (lane == 0) base = atomicAdd(counter, cnt);
+                base = __shfl_sync(kFull, base, 0);
+                if (base + cnt >= n_paths) exhausted = true;
+                if (!have) {
+                    const uint32_t my = base + __popc(need & lanes_below);
+                    if (my < n_paths) {
+                        p = my;
+                        if (nl == 0) {
+                            results[p] = {0.f, 0u, pm::kMissWord, pm::kDigestSeed};
+                            clear_unused(bounce_hits, pp, p, 0);
+                        } else {
+                            path_start(ps, pp, p, prim_rays, prim_hits, hit_list, nl, st, ro, rd);
+                            r = to_ray(ro, rd);
+                            trav_init(s, sc);
+                            plain = sc.finite && ray_is_plain(r);
+                            have = true;
+                        }
+                    }
+                }
+            }
+        }
+        if (__ballot_sync(kFull, have) == 0) {
+            if (exhausted) break;
+            continue;
+        }
+        for (int it = 1;; ++it) {
+            if (have) {
+                if (plain)
+                    trav_step<STACK, false, true>(s, sc, r, stk, stride, err);
+                else
+                    trav_step<STACK, false, false>(s, sc, r, stk, stride, err);
+                if (s.done) {
+                    record_bounce(bounce_hits, pp, p, st.bounce, s.hit);
+                    grt_path_result res;
+                    if (path_bounce(ps, pp, st, s.hit, ro, rd, res)) {
+                        r = to_ray(ro, rd);
+                        trav_init(s, sc);
+                        plain = sc.finite && ray_is_plain(r);
+                    } else {
+                        results[p] = res;
+                        clear_unused(bounce_hits, pp, p, st.bounce);
+                        have = false;
+                    }
+                }
+            }
+            if (it % refill_period == 0) {
+                const int busy = __popc(__ballot_sync(kFull, have));
+                if (busy == 0 || (!exhausted && busy < refill_threshold)) break;
+            }
+        }
+    }
+}
+
+template <int STACK>
+cudaError_t fused_launch(const dev_scene &sc, const pt_scene &ps, const pt_params_dev &pp, const float4 *prim_rays,
+                         const grt_hit *prim_hits, const uint32_t *hit_list, const uint32_t *n_list, uint32_t n_paths,
+                         grt_path_result *results, grt_hit *bounce_hits, const launch_params &lp, unsigned *err,
+                         unsigned *counter, cudaStream_t st) {
+    const size_t smem = (size_t)STACK * lp.block_threads * sizeof(int);
+    auto kern = k_pt_fused<STACK>;
+    cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
+    if (e != cudaSuccess) return e;
+    kern<<<lp.grid_blocks, lp.block_threads, smem, st>>>(sc, ps, pp, prim_rays, prim_hits, hit_list, n_list, n_paths,
+                                                         results, bounce_hits, err, counter, lp.refill_threshold,
+                                                         lp.refill_period);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+size_t compact_scratch_bytes(uint32_t n) { return (size_t)((n + kTile - 1) / kTile + 1) * sizeof(uint32_t); }
+
+cudaError_t launch_compact_hits(const grt_hit *hits, uint32_t n, uint32_t *out_indices, uint32_t *count,
+                                uint32_t *scratch, cudaStream_t st) {
+    const uint32_t nb = (n + kTile - 1) / kTile;
+    if (nb == 0) return cudaMemsetAsync(count, 0, sizeof(uint32_t), st);
+    k_count_valid<<<nb, 256, 0, st>>>(hits, n, scratch);
+    k_scan_counts<<<1, 1024, 0, st>>>(scratch, nb, count);
+    k_scatter_indices<<<nb, 256, 0, st>>>(hits, n, scratch, out_indices);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_shadow_rays(const pt_scene &ps, const float4 *rays, const grt_hit *hits, uint32_t n,
+                               const float light[3], float eps, float4 *out_rays, uint32_t *count, uint32_t *scratch,
+                               cudaStream_t st) {
+    const uint32_t nb = (n + kTile - 1) / kTile;
+    if (nb == 0) return cudaMemsetAsync(count, 0, sizeof(uint32_t), st);
+    k_count_valid<<<nb, 256, 0, st>>>(hits, n, scratch);
+    k_scan_counts<<<1, 1024, 0, st>>>(scratch, nb, count);
+    k_scatter_shadow<<<nb, 256, 0, st>>>(hits, n, scratch, rays, ps, light[0], light[1], light[2], eps, out_rays);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_wavefront_init(const pt_scene &ps, const pt_params_dev &pp, const float4 *prim_rays,
+                                  const grt_hit *prim_hits, const uint32_t *hit_list, const uint32_t *n_list,
+                                  uint32_t n_paths, void *states, uint32_t *queue, float4 *rays,
+                                  grt_path_result *results, uint32_t *n_queue, cudaStream_t st) {
+    const uint32_t nb = (n_paths + 255) / 256;
+    k_wf_init<<<nb, 256, 0, st>>>(ps, pp, prim_rays, prim_hits, hit_list, n_list, n_paths, (wf_state *)states, queue,
+                                  rays, results, n_queue);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_wavefront_shade(const pt_scene &ps, const pt_params_dev &pp, uint32_t max_n, const uint32_t *n_in,
+                                   const uint32_t *queue_in, const float4 *rays_in, const grt_hit *hits, void *states,
+                                   uint32_t *n_out, uint32_t *queue_out, float4 *rays_out, grt_path_result *results,
+                                   grt_hit *bounce_hits, cudaStream_t st) {
+    const uint32_t nb = (max_n + 255) / 256;
+    k_wf_shade<<<nb, 256, 0, st>>>(ps, pp, n_in, queue_in, rays_in, hits, (wf_state *)states, n_out, queue_out,
+                                   rays_out, results, bounce_hits);
+    return cudaGetLastError();
+}
+
+size_t wavefront_state_bytes() { return sizeof(wf_state); }
+
+cudaError_t launch_fused(const dev_scene &sc, const pt_scene &ps, const pt_params_dev &pp, const float4 *prim_rays,
+                         const grt_hit *prim_hits, const uint32_t *hit_list, const uint32_t *n_list, uint32_t n_paths,
+                         grt_path_result *results, grt_hit *bounce_hits, const launch_params &lp, unsigned *err,
+                         unsigned *counter, cudaStream_t st) {
+    if (n_paths == 0) return cudaSuccess;
+    if (lp.stack_entries <= kStackSmall)
+        return fused_launch<kStackSmall>(sc, ps, pp, prim_rays, prim_hits, hit_list, n_list, n_paths, results,
+                                         bounce_hits, lp, err, counter, st);
+    return fused_launch<kStackLarge>(sc, ps, pp, prim_rays, prim_hits, hit_list, n_list, n_paths, results, bounce_hits,
+                                     lp, err, counter, st);
+}
+
+cudaError_t prepare_pt_kernels() {
+    const int bytes = kStackLarge * 256 * (int)sizeof(int);
+    for (const void *f : {(const void *)k_pt_fused<kStackSmall>, (const void *)k_pt_fused<kStackLarge>}) {
+        cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+int fused_blocks_per_sm(int block_threads, int stack_entries) {
+    int blocks = 0;
+    const bool small = stack_entries <= kStackSmall;
+    const size_t smem = (size_t)(small ? kStackSmall : kStackLarge) * block_threads * sizeof(int);
+    const void *fn = small ? (const void *)k_pt_fused<kStackSmall> : (const void *)k_pt_fused<kStackLarge>;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, block_threads, smem) != cudaSuccess) return 1;
+    return blocks > 0 ? blocks : 1;
+}
+
+}  // namespace grt

@@ -18,11 +18,13 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 
-template <int STACK, bool ANY>
+template <int STACK, bool ANY, bool COUNT>
 __global__ void __launch_bounds__(256) k_trace_plain(const float4 *__restrict__ rays, grt_hit *__restrict__ hits,
-                                                     uint32_t n, dev_scene sc, unsigned *err) {
+                                                     uint32_t n, const uint32_t *__restrict__ n_dev, dev_scene sc,
+                                                     unsigned *err, unsigned long long *counters) {
     extern __shared__ int s_stack[];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n_dev) n = *n_dev;  // ray count produced on the device (wavefront queues)
     if (i >= n) return;
     const ray_t r = load_ray(rays, i);
     trav_t s;
@@ -30,11 +32,16 @@ __global__ void __launch_bounds__(256) k_trace_plain(const float4 *__restrict__ 
     int *stk = s_stack + threadIdx.x;
     const int stride = blockDim.x;
     if (sc.finite && ray_is_plain(r)) {
-        while (!s.done) trav_step<STACK, ANY, true>(s, sc, r, stk, stride, err);
+        while (!s.done) trav_step<STACK, ANY, true, COUNT>(s, sc, r, stk, stride, err);
     } else {
-        while (!s.done) trav_step<STACK, ANY, false>(s, sc, r, stk, stride, err);
+        while (!s.done) trav_step<STACK, ANY, false, COUNT>(s, sc, r, stk, stride, err);
     }
     store_hit<ANY>(hits, i, s);
+    if (COUNT) {
+        atomicAdd(counters + 0, 1ull);
+        atomicAdd(counters + 1, (unsigned long long)s.n_inner);
+        atomicAdd(counters + 2, (unsigned long long)s.n_tri);
+    }
 }
 
 template <int STACK, bool ANY>
@@ -101,17 +108,15 @@ __global__ void __launch_bounds__(256) k_trace_persistent(const float4 *__restri
 }
 
 template <int STACK, bool ANY>
-cudaError_t plain_launch(const dev_scene &sc, const float4 *rays, grt_hit *hits, uint32_t n, const launch_params &lp,
-                         unsigned *err, cudaStream_t st) {
+cudaError_t plain_launch(const dev_scene &sc, const float4 *rays, grt_hit *hits, uint32_t n, const uint32_t *n_dev,
+                         const launch_params &lp, unsigned *err, cudaStream_t st) {
     const int bt = lp.block_threads;
     const size_t smem = (size_t)STACK * bt * sizeof(int);
-    auto kern = k_trace_plain<STACK, ANY>;
-    if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-    }
     const uint32_t blocks = (n + bt - 1) / bt;
-    kern<<<blocks, bt, smem, st>>>(rays, hits, n, sc, err);
+    if (lp.counters)
+        k_trace_plain<STACK, ANY, true><<<blocks, bt, smem, st>>>(rays, hits, n, n_dev, sc, err, lp.counters);
+    else
+        k_trace_plain<STACK, ANY, false><<<blocks, bt, smem, st>>>(rays, hits, n, n_dev, sc, err, nullptr);
     return cudaGetLastError();
 }
 
@@ -121,10 +126,6 @@ cudaError_t persistent_launch(const dev_scene &sc, const float4 *rays, grt_hit *
     const int bt = lp.block_threads;
     const size_t smem = (size_t)STACK * bt * sizeof(int);
     auto kern = k_trace_persistent<STACK, ANY>;
-    if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-    }
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
     kern<<<lp.grid_blocks, bt, smem, st>>>(rays, hits, n, sc, err, counter, lp.refill_threshold, lp.refill_period);
@@ -134,13 +135,13 @@ cudaError_t persistent_launch(const dev_scene &sc, const float4 *rays, grt_hit *
 }  // namespace
 
 cudaError_t launch_trace_plain(const dev_scene &sc, const float4 *rays, grt_hit *hits, uint32_t n, bool any_hit,
-                               const launch_params &lp, unsigned *err, cudaStream_t stream) {
+                               const launch_params &lp, unsigned *err, cudaStream_t stream, const uint32_t *n_dev) {
     if (n == 0) return cudaSuccess;
     if (lp.stack_entries <= kStackSmall)
-        return any_hit ? plain_launch<kStackSmall, true>(sc, rays, hits, n, lp, err, stream)
-                       : plain_launch<kStackSmall, false>(sc, rays, hits, n, lp, err, stream);
-    return any_hit ? plain_launch<kStackLarge, true>(sc, rays, hits, n, lp, err, stream)
-                   : plain_launch<kStackLarge, false>(sc, rays, hits, n, lp, err, stream);
+        return any_hit ? plain_launch<kStackSmall, true>(sc, rays, hits, n, n_dev, lp, err, stream)
+                       : plain_launch<kStackSmall, false>(sc, rays, hits, n, n_dev, lp, err, stream);
+    return any_hit ? plain_launch<kStackLarge, true>(sc, rays, hits, n, n_dev, lp, err, stream)
+                   : plain_launch<kStackLarge, false>(sc, rays, hits, n, n_dev, lp, err, stream);
 }
 
 cudaError_t launch_trace_persistent(const dev_scene &sc, const float4 *rays, grt_hit *hits, uint32_t n, bool any_hit,
@@ -153,6 +154,27 @@ cudaError_t launch_trace_persistent(const dev_scene &sc, const float4 *rays, grt
                    : persistent_launch<kStackLarge, false>(sc, rays, hits, n, lp, err, counter, stream);
 }
 
+cudaError_t prepare_trace_kernels() {
+    const int bytes = kStackLarge * 256 * (int)sizeof(int);  // largest stack variant at 256 threads
+    const void *fns[] = {(const void *)k_trace_plain<kStackSmall, false, false>,
+                         (const void *)k_trace_plain<kStackSmall, true, false>,
+                         (const void *)k_trace_plain<kStackLarge, false, false>,
+                         (const void *)k_trace_plain<kStackLarge, true, false>,
+                         (const void *)k_trace_plain<kStackSmall, false, true>,
+                         (const void *)k_trace_plain<kStackSmall, true, true>,
+                         (const void *)k_trace_plain<kStackLarge, false, true>,
+                         (const void *)k_trace_plain<kStackLarge, true, true>,
+                         (const void *)k_trace_persistent<kStackSmall, false>,
+                         (const void *)k_trace_persistent<kStackSmall, true>,
+                         (const void *)k_trace_persistent<kStackLarge, false>,
+                         (const void *)k_trace_persistent<kStackLarge, true>};
+    for (const void *f : fns) {
+        cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 int persistent_blocks_per_sm(int block_threads, int stack_entries, bool any_hit) {
     int blocks = 0;
     const bool small = stack_entries <= kStackSmall;
@@ -161,7 +183,6 @@ int persistent_blocks_per_sm(int block_threads, int stack_entries, bool any_hit)
                                       : (const void *)k_trace_persistent<kStackSmall, false>)
                            : (any_hit ? (const void *)k_trace_persistent<kStackLarge, true>
                                       : (const void *)k_trace_persistent<kStackLarge, false>);
-    if (smem > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, block_threads, smem) != cudaSuccess) return 1;
     return blocks > 0 ? blocks : 1;
 }

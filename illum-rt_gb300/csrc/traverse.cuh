@@ -127,6 +127,7 @@ struct trav_t {
     uint32_t steps;
     bool done;
     bool found;  // any-hit: an occluder was found
+    uint32_t n_inner, n_tri;  // inner nodes visited and triangles tested (counting kernels only)
     hit_t hit;
 };
 
@@ -136,6 +137,8 @@ __device__ __forceinline__ void trav_init(trav_t &s, const dev_scene &sc) {
     s.steps = 0;
     s.done = sc.empty != 0;
     s.found = false;
+    s.n_inner = 0;
+    s.n_tri = 0;
     s.hit.t = FLT_MAX;
     s.hit.b = 0.f;
     s.hit.g = 0.f;
@@ -145,7 +148,7 @@ __device__ __forceinline__ void trav_init(trav_t &s, const dev_scene &sc) {
 // One traversal step: one inner node (two box tests) or one leaf (its triangle tests).
 // Mirrors one pop of the reference loop (rt/cpu/bvh2.cpp:82-127 / 147-182): the near child is
 // kept in `cur` instead of being pushed and popped straight back.
-template <int STACK, bool ANY, bool PLAIN>
+template <int STACK, bool ANY, bool PLAIN, bool COUNT = false>
 __device__ __forceinline__ void trav_step(trav_t &s, const dev_scene &sc, const ray_t &r, int *stk, int stride,
                                           unsigned *err) {
     if (++s.steps > kStepLimit) {
@@ -154,6 +157,7 @@ __device__ __forceinline__ void trav_step(trav_t &s, const dev_scene &sc, const 
         return;
     }
     if (s.cur >= 0) {
+        if (COUNT) ++s.n_inner;
         const float4 *np = sc.nodes + 4 * (size_t)s.cur;
         const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3);
         float dl, dr;
@@ -185,6 +189,7 @@ __device__ __forceinline__ void trav_step(trav_t &s, const dev_scene &sc, const 
         leaf_range(s.cur, first, count);
         const float4 *rp = sc.records + 3 * (size_t)first;
         for (uint32_t k = 0; k < count; ++k) {
+            if (COUNT) ++s.n_tri;
             const float4 p0 = __ldg(rp + 3 * k), p1 = __ldg(rp + 3 * k + 1), p2 = __ldg(rp + 3 * k + 2);
             float t, b, g;
             if (tri_test(p0, p1, p2, r, t, b, g) && (ANY || t < s.hit.t)) {

@@ -162,9 +162,73 @@ grt_status grt_trace(grt_ctx *ctx, const float *rays_dev, grt_hit *hits_dev, uin
  * waits. Uses context-owned device and pinned staging buffers. */
 grt_status grt_trace_host(grt_ctx *ctx, const float *rays_host, grt_hit *hits_host, uint32_t n, int any_hit);
 
+/* Traversal statistics: while counters_dev (three uint64 in device memory) is set, every ray
+ * traced by the one-thread-per-ray kernel (tracer "while-while", and the per-bounce traces of
+ * GRT_PT_WAVEFRONT) adds 1 to counters_dev[0], its inner-node visits to [1] and its triangle
+ * tests to [2]. The counting kernel is a separate, slower variant; NULL switches it off. */
+grt_status grt_set_traversal_counters(grt_ctx *ctx, unsigned long long *counters_dev);
+
 /* Waits for `stream` (at most timeout_ms milliseconds; 0 = no limit) and returns the first
  * error flagged by a kernel since the previous check. */
 grt_status grt_check(grt_ctx *ctx, grt_stream_t stream, uint32_t timeout_ms);
+
+/* ---- ray generation steps around the traversal ---------------------------------------- */
+
+/* Stable compaction of the valid hits (t != FLT_MAX) of n hit records: indices_dev receives
+ * their ray indices in increasing order and *count_dev their number. */
+grt_status grt_compact_hits(grt_ctx *ctx, const grt_hit *hits_dev, uint32_t n, uint32_t *indices_dev,
+                            uint32_t *count_dev, grt_stream_t stream);
+
+/* One shadow ray per valid hit, in ray order (the any-hit rays of the reference's direct
+ * lighting, gi/direct.cpp:499-534 with rt/cuda/bounce.cu:194-196): origin = hit point moved by
+ * eps along the geometric normal facing the incoming ray, direction towards `light`,
+ * t_min = eps, t_max = distance - eps (ray::length_exclusive, libgi/rt.h:30). shadow_rays_dev
+ * needs room for n rays; *count_dev receives the number written. */
+grt_status grt_shadow_rays(grt_ctx *ctx, const float *rays_dev, const grt_hit *hits_dev, uint32_t n,
+                           const float light[3], float eps, float *shadow_rays_dev, uint32_t *count_dev,
+                           grt_stream_t stream);
+
+/* One grey albedo per material id (the material id is the w of each triangle); ids without
+ * an entry use 0.8. n = 0 clears the table. */
+grt_status grt_set_materials(grt_ctx *ctx, const float *albedo, uint32_t n);
+
+/* ---- diffuse multi-bounce path tracing ------------------------------------------------ */
+
+enum { GRT_PT_WAVEFRONT = 0, GRT_PT_FUSED = 1 };
+
+typedef struct grt_pt_params {
+    uint32_t max_bounces; /* bounce rays per path, default 5 */
+    uint32_t rr_start;    /* Russian roulette decides before bounce rays rr_start, rr_start+1, ... (3) */
+    float rr_continue;    /* survival probability of the roulette (0.8); survivors are reweighted */
+    float eps;            /* origin offset along the normal and t_min of bounce rays (1e-4) */
+    uint64_t seed;        /* path p draws from PCG32 stream seed + p */
+    int mode;             /* GRT_PT_WAVEFRONT (one kernel per bounce) or GRT_PT_FUSED (persistent) */
+    int use_graph;        /* capture the step once and replay it as a CUDA graph (stream must not be NULL) */
+} grt_pt_params;
+
+/* Result of one path: radiance = product of albedos (and roulette weights) times the sky
+ * 0.5 + 0.5 d.y if the path escaped, else 0; bounces = bounce rays traced; last_ref = last hit
+ * triangle (0xFFFFFFFF if none); digest = FNV-1a over (ref, t bits) of every bounce hit and a
+ * 0xFFFFFFFF word for the escape. */
+typedef struct grt_path_result {
+    float radiance;
+    uint32_t bounces;
+    uint32_t last_ref;
+    uint32_t digest;
+} grt_path_result;
+
+void grt_pt_params_default(grt_pt_params *params);
+
+/* Traces n_paths diffuse paths. Path p starts at the valid primary hit number (p mod H) in ray
+ * order, H being the number of valid hits among prim_hits_dev (n_primary records for the rays
+ * prim_rays_dev). Each bounce samples a cosine-weighted direction around the facing geometric
+ * normal (k::sample_cos_dir, rt/cuda/bounce.cu:91-142, with libgi/sampling.h:32-36 and
+ * libgi/util.h:212-232), from an origin moved eps along that normal. results_dev receives
+ * n_paths records; bounce_hits_dev (optional) n_paths * max_bounces closest-hit records, the
+ * slots after a path's last bounce zeroed. Both modes give identical results. */
+grt_status grt_pathtrace(grt_ctx *ctx, const grt_pt_params *params, const float *prim_rays_dev,
+                         const grt_hit *prim_hits_dev, uint32_t n_primary, uint32_t n_paths,
+                         grt_path_result *results_dev, grt_hit *bounce_hits_dev, grt_stream_t stream);
 
 #ifdef __cplusplus
 }

@@ -533,6 +533,106 @@ inline void set_threads(int threads) {
     if (threads > 0) omp_set_num_threads(threads);
 }
 
+
+// ---- ray generation around the traversal --------------------------------------------------
+//
+// Restatement, for checking, of the product's bounce and shadow-ray definitions: PCG32
+// (libgi/random.h:59-96), cosine_sample_hemisphere / uniform_sample_disk
+// (libgi/sampling.h:13-17, 32-36) with sin/cos of 2*pi*u from the Taylor polynomials of the
+// remaining quarter-turn angle, align (libgi/util.h:212-218), flip_normals_to_ray
+// (libgi/util.h:221-225), and length_exclusive (libgi/rt.h:30). Plain float arithmetic; the
+// file is compiled with -ffp-contract=off so each operation rounds as written.
+
+struct rng32 {
+    uint64_t state = 0, inc = 1;
+    uint32_t next() {
+        uint64_t old = state;
+        state = old * 0x5851f42d4c957f2dULL + inc;
+        uint32_t x = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+        uint32_t rot = (uint32_t)(old >> 59u);
+        return (x >> rot) | (x << ((~rot + 1u) & 31u));
+    }
+    void seq(uint64_t s) {
+        state = 0u;
+        inc = (s << 1u) | 1u;
+        next();
+        state += 0x853c49e6748fea9bULL;
+        next();
+    }
+    float uniform() {
+        float f = (float)next() * 0x1p-32f;
+        return f < 0x1.fffffep-1f ? f : 0x1.fffffep-1f;
+    }
+};
+
+inline void turn_sincos(float u, float &s, float &c) {
+    float t4 = u * 4.0f;
+    int q = (int)t4;
+    float x = (t4 - (float)q) * 0x1.921fb6p+0f;
+    float x2 = x * x;
+    const float sc[7] = {0x1.612462p-33f, -0x1.ae6456p-26f, 0x1.71de3ap-19f, -0x1.a01a02p-13f,
+                         0x1.111112p-7f, -0x1.555556p-3f, 1.0f};
+    const float cc[7] = {0x1.1eed8ep-29f, -0x1.27e4fcp-22f, 0x1.a01a02p-16f, -0x1.6c16c2p-10f,
+                         0x1.555556p-5f, -0.5f, 1.0f};
+    float ps = sc[0], pc = cc[0];
+    for (int k = 1; k < 7; ++k) {
+        ps = ps * x2 + sc[k];
+        pc = pc * x2 + cc[k];
+    }
+    float sn = ps * x;
+    switch (q & 3) {
+        case 0: s = sn; c = pc; break;
+        case 1: s = pc; c = -sn; break;
+        case 2: s = -sn; c = -pc; break;
+        default: s = -pc; c = sn; break;
+    }
+}
+
+inline v3 vsub(v3 a, v3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline float vdot(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+inline v3 facing_normal(const scene &sc, uint32_t tri, v3 d, uint32_t &mat) {
+    const uint32_t *t = sc.t4 + 4 * (size_t)tri;
+    mat = t[3];
+    v3 a = sc.vert(t[0]), b = sc.vert(t[1]), c = sc.vert(t[2]);
+    v3 e1 = vsub(b, a), e2 = vsub(c, a);
+    v3 n = {e1.y * e2.z - e1.z * e2.y, e1.z * e2.x - e1.x * e2.z, e1.x * e2.y - e1.y * e2.x};
+    float inv = 1.0f / std::sqrt(vdot(n, n));
+    n = {n.x * inv, n.y * inv, n.z * inv};
+    if (vdot(d, n) > 0.f) n = {-n.x, -n.y, -n.z};
+    return n;
+}
+
+inline v3 offset_point(v3 o, v3 d, float t, v3 n, float eps) {
+    return {(o.x + t * d.x) + eps * n.x, (o.y + t * d.y) + eps * n.y, (o.z + t * d.z) + eps * n.z};
+}
+
+inline v3 cosine_dir(float u0, float u1, v3 n) {
+    float r = std::sqrt(u0), sn, cs;
+    turn_sincos(u1, sn, cs);
+    float dx = r * cs, dy = r * sn;
+    float z = (1.0f - dx * dx) - dy * dy;
+    v3 v = {dx, dy, z > 0.f ? std::sqrt(z) : 0.f};
+    float s = std::signbit(n.z) ? -1.0f : 1.0f;
+    v3 w = {v.x, v.y, v.z * s};
+    v3 hh = {n.x, n.y, n.z + s};
+    float k = vdot(w, hh) / (1.0f + (n.z < 0.f ? -n.z : n.z));
+    return {k * hh.x - w.x, k * hh.y - w.y, k * hh.z - w.z};
+}
+
+inline uint32_t fnv(uint32_t h, uint32_t w) { return (h ^ w) * 16777619u; }
+inline uint32_t fbits(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    return u;
+}
+
+struct pt_params {
+    uint32_t max_bounces, rr_start;
+    float rr_continue, eps;
+    uint64_t seed;
+};
+
 }  // namespace orc
 
 using namespace orc;
@@ -630,6 +730,120 @@ void orc_any(void *hp, const float *rays8, uint64_t n, uint8_t *occluded, uint32
             counts[3 * i + 1] = c.tris;
             counts[3 * i + 2] = c.max_sp;
         }
+    }
+}
+
+
+// Valid hits (t != FLT_MAX) in ray order.
+static std::vector<uint32_t> valid_hits(const float *hits4, uint64_t n) {
+    std::vector<uint32_t> out;
+    for (uint64_t i = 0; i < n; ++i)
+        if (hits4[4 * i] != FLT_MAX) out.push_back((uint32_t)i);
+    return out;
+}
+
+// Shadow rays towards `light`, one per valid hit, in ray order; returns their number.
+uint32_t orc_shadow_rays(void *hp, const float *rays8, const float *hits4, uint64_t n, const float *light, float eps,
+                         float *out8) {
+    bvh *h = (bvh *)hp;
+    std::vector<uint32_t> idx = valid_hits(hits4, n);
+    for (size_t k = 0; k < idx.size(); ++k) {
+        const float *r = rays8 + 8 * (size_t)idx[k];
+        const float *hit = hits4 + 4 * (size_t)idx[k];
+        uint32_t ref, mat;
+        std::memcpy(&ref, hit + 3, 4);
+        v3 o = {r[0], r[1], r[2]}, d = {r[4], r[5], r[6]};
+        v3 nrm = facing_normal(h->sc, ref, d, mat);
+        v3 p = offset_point(o, d, hit[0], nrm, eps);
+        v3 to = {light[0] - p.x, light[1] - p.y, light[2] - p.z};
+        float dist = std::sqrt(vdot(to, to));
+        float *w = out8 + 8 * k;
+        w[0] = p.x; w[1] = p.y; w[2] = p.z; w[3] = eps;
+        w[4] = to.x / dist; w[5] = to.y / dist; w[6] = to.z / dist; w[7] = dist - eps;
+    }
+    return (uint32_t)idx.size();
+}
+
+// Diffuse paths (see grt_pathtrace): results4 = (radiance, bounces, last_ref, digest) per
+// path; bounce_hits (optional) = max_bounces hit records per path, unused slots zero.
+void orc_pathtrace(void *hp, const float *prim_rays8, const float *prim_hits4, uint64_t n_primary, uint64_t n_paths,
+                   uint32_t max_bounces, uint32_t rr_start, float rr_continue, float eps, uint64_t seed,
+                   const float *albedo, uint32_t n_albedo, uint32_t *results4, float *bounce_hits,
+                   uint64_t *totals3, int threads) {
+    bvh *h = (bvh *)hp;
+    set_threads(threads);
+    std::vector<uint32_t> H = valid_hits(prim_hits4, n_primary);
+    uint64_t t_rays = 0, t_inner = 0, t_tri = 0;
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : t_rays, t_inner, t_tri)
+    for (int64_t p = 0; p < (int64_t)n_paths; ++p) {
+        uint32_t *res = results4 + 4 * p;
+        float *bh = bounce_hits ? bounce_hits + 4 * (size_t)p * max_bounces : nullptr;
+        if (bh) std::memset(bh, 0, 16 * (size_t)max_bounces);
+        if (H.empty()) {
+            float zero = 0.f;
+            std::memcpy(res, &zero, 4);
+            res[1] = 0;
+            res[2] = 0xFFFFFFFFu;
+            res[3] = 2166136261u;
+            continue;
+        }
+        uint32_t i = H[(uint64_t)p % H.size()];
+        const float *pr = prim_rays8 + 8 * (size_t)i;
+        const float *ph = prim_hits4 + 4 * (size_t)i;
+        uint32_t pref, mat;
+        std::memcpy(&pref, ph + 3, 4);
+        v3 o = {pr[0], pr[1], pr[2]}, d = {pr[4], pr[5], pr[6]};
+        rng32 rng;
+        rng.seq(seed + (uint64_t)p);
+        v3 n = facing_normal(h->sc, pref, d, mat);
+        v3 org = offset_point(o, d, ph[0], n, eps);
+        float u0 = rng.uniform(), u1 = rng.uniform();
+        v3 dir = cosine_dir(u0, u1, n);
+        float thr = 1.0f, radiance = 0.f;
+        uint32_t digest = 2166136261u, last = 0xFFFFFFFFu, bounce = 1;
+        for (;;) {
+            float rr[8] = {org.x, org.y, org.z, eps, dir.x, dir.y, dir.z, FLT_MAX};
+            counters cnt;
+            hit hh = closest_hit(*h, load_ray(rr), &cnt);
+            t_rays += 1;
+            t_inner += cnt.inner;
+            t_tri += cnt.tris;
+            if (bh) {
+                float *w = bh + 4 * (bounce - 1);
+                w[0] = hh.t;
+                w[1] = hh.t != FLT_MAX ? hh.beta : 0.f;
+                w[2] = hh.t != FLT_MAX ? hh.gamma : 0.f;
+                std::memcpy(w + 3, &hh.ref, 4);
+            }
+            if (hh.t == FLT_MAX) {
+                digest = fnv(digest, 0xFFFFFFFFu);
+                radiance = thr * (0.5f + 0.5f * dir.y);
+                break;
+            }
+            digest = fnv(fnv(digest, hh.ref), fbits(hh.t));
+            last = hh.ref;
+            v3 nn = facing_normal(h->sc, hh.ref, dir, mat);
+            thr = thr * (mat < n_albedo ? albedo[mat] : 0.8f);
+            if (bounce >= max_bounces) break;
+            if (bounce + 1 >= rr_start) {
+                if (!(rng.uniform() < rr_continue)) break;
+                thr = thr / rr_continue;
+            }
+            org = offset_point(org, dir, hh.t, nn, eps);
+            u0 = rng.uniform();
+            u1 = rng.uniform();
+            dir = cosine_dir(u0, u1, nn);
+            ++bounce;
+        }
+        std::memcpy(res, &radiance, 4);
+        res[1] = bounce;
+        res[2] = last;
+        res[3] = digest;
+    }
+    if (totals3) {
+        totals3[0] = t_rays;
+        totals3[1] = t_inner;
+        totals3[2] = t_tri;
     }
 }
 

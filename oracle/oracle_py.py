@@ -109,6 +109,38 @@ class OracleBVH(_BVHBase):
         self.lib.orc_closest(self.h, _p(rays), n, _p(out), _p(cnt) if counts else None, threads)
         return out, cnt
 
+    def shadow_rays(self, rays, hits, light, eps=1e-4):
+        """Shadow rays of the valid hits, in ray order (float32 [count, 8])."""
+        rays = np.ascontiguousarray(rays, np.float32)
+        hits = np.ascontiguousarray(hits, np.float32)
+        out = np.zeros((rays.shape[0], 8), np.float32)
+        lt = np.asarray(light, np.float32)
+        f = self.lib.orc_shadow_rays
+        f.restype = ctypes.c_uint32
+        f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p,
+                      ctypes.c_float, ctypes.c_void_p]
+        cnt = f(self.h, _p(rays), _p(hits), rays.shape[0], _p(lt), eps, _p(out))
+        return out[:cnt]
+
+    def pathtrace(self, prim_rays, prim_hits, n_paths, max_bounces=5, rr_start=3, rr_continue=0.8, eps=1e-4, seed=0,
+                  albedo=None, bounce_hits=False, threads=0, totals=None):
+        """Diffuse paths as grt_pathtrace defines them: (results uint32 [n, 4] with the radiance as
+        float bits in column 0, bounce hit records float32 [n, max_bounces, 4] or None). `totals`,
+        a uint64 array of 3, receives (bounce rays, inner-node visits, triangle tests)."""
+        prim_rays = np.ascontiguousarray(prim_rays, np.float32)
+        prim_hits = np.ascontiguousarray(prim_hits, np.float32)
+        alb = np.ascontiguousarray(albedo if albedo is not None else np.zeros(0), np.float32)
+        res = np.zeros((n_paths, 4), np.uint32)
+        bh = np.zeros((n_paths, max_bounces, 4), np.float32) if bounce_hits else None
+        f = self.lib.orc_pathtrace
+        f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64,
+                      ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, ctypes.c_float, ctypes.c_uint64,
+                      ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+        f(self.h, _p(prim_rays), _p(prim_hits), prim_rays.shape[0], n_paths, max_bounces, rr_start, rr_continue, eps,
+          seed, _p(alb) if alb.size else None, alb.size, _p(res), _p(bh) if bh is not None else None,
+          _p(totals) if totals is not None else None, threads)
+        return res, bh
+
     def any(self, rays, threads=0, counts=False):
         rays = np.ascontiguousarray(rays, np.float32)
         n = rays.shape[0]
