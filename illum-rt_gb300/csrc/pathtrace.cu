@@ -12,6 +12,8 @@
 //     a warp's lanes are still busy.
 // Both produce the same per-path results: the math is shared (pt_math.cuh) and each path's
 // random stream depends only on its index.
+#include <mutex>
+
 #include "pathtrace.hpp"
 #include "pt_math.cuh"
 #include "traverse.cuh"
@@ -501,3 +503,58 @@ int fused_blocks_per_sm(int block_threads, int stack_entries) {
 }
 
 }  // namespace grt
+
+// ---- allocation-free compaction ------------------------------------------------------------
+//
+// grt_compact_hits_static is grt_compact_hits for callers that must not allocate device
+// memory: code running while a CUDA graph is being captured (cudaMalloc is not allowed there),
+// or code embedded in a host application whose device memory is owned by its own pool. Its only
+// temporary storage, one count per 2048-hit tile, lives in the fixed array below, which every
+// GPU that loads this library holds until the process exits.
+
+namespace grt {
+namespace {
+
+constexpr uint32_t kStaticTiles = 16384;  // 64 KiB of tile counts: up to 16384 * 2048 hits
+static_assert((uint64_t)kStaticTiles * kTile == GRT_COMPACT_STATIC_MAX_HITS, "capacity mismatch");
+
+static __device__ __align__(256) uint32_t g_compact_tiles[kStaticTiles];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_tiles_mutex;
+uint32_t *g_tiles_addr[kMaxDevices] = {};
+
+// Device address of g_compact_tiles on the current device, looked up once per device. In host
+// code the symbol itself is only a host-side stand-in, never a device address.
+cudaError_t static_tiles(uint32_t **out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_tiles_mutex);
+    if (!g_tiles_addr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_compact_tiles);
+        if (e != cudaSuccess) return e;
+        g_tiles_addr[dev] = (uint32_t *)p;
+    }
+    *out = g_tiles_addr[dev];
+    return cudaSuccess;
+}
+
+}  // namespace
+}  // namespace grt
+
+extern "C" grt_status grt_compact_hits_static(const grt_hit *hits_dev, uint32_t n, uint32_t *indices_dev,
+                                              uint32_t *count_dev, grt_stream_t stream) {
+    if (!count_dev || (n && (!hits_dev || !indices_dev))) return GRT_ERR_INVALID_ARG;
+    if (n > GRT_COMPACT_STATIC_MAX_HITS) return GRT_ERR_TOO_LARGE;
+    uint32_t *tiles = nullptr;
+    cudaError_t e = grt::static_tiles(&tiles);
+    if (e == cudaSuccess) e = grt::launch_compact_hits(hits_dev, n, indices_dev, count_dev, tiles, (cudaStream_t)stream);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return GRT_ERR_CUDA;
+    }
+    return GRT_OK;
+}

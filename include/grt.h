@@ -55,7 +55,8 @@ typedef enum grt_status {
     GRT_ERR_NOT_BUILT = 6,      /* trace called before a successful build */
     GRT_ERR_TRAVERSAL = 7,      /* a kernel flagged a stack overflow or hit its step limit */
     GRT_ERR_UNKNOWN_TRACER = 8, /* grt_select_tracer: no tracer of that name */
-    GRT_ERR_NO_DEVICE = 9       /* no CUDA device of the requested ordinal */
+    GRT_ERR_NO_DEVICE = 9,      /* no CUDA device of the requested ordinal */
+    GRT_ERR_TOO_LARGE = 10      /* input exceeds the fixed capacity of grt_compact_hits_static */
 } grt_status;
 
 /* One hit record, 16 bytes, the layout of wf::cuda::tri_is (rt/cuda/base.h:32-41).
@@ -178,6 +179,22 @@ grt_status grt_check(grt_ctx *ctx, grt_stream_t stream, uint32_t timeout_ms);
  * their ray indices in increasing order and *count_dev their number. */
 grt_status grt_compact_hits(grt_ctx *ctx, const grt_hit *hits_dev, uint32_t n, uint32_t *indices_dev,
                             uint32_t *count_dev, grt_stream_t stream);
+
+/* Allocation-free variant of grt_compact_hits. It has no counterpart in the reference; it is
+ * for callers that cannot call cudaMalloc: code that runs while a CUDA graph is being captured,
+ * or a host application whose device memory belongs to its own pool. It needs no context, and
+ * its only temporary storage (one count per 2048-hit tile) is a fixed 64 KiB array in device
+ * memory that every GPU loading this library holds until the process exits. Limits:
+ *   - n at most GRT_COMPACT_STATIC_MAX_HITS; larger n returns GRT_ERR_TOO_LARGE, nothing runs;
+ *   - all calls share that one array, so calls whose kernels overlap on a GPU (for example on
+ *     two streams at once) race and give wrong results: order them on one stream;
+ *   - the first call on each device looks up the array's device address
+ *     (cudaGetSymbolAddress) with that device current; make that first call before any stream
+ *     capture begins.
+ * The array keeps the last call's tile counts; every call overwrites the counts it reads. */
+#define GRT_COMPACT_STATIC_MAX_HITS 33554432u
+grt_status grt_compact_hits_static(const grt_hit *hits_dev, uint32_t n, uint32_t *indices_dev, uint32_t *count_dev,
+                                   grt_stream_t stream);
 
 /* One shadow ray per valid hit, in ray order (the any-hit rays of the reference's direct
  * lighting, gi/direct.cpp:499-534 with rt/cuda/bounce.cu:194-196): origin = hit point moved by
