@@ -1,0 +1,107 @@
+"""Autotuner for the persistent kernels: warps per block, refill threshold and period, leaf size.
+
+For every candidate it builds the scene's BVH with that leaf size (the reference builder's
+`max_triangles_per_node`), sets the launch parameters through grt_set_tuning and times the
+fused path-tracing step (persistent primary trace + fused bounce loop) with CUDA events; the
+fastest configuration is written to tuning.json under "<GPU name>|<scene class>", where
+bench.py picks it up. Results do not depend on the launch parameters; a different leaf size
+gives a different (equally reference-built) BVH.
+
+Usage: python illum-rt_gb300/autotune.py [--quick] [--paths N]
+"""
+from __future__ import annotations
+
+import argparse
+import itertools
+import json
+import os
+import sys
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+TABLE = os.path.join(HERE, "tuning.json")
+
+
+def _load_pkg():
+    sys.path.insert(0, os.path.dirname(HERE))
+    import __graft_entry__ as ge
+    ge.load_package()
+    from illum_rt_gb300 import api, workloads
+    return api, workloads
+
+
+def time_config(rt, api, rays, hits, results, n_paths, stream, reps=3) -> float:
+    import torch
+    p = api.BatchRayTracer.pt_params(mode=api.PT_FUSED, use_graph=0)
+    best = float("inf")
+    for i in range(reps + 1):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        rt.trace(rays, hits, False, stream.cuda_stream)
+        rt.pathtrace(p, rays, hits, n_paths, results, None, stream.cuda_stream)
+        e1.record(stream)
+        e1.synchronize()
+        if i:  # the first run is a warm-up
+            best = min(best, e0.elapsed_time(e1))
+    rt.check(stream.cuda_stream)
+    return best
+
+
+def tune(quick: bool = False, n_paths: int = 4 << 20, res: int = 1024, log=print) -> dict:
+    import torch
+    api, wl = _load_pkg()
+    sc, rays_np = wl.spheres_primary(res=res)
+    rays = torch.from_numpy(rays_np).cuda()
+    hits = torch.zeros((rays.shape[0], 4), device="cuda")
+    results = torch.zeros((n_paths, 4), dtype=torch.int32, device="cuda")
+    stream = torch.cuda.Stream()
+    rt = api.BatchRayTracer(0)
+    rt.select("persistent-while-while")
+    leaf_sizes = [4] if quick else [2, 3, 4, 6, 8]
+    blocks = [128] if quick else [64, 128, 256]
+    thresholds = [12, 20, 28] if quick else [8, 12, 16, 20, 24, 28, 32]
+    periods = [1, 4] if quick else [1, 2, 4, 8]
+    best = None
+    t0 = time.time()
+    for leaf in leaf_sizes:
+        rt.build(sc.vpos, sc.tris, max_tris=leaf)
+        for bt, th, per in itertools.product(blocks, thresholds, periods):
+            rt.set_tuning(block_threads=bt, refill_threshold=th, refill_period=per, blocks_per_sm=0)
+            ms = time_config(rt, api, rays, hits, results, n_paths, stream)
+            cfg = {"max_tris": leaf, "block_threads": bt, "refill_threshold": th, "refill_period": per, "ms": ms}
+            log(json.dumps(cfg))
+            if best is None or ms < best["ms"]:
+                best = cfg
+    rt.close()
+    best["searched"] = len(leaf_sizes) * len(blocks) * len(thresholds) * len(periods)
+    best["seconds"] = round(time.time() - t0, 1)
+    return best
+
+
+def save(best: dict, gpu_name: str, scene: str = "spheres"):
+    table = {}
+    if os.path.exists(TABLE):
+        with open(TABLE) as f:
+            table = json.load(f)
+    table[f"{gpu_name}|{scene}"] = best
+    with open(TABLE, "w") as f:
+        json.dump(table, f, indent=1, sort_keys=True)
+
+
+if __name__ == "__main__":
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--quick", action="store_true")
+    ap.add_argument("--paths", type=int, default=4 << 20)
+    ap.add_argument("--out", default=None, help="also write the log of every candidate here")
+    a = ap.parse_args()
+    import torch
+    logf = open(a.out, "w") if a.out else None
+
+    def log(line):
+        print(line, flush=True)
+        if logf:
+            logf.write(line + "\n")
+
+    best = tune(quick=a.quick, n_paths=a.paths, log=log)
+    save(best, torch.cuda.get_device_name(0))
+    log("best " + json.dumps(best))

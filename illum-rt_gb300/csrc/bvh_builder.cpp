@@ -443,7 +443,7 @@ bool flatten_bvh(const ref_tree &tree, const float *vpos4, const uint32_t *tris4
         r[4] = a[0] - b[0];
         r[5] = a[1] - b[1];
         r[6] = a[2] - b[2];
-        r[7] = 0.f;
+        std::memcpy(r + 7, t + 3, 4);  // material id, for shading without a triangle fetch
         r[8] = a[0] - c[0];
         r[9] = a[1] - c[1];
         r[10] = a[2] - c[2];

@@ -44,7 +44,7 @@ bool build_reference_bvh(const float *vpos4, uint32_t nv, const uint32_t *tris4,
 // (count - 1), `first` indexing the triangle records, so leaves never need a fetch of their own.
 // Triangle record (48 bytes, three float4), in leaf order:
 //   [0] v0.xyz, w = original triangle id (int bits)
-//   [1] v0 - v1 (the a, b, c of the reference's Cramer test, libgi/intersect.h:27-29)
+//   [1] v0 - v1 (the a, b, c of the reference's Cramer test, libgi/intersect.h:27-29), w = material id
 //   [2] v0 - v2 (d, e, f, libgi/intersect.h:32-34)
 // Subtracting on the host in float gives the same bits as the reference's per-test subtraction.
 struct flat_bvh {

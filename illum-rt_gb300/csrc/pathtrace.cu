@@ -182,11 +182,25 @@ __device__ __forceinline__ void path_start(const pt_scene &ps, const pt_params_d
     rd = make_float4(dir.x, dir.y, dir.z, FLT_MAX);
 }
 
-// Consumes the closest hit of the current bounce ray (ro, rd). Returns true if the path goes
-// on, with (ro, rd) replaced by the next ray; otherwise fills `res`.
-__device__ __forceinline__ bool path_bounce(const pt_scene &ps, const pt_params_dev &pp, path_t &st, const hit_t &h,
-                                            float4 &ro, float4 &rd, grt_path_result &res) {
-    const pm::f3 o = {ro.x, ro.y, ro.z}, d = {rd.x, rd.y, rd.z};
+// Facing normal and material of a hit from its triangle record (v0, v0 - v1 with the material
+// id in w, v0 - v2): cross(v0 - v1, v0 - v2) equals cross(v1 - v0, v2 - v0) bit for bit, because
+// a rounded difference negates exactly, so this is the same normal tri_normal computes.
+__device__ __forceinline__ pm::f3 record_normal(const float4 *__restrict__ records, uint32_t rec, pm::f3 d,
+                                                uint32_t &material) {
+    const float4 p1 = __ldg(records + 3 * (size_t)rec + 1), p2 = __ldg(records + 3 * (size_t)rec + 2);
+    material = __float_as_uint(p1.w);
+    pm::f3 n = pm::normalize3(pm::cross3({p1.x, p1.y, p1.z}, {p2.x, p2.y, p2.z}));
+    if (pm::dot3(d, n) > 0.f) n = {-n.x, -n.y, -n.z};
+    return n;
+}
+
+// Consumes the closest hit of the current bounce ray (o, d). Returns true if the path goes on,
+// with (o, d) replaced by the next ray's origin and direction; otherwise fills `res`.
+// FROM_RECORD: take normal and material from the hit's triangle record instead of the
+// triangle and vertex arrays.
+template <bool FROM_RECORD>
+__device__ __forceinline__ bool path_bounce(const pt_scene &ps, const float4 *records, const pt_params_dev &pp,
+                                            path_t &st, const hit_t &h, pm::f3 &o, pm::f3 &d, grt_path_result &res) {
     if (h.t == FLT_MAX) {  // escaped: collects the sky
         st.digest = pm::digest_word(st.digest, pm::kMissWord);
         res = {pm::mul(st.thr, pm::sky(d)), st.bounce, st.last_ref, st.digest};
@@ -195,7 +209,7 @@ __device__ __forceinline__ bool path_bounce(const pt_scene &ps, const pt_params_
     st.digest = pm::digest_word(pm::digest_word(st.digest, h.ref), __float_as_uint(h.t));
     st.last_ref = h.ref;
     uint32_t m;
-    const pm::f3 n = tri_normal(ps, h.ref, d, m);
+    const pm::f3 n = FROM_RECORD ? record_normal(records, h.rec, d, m) : tri_normal(ps, h.ref, d, m);
     st.thr = pm::mul(st.thr, albedo_of(ps, m));
     if (st.bounce >= pp.max_bounces) {
         res = {0.f, st.bounce, st.last_ref, st.digest};
@@ -208,11 +222,9 @@ __device__ __forceinline__ bool path_bounce(const pt_scene &ps, const pt_params_
         }
         st.thr = pm::div(st.thr, pp.rr_continue);
     }
-    const pm::f3 org = pm::offset_hit_point(o, d, h.t, n, pp.eps);
+    o = pm::offset_hit_point(o, d, h.t, n, pp.eps);
     const float u0 = st.rng.uniform(), u1 = st.rng.uniform();
-    const pm::f3 dir = pm::align(pm::cosine_sample_hemisphere(u0, u1), n);
-    ro = make_float4(org.x, org.y, org.z, pp.eps);
-    rd = make_float4(dir.x, dir.y, dir.z, FLT_MAX);
+    d = pm::align(pm::cosine_sample_hemisphere(u0, u1), n);
     ++st.bounce;
     return true;
 }
@@ -231,16 +243,16 @@ __device__ __forceinline__ void clear_unused(grt_hit *bounce_hits, const pt_para
             reinterpret_cast<float4 *>(bounce_hits)[(size_t)p * pp.max_bounces + k] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
-__device__ __forceinline__ ray_t to_ray(const float4 &a, const float4 &d) {
+__device__ __forceinline__ ray_t make_ray(pm::f3 o, pm::f3 d, float tmin, float tmax) {
     ray_t r;
-    r.ox = a.x;
-    r.oy = a.y;
-    r.oz = a.z;
-    r.tmin = a.w;
+    r.ox = o.x;
+    r.oy = o.y;
+    r.oz = o.z;
+    r.tmin = tmin;
     r.dx = d.x;
     r.dy = d.y;
     r.dz = d.z;
-    r.tmax = d.w;
+    r.tmax = tmax;
     r.ix = __fdiv_rn(1.0f, d.x);
     r.iy = __fdiv_rn(1.0f, d.y);
     r.iz = __fdiv_rn(1.0f, d.z);
@@ -302,10 +314,13 @@ __global__ void k_wf_shade(pt_scene ps, pt_params_dev pp, const uint32_t *__rest
             ro = rays_in[2 * (size_t)k];
             rd = rays_in[2 * (size_t)k + 1];
             const float4 hv = reinterpret_cast<const float4 *>(hits)[k];
-            hit_t h = {hv.x, hv.y, hv.z, __float_as_uint(hv.w)};
+            hit_t h = {hv.x, hv.y, hv.z, __float_as_uint(hv.w), 0u};
             record_bounce(bounce_hits, pp, p, st.bounce, h);
             grt_path_result res;
-            go_on = path_bounce(ps, pp, st, h, ro, rd, res);
+            pm::f3 o = {ro.x, ro.y, ro.z}, d = {rd.x, rd.y, rd.z};
+            go_on = path_bounce<false>(ps, nullptr, pp, st, h, o, d, res);
+            ro = make_float4(o.x, o.y, o.z, pp.eps);
+            rd = make_float4(d.x, d.y, d.z, FLT_MAX);
             if (go_on) {
                 states[p] = {st.rng.state, st.rng.inc, st.thr, st.digest, st.bounce, st.last_ref};
             } else {
@@ -331,6 +346,12 @@ __global__ void k_wf_shade(pt_scene ps, pt_params_dev pp, const uint32_t *__rest
 
 // ---- fused persistent form ----------------------------------------------------------------
 
+// Each warp alternates between two phases. In the traversal phase the lanes that hold a ray
+// run trav_iter; a lane whose ray ends keeps its closest hit and waits. When fewer than
+// `refill_threshold` lanes are still traversing, the warp enters the shade phase: all waiting
+// lanes shade their hit together (Russian roulette, next bounce direction) and go back to
+// traversal, or finish their path and take a new one from the global path counter. Shading and
+// path set-up therefore run warp-coherently instead of one lane at a time.
 template <int STACK>
 __global__ void __launch_bounds__(256) k_pt_fused(dev_scene sc, pt_scene ps, pt_params_dev pp,
                                                   const float4 *__restrict__ prim_rays,
@@ -348,19 +369,37 @@ __global__ void __launch_bounds__(256) k_pt_fused(dev_scene sc, pt_scene ps, pt_
     trav_t s;
     ray_t r;
     path_t st;
-    float4 ro, rd;
     uint32_t p = 0;
-    bool have = false, plain = false, exhausted = false;
+    bool tracing = false;   // the lane's ray is being traversed
+    bool waiting = false;   // the lane's ray has ended and its hit waits to be shaded
+    bool plain = false, exhausted = false;
     for (;;) {
+        // shade phase: waiting lanes consume their hit
+        if (waiting) {
+            waiting = false;
+            record_bounce(bounce_hits, pp, p, st.bounce, s.hit);
+            pm::f3 o = {r.ox, r.oy, r.oz}, d = {r.dx, r.dy, r.dz};
+            grt_path_result res;
+            if (path_bounce<true>(ps, sc.records, pp, st, s.hit, o, d, res)) {
+                r = make_ray(o, d, pp.eps, FLT_MAX);
+                trav_init(s, sc);
+                plain = sc.finite && ray_is_plain(r);
+                tracing = true;
+            } else {
+                results[p] = res;
+                clear_unused(bounce_hits, pp, p, st.bounce);
+            }
+        }
+        // refill phase: lanes without a path take the next ones
         if (!exhausted) {
-            const unsigned need = __ballot_sync(kFull, !have);
+            const unsigned need = __ballot_sync(kFull, !tracing);
             if (need) {
                 const unsigned cnt = __popc(need);
                 unsigned base = 0;
                 if (lane == 0) base = atomicAdd(counter, cnt);
                 base = __shfl_sync(kFull, base, 0);
                 if (base + cnt >= n_paths) exhausted = true;
-                if (!have) {
+                if (!tracing) {
                     const uint32_t my = base + __popc(need & lanes_below);
                     if (my < n_paths) {
                         p = my;
@@ -368,43 +407,36 @@ __global__ void __launch_bounds__(256) k_pt_fused(dev_scene sc, pt_scene ps, pt_
                             results[p] = {0.f, 0u, pm::kMissWord, pm::kDigestSeed};
                             clear_unused(bounce_hits, pp, p, 0);
                         } else {
+                            float4 ro, rd;
                             path_start(ps, pp, p, prim_rays, prim_hits, hit_list, nl, st, ro, rd);
-                            r = to_ray(ro, rd);
+                            r = make_ray({ro.x, ro.y, ro.z}, {rd.x, rd.y, rd.z}, ro.w, rd.w);
                             trav_init(s, sc);
                             plain = sc.finite && ray_is_plain(r);
-                            have = true;
+                            tracing = true;
                         }
                     }
                 }
             }
         }
-        if (__ballot_sync(kFull, have) == 0) {
+        if (__ballot_sync(kFull, tracing) == 0) {
             if (exhausted) break;
             continue;
         }
+        // traversal phase
         for (int it = 1;; ++it) {
-            if (have) {
+            if (tracing) {
                 if (plain)
-                    trav_step<STACK, false, true>(s, sc, r, stk, stride, err);
+                    trav_iter<STACK, false, true>(s, sc, r, stk, stride, err);
                 else
-                    trav_step<STACK, false, false>(s, sc, r, stk, stride, err);
+                    trav_iter<STACK, false, false>(s, sc, r, stk, stride, err);
                 if (s.done) {
-                    record_bounce(bounce_hits, pp, p, st.bounce, s.hit);
-                    grt_path_result res;
-                    if (path_bounce(ps, pp, st, s.hit, ro, rd, res)) {
-                        r = to_ray(ro, rd);
-                        trav_init(s, sc);
-                        plain = sc.finite && ray_is_plain(r);
-                    } else {
-                        results[p] = res;
-                        clear_unused(bounce_hits, pp, p, st.bounce);
-                        have = false;
-                    }
+                    tracing = false;
+                    waiting = true;
                 }
             }
             if (it % refill_period == 0) {
-                const int busy = __popc(__ballot_sync(kFull, have));
-                if (busy == 0 || (!exhausted && busy < refill_threshold)) break;
+                const int busy = __popc(__ballot_sync(kFull, tracing));
+                if (busy < refill_threshold) break;
             }
         }
     }

@@ -8,7 +8,7 @@
 //     dynamicwhilewhile_trace, rt/cuda/trace-kernels.cu:702-876, restructured so that every
 //     ballot is taken by all 32 lanes at a uniform point of the loop, and the counter is reset
 //     by the host before the launch instead of by the kernel's own threads).
-// Both walk the BVH with trav_step (traverse.cuh), so their results are identical to each
+// Both walk the BVH with trav_iter (traverse.cuh), so their results are identical to each
 // other and to the reference CPU tracer.
 #include "traverse.cuh"
 
@@ -32,9 +32,9 @@ __global__ void __launch_bounds__(256) k_trace_plain(const float4 *__restrict__ 
     int *stk = s_stack + threadIdx.x;
     const int stride = blockDim.x;
     if (sc.finite && ray_is_plain(r)) {
-        while (!s.done) trav_step<STACK, ANY, true, COUNT>(s, sc, r, stk, stride, err);
+        while (!s.done) trav_iter<STACK, ANY, true, COUNT>(s, sc, r, stk, stride, err);
     } else {
-        while (!s.done) trav_step<STACK, ANY, false, COUNT>(s, sc, r, stk, stride, err);
+        while (!s.done) trav_iter<STACK, ANY, false, COUNT>(s, sc, r, stk, stride, err);
     }
     store_hit<ANY>(hits, i, s);
     if (COUNT) {
@@ -87,13 +87,13 @@ __global__ void __launch_bounds__(256) k_trace_persistent(const float4 *__restri
             if (exhausted) break;
             continue;
         }
-        // traverse; every `refill_period` steps the warp counts its busy lanes
+        // traverse; every `refill_period` iterations the warp counts its busy lanes
         for (int it = 1;; ++it) {
             if (have) {
                 if (plain)
-                    trav_step<STACK, ANY, true>(s, sc, r, stk, stride, err);
+                    trav_iter<STACK, ANY, true>(s, sc, r, stk, stride, err);
                 else
-                    trav_step<STACK, ANY, false>(s, sc, r, stk, stride, err);
+                    trav_iter<STACK, ANY, false>(s, sc, r, stk, stride, err);
                 if (s.done) {
                     store_hit<ANY>(hits, idx, s);
                     have = false;

@@ -25,6 +25,7 @@ struct ray_t {
 struct hit_t {
     float t, b, g;
     uint32_t ref;
+    uint32_t rec;  // triangle record of the hit (device layout index)
 };
 
 __device__ __forceinline__ ray_t load_ray(const float4 *__restrict__ rays, uint32_t i) {
@@ -143,20 +144,24 @@ __device__ __forceinline__ void trav_init(trav_t &s, const dev_scene &sc) {
     s.hit.b = 0.f;
     s.hit.g = 0.f;
     s.hit.ref = 0u;
+    s.hit.rec = 0u;
 }
 
-// One traversal step: one inner node (two box tests) or one leaf (its triangle tests).
-// Mirrors one pop of the reference loop (rt/cpu/bvh2.cpp:82-127 / 147-182): the near child is
-// kept in `cur` instead of being pushed and popped straight back.
+// One traversal iteration in the while-while order: inner nodes (two box tests each) until the
+// ray reaches a leaf or ends, then that leaf's triangle tests. Per ray this is exactly the
+// reference's sequence of pops (rt/cpu/bvh2.cpp:82-127 / 147-182): the near child is kept in
+// `cur` instead of being pushed and popped straight back, and a leaf is tested when it would
+// be popped. Grouping a warp's node visits in one loop and its leaf tests after it keeps the
+// lanes on the same code path far more often than one node-or-leaf per iteration would.
 template <int STACK, bool ANY, bool PLAIN, bool COUNT = false>
-__device__ __forceinline__ void trav_step(trav_t &s, const dev_scene &sc, const ray_t &r, int *stk, int stride,
+__device__ __forceinline__ void trav_iter(trav_t &s, const dev_scene &sc, const ray_t &r, int *stk, int stride,
                                           unsigned *err) {
-    if (++s.steps > kStepLimit) {
-        atomicOr(err, ERR_STEP_LIMIT);
-        s.done = true;
-        return;
-    }
-    if (s.cur >= 0) {
+    while (s.cur >= 0) {
+        if (++s.steps > kStepLimit) {
+            atomicOr(err, ERR_STEP_LIMIT);
+            s.done = true;
+            return;
+        }
         if (COUNT) ++s.n_inner;
         const float4 *np = sc.nodes + 4 * (size_t)s.cur;
         const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3);
@@ -178,30 +183,39 @@ __device__ __forceinline__ void trav_step(trav_t &s, const dev_scene &sc, const 
             stk[s.sp * stride] = left_first ? cr : cl;
             ++s.sp;
             s.cur = left_first ? cl : cr;
-            return;
-        }
-        if (hl || hr) {
+        } else if (hl || hr) {
             s.cur = hl ? cl : cr;
-            return;
+        } else {
+            if (s.sp == 0) {
+                s.done = true;
+                return;
+            }
+            --s.sp;
+            s.cur = stk[s.sp * stride];
         }
-    } else {
-        uint32_t first, count;
-        leaf_range(s.cur, first, count);
-        const float4 *rp = sc.records + 3 * (size_t)first;
-        for (uint32_t k = 0; k < count; ++k) {
-            if (COUNT) ++s.n_tri;
-            const float4 p0 = __ldg(rp + 3 * k), p1 = __ldg(rp + 3 * k + 1), p2 = __ldg(rp + 3 * k + 2);
-            float t, b, g;
-            if (tri_test(p0, p1, p2, r, t, b, g) && (ANY || t < s.hit.t)) {
-                s.hit.t = t;
-                s.hit.b = b;
-                s.hit.g = g;
-                s.hit.ref = __float_as_uint(p0.w);
-                if (ANY) {
-                    s.found = true;
-                    s.done = true;
-                    return;
-                }
+    }
+    if (++s.steps > kStepLimit) {
+        atomicOr(err, ERR_STEP_LIMIT);
+        s.done = true;
+        return;
+    }
+    uint32_t first, count;
+    leaf_range(s.cur, first, count);
+    const float4 *rp = sc.records + 3 * (size_t)first;
+    for (uint32_t k = 0; k < count; ++k) {
+        if (COUNT) ++s.n_tri;
+        const float4 p0 = __ldg(rp + 3 * k), p1 = __ldg(rp + 3 * k + 1), p2 = __ldg(rp + 3 * k + 2);
+        float t, b, g;
+        if (tri_test(p0, p1, p2, r, t, b, g) && (ANY || t < s.hit.t)) {
+            s.hit.t = t;
+            s.hit.b = b;
+            s.hit.g = g;
+            s.hit.ref = __float_as_uint(p0.w);
+            s.hit.rec = first + k;
+            if (ANY) {
+                s.found = true;
+                s.done = true;
+                return;
             }
         }
     }
