@@ -47,6 +47,8 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="run one tuned and one plain step with 1,048,576 paths and exit (for ncu captures)")
     return ap.parse_args()
 
 
@@ -148,12 +150,13 @@ class Step:
         self.n_primary = rays.shape[0]
         self.rt = api.BatchRayTracer(device)
         self.build_info = self.rt.build(sc.vpos, sc.tris, max_tris=tuning.get("max_tris", 4))
-        self.rt_plain = api.BatchRayTracer(device)  # the reference's CUDA defaults, untuned
+        self.rt_plain = api.BatchRayTracer(device)  # the reference's CUDA build defaults, untuned
         self.rt_plain.build(sc.vpos, sc.tris)
         self.rt_plain.select("while-while")
-        self.rt.select("persistent-while-while")
+        self.rt.select(tuning.get("tracer", "persistent-while-while"))
         kw = {k: v for k, v in tuning.items() if k in ("block_threads", "blocks_per_sm", "refill_threshold",
                                                          "refill_period", "stack_entries")}
+        self.tracer = tuning.get("tracer", "persistent-while-while")
         if kw:
             self.rt.set_tuning(**kw)
         self.dev = torch.device("cuda", device)
@@ -271,6 +274,16 @@ def run_gb300(args):
     tuning = load_tuning(gpu_name)
     step = Step(api, wl, local, tuning)
 
+    # the plain baseline runs in whichever loop order is faster for it (one thread per ray)
+    plain_times = {}
+    for order in ("while-while", "if-if"):
+        step.rt_plain.select(order)
+        for _ in range(2):
+            step.plain()
+        plain_times[order] = statistics.median(time_steps(step, step.plain, 3)[0])
+    plain_order = min(plain_times, key=plain_times.get)
+    step.rt_plain.select(plain_order)
+
     # rays per step of each form (identical work: same paths, same bounces)
     step.plain()
     step.rt_plain.check(step.sp)
@@ -343,7 +356,8 @@ def run_gb300(args):
                    "l2": "flushed between timed steps (512 MB write)", "parallelism": f"replicas x{world}",
                    "tuning": tuning or "defaults"},
         "plain_wavefront": {"value": round(plain_value, 1), "ms_per_step": round(statistics.mean(plain_ms), 4),
-                            "rays_per_step": rays_plain},
+                            "rays_per_step": rays_plain, "loop_order": plain_order,
+                            "order_ms": {k: round(v, 4) for k, v in plain_times.items()}},
         "speedup_vs_plain": round(value / plain_value, 3),
         "e2e": {"value": round(e2e_value, 1), "unit": "Mrays/s", "ms_per_step": round(statistics.mean(e2e_ms), 4),
                 "h2d_bytes_per_step": int(step.n_primary * 32), "d2h_bytes_per_step": int(N_PATHS * 16)},
@@ -405,9 +419,30 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_profile_case():
+    """One tuned step, then one plain step (no graphs, 1,048,576 paths): a small case whose
+    launches ncu can capture one by one."""
+    import torch
+    import __graft_entry__ as ge
+    global N_PATHS
+    N_PATHS = 1 << 20
+    ge.load_package()
+    from illum_rt_gb300 import api, workloads as wl
+    step = Step(api, wl, 0, load_tuning(torch.cuda.get_device_name(0)))
+    step.p_fused.use_graph = 0
+    step.p_plain.use_graph = 0
+    step.tuned()
+    step.plain()
+    step.rt.check(step.sp)
+    step.rt_plain.check(step.sp)
+    print(json.dumps({"profile_case": "ok", "paths": N_PATHS, "rays": rays_in_results(step)}))
+
+
 def main():
     args = parse_args()
-    if args.impl == "reference":
+    if args.profile_case:
+        run_profile_case()
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gb300(args)

@@ -1,4 +1,5 @@
-"""Autotuner for the persistent kernels: warps per block, refill threshold and period, leaf size.
+"""Autotuner for the persistent kernels: loop order, warps per block, refill threshold and
+period, leaf size.
 
 For every candidate it builds the scene's BVH with that leaf size (the reference builder's
 `max_triangles_per_node`), sets the launch parameters through grt_set_tuning and times the
@@ -56,7 +57,7 @@ def tune(quick: bool = False, n_paths: int = 4 << 20, res: int = 1024, log=print
     results = torch.zeros((n_paths, 4), dtype=torch.int32, device="cuda")
     stream = torch.cuda.Stream()
     rt = api.BatchRayTracer(0)
-    rt.select("persistent-while-while")
+    orders = ["persistent-while-while"] if quick else ["persistent-while-while", "persistent-if-if"]
     leaf_sizes = [4] if quick else [2, 3, 4, 6, 8]
     blocks = [128] if quick else [64, 128, 256]
     thresholds = [12, 20, 28] if quick else [8, 12, 16, 20, 24, 28, 32]
@@ -65,15 +66,17 @@ def tune(quick: bool = False, n_paths: int = 4 << 20, res: int = 1024, log=print
     t0 = time.time()
     for leaf in leaf_sizes:
         rt.build(sc.vpos, sc.tris, max_tris=leaf)
-        for bt, th, per in itertools.product(blocks, thresholds, periods):
+        for tracer, bt, th, per in itertools.product(orders, blocks, thresholds, periods):
+            rt.select(tracer)
             rt.set_tuning(block_threads=bt, refill_threshold=th, refill_period=per, blocks_per_sm=0)
             ms = time_config(rt, api, rays, hits, results, n_paths, stream)
-            cfg = {"max_tris": leaf, "block_threads": bt, "refill_threshold": th, "refill_period": per, "ms": ms}
+            cfg = {"tracer": tracer, "max_tris": leaf, "block_threads": bt, "refill_threshold": th,
+                   "refill_period": per, "ms": ms}
             log(json.dumps(cfg))
             if best is None or ms < best["ms"]:
                 best = cfg
     rt.close()
-    best["searched"] = len(leaf_sizes) * len(blocks) * len(thresholds) * len(periods)
+    best["searched"] = len(orders) * len(leaf_sizes) * len(blocks) * len(thresholds) * len(periods)
     best["seconds"] = round(time.time() - t0, 1)
     return best
 

@@ -199,9 +199,9 @@ void grt_host_bvh_free(grt_host_bvh *h) { delete h; }
 grt_status grt_select_tracer(grt_ctx *c, const char *name) {
     if (!c || !name) return GRT_ERR_INVALID_ARG;
     std::string n(name);
-    if (n == "default") n = kTracerNames[0];
-    for (int i = 0; i < 2; ++i)
-        if (n == kTracerNames[i]) {
+    if (n == "default") n = kTracers[0].name;
+    for (int i = 0; i < kNumTracers; ++i)
+        if (n == kTracers[i].name) {
             c->tracer = i;
             return GRT_OK;
         }
@@ -235,7 +235,7 @@ grt_status grt_trace(grt_ctx *c, const float *rays_dev, grt_hit *hits_dev, uint3
     device_guard g(c->device);
     grt::launch_params lp = params_for(c, any_hit != 0);
     cudaError_t e;
-    if (c->tracer == 1)
+    if (kTracers[c->tracer].persistent)
         e = grt::launch_trace_persistent(c->sc, (const float4 *)rays_dev, hits_dev, n, any_hit != 0, lp, c->d_err,
                                          c->d_counter, (cudaStream_t)stream);
     else

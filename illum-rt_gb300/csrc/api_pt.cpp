@@ -187,7 +187,7 @@ grt_status grt_pathtrace(grt_ctx *c, const grt_pt_params *params, const float *p
     launch_params lp_trace = params_for(c, false);  // one-thread-per-ray kernel of the wavefront form
     launch_params lp = lp_trace;
     lp.grid_blocks = (c->tuning.blocks_per_sm > 0 ? c->tuning.blocks_per_sm
-                                                  : fused_blocks_per_sm(lp.block_threads, lp.stack_entries)) *
+                                                  : fused_blocks_per_sm(lp.block_threads, lp.stack_entries, lp.order)) *
                      c->num_sms;
     cudaStream_t st = (cudaStream_t)stream;
     if (!p.use_graph) {

@@ -21,7 +21,7 @@ struct grt_ctx {
     void *d_nodes = nullptr, *d_recs = nullptr, *d_vpos = nullptr, *d_tris = nullptr;
     uint32_t nv = 0, nt = 0, depth = 0;
     grt_bvh_stats stats{};
-    int tracer = 0;  // 0 while-while, 1 persistent-while-while
+    int tracer = 0;  // index into kTracers
     grt_tuning tuning{};
     unsigned *d_err = nullptr;      // error bits ORed in by kernels
     unsigned *d_counter = nullptr;  // ray counter of the persistent kernel
@@ -79,7 +79,18 @@ inline double ms_since(std::chrono::steady_clock::time_point t0) {
     return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
-inline const char *kTracerNames[] = {"while-while", "persistent-while-while"};
+// The tracers a context can select (the reference's `raytracer` names for the same loop
+// shapes, rt/cuda/platform.cpp:34-56).
+struct tracer_kind {
+    const char *name;
+    bool persistent;
+    int order;
+};
+inline const tracer_kind kTracers[] = {{"while-while", false, WHILE_WHILE},
+                                       {"persistent-while-while", true, WHILE_WHILE},
+                                       {"if-if", false, IF_IF},
+                                       {"persistent-if-if", true, IF_IF}};
+inline const int kNumTracers = 4;
 
 inline launch_params params_for(grt_ctx *c, bool any_hit) {
     grt::launch_params lp{};
@@ -90,9 +101,11 @@ inline launch_params params_for(grt_ctx *c, bool any_hit) {
     lp.refill_threshold = t.refill_threshold > 0 ? t.refill_threshold : 20;
     lp.refill_period = t.refill_period > 0 ? t.refill_period : 4;
     lp.counters = c->d_trav_counters;
-    if (c->tracer == 1) {
+    lp.order = kTracers[c->tracer].order;
+    if (kTracers[c->tracer].persistent) {
         int per_sm = t.blocks_per_sm > 0 ? t.blocks_per_sm
-                                         : grt::persistent_blocks_per_sm(lp.block_threads, lp.stack_entries, any_hit);
+                                         : grt::persistent_blocks_per_sm(lp.block_threads, lp.stack_entries, any_hit,
+                                                                         lp.order);
         lp.grid_blocks = per_sm * c->num_sms;
     }
     return lp;

@@ -30,12 +30,17 @@ static const int kStackLarge = 64;
 // kernel given a corrupted tree.
 static const uint32_t kStepLimit = 1u << 26;
 
+// Loop orders of the traversal kernels (traverse.cuh): one node or leaf per iteration, or
+// inner nodes until a leaf and then that leaf.
+enum loop_order : int { IF_IF = 0, WHILE_WHILE = 1 };
+
 struct launch_params {
     int block_threads;
     int grid_blocks;        // persistent kernels: total resident blocks
     int refill_threshold;
     int refill_period;
     int stack_entries;
+    int order;                     // loop_order
     unsigned long long *counters;  // one-thread-per-ray kernel: rays, inner nodes, triangle tests (or null)
 };
 
@@ -53,6 +58,6 @@ cudaError_t launch_trace_persistent(const dev_scene &sc, const float4 *rays, grt
 cudaError_t prepare_trace_kernels();
 
 // Occupancy of the persistent kernel for a block size and stack variant (blocks per SM).
-int persistent_blocks_per_sm(int block_threads, int stack_entries, bool any_hit);
+int persistent_blocks_per_sm(int block_threads, int stack_entries, bool any_hit, int order);
 
 }  // namespace grt

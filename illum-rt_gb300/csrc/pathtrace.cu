@@ -352,7 +352,7 @@ __global__ void k_wf_shade(pt_scene ps, pt_params_dev pp, const uint32_t *__rest
 // lanes shade their hit together (Russian roulette, next bounce direction) and go back to
 // traversal, or finish their path and take a new one from the global path counter. Shading and
 // path set-up therefore run warp-coherently instead of one lane at a time.
-template <int STACK>
+template <int ORDER, int STACK>
 __global__ void __launch_bounds__(256) k_pt_fused(dev_scene sc, pt_scene ps, pt_params_dev pp,
                                                   const float4 *__restrict__ prim_rays,
                                                   const grt_hit *__restrict__ prim_hits,
@@ -426,9 +426,9 @@ __global__ void __launch_bounds__(256) k_pt_fused(dev_scene sc, pt_scene ps, pt_
         for (int it = 1;; ++it) {
             if (tracing) {
                 if (plain)
-                    trav_iter<STACK, false, true>(s, sc, r, stk, stride, err);
+                    trav_advance<ORDER, STACK, false, true>(s, sc, r, stk, stride, err);
                 else
-                    trav_iter<STACK, false, false>(s, sc, r, stk, stride, err);
+                    trav_advance<ORDER, STACK, false, false>(s, sc, r, stk, stride, err);
                 if (s.done) {
                     tracing = false;
                     waiting = true;
@@ -442,13 +442,13 @@ __global__ void __launch_bounds__(256) k_pt_fused(dev_scene sc, pt_scene ps, pt_
     }
 }
 
-template <int STACK>
+template <int ORDER, int STACK>
 cudaError_t fused_launch(const dev_scene &sc, const pt_scene &ps, const pt_params_dev &pp, const float4 *prim_rays,
                          const grt_hit *prim_hits, const uint32_t *hit_list, const uint32_t *n_list, uint32_t n_paths,
                          grt_path_result *results, grt_hit *bounce_hits, const launch_params &lp, unsigned *err,
                          unsigned *counter, cudaStream_t st) {
     const size_t smem = (size_t)STACK * lp.block_threads * sizeof(int);
-    auto kern = k_pt_fused<STACK>;
+    auto kern = k_pt_fused<ORDER, STACK>;
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
     kern<<<lp.grid_blocks, lp.block_threads, smem, st>>>(sc, ps, pp, prim_rays, prim_hits, hit_list, n_list, n_paths,
@@ -509,27 +509,31 @@ cudaError_t launch_fused(const dev_scene &sc, const pt_scene &ps, const pt_param
                          grt_path_result *results, grt_hit *bounce_hits, const launch_params &lp, unsigned *err,
                          unsigned *counter, cudaStream_t st) {
     if (n_paths == 0) return cudaSuccess;
-    if (lp.stack_entries <= kStackSmall)
-        return fused_launch<kStackSmall>(sc, ps, pp, prim_rays, prim_hits, hit_list, n_list, n_paths, results,
-                                         bounce_hits, lp, err, counter, st);
-    return fused_launch<kStackLarge>(sc, ps, pp, prim_rays, prim_hits, hit_list, n_list, n_paths, results, bounce_hits,
-                                     lp, err, counter, st);
+    const bool small = lp.stack_entries <= kStackSmall;
+    auto f = lp.order == WHILE_WHILE ? (small ? fused_launch<WHILE_WHILE, kStackSmall> : fused_launch<WHILE_WHILE, kStackLarge>)
+                                     : (small ? fused_launch<IF_IF, kStackSmall> : fused_launch<IF_IF, kStackLarge>);
+    return f(sc, ps, pp, prim_rays, prim_hits, hit_list, n_list, n_paths, results, bounce_hits, lp, err, counter, st);
 }
 
 cudaError_t prepare_pt_kernels() {
     const int bytes = kStackLarge * 256 * (int)sizeof(int);
-    for (const void *f : {(const void *)k_pt_fused<kStackSmall>, (const void *)k_pt_fused<kStackLarge>}) {
+    for (const void *f : {(const void *)k_pt_fused<IF_IF, kStackSmall>, (const void *)k_pt_fused<IF_IF, kStackLarge>,
+                          (const void *)k_pt_fused<WHILE_WHILE, kStackSmall>,
+                          (const void *)k_pt_fused<WHILE_WHILE, kStackLarge>}) {
         cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
 }
 
-int fused_blocks_per_sm(int block_threads, int stack_entries) {
+int fused_blocks_per_sm(int block_threads, int stack_entries, int order) {
     int blocks = 0;
     const bool small = stack_entries <= kStackSmall;
     const size_t smem = (size_t)(small ? kStackSmall : kStackLarge) * block_threads * sizeof(int);
-    const void *fn = small ? (const void *)k_pt_fused<kStackSmall> : (const void *)k_pt_fused<kStackLarge>;
+    const void *fn = order == WHILE_WHILE
+                         ? (small ? (const void *)k_pt_fused<WHILE_WHILE, kStackSmall>
+                                  : (const void *)k_pt_fused<WHILE_WHILE, kStackLarge>)
+                         : (small ? (const void *)k_pt_fused<IF_IF, kStackSmall> : (const void *)k_pt_fused<IF_IF, kStackLarge>);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, block_threads, smem) != cudaSuccess) return 1;
     return blocks > 0 ? blocks : 1;
 }

@@ -1,15 +1,16 @@
 // Closest-hit / any-hit traversal kernels for sm_103a.
 //
-// Two tracers replace the reference's CUDA variants (rt/cuda/trace-kernels.cu):
-//   * k_trace_plain  — "while-while": one thread per ray, the wavefront baseline
-//     (the role of whilewhile_trace, rt/cuda/trace-kernels.cu:292-316);
+// Two kernel shapes replace the reference's CUDA variants (rt/cuda/trace-kernels.cu), each in
+// the if-if and the while-while loop order (traverse.cuh):
+//   * k_trace_plain — one thread per ray, the wavefront baseline (the role of ifif_trace and
+//     whilewhile_trace, rt/cuda/trace-kernels.cu:238-316);
 //   * k_trace_persistent — persistent warps that refill lanes whose ray finished from a global
 //     ray counter whenever fewer than `refill_threshold` lanes are still busy (the idea of
 //     dynamicwhilewhile_trace, rt/cuda/trace-kernels.cu:702-876, restructured so that every
 //     ballot is taken by all 32 lanes at a uniform point of the loop, and the counter is reset
 //     by the host before the launch instead of by the kernel's own threads).
-// Both walk the BVH with trav_iter (traverse.cuh), so their results are identical to each
-// other and to the reference CPU tracer.
+// All of them visit each ray's nodes in the reference's order, so their results are identical
+// to each other and to the reference CPU tracer.
 #include "traverse.cuh"
 
 namespace grt {
@@ -18,7 +19,7 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 
-template <int STACK, bool ANY, bool COUNT>
+template <int ORDER, int STACK, bool ANY, bool COUNT>
 __global__ void __launch_bounds__(256) k_trace_plain(const float4 *__restrict__ rays, grt_hit *__restrict__ hits,
                                                      uint32_t n, const uint32_t *__restrict__ n_dev, dev_scene sc,
                                                      unsigned *err, unsigned long long *counters) {
@@ -32,9 +33,9 @@ __global__ void __launch_bounds__(256) k_trace_plain(const float4 *__restrict__ 
     int *stk = s_stack + threadIdx.x;
     const int stride = blockDim.x;
     if (sc.finite && ray_is_plain(r)) {
-        while (!s.done) trav_iter<STACK, ANY, true, COUNT>(s, sc, r, stk, stride, err);
+        while (!s.done) trav_advance<ORDER, STACK, ANY, true, COUNT>(s, sc, r, stk, stride, err);
     } else {
-        while (!s.done) trav_iter<STACK, ANY, false, COUNT>(s, sc, r, stk, stride, err);
+        while (!s.done) trav_advance<ORDER, STACK, ANY, false, COUNT>(s, sc, r, stk, stride, err);
     }
     store_hit<ANY>(hits, i, s);
     if (COUNT) {
@@ -44,7 +45,7 @@ __global__ void __launch_bounds__(256) k_trace_plain(const float4 *__restrict__ 
     }
 }
 
-template <int STACK, bool ANY>
+template <int ORDER, int STACK, bool ANY>
 __global__ void __launch_bounds__(256) k_trace_persistent(const float4 *__restrict__ rays, grt_hit *__restrict__ hits,
                                                           uint32_t n, dev_scene sc, unsigned *err,
                                                           unsigned *counter, int refill_threshold, int refill_period) {
@@ -91,9 +92,9 @@ __global__ void __launch_bounds__(256) k_trace_persistent(const float4 *__restri
         for (int it = 1;; ++it) {
             if (have) {
                 if (plain)
-                    trav_iter<STACK, ANY, true>(s, sc, r, stk, stride, err);
+                    trav_advance<ORDER, STACK, ANY, true>(s, sc, r, stk, stride, err);
                 else
-                    trav_iter<STACK, ANY, false>(s, sc, r, stk, stride, err);
+                    trav_advance<ORDER, STACK, ANY, false>(s, sc, r, stk, stride, err);
                 if (s.done) {
                     store_hit<ANY>(hits, idx, s);
                     have = false;
@@ -107,83 +108,94 @@ __global__ void __launch_bounds__(256) k_trace_persistent(const float4 *__restri
     }
 }
 
-template <int STACK, bool ANY>
+template <int ORDER, int STACK, bool ANY>
 cudaError_t plain_launch(const dev_scene &sc, const float4 *rays, grt_hit *hits, uint32_t n, const uint32_t *n_dev,
                          const launch_params &lp, unsigned *err, cudaStream_t st) {
     const int bt = lp.block_threads;
     const size_t smem = (size_t)STACK * bt * sizeof(int);
     const uint32_t blocks = (n + bt - 1) / bt;
     if (lp.counters)
-        k_trace_plain<STACK, ANY, true><<<blocks, bt, smem, st>>>(rays, hits, n, n_dev, sc, err, lp.counters);
+        k_trace_plain<ORDER, STACK, ANY, true><<<blocks, bt, smem, st>>>(rays, hits, n, n_dev, sc, err, lp.counters);
     else
-        k_trace_plain<STACK, ANY, false><<<blocks, bt, smem, st>>>(rays, hits, n, n_dev, sc, err, nullptr);
+        k_trace_plain<ORDER, STACK, ANY, false><<<blocks, bt, smem, st>>>(rays, hits, n, n_dev, sc, err, nullptr);
     return cudaGetLastError();
 }
 
-template <int STACK, bool ANY>
+template <int ORDER, int STACK, bool ANY>
 cudaError_t persistent_launch(const dev_scene &sc, const float4 *rays, grt_hit *hits, uint32_t n,
                               const launch_params &lp, unsigned *err, unsigned *counter, cudaStream_t st) {
     const int bt = lp.block_threads;
     const size_t smem = (size_t)STACK * bt * sizeof(int);
-    auto kern = k_trace_persistent<STACK, ANY>;
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
-    kern<<<lp.grid_blocks, bt, smem, st>>>(rays, hits, n, sc, err, counter, lp.refill_threshold, lp.refill_period);
+    k_trace_persistent<ORDER, STACK, ANY><<<lp.grid_blocks, bt, smem, st>>>(rays, hits, n, sc, err, counter,
+                                                                            lp.refill_threshold, lp.refill_period);
     return cudaGetLastError();
 }
+
+// Dispatch of the runtime choices (loop order, stack variant, any-hit) to template instances.
+template <template <int, int, bool> class F, typename... A>
+cudaError_t dispatch(int order, int stack_entries, bool any_hit, A &&...a) {
+    const bool small = stack_entries <= kStackSmall;
+    if (order == WHILE_WHILE) {
+        if (small)
+            return any_hit ? F<WHILE_WHILE, kStackSmall, true>::run(a...) : F<WHILE_WHILE, kStackSmall, false>::run(a...);
+        return any_hit ? F<WHILE_WHILE, kStackLarge, true>::run(a...) : F<WHILE_WHILE, kStackLarge, false>::run(a...);
+    }
+    if (small) return any_hit ? F<IF_IF, kStackSmall, true>::run(a...) : F<IF_IF, kStackSmall, false>::run(a...);
+    return any_hit ? F<IF_IF, kStackLarge, true>::run(a...) : F<IF_IF, kStackLarge, false>::run(a...);
+}
+
+template <int O, int S, bool A> struct plain_f {
+    template <typename... X> static cudaError_t run(X &&...x) { return plain_launch<O, S, A>(x...); }
+};
+template <int O, int S, bool A> struct persistent_f {
+    template <typename... X> static cudaError_t run(X &&...x) { return persistent_launch<O, S, A>(x...); }
+};
+template <int O, int S, bool A> struct attr_f {
+    static cudaError_t run(int bytes) {
+        const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+        cudaError_t e = cudaFuncSetAttribute(k_trace_plain<O, S, A, false>, a, bytes);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_plain<O, S, A, true>, a, bytes);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_persistent<O, S, A>, a, bytes);
+        return e;
+    }
+};
+template <int O, int S, bool A> struct occupancy_f {
+    static cudaError_t run(int block_threads, int *blocks) {
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_trace_persistent<O, S, A>, block_threads,
+                                                             (size_t)S * block_threads * sizeof(int));
+    }
+};
 
 }  // namespace
 
 cudaError_t launch_trace_plain(const dev_scene &sc, const float4 *rays, grt_hit *hits, uint32_t n, bool any_hit,
                                const launch_params &lp, unsigned *err, cudaStream_t stream, const uint32_t *n_dev) {
     if (n == 0) return cudaSuccess;
-    if (lp.stack_entries <= kStackSmall)
-        return any_hit ? plain_launch<kStackSmall, true>(sc, rays, hits, n, n_dev, lp, err, stream)
-                       : plain_launch<kStackSmall, false>(sc, rays, hits, n, n_dev, lp, err, stream);
-    return any_hit ? plain_launch<kStackLarge, true>(sc, rays, hits, n, n_dev, lp, err, stream)
-                   : plain_launch<kStackLarge, false>(sc, rays, hits, n, n_dev, lp, err, stream);
+    return dispatch<plain_f>(lp.order, lp.stack_entries, any_hit, sc, rays, hits, n, n_dev, lp, err, stream);
 }
 
 cudaError_t launch_trace_persistent(const dev_scene &sc, const float4 *rays, grt_hit *hits, uint32_t n, bool any_hit,
                                     const launch_params &lp, unsigned *err, unsigned *counter, cudaStream_t stream) {
     if (n == 0) return cudaSuccess;
-    if (lp.stack_entries <= kStackSmall)
-        return any_hit ? persistent_launch<kStackSmall, true>(sc, rays, hits, n, lp, err, counter, stream)
-                       : persistent_launch<kStackSmall, false>(sc, rays, hits, n, lp, err, counter, stream);
-    return any_hit ? persistent_launch<kStackLarge, true>(sc, rays, hits, n, lp, err, counter, stream)
-                   : persistent_launch<kStackLarge, false>(sc, rays, hits, n, lp, err, counter, stream);
+    return dispatch<persistent_f>(lp.order, lp.stack_entries, any_hit, sc, rays, hits, n, lp, err, counter, stream);
 }
 
 cudaError_t prepare_trace_kernels() {
     const int bytes = kStackLarge * 256 * (int)sizeof(int);  // largest stack variant at 256 threads
-    const void *fns[] = {(const void *)k_trace_plain<kStackSmall, false, false>,
-                         (const void *)k_trace_plain<kStackSmall, true, false>,
-                         (const void *)k_trace_plain<kStackLarge, false, false>,
-                         (const void *)k_trace_plain<kStackLarge, true, false>,
-                         (const void *)k_trace_plain<kStackSmall, false, true>,
-                         (const void *)k_trace_plain<kStackSmall, true, true>,
-                         (const void *)k_trace_plain<kStackLarge, false, true>,
-                         (const void *)k_trace_plain<kStackLarge, true, true>,
-                         (const void *)k_trace_persistent<kStackSmall, false>,
-                         (const void *)k_trace_persistent<kStackSmall, true>,
-                         (const void *)k_trace_persistent<kStackLarge, false>,
-                         (const void *)k_trace_persistent<kStackLarge, true>};
-    for (const void *f : fns) {
-        cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-        if (e != cudaSuccess) return e;
-    }
+    for (int order : {(int)IF_IF, (int)WHILE_WHILE})
+        for (int stack : {kStackSmall, kStackLarge})
+            for (bool any : {false, true}) {
+                cudaError_t e = dispatch<attr_f>(order, stack, any, bytes);
+                if (e != cudaSuccess) return e;
+            }
     return cudaSuccess;
 }
 
-int persistent_blocks_per_sm(int block_threads, int stack_entries, bool any_hit) {
+int persistent_blocks_per_sm(int block_threads, int stack_entries, bool any_hit, int order) {
     int blocks = 0;
-    const bool small = stack_entries <= kStackSmall;
-    const size_t smem = (size_t)(small ? kStackSmall : kStackLarge) * block_threads * sizeof(int);
-    const void *fn = small ? (any_hit ? (const void *)k_trace_persistent<kStackSmall, true>
-                                      : (const void *)k_trace_persistent<kStackSmall, false>)
-                           : (any_hit ? (const void *)k_trace_persistent<kStackLarge, true>
-                                      : (const void *)k_trace_persistent<kStackLarge, false>);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, block_threads, smem) != cudaSuccess) return 1;
+    if (dispatch<occupancy_f>(order, stack_entries, any_hit, block_threads, &blocks) != cudaSuccess) return 1;
     return blocks > 0 ? blocks : 1;
 }
 

@@ -227,6 +227,84 @@ __device__ __forceinline__ void trav_iter(trav_t &s, const dev_scene &sc, const 
     s.cur = stk[s.sp * stride];
 }
 
+// The if-if order: one inner node or one leaf per call (the reference's if-if tracer,
+// rt/cuda/trace-kernels.cu:1058-1149, visits in the same per-ray order as while-while). Lanes of
+// a warp at nodes and lanes at leaves take different branches in the same call.
+template <int STACK, bool ANY, bool PLAIN, bool COUNT = false>
+__device__ __forceinline__ void trav_step(trav_t &s, const dev_scene &sc, const ray_t &r, int *stk, int stride,
+                                          unsigned *err) {
+    if (++s.steps > kStepLimit) {
+        atomicOr(err, ERR_STEP_LIMIT);
+        s.done = true;
+        return;
+    }
+    if (s.cur >= 0) {
+        if (COUNT) ++s.n_inner;
+        const float4 *np = sc.nodes + 4 * (size_t)s.cur;
+        const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3);
+        float dl, dr;
+        bool hl = slab<PLAIN>(n0.x, n0.y, n0.z, n1.x, n1.y, n1.z, r, dl);
+        bool hr = slab<PLAIN>(n2.x, n2.y, n2.z, n3.x, n3.y, n3.z, r, dr);
+        if (!ANY) {
+            hl = hl && dl < s.hit.t;
+            hr = hr && dr < s.hit.t;
+        }
+        const int32_t cl = __float_as_int(n0.w), cr = __float_as_int(n2.w);
+        if (hl && hr) {
+            const bool left_first = dl < dr;
+            if (s.sp >= STACK) {
+                atomicOr(err, ERR_STACK_OVERFLOW);
+                s.done = true;
+                return;
+            }
+            stk[s.sp * stride] = left_first ? cr : cl;
+            ++s.sp;
+            s.cur = left_first ? cl : cr;
+            return;
+        }
+        if (hl || hr) {
+            s.cur = hl ? cl : cr;
+            return;
+        }
+    } else {
+        uint32_t first, count;
+        leaf_range(s.cur, first, count);
+        const float4 *rp = sc.records + 3 * (size_t)first;
+        for (uint32_t k = 0; k < count; ++k) {
+            if (COUNT) ++s.n_tri;
+            const float4 p0 = __ldg(rp + 3 * k), p1 = __ldg(rp + 3 * k + 1), p2 = __ldg(rp + 3 * k + 2);
+            float t, b, g;
+            if (tri_test(p0, p1, p2, r, t, b, g) && (ANY || t < s.hit.t)) {
+                s.hit.t = t;
+                s.hit.b = b;
+                s.hit.g = g;
+                s.hit.ref = __float_as_uint(p0.w);
+                s.hit.rec = first + k;
+                if (ANY) {
+                    s.found = true;
+                    s.done = true;
+                    return;
+                }
+            }
+        }
+    }
+    if (s.sp == 0) {
+        s.done = true;
+        return;
+    }
+    --s.sp;
+    s.cur = stk[s.sp * stride];
+}
+
+template <int ORDER, int STACK, bool ANY, bool PLAIN, bool COUNT = false>
+__device__ __forceinline__ void trav_advance(trav_t &s, const dev_scene &sc, const ray_t &r, int *stk, int stride,
+                                             unsigned *err) {
+    if (ORDER == WHILE_WHILE)
+        trav_iter<STACK, ANY, PLAIN, COUNT>(s, sc, r, stk, stride, err);
+    else
+        trav_step<STACK, ANY, PLAIN, COUNT>(s, sc, r, stk, stride, err);
+}
+
 // Writes one result in the reference's encodings (see include/grt.h).
 template <bool ANY>
 __device__ __forceinline__ void store_hit(grt_hit *hits, uint32_t i, const trav_t &s) {

@@ -77,11 +77,13 @@ def test_shadow_rays_and_any_hit(spheres_setup):
     s["rt"].select("while-while")
 
 
+@pytest.mark.parametrize("tracer", ["while-while", "if-if"])
 @pytest.mark.parametrize("mode,graph", [(0, 0), (1, 0), (0, 1), (1, 1)], ids=["wavefront", "fused", "wavefront-graph",
                                                                           "fused-graph"])
-def test_pathtrace_matches_oracle(api, spheres_setup, mode, graph):
+def test_pathtrace_matches_oracle(api, spheres_setup, mode, graph, tracer):
     import torch
     s = spheres_setup
+    s["rt"].select(tracer)  # the loop order of the per-bounce and the fused kernels
     n_paths = 300_000
     params = api.BatchRayTracer.pt_params(mode=mode, use_graph=graph, seed=7)
     res = torch.zeros((n_paths, 4), dtype=torch.int32, device="cuda")
@@ -103,6 +105,7 @@ def test_pathtrace_matches_oracle(api, spheres_setup, mode, graph):
     # Russian roulette before bounce ray 3: about 0.8 of the paths whose second bounce hit go on
     second_hit = (bounces >= 2) & (want_bh[:, 1, 0] < np.float32(3.4028234663852886e38))
     assert 0.75 < (bounces >= 3).sum() / max(1, second_hit.sum()) < 0.85
+    s["rt"].select("while-while")
 
 
 def test_pathtrace_no_primary_hit(api, spheres_setup):

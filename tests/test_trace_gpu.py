@@ -14,7 +14,7 @@ def _needs_cuda():
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
 
-TRACERS = ["while-while", "persistent-while-while"]
+TRACERS = ["while-while", "persistent-while-while", "if-if", "persistent-if-if"]
 
 
 def _trace(rt, rays_np, any_hit):
