@@ -276,7 +276,7 @@ def run_gb300(args):
 
     # the plain baseline runs in whichever loop order is faster for it (one thread per ray)
     plain_times = {}
-    for order in ("while-while", "if-if"):
+    for order in ("while-while", "if-if", "speculative-while-while"):
         step.rt_plain.select(order)
         for _ in range(2):
             step.plain()

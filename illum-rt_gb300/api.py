@@ -21,7 +21,9 @@ STATUS_NAMES = {0: "GRT_OK", 1: "GRT_ERR_INVALID_ARG", 2: "GRT_ERR_OOM", 3: "GRT
                 5: "GRT_ERR_BVH_TOO_DEEP", 6: "GRT_ERR_NOT_BUILT", 7: "GRT_ERR_TRAVERSAL",
                 8: "GRT_ERR_UNKNOWN_TRACER", 9: "GRT_ERR_NO_DEVICE"}
 SPLIT = {"om": 0, "sm": 1, "sah": 2}
-TRACERS = ("while-while", "persistent-while-while", "if-if", "persistent-if-if")
+TRACERS = ("while-while", "persistent-while-while", "if-if", "persistent-if-if", "speculative-while-while",
+           "persistent-speculative-while-while")
+EXACT_TRACERS = TRACERS[:4]  # per-ray visit order of the reference: bit-identical results
 
 
 class GRTError(RuntimeError):

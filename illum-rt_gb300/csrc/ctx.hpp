@@ -89,8 +89,10 @@ struct tracer_kind {
 inline const tracer_kind kTracers[] = {{"while-while", false, WHILE_WHILE},
                                        {"persistent-while-while", true, WHILE_WHILE},
                                        {"if-if", false, IF_IF},
-                                       {"persistent-if-if", true, IF_IF}};
-inline const int kNumTracers = 4;
+                                       {"persistent-if-if", true, IF_IF},
+                                       {"speculative-while-while", false, SPECULATIVE},
+                                       {"persistent-speculative-while-while", true, SPECULATIVE}};
+inline const int kNumTracers = 6;
 
 inline launch_params params_for(grt_ctx *c, bool any_hit) {
     grt::launch_params lp{};

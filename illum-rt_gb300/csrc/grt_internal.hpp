@@ -30,9 +30,10 @@ static const int kStackLarge = 64;
 // kernel given a corrupted tree.
 static const uint32_t kStepLimit = 1u << 26;
 
-// Loop orders of the traversal kernels (traverse.cuh): one node or leaf per iteration, or
-// inner nodes until a leaf and then that leaf.
-enum loop_order : int { IF_IF = 0, WHILE_WHILE = 1 };
+// Loop orders of the traversal kernels (traverse.cuh): one node or leaf per iteration; inner
+// nodes until a leaf and then that leaf; speculative while-while (postponed leaves, results
+// equal to the reference's except near-ties).
+enum loop_order : int { IF_IF = 0, WHILE_WHILE = 1, SPECULATIVE = 2 };
 
 struct launch_params {
     int block_threads;

@@ -424,15 +424,10 @@ __global__ void __launch_bounds__(256) k_pt_fused(dev_scene sc, pt_scene ps, pt_
         }
         // traversal phase
         for (int it = 1;; ++it) {
-            if (tracing) {
-                if (plain)
-                    trav_advance<ORDER, STACK, false, true>(s, sc, r, stk, stride, err);
-                else
-                    trav_advance<ORDER, STACK, false, false>(s, sc, r, stk, stride, err);
-                if (s.done) {
-                    tracing = false;
-                    waiting = true;
-                }
+            trav_advance<ORDER, STACK, false>(s, tracing, plain, sc, r, stk, stride, err);
+            if (tracing && s.done) {
+                tracing = false;
+                waiting = true;
             }
             if (it % refill_period == 0) {
                 const int busy = __popc(__ballot_sync(kFull, tracing));
@@ -510,8 +505,11 @@ cudaError_t launch_fused(const dev_scene &sc, const pt_scene &ps, const pt_param
                          unsigned *counter, cudaStream_t st) {
     if (n_paths == 0) return cudaSuccess;
     const bool small = lp.stack_entries <= kStackSmall;
-    auto f = lp.order == WHILE_WHILE ? (small ? fused_launch<WHILE_WHILE, kStackSmall> : fused_launch<WHILE_WHILE, kStackLarge>)
-                                     : (small ? fused_launch<IF_IF, kStackSmall> : fused_launch<IF_IF, kStackLarge>);
+    auto f = lp.order == WHILE_WHILE
+                 ? (small ? fused_launch<WHILE_WHILE, kStackSmall> : fused_launch<WHILE_WHILE, kStackLarge>)
+                 : lp.order == SPECULATIVE
+                       ? (small ? fused_launch<SPECULATIVE, kStackSmall> : fused_launch<SPECULATIVE, kStackLarge>)
+                       : (small ? fused_launch<IF_IF, kStackSmall> : fused_launch<IF_IF, kStackLarge>);
     return f(sc, ps, pp, prim_rays, prim_hits, hit_list, n_list, n_paths, results, bounce_hits, lp, err, counter, st);
 }
 
@@ -519,7 +517,9 @@ cudaError_t prepare_pt_kernels() {
     const int bytes = kStackLarge * 256 * (int)sizeof(int);
     for (const void *f : {(const void *)k_pt_fused<IF_IF, kStackSmall>, (const void *)k_pt_fused<IF_IF, kStackLarge>,
                           (const void *)k_pt_fused<WHILE_WHILE, kStackSmall>,
-                          (const void *)k_pt_fused<WHILE_WHILE, kStackLarge>}) {
+                          (const void *)k_pt_fused<WHILE_WHILE, kStackLarge>,
+                          (const void *)k_pt_fused<SPECULATIVE, kStackSmall>,
+                          (const void *)k_pt_fused<SPECULATIVE, kStackLarge>}) {
         cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
         if (e != cudaSuccess) return e;
     }
@@ -533,6 +533,9 @@ int fused_blocks_per_sm(int block_threads, int stack_entries, int order) {
     const void *fn = order == WHILE_WHILE
                          ? (small ? (const void *)k_pt_fused<WHILE_WHILE, kStackSmall>
                                   : (const void *)k_pt_fused<WHILE_WHILE, kStackLarge>)
+                     : order == SPECULATIVE
+                         ? (small ? (const void *)k_pt_fused<SPECULATIVE, kStackSmall>
+                                  : (const void *)k_pt_fused<SPECULATIVE, kStackLarge>)
                          : (small ? (const void *)k_pt_fused<IF_IF, kStackSmall> : (const void *)k_pt_fused<IF_IF, kStackLarge>);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, block_threads, smem) != cudaSuccess) return 1;
     return blocks > 0 ? blocks : 1;

@@ -1,7 +1,7 @@
 // Closest-hit / any-hit traversal kernels for sm_103a.
 //
 // Two kernel shapes replace the reference's CUDA variants (rt/cuda/trace-kernels.cu), each in
-// the if-if and the while-while loop order (traverse.cuh):
+// the if-if, while-while and speculative while-while loop orders (traverse.cuh):
 //   * k_trace_plain — one thread per ray, the wavefront baseline (the role of ifif_trace and
 //     whilewhile_trace, rt/cuda/trace-kernels.cu:238-316);
 //   * k_trace_persistent — persistent warps that refill lanes whose ray finished from a global
@@ -9,8 +9,9 @@
 //     dynamicwhilewhile_trace, rt/cuda/trace-kernels.cu:702-876, restructured so that every
 //     ballot is taken by all 32 lanes at a uniform point of the loop, and the counter is reset
 //     by the host before the launch instead of by the kernel's own threads).
-// All of them visit each ray's nodes in the reference's order, so their results are identical
-// to each other and to the reference CPU tracer.
+// In the if-if and while-while orders every ray visits its nodes in the reference's order, so
+// results are identical to the reference CPU tracer; the speculative order may differ from it
+// in near-ties only.
 #include "traverse.cuh"
 
 namespace grt {
@@ -26,16 +27,21 @@ __global__ void __launch_bounds__(256) k_trace_plain(const float4 *__restrict__ 
     extern __shared__ int s_stack[];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (n_dev) n = *n_dev;  // ray count produced on the device (wavefront queues)
-    if (i >= n) return;
-    const ray_t r = load_ray(rays, i);
+    const bool active = i < n;
+    if (ORDER != SPECULATIVE && !active) return;
+    ray_t r = {};
+    if (active) r = load_ray(rays, i);
     trav_t s;
     trav_init(s, sc);
     int *stk = s_stack + threadIdx.x;
     const int stride = blockDim.x;
-    if (sc.finite && ray_is_plain(r)) {
-        while (!s.done) trav_advance<ORDER, STACK, ANY, true, COUNT>(s, sc, r, stk, stride, err);
+    const bool plain = active && sc.finite && ray_is_plain(r);
+    if (ORDER == SPECULATIVE) {  // the whole warp stays in the loop until its last ray ends
+        while (__any_sync(kFull, active && !s.done))
+            trav_advance<ORDER, STACK, ANY, COUNT>(s, active, plain, sc, r, stk, stride, err);
+        if (!active) return;
     } else {
-        while (!s.done) trav_advance<ORDER, STACK, ANY, false, COUNT>(s, sc, r, stk, stride, err);
+        while (!s.done) trav_advance<ORDER, STACK, ANY, COUNT>(s, true, plain, sc, r, stk, stride, err);
     }
     store_hit<ANY>(hits, i, s);
     if (COUNT) {
@@ -90,15 +96,10 @@ __global__ void __launch_bounds__(256) k_trace_persistent(const float4 *__restri
         }
         // traverse; every `refill_period` iterations the warp counts its busy lanes
         for (int it = 1;; ++it) {
-            if (have) {
-                if (plain)
-                    trav_advance<ORDER, STACK, ANY, true>(s, sc, r, stk, stride, err);
-                else
-                    trav_advance<ORDER, STACK, ANY, false>(s, sc, r, stk, stride, err);
-                if (s.done) {
-                    store_hit<ANY>(hits, idx, s);
-                    have = false;
-                }
+            trav_advance<ORDER, STACK, ANY>(s, have, plain, sc, r, stk, stride, err);
+            if (have && s.done) {
+                store_hit<ANY>(hits, idx, s);
+                have = false;
             }
             if (it % refill_period == 0) {
                 const int busy = __popc(__ballot_sync(kFull, have));
@@ -137,6 +138,11 @@ cudaError_t persistent_launch(const dev_scene &sc, const float4 *rays, grt_hit *
 template <template <int, int, bool> class F, typename... A>
 cudaError_t dispatch(int order, int stack_entries, bool any_hit, A &&...a) {
     const bool small = stack_entries <= kStackSmall;
+    if (order == SPECULATIVE) {
+        if (small)
+            return any_hit ? F<SPECULATIVE, kStackSmall, true>::run(a...) : F<SPECULATIVE, kStackSmall, false>::run(a...);
+        return any_hit ? F<SPECULATIVE, kStackLarge, true>::run(a...) : F<SPECULATIVE, kStackLarge, false>::run(a...);
+    }
     if (order == WHILE_WHILE) {
         if (small)
             return any_hit ? F<WHILE_WHILE, kStackSmall, true>::run(a...) : F<WHILE_WHILE, kStackSmall, false>::run(a...);
@@ -184,7 +190,7 @@ cudaError_t launch_trace_persistent(const dev_scene &sc, const float4 *rays, grt
 
 cudaError_t prepare_trace_kernels() {
     const int bytes = kStackLarge * 256 * (int)sizeof(int);  // largest stack variant at 256 threads
-    for (int order : {(int)IF_IF, (int)WHILE_WHILE})
+    for (int order : {(int)IF_IF, (int)WHILE_WHILE, (int)SPECULATIVE})
         for (int stack : {kStackSmall, kStackLarge})
             for (bool any : {false, true}) {
                 cudaError_t e = dispatch<attr_f>(order, stack, any, bytes);

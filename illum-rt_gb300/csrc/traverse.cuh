@@ -80,11 +80,20 @@ __device__ __forceinline__ bool slab(float lx, float ly, float lz, float hx, flo
 }
 
 // Cramer's rule test of the reference (libgi/intersect.h:36-67) on a triangle record
-// (v0, v0 - v1, v0 - v2). The sign tests before the divisions only discard cases whose
-// quotients cannot pass the reference's `beta > 0` / `gamma > 0` (zero numerator, or
-// numerator and determinant of opposite sign), so the outcome is unchanged.
+// (v0, v0 - v1, v0 - v2), every operation rounded as the reference rounds it.
+//
+// Before the three IEEE divisions, cheap tests discard cases whose rounded quotients could not
+// pass the reference's conditions anyway, so the outcome is unchanged:
+//   * beta == 0 or sign(beta) != sign(M): beta/M > 0 fails; the same for gamma;
+//   * |beta| + |gamma| >= |M| (1 + 2^-19) (with |M| in [2^-100, 2^100]): the exact sum of the
+//     quotients is at least 1 + 2^-20, so their rounded sum exceeds 1;
+//   * tt/M <= 0 while t_min >= 0: t > t_min fails;
+//   * |tt| >= fl(|M| t_limit) (1 + 2^-20) with the product normal: the exact quotient exceeds
+//     t_limit, so the rounded one is >= t_limit, where t_limit is t_max (any-hit) or
+//     min(t_max, closest t) (closest-hit, whose caller rejects t >= closest t).
+// The margins cover the at most three roundings in each bound.
 __device__ __forceinline__ bool tri_test(const float4 &p0, const float4 &p1, const float4 &p2, const ray_t &r,
-                                         float &t_out, float &b_out, float &g_out) {
+                                         float t_limit, float &t_out, float &b_out, float &g_out) {
     const float a = p1.x, b = p1.y, c = p1.z;
     const float d = p2.x, e = p2.y, f = p2.z;
     const float g = r.dx, h = r.dy, i = r.dz;
@@ -101,6 +110,17 @@ __device__ __forceinline__ bool tri_test(const float4 &p0, const float4 &p1, con
     float gamma = __fadd_rn(__fadd_rn(__fmul_rn(i, c1), __fmul_rn(h, c2)), __fmul_rn(g, c3));
     if (gamma == 0.f || ((__float_as_uint(gamma) ^ __float_as_uint(M)) & 0x80000000u)) return false;
     float tt = -__fadd_rn(__fadd_rn(__fmul_rn(f, c1), __fmul_rn(e, c2)), __fmul_rn(d, c3));
+    const float at = signbit(M) ? -tt : tt;  // sign of the quotient tt / M
+    if (r.tmin >= 0.f && at <= 0.f) return false;
+    const float aM = fabsf(M);
+    if (aM >= 0x1p-100f && aM <= 0x1p100f) {
+        if (__fadd_rn(fabsf(beta), fabsf(gamma)) >= __fmul_rn(aM, 0x1.00002p0f)) return false;
+        if (at > 0.f) {
+            if (t_limit <= 0.f) return false;
+            const float pl = __fmul_rn(aM, t_limit);
+            if (pl >= FLT_MIN && at >= __fmul_rn(pl, 0x1.00001p0f)) return false;
+        }
+    }
     beta = __fdiv_rn(beta, M);
     gamma = __fdiv_rn(gamma, M);
     tt = __fdiv_rn(tt, M);
@@ -128,6 +148,8 @@ struct trav_t {
     uint32_t steps;
     bool done;
     bool found;  // any-hit: an occluder was found
+    bool more;     // speculative order: `cur` holds a node or leaf still to visit
+    int32_t pend;  // speculative order: postponed leaf (0 = none; leaf references are negative)
     uint32_t n_inner, n_tri;  // inner nodes visited and triangles tested (counting kernels only)
     hit_t hit;
 };
@@ -138,6 +160,8 @@ __device__ __forceinline__ void trav_init(trav_t &s, const dev_scene &sc) {
     s.steps = 0;
     s.done = sc.empty != 0;
     s.found = false;
+    s.more = true;
+    s.pend = 0;
     s.n_inner = 0;
     s.n_tri = 0;
     s.hit.t = FLT_MAX;
@@ -206,7 +230,7 @@ __device__ __forceinline__ void trav_iter(trav_t &s, const dev_scene &sc, const 
         if (COUNT) ++s.n_tri;
         const float4 p0 = __ldg(rp + 3 * k), p1 = __ldg(rp + 3 * k + 1), p2 = __ldg(rp + 3 * k + 2);
         float t, b, g;
-        if (tri_test(p0, p1, p2, r, t, b, g) && (ANY || t < s.hit.t)) {
+        if (tri_test(p0, p1, p2, r, ANY ? r.tmax : fminf(r.tmax, s.hit.t), t, b, g) && (ANY || t < s.hit.t)) {
             s.hit.t = t;
             s.hit.b = b;
             s.hit.g = g;
@@ -274,7 +298,7 @@ __device__ __forceinline__ void trav_step(trav_t &s, const dev_scene &sc, const 
             if (COUNT) ++s.n_tri;
             const float4 p0 = __ldg(rp + 3 * k), p1 = __ldg(rp + 3 * k + 1), p2 = __ldg(rp + 3 * k + 2);
             float t, b, g;
-            if (tri_test(p0, p1, p2, r, t, b, g) && (ANY || t < s.hit.t)) {
+            if (tri_test(p0, p1, p2, r, ANY ? r.tmax : fminf(r.tmax, s.hit.t), t, b, g) && (ANY || t < s.hit.t)) {
                 s.hit.t = t;
                 s.hit.b = b;
                 s.hit.g = g;
@@ -296,13 +320,129 @@ __device__ __forceinline__ void trav_step(trav_t &s, const dev_scene &sc, const 
     s.cur = stk[s.sp * stride];
 }
 
-template <int ORDER, int STACK, bool ANY, bool PLAIN, bool COUNT = false>
-__device__ __forceinline__ void trav_advance(trav_t &s, const dev_scene &sc, const ray_t &r, int *stk, int stride,
-                                             unsigned *err) {
-    if (ORDER == WHILE_WHILE)
-        trav_iter<STACK, ANY, PLAIN, COUNT>(s, sc, r, stk, stride, err);
-    else
-        trav_step<STACK, ANY, PLAIN, COUNT>(s, sc, r, stk, stride, err);
+// Inner-node visit shared by the speculative order: box tests of `cur`, then near child,
+// push of the far child, or pop. Clears `more` when the stack runs empty.
+template <int STACK, bool ANY, bool PLAIN>
+__device__ __forceinline__ void spec_node(trav_t &s, const dev_scene &sc, const ray_t &r, int *stk, int stride,
+                                          unsigned *err) {
+    const float4 *np = sc.nodes + 4 * (size_t)s.cur;
+    const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3);
+    float dl, dr;
+    bool hl = slab<PLAIN>(n0.x, n0.y, n0.z, n1.x, n1.y, n1.z, r, dl);
+    bool hr = slab<PLAIN>(n2.x, n2.y, n2.z, n3.x, n3.y, n3.z, r, dr);
+    if (!ANY) {
+        hl = hl && dl < s.hit.t;
+        hr = hr && dr < s.hit.t;
+    }
+    const int32_t cl = __float_as_int(n0.w), cr = __float_as_int(n2.w);
+    if (hl && hr) {
+        const bool left_first = dl < dr;
+        if (s.sp >= STACK) {
+            atomicOr(err, ERR_STACK_OVERFLOW);
+            s.done = true;
+            return;
+        }
+        stk[s.sp * stride] = left_first ? cr : cl;
+        ++s.sp;
+        s.cur = left_first ? cl : cr;
+    } else if (hl || hr) {
+        s.cur = hl ? cl : cr;
+    } else if (s.sp == 0) {
+        s.more = false;
+    } else {
+        --s.sp;
+        s.cur = stk[s.sp * stride];
+    }
+}
+
+// The speculative while-while order (the reference's speculativewhilewhile_traversal,
+// rt/cuda/trace-kernels.cu:1433-1540, after Aila and Laine): a lane that reaches a leaf
+// postpones it and keeps visiting inner nodes while other lanes of the warp are still looking
+// for their first leaf; then all postponed leaves are tested together. Every lane of the warp
+// must call this together (it ballots over the full warp); `active` marks lanes with a ray.
+// Each ray's leaves are still tested in the reference's order, but node tests after a
+// postponed leaf use the closest hit from before that leaf, so the ray may visit nodes the
+// reference would have culled. A triangle found there can replace the reference's answer only
+// if its t lies within rounding of the culled box's entry distance: a near-tie.
+template <int STACK, bool ANY, bool COUNT>
+__device__ __forceinline__ void trav_spec_iter(trav_t &s, bool active, bool plain, const dev_scene &sc,
+                                               const ray_t &r, int *stk, int stride, unsigned *err) {
+    const bool mine = active && !s.done;
+    for (;;) {
+        if (mine && !s.done && s.more && s.cur >= 0) {
+            if (++s.steps > kStepLimit) {
+                atomicOr(err, ERR_STEP_LIMIT);
+                s.done = true;
+            } else {
+                if (COUNT) ++s.n_inner;
+                if (plain)
+                    spec_node<STACK, ANY, true>(s, sc, r, stk, stride, err);
+                else
+                    spec_node<STACK, ANY, false>(s, sc, r, stk, stride, err);
+            }
+        }
+        if (mine && !s.done && s.more && s.cur < 0 && s.pend == 0) {
+            s.pend = s.cur;  // postpone the leaf and go on with the next node
+            if (s.sp == 0) {
+                s.more = false;
+            } else {
+                --s.sp;
+                s.cur = stk[s.sp * stride];
+            }
+        }
+        const bool searching = mine && !s.done && s.more && s.pend == 0;
+        if (!__any_sync(0xffffffffu, searching)) break;
+    }
+    if (mine && !s.done) {
+        if (s.pend != 0) {
+            uint32_t first, count;
+            leaf_range(s.pend, first, count);
+            s.pend = 0;
+            ++s.steps;
+            const float4 *rp = sc.records + 3 * (size_t)first;
+            for (uint32_t k = 0; k < count; ++k) {
+                if (COUNT) ++s.n_tri;
+                const float4 p0 = __ldg(rp + 3 * k), p1 = __ldg(rp + 3 * k + 1), p2 = __ldg(rp + 3 * k + 2);
+                float t, b, g;
+                if (tri_test(p0, p1, p2, r, ANY ? r.tmax : fminf(r.tmax, s.hit.t), t, b, g) && (ANY || t < s.hit.t)) {
+                    s.hit.t = t;
+                    s.hit.b = b;
+                    s.hit.g = g;
+                    s.hit.ref = __float_as_uint(p0.w);
+                    s.hit.rec = first + k;
+                    if (ANY) {
+                        s.found = true;
+                        s.done = true;
+                        break;
+                    }
+                }
+            }
+        }
+        if (!s.done && !s.more && s.pend == 0) s.done = true;
+    }
+}
+
+// Advances the traversal of this lane's ray by one iteration of the chosen loop order. Called
+// by all 32 lanes of a warp together (the speculative order needs that); `active` is false on
+// lanes without a ray, `plain` selects the min/max slab test (see ray_is_plain).
+template <int ORDER, int STACK, bool ANY, bool COUNT = false>
+__device__ __forceinline__ void trav_advance(trav_t &s, bool active, bool plain, const dev_scene &sc, const ray_t &r,
+                                             int *stk, int stride, unsigned *err) {
+    if (ORDER == SPECULATIVE) {
+        trav_spec_iter<STACK, ANY, COUNT>(s, active, plain, sc, r, stk, stride, err);
+    } else if (active && !s.done) {
+        if (ORDER == WHILE_WHILE) {
+            if (plain)
+                trav_iter<STACK, ANY, true, COUNT>(s, sc, r, stk, stride, err);
+            else
+                trav_iter<STACK, ANY, false, COUNT>(s, sc, r, stk, stride, err);
+        } else {
+            if (plain)
+                trav_step<STACK, ANY, true, COUNT>(s, sc, r, stk, stride, err);
+            else
+                trav_step<STACK, ANY, false, COUNT>(s, sc, r, stk, stride, err);
+        }
+    }
 }
 
 // Writes one result in the reference's encodings (see include/grt.h).

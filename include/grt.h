@@ -146,10 +146,13 @@ void grt_host_bvh_free(grt_host_bvh *bvh);
 
 /* ---- tracer selection (platform::select / `raytracer <name>`, rt/cuda/platform.cpp:102-131) */
 
-/* Names: "while-while" (default) and "if-if": one thread per ray, in the two loop orders of
- * the reference's tracers of those names; "persistent-while-while" and "persistent-if-if":
- * persistent warps with dynamic ray fetch. The loop order of the selected tracer is also the
- * one grt_pathtrace uses. All give identical results. Unknown name: GRT_ERR_UNKNOWN_TRACER. */
+/* Names: "while-while" (default), "if-if" and "speculative-while-while": one thread per ray,
+ * in the loop orders of the reference's tracers of those names; the same names prefixed with
+ * "persistent-": persistent warps with dynamic ray fetch. The loop order of the selected tracer
+ * is also the one grt_pathtrace uses. The if-if and while-while orders give results identical
+ * to the reference CPU tracer; the speculative order may differ from it in near-ties only (a
+ * different triangle whose t is within a few ulps of the reference's). Unknown name:
+ * GRT_ERR_UNKNOWN_TRACER. */
 grt_status grt_select_tracer(grt_ctx *ctx, const char *name);
 grt_status grt_set_tuning(grt_ctx *ctx, const grt_tuning *tuning);
 grt_status grt_get_tuning(grt_ctx *ctx, grt_tuning *tuning);

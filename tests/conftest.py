@@ -77,3 +77,26 @@ def golden_scenes(pkg):
             rays = g["rays"]
         out[name] = (v, t, rays, g["any_rays"])
     return out
+
+
+NEAR_TIE = 1e-6  # |t1 - t2| <= NEAR_TIE * t: the documented near-tie class
+
+
+def assert_hits_match(got: np.ndarray, want: np.ndarray, exact: bool, what: str = "hits"):
+    """Exact tracers: every hit record bit-identical. Speculative tracers: rows may name a
+    different triangle only as a near-tie (both hit, |t1 - t2| <= 1e-6 t); rows naming the same
+    triangle are bit-identical."""
+    g = np.ascontiguousarray(got, np.float32)
+    w = np.ascontiguousarray(want, np.float32)
+    same = same_bits(g, w)
+    if exact:
+        bad = ~same
+        assert not bad.any(), f"{bad.sum()} of {bad.size} {what} differ, first rows {np.nonzero(bad)[0][:5]}"
+        return 0
+    diff_ref = g.view(np.uint32)[:, 3] != w.view(np.uint32)[:, 3]
+    assert (same | diff_ref).all(), f"{what}: same triangle but different t/beta/gamma"
+    rows = np.nonzero(diff_ref)[0]
+    tg, tw = g[rows, 0].astype(np.float64), w[rows, 0].astype(np.float64)
+    near = (tg < 3e38) & (tw < 3e38) & (np.abs(tg - tw) <= NEAR_TIE * np.abs(tw))
+    assert near.all(), f"{what}: {(~near).sum()} differences are not near-ties, rows {rows[~near][:5]}"
+    return int(rows.size)

@@ -77,7 +77,7 @@ def test_shadow_rays_and_any_hit(spheres_setup):
     s["rt"].select("while-while")
 
 
-@pytest.mark.parametrize("tracer", ["while-while", "if-if"])
+@pytest.mark.parametrize("tracer", ["while-while", "if-if", "speculative-while-while"])
 @pytest.mark.parametrize("mode,graph", [(0, 0), (1, 0), (0, 1), (1, 1)], ids=["wavefront", "fused", "wavefront-graph",
                                                                           "fused-graph"])
 def test_pathtrace_matches_oracle(api, spheres_setup, mode, graph, tracer):
@@ -97,9 +97,21 @@ def test_pathtrace_matches_oracle(api, spheres_setup, mode, graph, tracer):
     torch.cuda.synchronize()
     want, want_bh = s["o"].pathtrace(s["rays"], s["prim_hits"], n_paths, seed=7, albedo=s["albedo"], bounce_hits=True)
     got = res.cpu().numpy().view(np.uint32)
+    got_bh = bh.cpu().numpy()
     bad = (got != want).any(axis=1)
-    assert not bad.any(), f"{bad.sum()} paths differ, first {np.nonzero(bad)[0][:5]}"
-    assert (bh.cpu().numpy().view(np.uint32) == want_bh.view(np.uint32)).all()
+    if "speculative" in tracer:
+        # a path may leave the reference's only through a near-tie at its first differing bounce
+        assert bad.sum() <= 1e-4 * n_paths
+        for p in np.nonzero(bad)[0]:
+            k = int(np.nonzero((got_bh[p].view(np.uint32) != want_bh[p].view(np.uint32)).any(axis=1))[0][0])
+            tg, tw = float(got_bh[p, k, 0]), float(want_bh[p, k, 0])
+            assert tg < 3e38 and tw < 3e38 and abs(tg - tw) <= 1e-6 * tw, (p, k, tg, tw)
+        got, want_bh_cmp = got[~bad], want_bh[~bad]
+        assert (got_bh[~bad].view(np.uint32) == want_bh_cmp.view(np.uint32)).all()
+        got = res.cpu().numpy().view(np.uint32)
+    else:
+        assert not bad.any(), f"{bad.sum()} paths differ, first {np.nonzero(bad)[0][:5]}"
+        assert (got_bh.view(np.uint32) == want_bh.view(np.uint32)).all()
     bounces = got[:, 1]
     assert bounces.min() >= 1 and bounces.max() == 5
     # Russian roulette before bounce ray 3: about 0.8 of the paths whose second bounce hit go on

@@ -3,7 +3,7 @@ closest hits (triangle, t, beta, gamma bit for bit) and any-hit answers."""
 import numpy as np
 import pytest
 
-from conftest import GOLDEN_CASES, load_golden, same_bits
+from conftest import GOLDEN_CASES, assert_hits_match, load_golden, same_bits
 
 pytestmark = pytest.mark.gpu
 
@@ -14,7 +14,12 @@ def _needs_cuda():
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
 
-TRACERS = ["while-while", "persistent-while-while", "if-if", "persistent-if-if"]
+TRACERS = ["while-while", "persistent-while-while", "if-if", "persistent-if-if", "speculative-while-while",
+           "persistent-speculative-while-while"]
+
+
+def exact(tracer):
+    return "speculative" not in tracer
 
 
 def _trace(rt, rays_np, any_hit):
@@ -38,8 +43,7 @@ def test_golden_closest_and_any(gpu_tracer, golden_scenes, name, tracer):
     gpu_tracer.build(v, t)
     gpu_tracer.select(tracer)
     got = _trace(gpu_tracer, rays, False)
-    bad = ~same_bits(got, g["closest"])
-    assert not bad.any(), f"{bad.sum()} of {bad.size} closest hits differ, first rows {np.nonzero(bad)[0][:5]}"
+    assert_hits_match(got, g["closest"], exact(tracer), f"{name} closest hits")
     got_any = _trace(gpu_tracer, any_rays, True)
     assert (occluded(got_any) == g["any_occluded"]).all()
     t_bits = got_any.view(np.uint32)[:, 0]
@@ -55,7 +59,7 @@ def test_spheres_primary_1024_matches_oracle(gpu_tracer, orc, wl, tracer):
     gpu_tracer.build(sc.vpos, sc.tris)
     gpu_tracer.select(tracer)
     got = _trace(gpu_tracer, rays, False)
-    assert same_bits(got, want).all()
+    assert_hits_match(got, want, exact(tracer))
     assert int(cnt[:, 2].max()) <= 24
 
 
@@ -69,7 +73,7 @@ def test_other_builders_match_oracle(gpu_tracer, orc, wl, builder):
     gpu_tracer.build(sc.vpos, sc.tris, planes=16, **builder)
     for tracer in TRACERS:
         gpu_tracer.select(tracer)
-        assert same_bits(_trace(gpu_tracer, rays, False), o.closest(rays)[0]).all()
+        assert_hits_match(_trace(gpu_tracer, rays, False), o.closest(rays)[0], exact(tracer))
         r2 = rays.copy()
         r2[:, 7] = 2.0
         assert (occluded(_trace(gpu_tracer, r2, True)) == o.any(r2)[0]).all()
