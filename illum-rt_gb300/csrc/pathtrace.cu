@@ -424,7 +424,12 @@ __global__ void __launch_bounds__(256) k_pt_fused(dev_scene sc, pt_scene ps, pt_
         }
         // traversal phase
         for (int it = 1;; ++it) {
-            trav_advance<ORDER, STACK, false>(s, tracing, plain, sc, r, stk, stride, err);
+            if (ORDER == SPECULATIVE)
+                trav_spec_iter<STACK, false, false>(s, tracing, plain, sc, r, stk, stride, err);
+            else if (tracing && plain)
+                trav_advance<ORDER, STACK, false, false, true>(s, sc, r, stk, stride, err);
+            else if (tracing)
+                trav_advance<ORDER, STACK, false, false, false>(s, sc, r, stk, stride, err);
             if (tracing && s.done) {
                 tracing = false;
                 waiting = true;

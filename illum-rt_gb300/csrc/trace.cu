@@ -38,10 +38,12 @@ __global__ void __launch_bounds__(256) k_trace_plain(const float4 *__restrict__ 
     const bool plain = active && sc.finite && ray_is_plain(r);
     if (ORDER == SPECULATIVE) {  // the whole warp stays in the loop until its last ray ends
         while (__any_sync(kFull, active && !s.done))
-            trav_advance<ORDER, STACK, ANY, COUNT>(s, active, plain, sc, r, stk, stride, err);
+            trav_spec_iter<STACK, ANY, COUNT>(s, active, plain, sc, r, stk, stride, err);
         if (!active) return;
+    } else if (plain) {  // one loop per slab variant: the choice is made once per ray
+        while (!s.done) trav_advance<ORDER, STACK, ANY, COUNT, true>(s, sc, r, stk, stride, err);
     } else {
-        while (!s.done) trav_advance<ORDER, STACK, ANY, COUNT>(s, true, plain, sc, r, stk, stride, err);
+        while (!s.done) trav_advance<ORDER, STACK, ANY, COUNT, false>(s, sc, r, stk, stride, err);
     }
     store_hit<ANY>(hits, i, s);
     if (COUNT) {
@@ -96,7 +98,12 @@ __global__ void __launch_bounds__(256) k_trace_persistent(const float4 *__restri
         }
         // traverse; every `refill_period` iterations the warp counts its busy lanes
         for (int it = 1;; ++it) {
-            trav_advance<ORDER, STACK, ANY>(s, have, plain, sc, r, stk, stride, err);
+            if (ORDER == SPECULATIVE)
+                trav_spec_iter<STACK, ANY, false>(s, have, plain, sc, r, stk, stride, err);
+            else if (have && plain)
+                trav_advance<ORDER, STACK, ANY, false, true>(s, sc, r, stk, stride, err);
+            else if (have)
+                trav_advance<ORDER, STACK, ANY, false, false>(s, sc, r, stk, stride, err);
             if (have && s.done) {
                 store_hit<ANY>(hits, idx, s);
                 have = false;

@@ -422,27 +422,15 @@ __device__ __forceinline__ void trav_spec_iter(trav_t &s, bool active, bool plai
     }
 }
 
-// Advances the traversal of this lane's ray by one iteration of the chosen loop order. Called
-// by all 32 lanes of a warp together (the speculative order needs that); `active` is false on
-// lanes without a ray, `plain` selects the min/max slab test (see ray_is_plain).
-template <int ORDER, int STACK, bool ANY, bool COUNT = false>
-__device__ __forceinline__ void trav_advance(trav_t &s, bool active, bool plain, const dev_scene &sc, const ray_t &r,
-                                             int *stk, int stride, unsigned *err) {
-    if (ORDER == SPECULATIVE) {
-        trav_spec_iter<STACK, ANY, COUNT>(s, active, plain, sc, r, stk, stride, err);
-    } else if (active && !s.done) {
-        if (ORDER == WHILE_WHILE) {
-            if (plain)
-                trav_iter<STACK, ANY, true, COUNT>(s, sc, r, stk, stride, err);
-            else
-                trav_iter<STACK, ANY, false, COUNT>(s, sc, r, stk, stride, err);
-        } else {
-            if (plain)
-                trav_step<STACK, ANY, true, COUNT>(s, sc, r, stk, stride, err);
-            else
-                trav_step<STACK, ANY, false, COUNT>(s, sc, r, stk, stride, err);
-        }
-    }
+// One iteration of a non-speculative loop order for this lane's ray (PLAIN: min/max slab test,
+// see ray_is_plain). The speculative order is trav_spec_iter, which the whole warp calls together.
+template <int ORDER, int STACK, bool ANY, bool COUNT, bool PLAIN>
+__device__ __forceinline__ void trav_advance(trav_t &s, const dev_scene &sc, const ray_t &r, int *stk, int stride,
+                                             unsigned *err) {
+    if (ORDER == WHILE_WHILE)
+        trav_iter<STACK, ANY, PLAIN, COUNT>(s, sc, r, stk, stride, err);
+    else
+        trav_step<STACK, ANY, PLAIN, COUNT>(s, sc, r, stk, stride, err);
 }
 
 // Writes one result in the reference's encodings (see include/grt.h).
