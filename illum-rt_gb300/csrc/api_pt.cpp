@@ -201,7 +201,8 @@ grt_status grt_pathtrace(grt_ctx *c, const grt_pt_params *params, const float *p
         fbits(p.rr_continue), fbits(p.eps), p.seed, (uint64_t)(uintptr_t)c->d_scratch, c->scene_generation,
         (uint64_t)(uintptr_t)c->d_albedo, c->n_albedo, (uint64_t)(uintptr_t)st, (uint64_t)lp.block_threads,
         (uint64_t)lp.grid_blocks, (uint64_t)lp.refill_threshold, (uint64_t)lp.refill_period,
-        (uint64_t)lp.stack_entries};
+        (uint64_t)lp.stack_entries, (uint64_t)lp.order, (uint64_t)lp_trace.block_threads,
+        (uint64_t)(uintptr_t)lp_trace.counters};
     if (!c->pt_graph.exec || c->pt_graph.key != key) {
         if (c->pt_graph.exec) cudaGraphExecDestroy(c->pt_graph.exec);
         c->pt_graph.exec = nullptr;

@@ -155,6 +155,49 @@ struct path_t {
     uint32_t last_ref;
 };
 
+// Path state of the fused kernel, kept in shared memory next to the traversal stacks (one
+// structure-of-arrays slot per thread) because only the shade phase touches it; the PCG32
+// increment is recomputed from the path index.
+struct path_slots {
+    uint64_t *rng;
+    float *thr;
+    uint32_t *digest, *bounce, *last_ref, *path;
+};
+
+__device__ __forceinline__ path_slots path_slots_at(int *smem_base, int stack_entries) {
+    const int bt = blockDim.x;
+    char *base = reinterpret_cast<char *>(smem_base + (size_t)stack_entries * bt);
+    path_slots ps;
+    ps.rng = reinterpret_cast<uint64_t *>(base);
+    ps.thr = reinterpret_cast<float *>(base + 8 * bt);
+    ps.digest = reinterpret_cast<uint32_t *>(base + 12 * bt);
+    ps.bounce = reinterpret_cast<uint32_t *>(base + 16 * bt);
+    ps.last_ref = reinterpret_cast<uint32_t *>(base + 20 * bt);
+    ps.path = reinterpret_cast<uint32_t *>(base + 24 * bt);
+    return ps;
+}
+constexpr int kPathSlotBytes = 28;
+
+__device__ __forceinline__ void path_save(const path_slots &sl, int t, uint32_t p, const path_t &st) {
+    sl.rng[t] = st.rng.state;
+    sl.thr[t] = st.thr;
+    sl.digest[t] = st.digest;
+    sl.bounce[t] = st.bounce;
+    sl.last_ref[t] = st.last_ref;
+    sl.path[t] = p;
+}
+
+__device__ __forceinline__ uint32_t path_load(const path_slots &sl, int t, uint64_t seed, path_t &st) {
+    const uint32_t p = sl.path[t];
+    st.rng.state = sl.rng[t];
+    st.rng.inc = ((seed + p) << 1u) | 1u;
+    st.thr = sl.thr[t];
+    st.digest = sl.digest[t];
+    st.bounce = sl.bounce[t];
+    st.last_ref = sl.last_ref[t];
+    return p;
+}
+
 __device__ __forceinline__ float albedo_of(const pt_scene &ps, uint32_t material) {
     return material < ps.n_albedo ? __ldg(ps.albedo + material) : 0.8f;
 }
@@ -365,11 +408,11 @@ __global__ void __launch_bounds__(256) k_pt_fused(dev_scene sc, pt_scene ps, pt_
     const unsigned lanes_below = (1u << lane) - 1u;
     int *stk = s_stack + threadIdx.x;
     const int stride = blockDim.x;
+    const path_slots slots = path_slots_at(s_stack, STACK);
+    const int me = threadIdx.x;
     const uint32_t nl = *n_list;
     trav_t s;
     ray_t r;
-    path_t st;
-    uint32_t p = 0;
     bool tracing = false;   // the lane's ray is being traversed
     bool waiting = false;   // the lane's ray has ended and its hit waits to be shaded
     bool plain = false, exhausted = false;
@@ -377,10 +420,13 @@ __global__ void __launch_bounds__(256) k_pt_fused(dev_scene sc, pt_scene ps, pt_
         // shade phase: waiting lanes consume their hit
         if (waiting) {
             waiting = false;
+            path_t st;
+            const uint32_t p = path_load(slots, me, pp.seed, st);
             record_bounce(bounce_hits, pp, p, st.bounce, s.hit);
             pm::f3 o = {r.ox, r.oy, r.oz}, d = {r.dx, r.dy, r.dz};
             grt_path_result res;
             if (path_bounce<true>(ps, sc.records, pp, st, s.hit, o, d, res)) {
+                path_save(slots, me, p, st);
                 r = make_ray(o, d, pp.eps, FLT_MAX);
                 trav_init(s, sc);
                 plain = sc.finite && ray_is_plain(r);
@@ -402,13 +448,14 @@ __global__ void __launch_bounds__(256) k_pt_fused(dev_scene sc, pt_scene ps, pt_
                 if (!tracing) {
                     const uint32_t my = base + __popc(need & lanes_below);
                     if (my < n_paths) {
-                        p = my;
                         if (nl == 0) {
-                            results[p] = {0.f, 0u, pm::kMissWord, pm::kDigestSeed};
-                            clear_unused(bounce_hits, pp, p, 0);
+                            results[my] = {0.f, 0u, pm::kMissWord, pm::kDigestSeed};
+                            clear_unused(bounce_hits, pp, my, 0);
                         } else {
+                            path_t st;
                             float4 ro, rd;
-                            path_start(ps, pp, p, prim_rays, prim_hits, hit_list, nl, st, ro, rd);
+                            path_start(ps, pp, my, prim_rays, prim_hits, hit_list, nl, st, ro, rd);
+                            path_save(slots, me, my, st);
                             r = make_ray({ro.x, ro.y, ro.z}, {rd.x, rd.y, rd.z}, ro.w, rd.w);
                             trav_init(s, sc);
                             plain = sc.finite && ray_is_plain(r);
@@ -447,7 +494,7 @@ cudaError_t fused_launch(const dev_scene &sc, const pt_scene &ps, const pt_param
                          const grt_hit *prim_hits, const uint32_t *hit_list, const uint32_t *n_list, uint32_t n_paths,
                          grt_path_result *results, grt_hit *bounce_hits, const launch_params &lp, unsigned *err,
                          unsigned *counter, cudaStream_t st) {
-    const size_t smem = (size_t)STACK * lp.block_threads * sizeof(int);
+    const size_t smem = (size_t)(STACK * sizeof(int) + kPathSlotBytes) * lp.block_threads;
     auto kern = k_pt_fused<ORDER, STACK>;
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
@@ -519,7 +566,7 @@ cudaError_t launch_fused(const dev_scene &sc, const pt_scene &ps, const pt_param
 }
 
 cudaError_t prepare_pt_kernels() {
-    const int bytes = kStackLarge * 256 * (int)sizeof(int);
+    const int bytes = (kStackLarge * (int)sizeof(int) + kPathSlotBytes) * 256;
     for (const void *f : {(const void *)k_pt_fused<IF_IF, kStackSmall>, (const void *)k_pt_fused<IF_IF, kStackLarge>,
                           (const void *)k_pt_fused<WHILE_WHILE, kStackSmall>,
                           (const void *)k_pt_fused<WHILE_WHILE, kStackLarge>,
@@ -534,7 +581,7 @@ cudaError_t prepare_pt_kernels() {
 int fused_blocks_per_sm(int block_threads, int stack_entries, int order) {
     int blocks = 0;
     const bool small = stack_entries <= kStackSmall;
-    const size_t smem = (size_t)(small ? kStackSmall : kStackLarge) * block_threads * sizeof(int);
+    const size_t smem = (size_t)((small ? kStackSmall : kStackLarge) * sizeof(int) + kPathSlotBytes) * block_threads;
     const void *fn = order == WHILE_WHILE
                          ? (small ? (const void *)k_pt_fused<WHILE_WHILE, kStackSmall>
                                   : (const void *)k_pt_fused<WHILE_WHILE, kStackLarge>)
