@@ -282,6 +282,11 @@ def run_gb300(args):
             step.plain()
         plain_times[order] = statistics.median(time_steps(step, step.plain, 3)[0])
     plain_order = min(plain_times, key=plain_times.get)
+    # for reference only: the same plain wavefront on the 4-wide layout
+    step.rt_plain.select("bvh4-speculative-while-while")
+    for _ in range(2):
+        step.plain()
+    plain_bvh4_ms = statistics.median(time_steps(step, step.plain, 3)[0])
     step.rt_plain.select(plain_order)
 
     # rays per step of each form (identical work: same paths, same bounces)
@@ -357,7 +362,8 @@ def run_gb300(args):
                    "tuning": tuning or "defaults"},
         "plain_wavefront": {"value": round(plain_value, 1), "ms_per_step": round(statistics.mean(plain_ms), 4),
                             "rays_per_step": rays_plain, "loop_order": plain_order,
-                            "order_ms": {k: round(v, 4) for k, v in plain_times.items()}},
+                            "order_ms": {k: round(v, 4) for k, v in plain_times.items()},
+                            "bvh4_speculative_ms": round(plain_bvh4_ms, 4)},
         "speedup_vs_plain": round(value / plain_value, 3),
         "e2e": {"value": round(e2e_value, 1), "unit": "Mrays/s", "ms_per_step": round(statistics.mean(e2e_ms), 4),
                 "h2d_bytes_per_step": int(step.n_primary * 32), "d2h_bytes_per_step": int(N_PATHS * 16)},

@@ -22,7 +22,8 @@ STATUS_NAMES = {0: "GRT_OK", 1: "GRT_ERR_INVALID_ARG", 2: "GRT_ERR_OOM", 3: "GRT
                 8: "GRT_ERR_UNKNOWN_TRACER", 9: "GRT_ERR_NO_DEVICE"}
 SPLIT = {"om": 0, "sm": 1, "sah": 2}
 TRACERS = ("while-while", "persistent-while-while", "if-if", "persistent-if-if", "speculative-while-while",
-           "persistent-speculative-while-while")
+           "persistent-speculative-while-while", "bvh4-speculative-while-while",
+           "persistent-bvh4-speculative-while-while")
 EXACT_TRACERS = TRACERS[:4]  # per-ray visit order of the reference: bit-identical results
 
 

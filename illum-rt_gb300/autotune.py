@@ -58,7 +58,8 @@ def tune(quick: bool = False, n_paths: int = 4 << 20, res: int = 1024, log=print
     stream = torch.cuda.Stream()
     rt = api.BatchRayTracer(0)
     orders = ["persistent-while-while"] if quick else ["persistent-while-while", "persistent-if-if",
-                                                       "persistent-speculative-while-while"]
+                                                       "persistent-speculative-while-while",
+                                                       "persistent-bvh4-speculative-while-while"]
     leaf_sizes = [4] if quick else [2, 3, 4, 6, 8]
     blocks = [128] if quick else [64, 128, 256]
     thresholds = [12, 20, 28] if quick else [8, 12, 16, 20, 24, 28, 32]

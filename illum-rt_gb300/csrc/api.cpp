@@ -99,6 +99,9 @@ grt_status grt_build(grt_ctx *c, const float *vpos4, uint32_t nv, const uint32_t
     grt::flat_bvh flat;
     if (!grt::flatten_bvh(tree, vpos4, tris4, flat, msg)) return fail(c, GRT_ERR_INVALID_ARG, msg);
     c->stats.flatten_ms = ms_since(t0);
+    grt::flat_bvh4 wide;
+    if (!grt::flatten_bvh4(tree, flat, wide, msg)) return fail(c, GRT_ERR_INVALID_ARG, msg);
+    c->stats.flatten_ms = ms_since(t0);
     if (flat.depth > (uint32_t)grt::kStackLarge)
         return fail(c, GRT_ERR_BVH_TOO_DEEP,
                     "BVH depth " + std::to_string(flat.depth) + " exceeds the largest traversal stack (" +
@@ -117,6 +120,7 @@ grt_status grt_build(grt_ctx *c, const float *vpos4, uint32_t nv, const uint32_t
         if (e == cudaSuccess) e = cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
     };
     up(&c->d_nodes, flat.nodes.data(), nb);
+    up(&c->d_nodes4, wide.nodes.data(), wide.nodes.size() * 4);
     up(&c->d_recs, flat.records.data(), rb);
     up(&c->d_vpos, vpos4, vb);
     up(&c->d_tris, tris4, tb);
@@ -129,6 +133,9 @@ grt_status grt_build(grt_ctx *c, const float *vpos4, uint32_t nv, const uint32_t
     c->sc.nodes = (const float4 *)c->d_nodes;
     c->sc.records = (const float4 *)c->d_recs;
     c->sc.root = flat.root;
+    c->sc.nodes4 = (const float4 *)c->d_nodes4;
+    c->sc.root4 = wide.root;
+    c->stack_bound4 = wide.stack_bound;
     c->sc.empty = flat.empty ? 1 : 0;
     c->sc.finite = finite ? 1 : 0;
     c->nv = nv;
@@ -138,7 +145,7 @@ grt_status grt_build(grt_ctx *c, const float *vpos4, uint32_t nv, const uint32_t
     c->stats.inner_nodes = flat.inner;
     c->stats.tri_records = (uint32_t)tree.index.size();
     c->stats.depth = flat.depth;
-    c->stats.device_bytes = nb + rb + vb + tb;
+    c->stats.device_bytes = nb + rb + vb + tb + wide.nodes.size() * 4;
     c->tree = std::move(tree);
     c->built = true;
     return GRT_OK;
@@ -232,6 +239,8 @@ grt_status grt_trace(grt_ctx *c, const float *rays_dev, grt_hit *hits_dev, uint3
     if (n > (1u << 31)) return fail(c, GRT_ERR_INVALID_ARG, "more than 2^31 rays in one call");
     if (!rays_dev || !hits_dev || !aligned16(rays_dev) || !aligned16(hits_dev))
         return fail(c, GRT_ERR_INVALID_ARG, "ray and hit buffers must be non-null and 16-byte aligned");
+    if (needed_stack(c) > grt::kStackLarge)
+        return fail(c, GRT_ERR_BVH_TOO_DEEP, "the selected tracer needs a deeper stack than the kernels have");
     device_guard g(c->device);
     grt::launch_params lp = params_for(c, any_hit != 0);
     cudaError_t e;

@@ -178,6 +178,8 @@ grt_status grt_pathtrace(grt_ctx *c, const grt_pt_params *params, const float *p
         return fail(c, GRT_ERR_INVALID_ARG, "invalid path-tracing parameters");
     if (p.use_graph && !stream)
         return fail(c, GRT_ERR_INVALID_ARG, "graph replay needs a stream other than the legacy default stream");
+    if (needed_stack(c) > grt::kStackLarge)
+        return fail(c, GRT_ERR_BVH_TOO_DEEP, "the selected tracer needs a deeper stack than the kernels have");
     device_guard g(c->device);
     const bool wavefront = p.mode == GRT_PT_WAVEFRONT;
     const pt_layout L = layout_for(n_primary, n_paths, wavefront);

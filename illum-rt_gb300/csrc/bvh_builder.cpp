@@ -16,6 +16,7 @@
 #include <cfloat>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <future>
 #include <thread>
 
@@ -449,6 +450,92 @@ bool flatten_bvh(const ref_tree &tree, const float *vpos4, const uint32_t *tris4
         r[10] = a[2] - c[2];
         r[11] = 0.f;
     }
+    return true;
+}
+
+bool flatten_bvh4(const ref_tree &tree, const flat_bvh &flat, flat_bvh4 &out, std::string &err) {
+    out = flat_bvh4();
+    if (flat.empty) return true;
+    const auto &N = tree.nodes;
+    auto leaf_ref = [&](int32_t link) {
+        const ref_node &c = N[link];
+        uint32_t first = (uint32_t)(-c.link_l), count = (uint32_t)(-c.link_r);
+        return ~(int32_t)((first << 4) | (count - 1));
+    };
+    if (!N[tree.root].inner()) {
+        out.root = leaf_ref((int32_t)tree.root);
+        return true;
+    }
+    struct child {
+        float lo[3], hi[3];
+        int32_t link;  // reference node
+    };
+    // explicit stack of (reference inner node, wide slot); wide slots are assigned in preorder
+    std::vector<std::pair<uint32_t, uint32_t>> todo;
+    std::vector<uint32_t> bound;   // stack bound of the subtree under each wide node
+    std::vector<std::vector<uint32_t>> kids;  // wide children of each wide node
+    auto new_node = [&]() {
+        out.nodes.resize(out.nodes.size() + 32, 0.f);
+        kids.emplace_back();
+        return (uint32_t)(out.nodes.size() / 32 - 1);
+    };
+    // recursive lambda via explicit function object (depth is at most the reference depth)
+    std::function<uint32_t(uint32_t)> build = [&](uint32_t bin) -> uint32_t {
+        const uint32_t w = new_node();
+        const ref_node &n = N[bin];
+        child ch[4];
+        int k = 0;
+        const float *boxes[2][2] = {{n.lmin, n.lmax}, {n.rmin, n.rmax}};
+        const int32_t links[2] = {n.link_l, n.link_r};
+        for (int side = 0; side < 2; ++side) {
+            const ref_node &c = N[links[side]];
+            if (c.inner()) {
+                const float *gb[2][2] = {{c.lmin, c.lmax}, {c.rmin, c.rmax}};
+                const int32_t gl[2] = {c.link_l, c.link_r};
+                for (int g = 0; g < 2; ++g) {
+                    std::memcpy(ch[k].lo, gb[g][0], 12);
+                    std::memcpy(ch[k].hi, gb[g][1], 12);
+                    ch[k++].link = gl[g];
+                }
+            } else {
+                std::memcpy(ch[k].lo, boxes[side][0], 12);
+                std::memcpy(ch[k].hi, boxes[side][1], 12);
+                ch[k++].link = links[side];
+            }
+        }
+        int32_t ref[4];
+        for (int i = 0; i < 4; ++i) {
+            if (i >= k) {
+                ref[i] = kEmptyChild;
+            } else if (N[ch[i].link].inner()) {
+                const uint32_t cw = build((uint32_t)ch[i].link);
+                kids[w].push_back(cw);
+                ref[i] = (int32_t)cw;
+            } else {
+                ref[i] = leaf_ref(ch[i].link);
+            }
+        }
+        float *d = out.nodes.data() + 32 * (size_t)w;
+        for (int i = 0; i < 4; ++i) {
+            const bool used = i < k;
+            const float inf = __builtin_inff();
+            for (int a = 0; a < 3; ++a) {
+                d[4 * (2 * a) + i] = used ? ch[i].lo[a] : inf;
+                d[4 * (2 * a + 1) + i] = used ? ch[i].hi[a] : inf;
+            }
+            std::memcpy(d + 24 + i, &ref[i], 4);
+        }
+        uint32_t sub = 0;
+        for (uint32_t cw : kids[w]) sub = std::max(sub, bound[cw]);
+        if (bound.size() <= w) bound.resize(w + 1, 0);
+        bound[w] = (uint32_t)(k - 1) + sub;
+        return w;
+    };
+    bound.reserve(N.size());
+    out.root = (int32_t)build(tree.root);
+    out.count = (uint32_t)(out.nodes.size() / 32);
+    out.stack_bound = bound[0];
+    (void)err;
     return true;
 }
 

@@ -61,4 +61,22 @@ static const uint32_t kMaxRecords = 1u << 27;
 
 bool flatten_bvh(const ref_tree &tree, const float *vpos4, const uint32_t *tris4, flat_bvh &out, std::string &err);
 
+// 4-wide device layout: the reference tree collapsed two levels at a time. A wide node holds
+// the children of a binary node's inner children (the grandchildren) and its leaf children,
+// 2 to 4 of them, with their boxes as the reference stores them. 128 bytes, eight float4:
+//   [0] lo.x of children 0..3   [1] hi.x   [2] lo.y   [3] hi.y   [4] lo.z   [5] hi.z
+//   [6] child references (int bits): >= 0 wide node, < 0 leaf (same encoding and the same
+//       triangle records as the binary layout), kEmptyChild for an unused slot
+//   [7] unused
+// Children appear in the reference's left-to-right order; wide nodes are in preorder.
+static const int32_t kEmptyChild = 0x7fffffff;
+struct flat_bvh4 {
+    std::vector<float> nodes;  // 32 floats per wide node
+    int32_t root = 0;          // wide node 0, or a leaf reference if the tree is one leaf
+    uint32_t count = 0;
+    uint32_t stack_bound = 0;  // most stack entries a traversal can hold
+};
+
+bool flatten_bvh4(const ref_tree &tree, const flat_bvh &flat, flat_bvh4 &out, std::string &err);
+
 }  // namespace grt

@@ -18,8 +18,8 @@ struct grt_ctx {
     bool built = false;
     grt::ref_tree tree;
     grt::dev_scene sc{};
-    void *d_nodes = nullptr, *d_recs = nullptr, *d_vpos = nullptr, *d_tris = nullptr;
-    uint32_t nv = 0, nt = 0, depth = 0;
+    void *d_nodes = nullptr, *d_recs = nullptr, *d_vpos = nullptr, *d_tris = nullptr, *d_nodes4 = nullptr;
+    uint32_t nv = 0, nt = 0, depth = 0, stack_bound4 = 0;
     grt_bvh_stats stats{};
     int tracer = 0;  // index into kTracers
     grt_tuning tuning{};
@@ -68,7 +68,7 @@ inline grt_status cuda_fail(grt_ctx *c, cudaError_t e, const char *what) {
 }
 
 inline void free_scene(grt_ctx *c) {
-    for (void **p : {&c->d_nodes, &c->d_recs, &c->d_vpos, &c->d_tris}) {
+    for (void **p : {&c->d_nodes, &c->d_recs, &c->d_vpos, &c->d_tris, &c->d_nodes4}) {
         if (*p) cudaFree(*p);
         *p = nullptr;
     }
@@ -91,14 +91,22 @@ inline const tracer_kind kTracers[] = {{"while-while", false, WHILE_WHILE},
                                        {"if-if", false, IF_IF},
                                        {"persistent-if-if", true, IF_IF},
                                        {"speculative-while-while", false, SPECULATIVE},
-                                       {"persistent-speculative-while-while", true, SPECULATIVE}};
-inline const int kNumTracers = 6;
+                                       {"persistent-speculative-while-while", true, SPECULATIVE},
+                                       {"bvh4-speculative-while-while", false, WIDE_SPECULATIVE},
+                                       {"persistent-bvh4-speculative-while-while", true, WIDE_SPECULATIVE}};
+inline const int kNumTracers = 8;
+
+// Stack entries the selected tracer needs on the current scene.
+inline int needed_stack(const grt_ctx *c) {
+    return kTracers[c->tracer].order == WIDE_SPECULATIVE ? (int)c->stack_bound4 : (int)c->depth;
+}
 
 inline launch_params params_for(grt_ctx *c, bool any_hit) {
     grt::launch_params lp{};
     const grt_tuning &t = c->tuning;
-    lp.stack_entries = t.stack_entries > 0 ? t.stack_entries : (int)c->depth;
-    if (lp.stack_entries < (int)c->depth) lp.stack_entries = (int)c->depth;
+    const int needed = needed_stack(c);
+    lp.stack_entries = t.stack_entries > 0 ? t.stack_entries : needed;
+    if (lp.stack_entries < needed) lp.stack_entries = needed;
     lp.block_threads = t.block_threads > 0 ? t.block_threads : 128;
     lp.refill_threshold = t.refill_threshold > 0 ? t.refill_threshold : 20;
     lp.refill_period = t.refill_period > 0 ? t.refill_period : 4;

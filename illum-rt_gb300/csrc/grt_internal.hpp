@@ -12,10 +12,11 @@ namespace grt {
 struct dev_scene {
     const float4 *nodes;    // 4 float4 per inner node (layout in bvh_builder.hpp)
     const float4 *records;  // 3 float4 per triangle record
+    const float4 *nodes4;   // 8 float4 per 4-wide node (flat_bvh4)
     int32_t root;           // child reference of the root
+    int32_t root4;          // child reference of the 4-wide root
     int32_t empty;          // 1: no triangles, every ray misses
     int32_t finite;         // 1: every vertex coordinate is finite (enables the min/max slab test)
-    int32_t pad;
 };
 
 // Bits a kernel ORs into the context's error word.
@@ -32,8 +33,10 @@ static const uint32_t kStepLimit = 1u << 26;
 
 // Loop orders of the traversal kernels (traverse.cuh): one node or leaf per iteration; inner
 // nodes until a leaf and then that leaf; speculative while-while (postponed leaves, results
-// equal to the reference's except near-ties).
-enum loop_order : int { IF_IF = 0, WHILE_WHILE = 1, SPECULATIVE = 2 };
+// equal to the reference's except near-ties); the speculative order over 4-wide nodes (the
+// same near-tie guarantee).
+enum loop_order : int { IF_IF = 0, WHILE_WHILE = 1, SPECULATIVE = 2, WIDE_SPECULATIVE = 3 };
+static const int32_t kEmptyWideChild = 0x7fffffff;  // unused slot of a 4-wide node
 
 struct launch_params {
     int block_threads;

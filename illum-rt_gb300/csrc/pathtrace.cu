@@ -409,6 +409,8 @@ __global__ void __launch_bounds__(256) k_pt_fused(dev_scene sc, pt_scene ps, pt_
     int *stk = s_stack + threadIdx.x;
     const int stride = blockDim.x;
     const path_slots slots = path_slots_at(s_stack, STACK);
+    constexpr bool SPEC = ORDER == SPECULATIVE || ORDER == WIDE_SPECULATIVE;
+    constexpr bool WIDE = ORDER == WIDE_SPECULATIVE;
     const int me = threadIdx.x;
     const uint32_t nl = *n_list;
     trav_t s;
@@ -428,7 +430,7 @@ __global__ void __launch_bounds__(256) k_pt_fused(dev_scene sc, pt_scene ps, pt_
             if (path_bounce<true>(ps, sc.records, pp, st, s.hit, o, d, res)) {
                 path_save(slots, me, p, st);
                 r = make_ray(o, d, pp.eps, FLT_MAX);
-                trav_init(s, sc);
+                trav_init(s, sc, WIDE);
                 plain = sc.finite && ray_is_plain(r);
                 tracing = true;
             } else {
@@ -457,7 +459,7 @@ __global__ void __launch_bounds__(256) k_pt_fused(dev_scene sc, pt_scene ps, pt_
                             path_start(ps, pp, my, prim_rays, prim_hits, hit_list, nl, st, ro, rd);
                             path_save(slots, me, my, st);
                             r = make_ray({ro.x, ro.y, ro.z}, {rd.x, rd.y, rd.z}, ro.w, rd.w);
-                            trav_init(s, sc);
+                            trav_init(s, sc, WIDE);
                             plain = sc.finite && ray_is_plain(r);
                             tracing = true;
                         }
@@ -471,8 +473,8 @@ __global__ void __launch_bounds__(256) k_pt_fused(dev_scene sc, pt_scene ps, pt_
         }
         // traversal phase
         for (int it = 1;; ++it) {
-            if (ORDER == SPECULATIVE)
-                trav_spec_iter<STACK, false, false>(s, tracing, plain, sc, r, stk, stride, err);
+            if (SPEC)
+                trav_spec_iter<STACK, false, false, WIDE>(s, tracing, plain, sc, r, stk, stride, err);
             else if (tracing && plain)
                 trav_advance<ORDER, STACK, false, false, true>(s, sc, r, stk, stride, err);
             else if (tracing)
@@ -559,9 +561,11 @@ cudaError_t launch_fused(const dev_scene &sc, const pt_scene &ps, const pt_param
     const bool small = lp.stack_entries <= kStackSmall;
     auto f = lp.order == WHILE_WHILE
                  ? (small ? fused_launch<WHILE_WHILE, kStackSmall> : fused_launch<WHILE_WHILE, kStackLarge>)
-                 : lp.order == SPECULATIVE
-                       ? (small ? fused_launch<SPECULATIVE, kStackSmall> : fused_launch<SPECULATIVE, kStackLarge>)
-                       : (small ? fused_launch<IF_IF, kStackSmall> : fused_launch<IF_IF, kStackLarge>);
+             : lp.order == SPECULATIVE
+                 ? (small ? fused_launch<SPECULATIVE, kStackSmall> : fused_launch<SPECULATIVE, kStackLarge>)
+             : lp.order == WIDE_SPECULATIVE
+                 ? (small ? fused_launch<WIDE_SPECULATIVE, kStackSmall> : fused_launch<WIDE_SPECULATIVE, kStackLarge>)
+                 : (small ? fused_launch<IF_IF, kStackSmall> : fused_launch<IF_IF, kStackLarge>);
     return f(sc, ps, pp, prim_rays, prim_hits, hit_list, n_list, n_paths, results, bounce_hits, lp, err, counter, st);
 }
 
@@ -571,7 +575,9 @@ cudaError_t prepare_pt_kernels() {
                           (const void *)k_pt_fused<WHILE_WHILE, kStackSmall>,
                           (const void *)k_pt_fused<WHILE_WHILE, kStackLarge>,
                           (const void *)k_pt_fused<SPECULATIVE, kStackSmall>,
-                          (const void *)k_pt_fused<SPECULATIVE, kStackLarge>}) {
+                          (const void *)k_pt_fused<SPECULATIVE, kStackLarge>,
+                          (const void *)k_pt_fused<WIDE_SPECULATIVE, kStackSmall>,
+                          (const void *)k_pt_fused<WIDE_SPECULATIVE, kStackLarge>}) {
         cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
         if (e != cudaSuccess) return e;
     }
@@ -588,6 +594,9 @@ int fused_blocks_per_sm(int block_threads, int stack_entries, int order) {
                      : order == SPECULATIVE
                          ? (small ? (const void *)k_pt_fused<SPECULATIVE, kStackSmall>
                                   : (const void *)k_pt_fused<SPECULATIVE, kStackLarge>)
+                     : order == WIDE_SPECULATIVE
+                         ? (small ? (const void *)k_pt_fused<WIDE_SPECULATIVE, kStackSmall>
+                                  : (const void *)k_pt_fused<WIDE_SPECULATIVE, kStackLarge>)
                          : (small ? (const void *)k_pt_fused<IF_IF, kStackSmall> : (const void *)k_pt_fused<IF_IF, kStackLarge>);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, block_threads, smem) != cudaSuccess) return 1;
     return blocks > 0 ? blocks : 1;

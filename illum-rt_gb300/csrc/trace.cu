@@ -28,17 +28,19 @@ __global__ void __launch_bounds__(256) k_trace_plain(const float4 *__restrict__ 
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (n_dev) n = *n_dev;  // ray count produced on the device (wavefront queues)
     const bool active = i < n;
-    if (ORDER != SPECULATIVE && !active) return;
+    constexpr bool SPEC = ORDER == SPECULATIVE || ORDER == WIDE_SPECULATIVE;
+    constexpr bool WIDE = ORDER == WIDE_SPECULATIVE;
+    if (!SPEC && !active) return;
     ray_t r = {};
     if (active) r = load_ray(rays, i);
     trav_t s;
-    trav_init(s, sc);
+    trav_init(s, sc, WIDE);
     int *stk = s_stack + threadIdx.x;
     const int stride = blockDim.x;
     const bool plain = active && sc.finite && ray_is_plain(r);
-    if (ORDER == SPECULATIVE) {  // the whole warp stays in the loop until its last ray ends
+    if (SPEC) {  // the whole warp stays in the loop until its last ray ends
         while (__any_sync(kFull, active && !s.done))
-            trav_spec_iter<STACK, ANY, COUNT>(s, active, plain, sc, r, stk, stride, err);
+            trav_spec_iter<STACK, ANY, COUNT, WIDE>(s, active, plain, sc, r, stk, stride, err);
         if (!active) return;
     } else if (plain) {  // one loop per slab variant: the choice is made once per ray
         while (!s.done) trav_advance<ORDER, STACK, ANY, COUNT, true>(s, sc, r, stk, stride, err);
@@ -58,6 +60,8 @@ __global__ void __launch_bounds__(256) k_trace_persistent(const float4 *__restri
                                                           uint32_t n, dev_scene sc, unsigned *err,
                                                           unsigned *counter, int refill_threshold, int refill_period) {
     extern __shared__ int s_stack[];
+    constexpr bool SPEC = ORDER == SPECULATIVE || ORDER == WIDE_SPECULATIVE;
+    constexpr bool WIDE = ORDER == WIDE_SPECULATIVE;
     const unsigned lane = threadIdx.x & 31u;
     const unsigned lanes_below = (1u << lane) - 1u;
     int *stk = s_stack + threadIdx.x;
@@ -81,7 +85,7 @@ __global__ void __launch_bounds__(256) k_trace_persistent(const float4 *__restri
                     if (my < n) {
                         idx = my;
                         r = load_ray(rays, my);
-                        trav_init(s, sc);
+                        trav_init(s, sc, WIDE);
                         plain = sc.finite && ray_is_plain(r);
                         have = true;
                         if (s.done) {  // empty scene
@@ -98,8 +102,8 @@ __global__ void __launch_bounds__(256) k_trace_persistent(const float4 *__restri
         }
         // traverse; every `refill_period` iterations the warp counts its busy lanes
         for (int it = 1;; ++it) {
-            if (ORDER == SPECULATIVE)
-                trav_spec_iter<STACK, ANY, false>(s, have, plain, sc, r, stk, stride, err);
+            if (SPEC)
+                trav_spec_iter<STACK, ANY, false, WIDE>(s, have, plain, sc, r, stk, stride, err);
             else if (have && plain)
                 trav_advance<ORDER, STACK, ANY, false, true>(s, sc, r, stk, stride, err);
             else if (have)
@@ -145,6 +149,13 @@ cudaError_t persistent_launch(const dev_scene &sc, const float4 *rays, grt_hit *
 template <template <int, int, bool> class F, typename... A>
 cudaError_t dispatch(int order, int stack_entries, bool any_hit, A &&...a) {
     const bool small = stack_entries <= kStackSmall;
+    if (order == WIDE_SPECULATIVE) {
+        if (small)
+            return any_hit ? F<WIDE_SPECULATIVE, kStackSmall, true>::run(a...)
+                           : F<WIDE_SPECULATIVE, kStackSmall, false>::run(a...);
+        return any_hit ? F<WIDE_SPECULATIVE, kStackLarge, true>::run(a...)
+                       : F<WIDE_SPECULATIVE, kStackLarge, false>::run(a...);
+    }
     if (order == SPECULATIVE) {
         if (small)
             return any_hit ? F<SPECULATIVE, kStackSmall, true>::run(a...) : F<SPECULATIVE, kStackSmall, false>::run(a...);
@@ -197,7 +208,7 @@ cudaError_t launch_trace_persistent(const dev_scene &sc, const float4 *rays, grt
 
 cudaError_t prepare_trace_kernels() {
     const int bytes = kStackLarge * 256 * (int)sizeof(int);  // largest stack variant at 256 threads
-    for (int order : {(int)IF_IF, (int)WHILE_WHILE, (int)SPECULATIVE})
+    for (int order : {(int)IF_IF, (int)WHILE_WHILE, (int)SPECULATIVE, (int)WIDE_SPECULATIVE})
         for (int stack : {kStackSmall, kStackLarge})
             for (bool any : {false, true}) {
                 cudaError_t e = dispatch<attr_f>(order, stack, any, bytes);

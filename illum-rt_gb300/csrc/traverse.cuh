@@ -154,8 +154,8 @@ struct trav_t {
     hit_t hit;
 };
 
-__device__ __forceinline__ void trav_init(trav_t &s, const dev_scene &sc) {
-    s.cur = sc.root;
+__device__ __forceinline__ void trav_init(trav_t &s, const dev_scene &sc, bool wide = false) {
+    s.cur = wide ? sc.root4 : sc.root;
     s.sp = 0;
     s.steps = 0;
     s.done = sc.empty != 0;
@@ -355,6 +355,77 @@ __device__ __forceinline__ void spec_node(trav_t &s, const dev_scene &sc, const 
     }
 }
 
+// Visit of a 4-wide node: four slab tests, the hit children ordered by entry distance (a
+// five-comparator sorting network), the nearest kept in `cur` and the others pushed farthest
+// first. Every child box is a subset of the binary box the collapse skipped, and rounding is
+// monotone, so a child the reference would reach is never culled here.
+template <int STACK, bool ANY, bool PLAIN>
+__device__ __forceinline__ void spec_node4(trav_t &s, const dev_scene &sc, const ray_t &r, int *stk, int stride,
+                                           unsigned *err) {
+    const float4 *np = sc.nodes4 + 8 * (size_t)s.cur;
+    const float4 lx = __ldg(np), hx = __ldg(np + 1), ly = __ldg(np + 2), hy = __ldg(np + 3);
+    const float4 lz = __ldg(np + 4), hz = __ldg(np + 5);
+    const int4 cr = __ldg(reinterpret_cast<const int4 *>(np + 6));
+    float k[4];
+    int c[4] = {cr.x, cr.y, cr.z, cr.w};
+    bool h0 = slab<PLAIN>(lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, r, k[0]);
+    bool h1 = slab<PLAIN>(lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, r, k[1]);
+    bool h2 = slab<PLAIN>(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, r, k[2]);
+    bool h3 = slab<PLAIN>(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, r, k[3]);
+    if (!ANY) {
+        h0 = h0 && k[0] < s.hit.t;
+        h1 = h1 && k[1] < s.hit.t;
+        h2 = h2 && k[2] < s.hit.t;
+        h3 = h3 && k[3] < s.hit.t;
+    }
+    const bool hit[4] = {h0, h1, h2, h3};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        if (!hit[i] || c[i] == kEmptyWideChild) {
+            c[i] = kEmptyWideChild;
+            k[i] = __int_as_float(0x7f800000);  // +inf
+        }
+    }
+#define GRT_CSWAP(a, b)                          \
+    if (k[b] < k[a]) {                           \
+        const float tk = k[a];                   \
+        k[a] = k[b];                             \
+        k[b] = tk;                               \
+        const int tc = c[a];                     \
+        c[a] = c[b];                             \
+        c[b] = tc;                               \
+    }
+    GRT_CSWAP(0, 1)
+    GRT_CSWAP(2, 3)
+    GRT_CSWAP(0, 2)
+    GRT_CSWAP(1, 3)
+    GRT_CSWAP(1, 2)
+#undef GRT_CSWAP
+    int32_t next = kEmptyWideChild;
+#pragma unroll
+    for (int i = 3; i >= 0; --i) {
+        if (c[i] == kEmptyWideChild) continue;
+        if (next != kEmptyWideChild) {
+            if (s.sp >= STACK) {
+                atomicOr(err, ERR_STACK_OVERFLOW);
+                s.done = true;
+                return;
+            }
+            stk[s.sp * stride] = next;
+            ++s.sp;
+        }
+        next = c[i];
+    }
+    if (next != kEmptyWideChild) {
+        s.cur = next;
+    } else if (s.sp == 0) {
+        s.more = false;
+    } else {
+        --s.sp;
+        s.cur = stk[s.sp * stride];
+    }
+}
+
 // The speculative while-while order (the reference's speculativewhilewhile_traversal,
 // rt/cuda/trace-kernels.cu:1433-1540, after Aila and Laine): a lane that reaches a leaf
 // postpones it and keeps visiting inner nodes while other lanes of the warp are still looking
@@ -364,7 +435,7 @@ __device__ __forceinline__ void spec_node(trav_t &s, const dev_scene &sc, const 
 // postponed leaf use the closest hit from before that leaf, so the ray may visit nodes the
 // reference would have culled. A triangle found there can replace the reference's answer only
 // if its t lies within rounding of the culled box's entry distance: a near-tie.
-template <int STACK, bool ANY, bool COUNT>
+template <int STACK, bool ANY, bool COUNT, bool WIDE = false>
 __device__ __forceinline__ void trav_spec_iter(trav_t &s, bool active, bool plain, const dev_scene &sc,
                                                const ray_t &r, int *stk, int stride, unsigned *err) {
     const bool mine = active && !s.done;
@@ -375,10 +446,17 @@ __device__ __forceinline__ void trav_spec_iter(trav_t &s, bool active, bool plai
                 s.done = true;
             } else {
                 if (COUNT) ++s.n_inner;
-                if (plain)
-                    spec_node<STACK, ANY, true>(s, sc, r, stk, stride, err);
-                else
-                    spec_node<STACK, ANY, false>(s, sc, r, stk, stride, err);
+                if (WIDE) {
+                    if (plain)
+                        spec_node4<STACK, ANY, true>(s, sc, r, stk, stride, err);
+                    else
+                        spec_node4<STACK, ANY, false>(s, sc, r, stk, stride, err);
+                } else {
+                    if (plain)
+                        spec_node<STACK, ANY, true>(s, sc, r, stk, stride, err);
+                    else
+                        spec_node<STACK, ANY, false>(s, sc, r, stk, stride, err);
+                }
             }
         }
         if (mine && !s.done && s.more && s.cur < 0 && s.pend == 0) {

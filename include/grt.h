@@ -147,10 +147,11 @@ void grt_host_bvh_free(grt_host_bvh *bvh);
 /* ---- tracer selection (platform::select / `raytracer <name>`, rt/cuda/platform.cpp:102-131) */
 
 /* Names: "while-while" (default), "if-if" and "speculative-while-while": one thread per ray,
- * in the loop orders of the reference's tracers of those names; the same names prefixed with
+ * in the loop orders of the reference's tracers of those names; "bvh4-speculative-while-while":
+ * the speculative order over the BVH collapsed into 4-wide nodes; the same names prefixed with
  * "persistent-": persistent warps with dynamic ray fetch. The loop order of the selected tracer
  * is also the one grt_pathtrace uses. The if-if and while-while orders give results identical
- * to the reference CPU tracer; the speculative order may differ from it in near-ties only (a
+ * to the reference CPU tracer; the speculative orders may differ from it in near-ties only (a
  * different triangle whose t is within a few ulps of the reference's). Unknown name:
  * GRT_ERR_UNKNOWN_TRACER. */
 grt_status grt_select_tracer(grt_ctx *ctx, const char *name);

@@ -77,7 +77,7 @@ def test_shadow_rays_and_any_hit(spheres_setup):
     s["rt"].select("while-while")
 
 
-@pytest.mark.parametrize("tracer", ["while-while", "if-if", "speculative-while-while"])
+@pytest.mark.parametrize("tracer", ["while-while", "if-if", "speculative-while-while", "bvh4-speculative-while-while"])
 @pytest.mark.parametrize("mode,graph", [(0, 0), (1, 0), (0, 1), (1, 1)], ids=["wavefront", "fused", "wavefront-graph",
                                                                           "fused-graph"])
 def test_pathtrace_matches_oracle(api, spheres_setup, mode, graph, tracer):

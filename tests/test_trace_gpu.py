@@ -15,7 +15,8 @@ def _needs_cuda():
         pytest.skip("no CUDA device")
 
 TRACERS = ["while-while", "persistent-while-while", "if-if", "persistent-if-if", "speculative-while-while",
-           "persistent-speculative-while-while"]
+           "persistent-speculative-while-while", "bvh4-speculative-while-while",
+           "persistent-bvh4-speculative-while-while"]
 
 
 def exact(tracer):
