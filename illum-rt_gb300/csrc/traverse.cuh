@@ -133,6 +133,15 @@ __device__ __forceinline__ bool tri_test(const float4 &p0, const float4 &p1, con
     return false;
 }
 
+// One 256-bit read-only load (two float4) from a 32-byte-aligned address: a 64-byte binary
+// node is two such loads (each half is one child's box and reference), four fewer L1 requests
+// per node than 128-bit loads.
+__device__ __forceinline__ void ldg256(const float4 *p, float4 &a, float4 &b) {
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p));
+}
+
 // Decoding of a leaf child reference: ~ref = (first << 4) | (count - 1).
 __device__ __forceinline__ void leaf_range(int32_t ref, uint32_t &first, uint32_t &count) {
     const uint32_t v = ~(uint32_t)ref;
@@ -188,7 +197,9 @@ __device__ __forceinline__ void trav_iter(trav_t &s, const dev_scene &sc, const 
         }
         if (COUNT) ++s.n_inner;
         const float4 *np = sc.nodes + 4 * (size_t)s.cur;
-        const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3);
+        float4 n0, n1, n2, n3;
+        ldg256(np, n0, n1);
+        ldg256(np + 2, n2, n3);
         float dl, dr;
         bool hl = slab<PLAIN>(n0.x, n0.y, n0.z, n1.x, n1.y, n1.z, r, dl);
         bool hr = slab<PLAIN>(n2.x, n2.y, n2.z, n3.x, n3.y, n3.z, r, dr);
@@ -265,7 +276,9 @@ __device__ __forceinline__ void trav_step(trav_t &s, const dev_scene &sc, const 
     if (s.cur >= 0) {
         if (COUNT) ++s.n_inner;
         const float4 *np = sc.nodes + 4 * (size_t)s.cur;
-        const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3);
+        float4 n0, n1, n2, n3;
+        ldg256(np, n0, n1);
+        ldg256(np + 2, n2, n3);
         float dl, dr;
         bool hl = slab<PLAIN>(n0.x, n0.y, n0.z, n1.x, n1.y, n1.z, r, dl);
         bool hr = slab<PLAIN>(n2.x, n2.y, n2.z, n3.x, n3.y, n3.z, r, dr);
@@ -326,7 +339,9 @@ template <int STACK, bool ANY, bool PLAIN>
 __device__ __forceinline__ void spec_node(trav_t &s, const dev_scene &sc, const ray_t &r, int *stk, int stride,
                                           unsigned *err) {
     const float4 *np = sc.nodes + 4 * (size_t)s.cur;
-    const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3);
+    float4 n0, n1, n2, n3;
+        ldg256(np, n0, n1);
+        ldg256(np + 2, n2, n3);
     float dl, dr;
     bool hl = slab<PLAIN>(n0.x, n0.y, n0.z, n1.x, n1.y, n1.z, r, dl);
     bool hr = slab<PLAIN>(n2.x, n2.y, n2.z, n3.x, n3.y, n3.z, r, dr);
@@ -363,9 +378,12 @@ template <int STACK, bool ANY, bool PLAIN>
 __device__ __forceinline__ void spec_node4(trav_t &s, const dev_scene &sc, const ray_t &r, int *stk, int stride,
                                            unsigned *err) {
     const float4 *np = sc.nodes4 + 8 * (size_t)s.cur;
-    const float4 lx = __ldg(np), hx = __ldg(np + 1), ly = __ldg(np + 2), hy = __ldg(np + 3);
-    const float4 lz = __ldg(np + 4), hz = __ldg(np + 5);
-    const int4 cr = __ldg(reinterpret_cast<const int4 *>(np + 6));
+    float4 lx, hx, ly, hy, lz, hz, crf, unused;
+    ldg256(np, lx, hx);
+    ldg256(np + 2, ly, hy);
+    ldg256(np + 4, lz, hz);
+    ldg256(np + 6, crf, unused);
+    const int4 cr = make_int4(__float_as_int(crf.x), __float_as_int(crf.y), __float_as_int(crf.z), __float_as_int(crf.w));
     float k[4];
     int c[4] = {cr.x, cr.y, cr.z, cr.w};
     bool h0 = slab<PLAIN>(lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, r, k[0]);
