@@ -60,6 +60,15 @@ class PtParams(ctypes.Structure):
 PT_WAVEFRONT, PT_FUSED = 0, 1
 
 
+class Mesh(ctypes.Structure):
+    _fields_ = [("vpos4", ctypes.c_void_p), ("nv", ctypes.c_uint32), ("tris4", ctypes.c_void_p), ("nt", ctypes.c_uint32)]
+
+
+class RayBatch(ctypes.Structure):
+    _fields_ = [("scene", ctypes.c_uint32), ("n", ctypes.c_uint32), ("rays_dev", ctypes.c_void_p),
+                ("hits_dev", ctypes.c_void_p)]
+
+
 class Config(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("reserved", ctypes.c_uint32)]
 
@@ -92,6 +101,11 @@ _PROTOS = {
     "grt_set_materials": (I, [VP, VP, U32]),
     "grt_pt_params_default": (None, [P(PtParams)]),
     "grt_pathtrace": (I, [VP, P(PtParams), VP, VP, U32, U32, VP, VP, VP]),
+    "grt_adjoint": (I, [VP, VP, VP, VP, U32, VP, U32, VP, VP, VP]),
+    "grt_build_scenes": (I, [VP, VP, U32, P(BvhOpts)]),
+    "grt_scene_info": (I, [VP, U32, P(BvhStats)]),
+    "grt_export_scene_bvh": (I, [VP, U32, VP, VP, P(U32)]),
+    "grt_trace_multi": (I, [VP, VP, U32, I, VP]),
 }
 
 
@@ -312,3 +326,39 @@ class BatchRayTracer:
         self._check(lib().grt_pathtrace(self.ctx, ctypes.byref(params), _ptr(prim_rays), _ptr(prim_hits),
                                         int(prim_rays.shape[0]), int(n_paths), _ptr(results),
                                         _ptr(bounce_hits) if bounce_hits is not None else None, VP(stream or 0)))
+
+    def adjoint(self, rays, hits, grad_hits, grad_vpos=None, grad_rays=None, vpos=None, stream=None):
+        """grt_adjoint: grad_hits [n, 3] = (dL/dt, dL/dbeta, dL/dgamma); grad_vpos [nv, 3] is added to,
+        grad_rays [n, 8] written. vpos: [nv, 3] or [nv, 4] float32 device tensor, or None for the
+        built scene's vertices."""
+        vstride = 0 if vpos is None else int(vpos.shape[1])
+        self._check(lib().grt_adjoint(self.ctx, _ptr(rays), _ptr(hits), _ptr(grad_hits), int(rays.shape[0]),
+                                      _ptr(vpos) if vpos is not None else None, vstride,
+                                      _ptr(grad_vpos) if grad_vpos is not None else None,
+                                      _ptr(grad_rays) if grad_rays is not None else None, VP(stream or 0)))
+
+    # -- many scenes in one launch ----------------------------------------------------------
+    def build_scenes(self, scenes, **opts) -> list:
+        """scenes: list of (vpos float32 [nv, 4], tris uint32 [nt, 4]). Returns per-scene stats."""
+        keep = [(np.ascontiguousarray(v, np.float32), np.ascontiguousarray(t, np.uint32)) for v, t in scenes]
+        arr = (Mesh * len(keep))(*[Mesh(_ptr(v), v.shape[0], _ptr(t), t.shape[0]) for v, t in keep])
+        o = make_opts(**{"split": self.bvh_type, "max_tris": self.bvh_max_tris_per_node, **opts})
+        self._check(lib().grt_build_scenes(self.ctx, arr, len(keep), ctypes.byref(o)))
+        out = []
+        for i in range(len(keep)):
+            st = BvhStats()
+            self._check(lib().grt_scene_info(self.ctx, i, ctypes.byref(st)))
+            out.append(st.as_dict())
+        return out
+
+    def export_scene_bvh(self, scene: int, ref_nodes: int, tri_records: int):
+        nodes = np.zeros((ref_nodes, 14), np.uint32)
+        index = np.zeros(tri_records, np.uint32)
+        root = U32()
+        self._check(lib().grt_export_scene_bvh(self.ctx, scene, _ptr(nodes), _ptr(index), ctypes.byref(root)))
+        return nodes, index, int(root.value)
+
+    def trace_multi(self, batches, any_hit=False, stream=None):
+        """batches: list of (scene, rays tensor [n, 8], hits tensor [n, 4])."""
+        arr = (RayBatch * len(batches))(*[RayBatch(s, int(r.shape[0]), _ptr(r), _ptr(h)) for s, r, h in batches])
+        self._check(lib().grt_trace_multi(self.ctx, arr, len(batches), int(any_hit), VP(stream or 0)))

@@ -1,0 +1,52 @@
+"""Differentiable closest hits for PyTorch, over the C-ABI.
+
+``closest_hits(tracer, vpos, tris, rays)`` returns (t, beta, gamma, ref) for every ray, with t,
+beta and gamma differentiable with respect to the vertex positions ``vpos`` [nv, 3] and the rays
+[n, 8] (origin in columns 0-2, direction in 4-6). The hit triangle of each ray is held fixed:
+the forward pass builds the BVH from the current vertices with the reference builder and
+traces with the selected tracer; the backward pass (grt_adjoint) recomputes each intersection
+from the vertices and propagates dL/d(t, beta, gamma) to the three vertices and the ray.
+Misses (t = FLT_MAX) get no gradient; mask them out of the loss.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+
+class _ClosestHits(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, vpos, rays, tracer, tris):
+        with torch.no_grad():
+            v4 = np.ones((vpos.shape[0], 4), np.float32)
+            v4[:, :3] = vpos.detach().cpu().numpy()
+            tracer.build(v4, tris)
+            hits = torch.empty((rays.shape[0], 4), dtype=torch.float32, device=rays.device)
+            stream = torch.cuda.current_stream(rays.device).cuda_stream
+            tracer.trace(rays.detach(), hits, False, stream)
+            tracer.check(stream)
+        ctx.save_for_backward(vpos, rays, hits)
+        ctx.tracer = tracer
+        ref = hits[:, 3].view(torch.int32)
+        ctx.mark_non_differentiable(ref)
+        return hits[:, 0].clone(), hits[:, 1].clone(), hits[:, 2].clone(), ref.clone()
+
+    @staticmethod
+    def backward(ctx, gt, gb, gg, _gref):
+        vpos, rays, hits = ctx.saved_tensors
+        n = rays.shape[0]
+        z = torch.zeros(n, dtype=torch.float32, device=rays.device)
+        grad3 = torch.stack([gt if gt is not None else z, gb if gb is not None else z,
+                             gg if gg is not None else z], dim=1).contiguous()
+        grad_v = torch.zeros((vpos.shape[0], 3), dtype=torch.float32, device=rays.device)
+        grad_r = torch.empty((n, 8), dtype=torch.float32, device=rays.device)
+        stream = torch.cuda.current_stream(rays.device).cuda_stream
+        ctx.tracer.adjoint(rays.detach().contiguous(), hits, grad3, grad_v, grad_r,
+                           vpos=vpos.detach().contiguous(), stream=stream)
+        return (grad_v if ctx.needs_input_grad[0] else None, grad_r if ctx.needs_input_grad[1] else None,
+                None, None)
+
+
+def closest_hits(tracer, vpos: torch.Tensor, tris: np.ndarray, rays: torch.Tensor):
+    """(t, beta, gamma, ref) of each ray, differentiable in vpos [nv, 3] and rays [n, 8]."""
+    return _ClosestHits.apply(vpos, rays, tracer, tris)

@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "ctx.hpp"
+#include "multi.hpp"
 #include "pathtrace.hpp"
 
 using namespace grt;
@@ -51,6 +52,7 @@ grt_status grt_create(const grt_config *cfg, grt_ctx **out) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = grt::prepare_trace_kernels();
     if (e == cudaSuccess) e = grt::prepare_pt_kernels();
+    if (e == cudaSuccess) e = grt::prepare_multi_kernels();
     if (e != cudaSuccess) {
         cudaGetLastError();
         if (c->d_err) cudaFree(c->d_err);
@@ -66,6 +68,7 @@ grt_status grt_destroy(grt_ctx *c) {
     {
         device_guard g(c->device);
         free_scene(c);
+        grt_free_multi(c);
         if (c->d_stage) cudaFree(c->d_stage);
         if (c->d_scratch) cudaFree(c->d_scratch);
         if (c->d_albedo) cudaFree(c->d_albedo);

@@ -7,6 +7,7 @@
 #include <cstring>
 
 #include "ctx.hpp"
+#include "adjoint.hpp"
 #include "pathtrace.hpp"
 
 using namespace grt;
@@ -228,6 +229,24 @@ grt_status grt_pathtrace(grt_ctx *c, const grt_pt_params *params, const float *p
     }
     cudaError_t e = cudaGraphLaunch(c->pt_graph.exec, st);
     return e == cudaSuccess ? GRT_OK : cuda_fail(c, e, "launching the path-tracing graph");
+}
+
+grt_status grt_adjoint(grt_ctx *c, const float *rays_dev, const grt_hit *hits_dev, const float *grad_hits_dev,
+                       uint32_t n, const float *vpos_dev, uint32_t vstride, float *grad_vpos_dev, float *grad_rays_dev,
+                       grt_stream_t stream) {
+    if (!c) return GRT_ERR_INVALID_ARG;
+    if (!c->built) return fail(c, GRT_ERR_NOT_BUILT, "grt_adjoint before a successful grt_build");
+    if (n == 0) return GRT_OK;
+    if (!rays_dev || !hits_dev || !grad_hits_dev || !aligned16(rays_dev) || !aligned16(hits_dev) ||
+        !aligned16(grad_rays_dev) || (vpos_dev && vstride != 3 && vstride != 4))
+        return fail(c, GRT_ERR_INVALID_ARG, "invalid buffer or vertex stride for grt_adjoint");
+    device_guard g(c->device);
+    const float4 *vp = vpos_dev ? (const float4 *)vpos_dev : (const float4 *)c->d_vpos;
+    const uint32_t stride = vpos_dev ? vstride : 4;
+    cudaError_t e = launch_adjoint((const float4 *)rays_dev, hits_dev, grad_hits_dev, n, vp, stride,
+                                   (const uint4 *)c->d_tris, grad_vpos_dev, (float4 *)grad_rays_dev,
+                                   (cudaStream_t)stream);
+    return e == cudaSuccess ? GRT_OK : cuda_fail(c, e, "launching the adjoint kernel");
 }
 
 }  // extern "C"

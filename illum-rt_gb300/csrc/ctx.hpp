@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <array>
 #include <chrono>
 #include <cstring>
 #include <string>
@@ -41,7 +42,19 @@ struct grt_ctx {
         cudaGraphExec_t exec = nullptr;
         std::vector<uint64_t> key;
     } pt_graph;
+    // scene set of the multi-scene path (grt_build_scenes)
+    struct multi_set {
+        uint32_t count = 0, max_depth = 0, max_bound4 = 0;
+        std::vector<grt::ref_tree> trees;
+        std::vector<grt_bvh_stats> stats;
+        void *d_nodes = nullptr, *d_recs = nullptr, *d_nodes4 = nullptr, *d_vpos = nullptr, *d_tris = nullptr;
+        void *d_table = nullptr;    // dev_scene per scene
+        void *d_batches = nullptr;  // multi_batch table of the last launch
+        uint32_t batch_cap = 0;
+    } ms;
 };
+
+void grt_free_multi(grt_ctx *c);
 
 namespace grt {
 

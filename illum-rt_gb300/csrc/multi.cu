@@ -1,0 +1,186 @@
+// One persistent launch over many scenes and uneven ray batches.
+//
+// The reference traces one scene per platform (wf::cuda::batch_rt, rt/cuda/base.h:403-429); a
+// batch of many small and large scenes would take one launch per scene, each with its own
+// tail. Here every batch (scene index, ray count, ray and hit buffers) gets a range of a global
+// ray index; persistent warps take rays from one counter, and each lane finds its batch by a
+// binary search over the batch offsets, then traverses with that batch's scene descriptor.
+// Lanes of one warp may work on different scenes at the same time.
+#include "multi.hpp"
+#include "traverse.cuh"
+
+namespace grt {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+// index of the last batch whose offset is <= g (offsets ascending, offsets[0] = 0)
+__device__ __forceinline__ uint32_t find_batch(const multi_batch *__restrict__ b, uint32_t nb, uint32_t g) {
+    uint32_t lo = 0, hi = nb;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&b[mid].offset) <= g)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+template <int ORDER, int STACK, bool ANY>
+__global__ void __launch_bounds__(256) k_trace_multi(const dev_scene *__restrict__ scenes,
+                                                     const multi_batch *__restrict__ batches, uint32_t nbatch,
+                                                     uint32_t total, unsigned *err, unsigned *counter,
+                                                     int refill_threshold, int refill_period) {
+    extern __shared__ int s_stack[];
+    constexpr bool SPEC = ORDER == SPECULATIVE || ORDER == WIDE_SPECULATIVE;
+    constexpr bool WIDE = ORDER == WIDE_SPECULATIVE;
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned lanes_below = (1u << lane) - 1u;
+    int *stk = s_stack + threadIdx.x;
+    const int stride = blockDim.x;
+    trav_t s;
+    ray_t r;
+    dev_scene sc{};
+    grt_hit *hits = nullptr;
+    uint32_t idx = 0;
+    bool have = false, plain = false, exhausted = false;
+    for (;;) {
+        if (!exhausted) {
+            const unsigned need = __ballot_sync(kFull, !have);
+            if (need) {
+                const unsigned cnt = __popc(need);
+                unsigned base = 0;
+                if (lane == 0) base = atomicAdd(counter, cnt);
+                base = __shfl_sync(kFull, base, 0);
+                if (base + cnt >= total) exhausted = true;
+                if (!have) {
+                    const uint32_t g = base + __popc(need & lanes_below);
+                    if (g < total) {
+                        const uint32_t b = find_batch(batches, nbatch, g);
+                        const multi_batch mb = batches[b];
+                        idx = g - mb.offset;
+                        sc = scenes[mb.scene];
+                        hits = mb.hits;
+                        r = load_ray(mb.rays, idx);
+                        trav_init(s, sc, WIDE);
+                        plain = sc.finite && ray_is_plain(r);
+                        have = true;
+                        if (s.done) {  // empty scene
+                            store_hit<ANY>(hits, idx, s);
+                            have = false;
+                        }
+                    }
+                }
+            }
+        }
+        if (__ballot_sync(kFull, have) == 0) {
+            if (exhausted) break;
+            continue;
+        }
+        for (int it = 1;; ++it) {
+            if (SPEC)
+                trav_spec_iter<STACK, ANY, false, WIDE>(s, have, plain, sc, r, stk, stride, err);
+            else if (have && plain)
+                trav_advance<ORDER, STACK, ANY, false, true>(s, sc, r, stk, stride, err);
+            else if (have)
+                trav_advance<ORDER, STACK, ANY, false, false>(s, sc, r, stk, stride, err);
+            if (have && s.done) {
+                store_hit<ANY>(hits, idx, s);
+                have = false;
+            }
+            if (it % refill_period == 0) {
+                const int busy = __popc(__ballot_sync(kFull, have));
+                if (busy == 0 || (!exhausted && busy < refill_threshold)) break;
+            }
+        }
+    }
+}
+
+template <int ORDER, int STACK, bool ANY>
+cudaError_t multi_launch(const dev_scene *scenes, const multi_batch *batches, uint32_t nbatch, uint32_t total,
+                         const launch_params &lp, unsigned *err, unsigned *counter, cudaStream_t st) {
+    const size_t smem = (size_t)STACK * lp.block_threads * sizeof(int);
+    cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
+    if (e != cudaSuccess) return e;
+    k_trace_multi<ORDER, STACK, ANY><<<lp.grid_blocks, lp.block_threads, smem, st>>>(
+        scenes, batches, nbatch, total, err, counter, lp.refill_threshold, lp.refill_period);
+    return cudaGetLastError();
+}
+
+template <int ORDER, int STACK>
+cudaError_t multi_any(bool any_hit, const dev_scene *scenes, const multi_batch *batches, uint32_t nbatch,
+                      uint32_t total, const launch_params &lp, unsigned *err, unsigned *counter, cudaStream_t st) {
+    return any_hit ? multi_launch<ORDER, STACK, true>(scenes, batches, nbatch, total, lp, err, counter, st)
+                   : multi_launch<ORDER, STACK, false>(scenes, batches, nbatch, total, lp, err, counter, st);
+}
+
+template <int ORDER>
+cudaError_t multi_stack(bool any_hit, const dev_scene *scenes, const multi_batch *batches, uint32_t nbatch,
+                        uint32_t total, const launch_params &lp, unsigned *err, unsigned *counter, cudaStream_t st) {
+    return lp.stack_entries <= kStackSmall
+               ? multi_any<ORDER, kStackSmall>(any_hit, scenes, batches, nbatch, total, lp, err, counter, st)
+               : multi_any<ORDER, kStackLarge>(any_hit, scenes, batches, nbatch, total, lp, err, counter, st);
+}
+
+template <int ORDER> cudaError_t attrs(int bytes) {
+    const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    cudaError_t e = cudaFuncSetAttribute(k_trace_multi<ORDER, kStackSmall, false>, a, bytes);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_multi<ORDER, kStackSmall, true>, a, bytes);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_multi<ORDER, kStackLarge, false>, a, bytes);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_multi<ORDER, kStackLarge, true>, a, bytes);
+    return e;
+}
+
+}  // namespace
+
+cudaError_t launch_trace_multi(const dev_scene *scenes, const multi_batch *batches, uint32_t nbatch, uint32_t total,
+                               bool any_hit, const launch_params &lp, unsigned *err, unsigned *counter,
+                               cudaStream_t st) {
+    if (total == 0) return cudaSuccess;
+    switch (lp.order) {
+        case WHILE_WHILE: return multi_stack<WHILE_WHILE>(any_hit, scenes, batches, nbatch, total, lp, err, counter, st);
+        case SPECULATIVE: return multi_stack<SPECULATIVE>(any_hit, scenes, batches, nbatch, total, lp, err, counter, st);
+        case WIDE_SPECULATIVE:
+            return multi_stack<WIDE_SPECULATIVE>(any_hit, scenes, batches, nbatch, total, lp, err, counter, st);
+        default: return multi_stack<IF_IF>(any_hit, scenes, batches, nbatch, total, lp, err, counter, st);
+    }
+}
+
+cudaError_t prepare_multi_kernels() {
+    const int bytes = kStackLarge * 256 * (int)sizeof(int);
+    cudaError_t e = attrs<IF_IF>(bytes);
+    if (e == cudaSuccess) e = attrs<WHILE_WHILE>(bytes);
+    if (e == cudaSuccess) e = attrs<SPECULATIVE>(bytes);
+    if (e == cudaSuccess) e = attrs<WIDE_SPECULATIVE>(bytes);
+    return e;
+}
+
+int multi_blocks_per_sm(int block_threads, int stack_entries, int order) {
+    int blocks = 0;
+    const bool small = stack_entries <= kStackSmall;
+    const size_t smem = (size_t)(small ? kStackSmall : kStackLarge) * block_threads * sizeof(int);
+    const void *fn = nullptr;
+    switch (order) {
+        case WHILE_WHILE:
+            fn = small ? (const void *)k_trace_multi<WHILE_WHILE, kStackSmall, false>
+                       : (const void *)k_trace_multi<WHILE_WHILE, kStackLarge, false>;
+            break;
+        case SPECULATIVE:
+            fn = small ? (const void *)k_trace_multi<SPECULATIVE, kStackSmall, false>
+                       : (const void *)k_trace_multi<SPECULATIVE, kStackLarge, false>;
+            break;
+        case WIDE_SPECULATIVE:
+            fn = small ? (const void *)k_trace_multi<WIDE_SPECULATIVE, kStackSmall, false>
+                       : (const void *)k_trace_multi<WIDE_SPECULATIVE, kStackLarge, false>;
+            break;
+        default:
+            fn = small ? (const void *)k_trace_multi<IF_IF, kStackSmall, false>
+                       : (const void *)k_trace_multi<IF_IF, kStackLarge, false>;
+    }
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, block_threads, smem) != cudaSuccess) return 1;
+    return blocks > 0 ? blocks : 1;
+}
+
+}  // namespace grt

@@ -253,6 +253,57 @@ grt_status grt_pathtrace(grt_ctx *ctx, const grt_pt_params *params, const float 
                          const grt_hit *prim_hits_dev, uint32_t n_primary, uint32_t n_paths,
                          grt_path_result *results_dev, grt_hit *bounce_hits_dev, grt_stream_t stream);
 
+/* ---- many scenes, uneven ray batches, one launch --------------------------------------- */
+
+/* One mesh of a scene set: host arrays in the layouts of grt_build. */
+typedef struct grt_mesh {
+    const float *vpos4;
+    uint32_t nv;
+    const uint32_t *tris4;
+    uint32_t nt;
+} grt_mesh;
+
+/* Builds `count` independent scenes (the reference builder, in parallel over scenes) into
+ * pooled device arrays; scene i is addressed by its index in `meshes`. Replaces any previous
+ * scene set; independent of the scene of grt_build. */
+grt_status grt_build_scenes(grt_ctx *ctx, const grt_mesh *meshes, uint32_t count, const grt_bvh_opts *opts);
+grt_status grt_scene_info(grt_ctx *ctx, uint32_t scene, grt_bvh_stats *out);
+grt_status grt_export_scene_bvh(grt_ctx *ctx, uint32_t scene, uint32_t *nodes14, uint32_t *index, uint32_t *root);
+
+/* One batch of rays against one scene of the set: DEVICE buffers as for grt_trace. */
+typedef struct grt_ray_batch {
+    uint32_t scene;
+    uint32_t n;
+    const float *rays_dev;
+    grt_hit *hits_dev;
+} grt_ray_batch;
+
+/* Traces all batches in ONE persistent launch (rays of different scenes share warps), in the
+ * loop order of the selected tracer, with the results grt_trace gives per scene. The batch
+ * table is a host array. Asynchronous on `stream`; batches of two calls on different streams
+ * must not overlap (the context keeps one device copy of the table). */
+grt_status grt_trace_multi(grt_ctx *ctx, const grt_ray_batch *batches, uint32_t count, int any_hit,
+                           grt_stream_t stream);
+
+/* ---- adjoint of the closest hit ------------------------------------------------------ */
+
+/* Gradients of a loss through closest hits, with each ray's hit triangle held fixed. There is
+ * no counterpart in the reference. For hit triangle (A, B, C) and ray (o, d) the intersection
+ * (t, beta, gamma) solves the reference's Cramer system (libgi/intersect.h:36-58); the kernel
+ * recomputes it from the current vertices and propagates
+ *   grad_hits_dev: n x 3 floats per ray, (dL/dt, dL/dbeta, dL/dgamma)
+ * back to
+ *   grad_vpos_dev: 3 floats per vertex, ADDED to (zero it first), or NULL;
+ *   grad_rays_dev: n x 8 floats, (dL/do xyz, 0, dL/dd xyz, 0), written, or NULL.
+ * hits_dev supplies the hit triangle of each ray (misses get zero gradients); vpos_dev holds the
+ * vertex positions with vstride floats per vertex (3 or 4), or is NULL for the vertices given
+ * to grt_build; triangles are those given to grt_build. Vertex contributions are combined per
+ * warp before the atomic adds, so the summation order (and the last bits) can vary from run to
+ * run. */
+grt_status grt_adjoint(grt_ctx *ctx, const float *rays_dev, const grt_hit *hits_dev, const float *grad_hits_dev,
+                       uint32_t n, const float *vpos_dev, uint32_t vstride, float *grad_vpos_dev, float *grad_rays_dev,
+                       grt_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

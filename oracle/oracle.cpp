@@ -852,3 +852,83 @@ int orc_max_threads() { return omp_get_max_threads(); }
 void orc_free(void *hp) { delete (bvh *)hp; }
 
 }  // extern "C"
+
+// ---- FP64 references for the adjoint (no counterpart in the reference) ---------------------
+//
+// The intersection of ray (o, d) with a FIXED triangle (A, B, C), in double precision, from the
+// same Cramer system as libgi/intersect.h:36-58: beta (A - B) + gamma (A - C) + t d = A - o.
+// No range tests: the triangle is given, so the values are defined even outside it.
+static void fixed_hit64(const double *A, const double *B, const double *C, const double *o, const double *d,
+                        double &t, double &beta, double &gamma) {
+    double a = A[0] - B[0], b = A[1] - B[1], c = A[2] - B[2];
+    double dd = A[0] - C[0], e = A[1] - C[1], f = A[2] - C[2];
+    double g = d[0], h = d[1], i = d[2];
+    double j = A[0] - o[0], k = A[1] - o[1], l = A[2] - o[2];
+    double c1 = e * i - h * f, c2 = g * f - dd * i, c3 = dd * h - e * g;
+    double M = a * c1 + b * c2 + c * c3;
+    beta = (j * c1 + k * c2 + l * c3) / M;
+    c1 = a * k - j * b;
+    c2 = j * c - a * l;
+    c3 = b * l - k * c;
+    gamma = (i * c1 + h * c2 + g * c3) / M;
+    t = -(f * c1 + e * c2 + dd * c3) / M;
+}
+
+extern "C" {
+
+// (t, beta, gamma) in double for each ray against its given triangle `refs[i]`.
+// vpos3: double [nv, 3]; rays6: double [n, 6] (o, d); out3: double [n, 3].
+void orc_fixed_hits64(const double *vpos3, const uint32_t *tris4, const double *rays6, const uint32_t *refs, uint64_t n,
+                      double *out3) {
+#pragma omp parallel for schedule(static)
+    for (int64_t r = 0; r < (int64_t)n; ++r) {
+        const uint32_t *t = tris4 + 4 * (size_t)refs[r];
+        fixed_hit64(vpos3 + 3 * (size_t)t[0], vpos3 + 3 * (size_t)t[1], vpos3 + 3 * (size_t)t[2], rays6 + 6 * r,
+                    rays6 + 6 * r + 3, out3[3 * r], out3[3 * r + 1], out3[3 * r + 2]);
+    }
+}
+
+// Analytic adjoint in double: with M = [A-B | A-C | d], x = (beta, gamma, t), g = dL/dx,
+// lambda = M^-T g; dA = lambda (1-beta-gamma), dB = lambda beta, dC = lambda gamma,
+// do = -lambda, dd = -lambda t. M^-T g is solved by Gaussian elimination with partial
+// pivoting (a different method from the kernel's cross products). grad3 per ray is
+// (dL/dt, dL/dbeta, dL/dgamma); rays with refs[i] == 0xFFFFFFFF are skipped.
+// Outputs: gv3 double [nv, 3] (accumulated), gr6 double [n, 6].
+void orc_adjoint64(const double *vpos3, const uint32_t *tris4, const double *rays6, const uint32_t *refs,
+                   const double *grad3, uint64_t n, double *gv3, double *gr6) {
+    for (uint64_t r = 0; r < n; ++r) {
+        double *gr = gr6 + 6 * r;
+        for (int q = 0; q < 6; ++q) gr[q] = 0;
+        if (refs[r] == 0xFFFFFFFFu) continue;
+        const uint32_t *t = tris4 + 4 * (size_t)refs[r];
+        const double *A = vpos3 + 3 * (size_t)t[0], *B = vpos3 + 3 * (size_t)t[1], *C = vpos3 + 3 * (size_t)t[2];
+        const double *o = rays6 + 6 * r, *d = rays6 + 6 * r + 3;
+        double tt, beta, gamma;
+        fixed_hit64(A, B, C, o, d, tt, beta, gamma);
+        // M^T lambda = g with rows of M^T: (A-B), (A-C), d and g = (g_beta, g_gamma, g_t)
+        double m[3][4] = {{A[0] - B[0], A[1] - B[1], A[2] - B[2], grad3[3 * r + 1]},
+                          {A[0] - C[0], A[1] - C[1], A[2] - C[2], grad3[3 * r + 2]},
+                          {d[0], d[1], d[2], grad3[3 * r + 0]}};
+        for (int col = 0; col < 3; ++col) {
+            int piv = col;
+            for (int row = col + 1; row < 3; ++row)
+                if (std::fabs(m[row][col]) > std::fabs(m[piv][col])) piv = row;
+            for (int q = 0; q < 4; ++q) std::swap(m[col][q], m[piv][q]);
+            for (int row = 0; row < 3; ++row) {
+                if (row == col) continue;
+                double fct = m[row][col] / m[col][col];
+                for (int q = col; q < 4; ++q) m[row][q] -= fct * m[col][q];
+            }
+        }
+        double lam[3] = {m[0][3] / m[0][0], m[1][3] / m[1][1], m[2][3] / m[2][2]};
+        for (int q = 0; q < 3; ++q) {
+            gv3[3 * (size_t)t[0] + q] += lam[q] * (1.0 - beta - gamma);
+            gv3[3 * (size_t)t[1] + q] += lam[q] * beta;
+            gv3[3 * (size_t)t[2] + q] += lam[q] * gamma;
+            gr[q] = -lam[q];
+            gr[3 + q] = -lam[q] * tt;
+        }
+    }
+}
+
+}  // extern "C"

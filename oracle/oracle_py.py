@@ -176,3 +176,35 @@ class ReferenceBVH(_BVHBase):
 def max_threads() -> int:
     lib = _load(ORACLE_SO, "orc_")
     return int(lib.orc_max_threads())
+
+
+def _orc():
+    return _load(ORACLE_SO, "orc_")
+
+
+def fixed_hits64(vpos3, tris4, rays6, refs):
+    """(t, beta, gamma) in double for each ray against its given triangle."""
+    vpos3 = np.ascontiguousarray(vpos3, np.float64)
+    rays6 = np.ascontiguousarray(rays6, np.float64)
+    tris4 = np.ascontiguousarray(tris4, np.uint32)
+    refs = np.ascontiguousarray(refs, np.uint32)
+    out = np.zeros((refs.shape[0], 3), np.float64)
+    f = _orc().orc_fixed_hits64
+    f.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_uint64, ctypes.c_void_p]
+    f(_p(vpos3), _p(tris4), _p(rays6), _p(refs), refs.shape[0], _p(out))
+    return out
+
+
+def adjoint64(vpos3, tris4, rays6, refs, grad3):
+    """FP64 analytic gradients: (dL/dvpos [nv, 3], dL/d(o, d) [n, 6]) for grad3 = (dt, dbeta, dgamma)."""
+    vpos3 = np.ascontiguousarray(vpos3, np.float64)
+    rays6 = np.ascontiguousarray(rays6, np.float64)
+    tris4 = np.ascontiguousarray(tris4, np.uint32)
+    refs = np.ascontiguousarray(refs, np.uint32)
+    grad3 = np.ascontiguousarray(grad3, np.float64)
+    gv = np.zeros_like(vpos3)
+    gr = np.zeros((refs.shape[0], 6), np.float64)
+    f = _orc().orc_adjoint64
+    f.argtypes = [ctypes.c_void_p] * 5 + [ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p]
+    f(_p(vpos3), _p(tris4), _p(rays6), _p(refs), _p(grad3), refs.shape[0], _p(gv), _p(gr))
+    return gv, gr
