@@ -2,7 +2,13 @@
 icosphere subdivided 6 times (81,920 triangles), vertices displaced radially by 0.05 N(0,1),
 512x512 pinhole rays, loss = sum w t + sum c (u,v-interpolated vertex scalar) over rays more than
 1e-3 barycentric from an edge. Checked against the FP64 analytic gradient of the oracle and
-against FP64 central finite differences (h = 1e-4), to 1e-3 relative."""
+against FP64 central finite differences, to 1e-3 relative.
+
+Silhouette vertices are hit by near-grazing rays whose derivatives change fast, and there plain
+central differences with h = 1e-4 carry percent-level truncation error (one such vertex reads
+369.2 at h = 1e-4, 363.74 at 1e-5, 363.688 at 1e-6, against 363.688 analytic). The check
+therefore uses the Richardson extrapolation of the central differences at h = 1e-4 and h/2,
+which removes the h^2 term."""
 import numpy as np
 import pytest
 
@@ -61,7 +67,7 @@ def test_forward_hits_match_oracle(adjoint_case, orc):
     t, b, g = adjoint_case["hits"]
     got = np.stack([t, b, g, adjoint_case["refs"].view(np.float32)], axis=1)
     assert (got.view(np.uint32) == want.view(np.uint32)).all()
-    assert adjoint_case["interior"].sum() > 0.3 * rays.shape[0]
+    assert adjoint_case["interior"].sum() > 0.2 * rays.shape[0]  # the sphere covers ~29% of the frame
 
 
 def test_gradients_match_fp64_analytic(adjoint_case, orc):
@@ -94,25 +100,26 @@ def test_gradients_match_fp64_finite_differences(adjoint_case, orc):
         interp = (1 - x[:, 1] - x[:, 2]) * s[tri[:, 0]] + x[:, 1] * s[tri[:, 1]] + x[:, 2] * s[tri[:, 2]]
         return float((w * x[:, 0]).sum() + (c * interp).sum())
 
-    h = 1e-4
+    def fd(f, x, idx, h=1e-4):
+        def central(hh):
+            xp, xm = x.copy(), x.copy()
+            xp[idx] += hh
+            xm[idx] -= hh
+            return (f(xp) - f(xm)) / (2 * hh)
+        return (4 * central(h / 2) - central(h)) / 3
+
     g = np.random.default_rng(7)
     used = np.unique(tri)
     checked = 0
     for k in g.choice(used, 24, replace=False):
         for a in range(3):
-            vp, vm = v64.copy(), v64.copy()
-            vp[k, a] += h
-            vm[k, a] -= h
-            fd = (loss(vp, r64) - loss(vm, r64)) / (2 * h)
-            assert abs(case["gv"][k, a] - fd) <= 1e-3 * max(abs(fd), 1e-2), (k, a, case["gv"][k, a], fd)
+            want = fd(lambda vv: loss(vv, r64), v64, (k, a))
+            assert abs(case["gv"][k, a] - want) <= 1e-3 * max(abs(want), 1e-2), (k, a, case["gv"][k, a], want)
             checked += 1
     gr = case["gr"][inter][:, [0, 1, 2, 4, 5, 6]]
     for r in g.choice(refs.size, 24, replace=False):
         for a in range(6):
-            rp, rm = r64.copy(), r64.copy()
-            rp[r, a] += h
-            rm[r, a] -= h
-            fd = (loss(v64, rp) - loss(v64, rm)) / (2 * h)
-            assert abs(gr[r, a] - fd) <= 1e-3 * max(abs(fd), 1e-2), (r, a, gr[r, a], fd)
+            want = fd(lambda rr: loss(v64, rr), r64, (r, a))
+            assert abs(gr[r, a] - want) <= 1e-3 * max(abs(want), 1e-2), (r, a, gr[r, a], want)
             checked += 1
     assert checked == 24 * 3 + 24 * 6
