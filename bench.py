@@ -48,7 +48,8 @@ def parse_args():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-case", action="store_true",
-                    help="run one tuned and one plain step with 1,048,576 paths and exit (for ncu captures)")
+                    help="run one tuned and one plain step (no graphs) and exit (for ncu captures)")
+    ap.add_argument("--profile-paths", type=int, default=1 << 20, help="paths of the --profile-case step")
     return ap.parse_args()
 
 
@@ -128,13 +129,32 @@ def load_tuning(gpu_name: str) -> dict:
 
 
 def profile_traffic():
-    """DRAM bytes per launch of the fused kernel from the committed ncu summary, if any."""
+    """DRAM bytes (read + write) per full-size launch of the fused kernel, from the line
+    `dram_bytes_per_launch: N` of the committed ncu summary, or None."""
     try:
-        with open(os.path.join(ROOT, "profiles", "k_pt_fused_spheres.json")) as f:
-            d = json.load(f)
-        return d
+        with open(os.path.join(ROOT, "profiles", "k_pt_fused_spheres.md")) as f:
+            for line in f:
+                if line.strip().startswith("dram_bytes_per_launch:"):
+                    return int(line.split(":", 1)[1].strip().replace(",", ""))
     except Exception:
-        return None
+        pass
+    return None
+
+
+def max_over_ranks(x: float, world: int, device: str = "cuda") -> float:
+    """The largest `x` over all ranks (the slowest rank's time); `x` itself for one rank."""
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(rays_per_step: int, steps: int, slowest_s: float, world: int) -> float:
+    """Whole-job Mrays/s of `world` replicas that each trace `rays_per_step` rays per step."""
+    return world * rays_per_step * steps / slowest_s / 1e6
 
 
 # ---- the GB300 arm --------------------------------------------------------------------------
@@ -153,6 +173,7 @@ class Step:
         self.rt_plain = api.BatchRayTracer(device)  # the reference's CUDA build defaults, untuned
         self.rt_plain.build(sc.vpos, sc.tris)
         self.rt_plain.select("while-while")
+        self.plain_order = "while-while"
         self.rt.select(tuning.get("tracer", "persistent-while-while"))
         kw = {k: v for k, v in tuning.items() if k in ("block_threads", "blocks_per_sm", "refill_threshold",
                                                          "refill_period", "stack_entries")}
@@ -203,6 +224,8 @@ class Step:
         kernel: 32 B ray + 16 B hit + 64 B per inner node + 48 B per triangle test."""
         torch = self.torch
         cnt = torch.zeros(3, dtype=torch.int64, device=self.dev)
+        # the exact reference order, so that the counts are the reference traversal's own
+        self.rt_plain.select("while-while")
         self.rt_plain.set_traversal_counters(cnt)
         self.rt_plain.trace(self.rays, self.hits, False, self.sp)
         self.rt_plain.check(self.sp)
@@ -213,6 +236,7 @@ class Step:
         self.rt_plain.check(self.sp)
         bounce = [int(x) for x in cnt.cpu()]
         self.rt_plain.set_traversal_counters(None)
+        self.rt_plain.select(self.plain_order)
         to_bytes = lambda c: 48 * c[0] + 64 * c[1] + 48 * c[2]
         return to_bytes(bounce), to_bytes(prim), bounce, prim
 
@@ -239,21 +263,45 @@ def time_steps(step: Step, fn, k: int, flush=True, split=False):
     return totals, parts
 
 
-def cpu_baseline(rays_np, n_paths_sample: int, threads: int = 0):
-    """The oracle port of the reference CPU tracer (OpenMP over rays, all host threads) on a
-    bounded sample of the same workload: all primary rays plus n_paths_sample diffuse paths."""
-    import __graft_entry__ as ge
-    from illum_rt_gb300 import workloads as wl
-    orc = ge.load_oracle()
-    sc = wl.spheres()
-    o = orc.OracleBVH(sc.vpos, sc.tris)
-    o.closest(rays_np[:4096])  # warm-up
-    t0 = time.perf_counter()
-    hits, _ = o.closest(rays_np, threads=threads)
-    res, _ = o.pathtrace(rays_np, hits, n_paths_sample, threads=threads)
-    dt = time.perf_counter() - t0
-    n = rays_np.shape[0] + int(res[:, 1].sum())
-    return n / dt / 1e6, n, dt, orc.max_threads() if threads == 0 else threads
+class CpuStep:
+    """One step of the workload on the host cores through the oracle port of the reference CPU
+    tracer (OpenMP over rays, rt/cpu/wavefront.cpp:53-70, all host threads): closest hits of the
+    1024x1024 primary rays, then the diffuse paths started at those hits."""
+
+    def __init__(self, rays_np, n_paths: int, threads: int = 0):
+        import __graft_entry__ as ge
+        from illum_rt_gb300 import workloads as wl
+        self.orc = ge.load_oracle()
+        sc = wl.spheres()
+        self.o = self.orc.OracleBVH(sc.vpos, sc.tris)
+        self.rays = rays_np
+        self.n_paths = n_paths
+        self.threads = threads
+
+    def cores(self) -> int:
+        return self.orc.max_threads() if self.threads == 0 else self.threads
+
+    def run(self):
+        """(rays traced, seconds) of one step."""
+        t0 = time.perf_counter()
+        hits, _ = self.o.closest(self.rays, threads=self.threads)
+        res, _ = self.o.pathtrace(self.rays, hits, self.n_paths, threads=self.threads)
+        dt = time.perf_counter() - t0
+        return self.rays.shape[0] + int(res[:, 1].sum()), dt
+
+
+def cpu_baseline(rays_np, min_seconds: float = 10.0, min_reps: int = 3):
+    """The full step on the host cores, one warm-up step, then repeated until at least
+    `min_seconds` of work; the median rate of the repetitions (Mrays/s)."""
+    cs = CpuStep(rays_np, N_PATHS)
+    cs.run()
+    rates, n_tot, t_tot = [], 0, 0.0
+    while t_tot < min_seconds or len(rates) < min_reps:
+        n, dt = cs.run()
+        rates.append(n / dt / 1e6)
+        n_tot += n
+        t_tot += dt
+    return statistics.median(rates), len(rates), n_tot, t_tot, cs.cores()
 
 
 def rays_in_results(step: Step) -> int:
@@ -282,6 +330,7 @@ def run_gb300(args):
             step.plain()
         plain_times[order] = statistics.median(time_steps(step, step.plain, 3)[0])
     plain_order = min(plain_times, key=plain_times.get)
+    step.plain_order = plain_order
     # for reference only: the same plain wavefront on the 4-wide layout
     step.rt_plain.select("bvh4-speculative-while-while")
     for _ in range(2):
@@ -303,13 +352,6 @@ def run_gb300(args):
         if world > 1:
             torch.distributed.barrier()
 
-    def max_over_ranks(x: float) -> float:
-        if world == 1:
-            return x
-        t = torch.tensor([x], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
-
     # warm-up (graphs get captured here)
     for _ in range(max(3, args.warmup)):
         step.tuned()
@@ -318,32 +360,33 @@ def run_gb300(args):
     step.rt.check(step.sp)
     step.rt_plain.check(step.sp)
 
+    # clocks are sampled over all three timed loops (the tuned loop alone is shorter than the
+    # sampling period)
     clocks = ClockSampler(local)
     barrier()
     clocks.start()
     tuned_ms, pt_ms = time_steps(step, step.tuned, args.steps, split=True)
     barrier()
-    clk = clocks.stop()
     plain_ms, _ = time_steps(step, step.plain, args.steps)
     e2e_ms, _ = time_steps(step, step.e2e, args.steps)
     barrier()
+    clk = clocks.stop()
     step.rt.check(step.sp)
     step.rt_plain.check(step.sp)
 
-    t_tuned = max_over_ranks(sum(tuned_ms) / 1e3)
-    t_plain = max_over_ranks(sum(plain_ms) / 1e3)
-    t_e2e = max_over_ranks(sum(e2e_ms) / 1e3)
-    value = world * rays_tuned * args.steps / t_tuned / 1e6
-    plain_value = world * rays_plain * args.steps / t_plain / 1e6
-    e2e_value = world * rays_tuned * args.steps / t_e2e / 1e6
+    t_tuned = max_over_ranks(sum(tuned_ms) / 1e3, world)
+    t_plain = max_over_ranks(sum(plain_ms) / 1e3, world)
+    t_e2e = max_over_ranks(sum(e2e_ms) / 1e3, world)
+    value = job_value(rays_tuned, args.steps, t_tuned, world)
+    plain_value = job_value(rays_plain, args.steps, t_plain, world)
+    e2e_value = job_value(rays_tuned, args.steps, t_e2e, world)
 
     # roofline of the dominant kernel (the fused persistent loop): algorithmic bytes of all its
     # bounce rays per launch / the pathtrace part of each timed step
     peak, peak_kind = measured_hbm_peak()
     pt_s = statistics.mean(pt_ms) / 1e3
     achieved = pt_bytes / pt_s / 1e9
-    prof = profile_traffic()
-    traffic = prof.get("dram_bytes_per_launch") if prof else None
+    traffic = profile_traffic()
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic,
                 "kernel": "k_pt_fused", "peak_source": peak_kind,
@@ -365,6 +408,7 @@ def run_gb300(args):
                             "order_ms": {k: round(v, 4) for k, v in plain_times.items()},
                             "bvh4_speculative_ms": round(plain_bvh4_ms, 4)},
         "speedup_vs_plain": round(value / plain_value, 3),
+        "speedup_vs_plain_while_while": round(plain_times["while-while"] / statistics.mean(tuned_ms), 3),
         "e2e": {"value": round(e2e_value, 1), "unit": "Mrays/s", "ms_per_step": round(statistics.mean(e2e_ms), 4),
                 "h2d_bytes_per_step": int(step.n_primary * 32), "d2h_bytes_per_step": int(N_PATHS * 16)},
         "gpu_launches": 5 * args.steps,
@@ -374,9 +418,10 @@ def run_gb300(args):
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         rays_np = step.h_rays.numpy()
-        v, n, dt, cores = cpu_baseline(rays_np, 1 << 20)
+        v, reps, n, dt, cores = cpu_baseline(rays_np)
         line["cpu_baseline"] = {"value": round(v, 2), "unit": "Mrays/s", "cores": cores, "kind": "port",
-                                "sample": f"1024x1024 primary rays + 1,048,576 diffuse paths ({n} rays, {dt:.2f} s)"}
+                                "sample": f"the full step (1024x1024 primary rays + 4,194,304 diffuse paths) "
+                                          f"x {reps} after 1 warm-up: {n} rays in {dt:.1f} s, median rate"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -386,52 +431,44 @@ def run_gb300(args):
 # ---- the reference arm: the reference's CPU tracer (oracle port) on the host cores ------------
 
 def run_reference(args):
+    """The reference's CPU tracer (the oracle port of rt/cpu/bvh2.cpp and wavefront.cpp) on the
+    host cores, rank 0 only: every step is the full workload (closest hits of the primary rays
+    and the diffuse paths from them)."""
     rank, world, _ = dist_info()
     if rank != 0:
         return
     import __graft_entry__ as ge
     ge.load_package()
     from illum_rt_gb300 import workloads as wl
-    orc = ge.load_oracle()
-    sc, rays = wl.spheres_primary(res=RES)
-    o = orc.OracleBVH(sc.vpos, sc.tris)
-    sample_rays = rays[: RES * RES // 4]  # every step: a quarter of the primary rays + 262,144 paths
-    hits_full, _ = o.closest(rays)
-    sample_paths = 1 << 18
-
-    def one():
-        t0 = time.perf_counter()
-        o.closest(sample_rays)
-        res, _ = o.pathtrace(rays, hits_full, sample_paths)
-        return sample_rays.shape[0] + int(res[:, 1].sum()), time.perf_counter() - t0
-
+    _, rays = wl.spheres_primary(res=RES)
+    cs = CpuStep(rays, N_PATHS)
     for _ in range(args.warmup):
-        one()
-    n_tot, t_tot, times = 0, 0.0, []
+        cs.run()
+    n_tot, t_tot = 0, 0.0
     for _ in range(args.steps):
-        n, dt = one()
+        n, dt = cs.run()
         n_tot += n
         t_tot += dt
-        times.append(dt)
     value = n_tot / t_tot / 1e6
-    cores = orc.max_threads()
+    cores = cs.cores()
     line = {"metric": METRIC, "value": round(value, 2), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(1e3 * t_tot / args.steps, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "impl": "reference",
-            "config": {"workload": WORKLOAD, "sample_per_step": "262,144 primary rays + 262,144 diffuse paths"},
+            "config": {"workload": WORKLOAD, "triangles": 262144, "primary_rays": rays.shape[0], "paths": N_PATHS,
+                       "rays_per_step": n_tot // max(1, args.steps)},
             "cpu_baseline": {"value": round(value, 2), "unit": "Mrays/s", "cores": cores, "kind": "port",
-                             "sample": "per step 262,144 primary rays + 262,144 diffuse paths, OpenMP over rays"},
+                             "sample": f"the full step x {args.steps} after {args.warmup} warm-up, OpenMP over rays"},
             "e2e": {"value": round(value, 2), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def run_profile_case():
-    """One tuned step, then one plain step (no graphs, 1,048,576 paths): a small case whose
-    launches ncu can capture one by one."""
+def run_profile_case(paths: int):
+    """One tuned step, then one plain step (no graphs; 1,048,576 paths unless asked otherwise):
+    a case whose launches ncu can capture one by one."""
     import torch
     import __graft_entry__ as ge
     global N_PATHS
-    N_PATHS = 1 << 20
+    N_PATHS = paths
     ge.load_package()
     from illum_rt_gb300 import api, workloads as wl
     step = Step(api, wl, 0, load_tuning(torch.cuda.get_device_name(0)))
@@ -447,7 +484,7 @@ def run_profile_case():
 def main():
     args = parse_args()
     if args.profile_case:
-        run_profile_case()
+        run_profile_case(args.profile_paths)
     elif args.impl == "reference":
         run_reference(args)
     else:
