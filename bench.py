@@ -28,6 +28,8 @@ import sys
 import tempfile
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -50,6 +52,8 @@ def parse_args():
     ap.add_argument("--profile-case", action="store_true",
                     help="run one tuned and one plain step (no graphs) and exit (for ncu captures)")
     ap.add_argument("--profile-paths", type=int, default=1 << 20, help="paths of the --profile-case step")
+    ap.add_argument("--workload", default="spheres", choices=["spheres", "soups64"],
+                    help="soups64: 64 uneven triangle soups traced in one launch, host vs GPU BVH builds")
     return ap.parse_args()
 
 
@@ -462,6 +466,73 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_soups64(args):
+    """64 triangle soups of log-uniform size in [1,024, 1,048,576] triangles with log-uniform ray
+    batches in [4,096, 1,048,576] (7,738,242 triangles, 10,745,442 rays), all batches in one
+    persistent launch. Reports the wall time of the host build (the reference builder, scenes in
+    parallel) and of the GPU build, and the trace rate on each tree."""
+    import torch
+    import __graft_entry__ as ge
+    ge.load_package()
+    from illum_rt_gb300 import api, workloads as wl
+    tris_n, rays_n = wl.multi_scene_sizes()
+    scenes, rays = [], []
+    for i, (nt, nr) in enumerate(zip(tris_n, rays_n)):
+        sc = wl.soup(1000 + i, nt, sigma=0.5)
+        lo, hi = sc.bounds()
+        scenes.append((sc.vpos, sc.tris))
+        rays.append(wl.shell_rays(2000 + i, lo, hi, nr))
+    d_scenes = [(torch.from_numpy(v).cuda(), torch.from_numpy(t.view(np.int32)).cuda()) for v, t in scenes]
+    d_rays = [torch.from_numpy(r).cuda() for r in rays]
+    hits = [torch.zeros((r.shape[0], 4), device="cuda") for r in rays]
+    n_rays = sum(r.shape[0] for r in rays)
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    tuning = load_tuning(torch.cuda.get_device_name(0))
+    out = {"metric": "Mrays/s closest-hit, 64 uneven soups in one launch", "unit": "Mrays/s", "n_gpus": 1,
+           "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "dtype": "f32",
+           "data": "synthetic (seeded)",
+           "config": {"workload": "soups64", "scenes": 64, "triangles": int(sum(tris_n)), "rays": int(n_rays),
+                      "l2": "inputs (344 MB of rays) larger than L2"}}
+
+    def timed_trace(rt):
+        batches = [(i, d_rays[i], hits[i]) for i in range(len(rays))]
+        for _ in range(max(3, args.warmup)):
+            rt.trace_multi(batches, stream=sp)
+        rt.check(sp)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            rt.trace_multi(batches, stream=sp)
+        e1.record(stream)
+        e1.synchronize()
+        rt.check(sp)
+        return e0.elapsed_time(e1) / args.steps
+
+    for kind in ("host", "gpu"):
+        rt = api.BatchRayTracer(0)
+        rt.select(tuning.get("tracer", "persistent-speculative-while-while"))
+        kw = {k: v for k, v in tuning.items() if k in ("block_threads", "refill_threshold", "refill_period")}
+        if kw:
+            rt.set_tuning(**kw)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        if kind == "host":
+            rt.build_scenes(scenes, max_tris=tuning.get("max_tris", 4))
+        else:
+            rt.build_scenes_device(d_scenes, max_tris=tuning.get("max_tris", 4), stream=sp)
+        build_s = time.perf_counter() - t0
+        ms = timed_trace(rt)
+        out[kind + "_tree"] = {"build_s": round(build_s, 4), "trace_ms": round(ms, 4),
+                               "Mrays_s": round(n_rays / ms / 1e3, 1),
+                               "end_to_end_s": round(build_s + ms / 1e3, 4)}
+        rt.close()
+    out["value"] = out["gpu_tree"]["Mrays_s"]
+    out["build_speedup_gpu_vs_host"] = round(out["host_tree"]["build_s"] / out["gpu_tree"]["build_s"], 1)
+    out["host_threads"] = os.cpu_count()
+    print(json.dumps(out), flush=True)
+
+
 def run_profile_case(paths: int):
     """One tuned step, then one plain step (no graphs; 1,048,576 paths unless asked otherwise):
     a case whose launches ncu can capture one by one."""
@@ -487,6 +558,8 @@ def main():
         run_profile_case(args.profile_paths)
     elif args.impl == "reference":
         run_reference(args)
+    elif args.workload == "soups64":
+        run_soups64(args)
     else:
         run_gb300(args)
 

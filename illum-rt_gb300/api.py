@@ -106,6 +106,8 @@ _PROTOS = {
     "grt_scene_info": (I, [VP, U32, P(BvhStats)]),
     "grt_export_scene_bvh": (I, [VP, U32, VP, VP, P(U32)]),
     "grt_trace_multi": (I, [VP, VP, U32, I, VP]),
+    "grt_build_device": (I, [VP, VP, U32, VP, U32, U32, VP]),
+    "grt_build_scenes_device": (I, [VP, VP, U32, U32, VP]),
 }
 
 
@@ -128,6 +130,12 @@ def _ptr(a) -> int:
     if isinstance(a, np.ndarray):
         return a.ctypes.data
     return a.data_ptr()  # torch tensor
+
+
+def _check_cuda_tensor(t, name: str, cols: int):
+    if not (hasattr(t, "is_cuda") and t.is_cuda and t.is_contiguous() and t.dim() == 2 and t.shape[1] == cols
+            and t.element_size() == 4):
+        raise ValueError(f"{name} must be a contiguous CUDA tensor of shape [n, {cols}] with 4-byte elements")
 
 
 def make_opts(split="sah", max_tris=4, planes=16, esc=True) -> BvhOpts:
@@ -240,6 +248,15 @@ class BatchRayTracer:
         self._check(lib().grt_build(self.ctx, _ptr(v), v.shape[0], _ptr(t), t.shape[0], ctypes.byref(o)))
         return self.info()
 
+    def build_device(self, vpos, tris, max_tris=None, stream=None) -> dict:
+        """The GPU builder (grt_build_device) on CUDA tensors: vpos float32 [nv, 4], tris
+        int32/uint32 [nt, 4]. Returns the build statistics."""
+        _check_cuda_tensor(vpos, "vpos", 4)
+        _check_cuda_tensor(tris, "tris", 4)
+        self._check(lib().grt_build_device(self.ctx, _ptr(vpos), int(vpos.shape[0]), _ptr(tris), int(tris.shape[0]),
+                                           int(max_tris or self.bvh_max_tris_per_node), VP(stream or 0)))
+        return self.info()
+
     def use(self, rd: RayData):
         self.rd = rd
 
@@ -346,6 +363,22 @@ class BatchRayTracer:
         self._check(lib().grt_build_scenes(self.ctx, arr, len(keep), ctypes.byref(o)))
         out = []
         for i in range(len(keep)):
+            st = BvhStats()
+            self._check(lib().grt_scene_info(self.ctx, i, ctypes.byref(st)))
+            out.append(st.as_dict())
+        return out
+
+    def build_scenes_device(self, scenes, max_tris=None, stream=None) -> list:
+        """The GPU builder over a scene set (grt_build_scenes_device): scenes is a list of
+        (vpos CUDA float32 [nv, 4], tris CUDA int32/uint32 [nt, 4]). Returns per-scene stats."""
+        for v, t in scenes:
+            _check_cuda_tensor(v, "vpos", 4)
+            _check_cuda_tensor(t, "tris", 4)
+        arr = (Mesh * len(scenes))(*[Mesh(_ptr(v), int(v.shape[0]), _ptr(t), int(t.shape[0])) for v, t in scenes])
+        self._check(lib().grt_build_scenes_device(self.ctx, arr, len(scenes), int(max_tris or self.bvh_max_tris_per_node),
+                                                  VP(stream or 0)))
+        out = []
+        for i in range(len(scenes)):
             st = BvhStats()
             self._check(lib().grt_scene_info(self.ctx, i, ctypes.byref(st)))
             out.append(st.as_dict())

@@ -1,0 +1,231 @@
+// C-ABI of the GPU builder (include/grt.h): grt_build_device for the context's scene and
+// grt_build_scenes_device for a scene set. The kernels are in gpu_build.cu; this file owns the
+// allocations, the read-back of each tree's depth and stack bound, and the checks the host
+// builder makes (indices in range, depth within the traversal stacks).
+#include <algorithm>
+#include <array>
+#include <chrono>
+#include <string>
+#include <vector>
+
+#include "ctx.hpp"
+#include "gpu_build.hpp"
+
+using namespace grt;
+
+namespace {
+
+constexpr uint32_t kMaxGpuTris = (1u << 27) - 1;  // leaf references hold 27-bit record indices
+
+// Device buffers of one build call that do not outlive it.
+struct build_temps {
+    void *scratch = nullptr;
+    int32_t *wide_index = nullptr;
+    int32_t *info = nullptr;
+    ~build_temps() {
+        for (void *p : {scratch, (void *)wide_index, (void *)info})
+            if (p) cudaFree(p);
+    }
+};
+
+grt_status check_info(grt_ctx *c, const int32_t *info, const std::string &what) {
+    if (info[GB_ERR] & GB_ERR_INDEX) return fail(c, GRT_ERR_INVALID_ARG, what + "a triangle index is beyond the vertex count");
+    if ((info[GB_ERR] & GB_ERR_DEPTH) || info[GB_DEPTH] > kStackLarge)
+        return fail(c, GRT_ERR_BVH_TOO_DEEP,
+                    what + "BVH depth " + std::to_string(info[GB_DEPTH]) +
+                        " exceeds the largest traversal stack (" + std::to_string(kStackLarge) + ")");
+    return GRT_OK;
+}
+
+bool bad_mesh(const grt_mesh &m) {
+    return (m.nv && !m.vpos4) || (m.nt && !m.tris4) || !aligned16(m.vpos4) || !aligned16(m.tris4) ||
+           m.nt > kMaxGpuTris;
+}
+
+}  // namespace
+
+extern "C" {
+
+grt_status grt_build_device(grt_ctx *c, const float *vpos4_dev, uint32_t nv, const uint32_t *tris4_dev, uint32_t nt,
+                            uint32_t max_tris, grt_stream_t stream) {
+    if (!c) return GRT_ERR_INVALID_ARG;
+    const grt_mesh m{vpos4_dev, nv, tris4_dev, nt};
+    if (bad_mesh(m)) return fail(c, GRT_ERR_INVALID_ARG, "null, misaligned or oversized vertex / triangle array");
+    if (max_tris < 1 || max_tris > 16) return fail(c, GRT_ERR_INVALID_ARG, "max_tris_per_node must be 1..16");
+    device_guard g(c->device);
+    free_scene(c);
+    ++c->scene_generation;
+    c->stats = grt_bvh_stats{};
+    c->tree = ref_tree();
+    const cudaStream_t st = (cudaStream_t)stream;
+    const auto t0 = std::chrono::steady_clock::now();
+
+    build_temps tmp;
+    const size_t nb = (size_t)std::max(nt, 2u) * 64, rb = (size_t)std::max(nt, 1u) * 48;
+    const size_t scratch = gpu_build_scratch_bytes(nt);
+    cudaError_t e = cudaMalloc(&c->d_nodes, nb);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_recs, rb);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_vpos, std::max<size_t>((size_t)nv * 16, 16));
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_tris, std::max<size_t>((size_t)nt * 16, 16));
+    if (e == cudaSuccess) e = cudaMalloc(&tmp.scratch, scratch);
+    if (e == cudaSuccess) e = cudaMalloc(&tmp.wide_index, (size_t)std::max(nt, 1u) * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&tmp.info, 8 * 4);
+    if (e == cudaSuccess && nv) e = cudaMemcpyAsync(c->d_vpos, vpos4_dev, (size_t)nv * 16, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess && nt) e = cudaMemcpyAsync(c->d_tris, tris4_dev, (size_t)nt * 16, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess)
+        e = gpu_build_binary((const float4 *)c->d_vpos, nv, (const uint4 *)c->d_tris, nt, (int)max_tris, tmp.scratch,
+                             scratch, (float4 *)c->d_nodes, (float4 *)c->d_recs, tmp.wide_index, tmp.info, st);
+    int32_t info[8] = {0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(info, tmp.info, sizeof(info), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        free_scene(c);
+        return cuda_fail(c, e, "building the BVH on the GPU");
+    }
+    grt_status s = check_info(c, info, "");
+    if (s != GRT_OK) {
+        free_scene(c);
+        return s;
+    }
+    const size_t wb = (size_t)std::max(info[GB_WIDE_NODES], 1) * 128;
+    e = cudaMalloc(&c->d_nodes4, wb);
+    if (e == cudaSuccess) e = gpu_build_wide((const float4 *)c->d_nodes, tmp.wide_index, nt, (float4 *)c->d_nodes4, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        free_scene(c);
+        return cuda_fail(c, e, "building the 4-wide BVH on the GPU");
+    }
+    c->sc.nodes = (const float4 *)c->d_nodes;
+    c->sc.records = (const float4 *)c->d_recs;
+    c->sc.nodes4 = (const float4 *)c->d_nodes4;
+    c->sc.root = nt ? info[GB_ROOT] : 0;
+    c->sc.root4 = nt ? info[GB_ROOT4] : 0;
+    c->sc.empty = nt == 0 ? 1 : 0;
+    c->sc.finite = info[GB_FINITE] ? 1 : 0;
+    c->stack_bound4 = (uint32_t)info[GB_BOUND4];
+    c->nv = nv;
+    c->nt = nt;
+    c->depth = (uint32_t)info[GB_DEPTH];
+    c->stats.build_ms = ms_since(t0);
+    c->stats.inner_nodes = (uint32_t)info[GB_INNER];
+    c->stats.tri_records = nt;
+    c->stats.depth = c->depth;
+    c->stats.device_bytes = nb + rb + wb + (size_t)nv * 16 + (size_t)nt * 16;
+    c->gpu_tree = true;
+    c->built = true;
+    return GRT_OK;
+}
+
+grt_status grt_build_scenes_device(grt_ctx *c, const grt_mesh *meshes, uint32_t count, uint32_t max_tris,
+                                   grt_stream_t stream) {
+    if (!c) return GRT_ERR_INVALID_ARG;
+    if (count == 0 || !meshes) return fail(c, GRT_ERR_INVALID_ARG, "no scenes");
+    if (max_tris < 1 || max_tris > 16) return fail(c, GRT_ERR_INVALID_ARG, "max_tris_per_node must be 1..16");
+    uint32_t most = 0;
+    for (uint32_t i = 0; i < count; ++i) {
+        if (bad_mesh(meshes[i]))
+            return fail(c, GRT_ERR_INVALID_ARG, "null, misaligned or oversized arrays in scene " + std::to_string(i));
+        most = std::max(most, meshes[i].nt);
+    }
+    device_guard g(c->device);
+    grt_free_multi(c);
+    ++c->scene_generation;
+    const cudaStream_t st = (cudaStream_t)stream;
+    const auto t0 = std::chrono::steady_clock::now();
+
+    // binary nodes, records and wide indices at 256-byte-aligned offsets of pooled arrays
+    auto a256 = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    std::vector<std::array<size_t, 3>> off(count);
+    size_t tot[3] = {0, 0, 0};
+    for (uint32_t i = 0; i < count; ++i) {
+        const uint32_t nt = meshes[i].nt;
+        const size_t sz[3] = {(size_t)std::max(nt, 2u) * 64, (size_t)std::max(nt, 1u) * 48, (size_t)std::max(nt, 1u) * 4};
+        for (int a = 0; a < 3; ++a) {
+            off[i][a] = tot[a];
+            tot[a] += a256(sz[a]);
+        }
+    }
+    build_temps tmp;
+    int32_t *wide_pool = nullptr;
+    const size_t scratch = gpu_build_scratch_bytes(most);
+    cudaError_t e = cudaMalloc(&c->ms.d_nodes, tot[0]);
+    if (e == cudaSuccess) e = cudaMalloc(&c->ms.d_recs, tot[1]);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&wide_pool, tot[2]);
+    if (e == cudaSuccess) e = cudaMalloc(&tmp.scratch, scratch);
+    if (e == cudaSuccess) e = cudaMalloc(&tmp.info, (size_t)count * 8 * 4);
+    tmp.wide_index = wide_pool;
+    for (uint32_t i = 0; i < count && e == cudaSuccess; ++i) {
+        const grt_mesh &m = meshes[i];
+        e = gpu_build_binary((const float4 *)m.vpos4, m.nv, (const uint4 *)m.tris4, m.nt, (int)max_tris, tmp.scratch,
+                             scratch, (float4 *)((char *)c->ms.d_nodes + off[i][0]),
+                             (float4 *)((char *)c->ms.d_recs + off[i][1]), (int32_t *)((char *)wide_pool + off[i][2]),
+                             tmp.info + 8 * (size_t)i, st);
+    }
+    std::vector<int32_t> info((size_t)count * 8, 0);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(info.data(), tmp.info, info.size() * 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        grt_free_multi(c);
+        return cuda_fail(c, e, "building the scene set on the GPU");
+    }
+    uint32_t max_depth = 0, max_bound4 = 0;
+    std::vector<size_t> off4(count);
+    size_t tot4 = 0;
+    for (uint32_t i = 0; i < count; ++i) {
+        const int32_t *f = info.data() + 8 * (size_t)i;
+        grt_status s = check_info(c, f, "scene " + std::to_string(i) + ": ");
+        if (s != GRT_OK) {
+            grt_free_multi(c);
+            return s;
+        }
+        max_depth = std::max(max_depth, (uint32_t)f[GB_DEPTH]);
+        max_bound4 = std::max(max_bound4, (uint32_t)f[GB_BOUND4]);
+        off4[i] = tot4;
+        tot4 += a256((size_t)std::max(f[GB_WIDE_NODES], 1) * 128);
+    }
+    e = cudaMalloc(&c->ms.d_nodes4, tot4);
+    for (uint32_t i = 0; i < count && e == cudaSuccess; ++i)
+        e = gpu_build_wide((const float4 *)((char *)c->ms.d_nodes + off[i][0]),
+                           (const int32_t *)((char *)wide_pool + off[i][2]), meshes[i].nt,
+                           (float4 *)((char *)c->ms.d_nodes4 + off4[i]), st);
+    std::vector<dev_scene> table(count);
+    for (uint32_t i = 0; i < count; ++i) {
+        const int32_t *f = info.data() + 8 * (size_t)i;
+        dev_scene &d = table[i];
+        d.nodes = (const float4 *)((char *)c->ms.d_nodes + off[i][0]);
+        d.records = (const float4 *)((char *)c->ms.d_recs + off[i][1]);
+        d.nodes4 = (const float4 *)((char *)c->ms.d_nodes4 + off4[i]);
+        d.root = meshes[i].nt ? f[GB_ROOT] : 0;
+        d.root4 = meshes[i].nt ? f[GB_ROOT4] : 0;
+        d.empty = meshes[i].nt == 0 ? 1 : 0;
+        d.finite = f[GB_FINITE] ? 1 : 0;
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&c->ms.d_table, count * sizeof(dev_scene));
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(c->ms.d_table, table.data(), count * sizeof(dev_scene), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        grt_free_multi(c);
+        return cuda_fail(c, e, "building the 4-wide scene set on the GPU");
+    }
+    const double build_ms = ms_since(t0);
+    c->ms.count = count;
+    c->ms.max_depth = max_depth;
+    c->ms.max_bound4 = max_bound4;
+    c->ms.gpu_tree = true;
+    c->ms.stats.resize(count);
+    for (uint32_t i = 0; i < count; ++i) {
+        const int32_t *f = info.data() + 8 * (size_t)i;
+        grt_bvh_stats &s = c->ms.stats[i];
+        s = grt_bvh_stats{};
+        s.inner_nodes = (uint32_t)f[GB_INNER];
+        s.tri_records = meshes[i].nt;
+        s.depth = (uint32_t)f[GB_DEPTH];
+        s.device_bytes = (size_t)std::max(meshes[i].nt, 2u) * 64 + (size_t)std::max(meshes[i].nt, 1u) * 48 +
+                         (size_t)std::max(f[GB_WIDE_NODES], 1) * 128;
+        s.build_ms = build_ms;  // wall time of the whole set
+    }
+    return GRT_OK;
+}
+
+}  // extern "C"

@@ -137,6 +137,7 @@ grt_status grt_scene_info(grt_ctx *c, uint32_t scene, grt_bvh_stats *out) {
 grt_status grt_export_scene_bvh(grt_ctx *c, uint32_t scene, uint32_t *nodes14, uint32_t *index, uint32_t *root) {
     if (!c) return GRT_ERR_INVALID_ARG;
     if (scene >= c->ms.count) return fail(c, GRT_ERR_INVALID_ARG, "no such scene");
+    if (c->ms.gpu_tree) return fail(c, GRT_ERR_INVALID_ARG, "a scene set built on the GPU has no reference trees to export");
     export_tree(c->ms.trees[scene], nodes14, index, root);
     return GRT_OK;
 }

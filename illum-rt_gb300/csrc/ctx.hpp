@@ -17,6 +17,7 @@ struct grt_ctx {
     int num_sms = 0;
     std::string err;
     bool built = false;
+    bool gpu_tree = false;  // built by grt_build_device: no reference tree to export
     grt::ref_tree tree;
     grt::dev_scene sc{};
     void *d_nodes = nullptr, *d_recs = nullptr, *d_vpos = nullptr, *d_tris = nullptr, *d_nodes4 = nullptr;
@@ -45,6 +46,7 @@ struct grt_ctx {
     // scene set of the multi-scene path (grt_build_scenes)
     struct multi_set {
         uint32_t count = 0, max_depth = 0, max_bound4 = 0;
+        bool gpu_tree = false;  // built by grt_build_scenes_device
         std::vector<grt::ref_tree> trees;
         std::vector<grt_bvh_stats> stats;
         void *d_nodes = nullptr, *d_recs = nullptr, *d_nodes4 = nullptr, *d_vpos = nullptr, *d_tris = nullptr;
@@ -86,6 +88,7 @@ inline void free_scene(grt_ctx *c) {
         *p = nullptr;
     }
     c->built = false;
+    c->gpu_tree = false;
 }
 
 inline double ms_since(std::chrono::steady_clock::time_point t0) {

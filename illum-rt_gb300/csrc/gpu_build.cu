@@ -1,0 +1,491 @@
+// BVH construction on the GPU.
+//
+// The reference builds every BVH on the host (rt/cuda/base.cpp:88-117 calls the CPU builder of
+// rt/cpu/bvh-ctor.h:371-503); for large or changing scenes that build, not traversal, is the
+// cost. This builder is a linear BVH (Karras, "Maximizing parallelism in the construction of
+// BVHs, octrees, and k-d trees", HPG 2012):
+//   1. per triangle: its box, and the bounds of all box centres (one pass);
+//   2. 30-bit Morton codes of the centres in those bounds, radix-sorted with the triangle index
+//      as value (a stable sort, so equal codes keep index order);
+//   3. the binary radix tree over the sorted codes, one thread per inner node (equal codes are
+//      told apart by their positions);
+//   4. boxes fitted bottom-up, one thread per leaf climbing while it is the second child to
+//      arrive at a node (an atomic counter per node; no thread ever waits for another). On the
+//      way up, a subtree of at most `max_leaf` triangles becomes one leaf when the surface-area
+//      cost of a leaf, A n, is not above that of keeping the split, A + S_l + S_r (traversal and
+//      intersection costs of 1, as in the reference's SAH, rt/cpu/bvh-ctor.h:477-487). Leaves are
+//      contiguous ranges of the sorted order, so records are stored in that order;
+//   5. the 4-wide tree: the binary inner nodes at even depth, each taking its children's
+//      children (the same collapse as flatten_bvh4 on the host).
+// The trees differ from the reference builder's, so closest hits equal the reference's except
+// near-ties, as for the speculative tracers.
+#include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
+
+#include <cfloat>
+
+#include "gpu_build.hpp"
+#include "grt_internal.hpp"
+
+namespace grt {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kMaxClimb = 128;  // a radix tree over 30-bit codes and 2^27 positions is < 60 deep
+
+__device__ __forceinline__ uint32_t ordered(float f) {
+    const uint32_t b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float unordered(uint32_t u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+__device__ __forceinline__ uint32_t spread10(uint32_t v) {  // 10 bits -> every third bit of 30
+    v &= 0x3ffu;
+    v = (v | (v << 16)) & 0x030000ffu;
+    v = (v | (v << 8)) & 0x0300f00fu;
+    v = (v | (v << 4)) & 0x030c30c3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+__device__ __forceinline__ float half_area(float4 lo, float4 hi) {
+    const float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
+    return dx * dy + dy * dz + dz * dx;
+}
+
+// 1. triangle boxes and the bounds of their centres
+__global__ void __launch_bounds__(kThreads) k_prims(const float4 *__restrict__ vpos, uint32_t nv,
+                                                    const uint4 *__restrict__ tris, uint32_t nt, float4 *lo_out,
+                                                    float4 *hi_out, uint32_t *cbounds, int32_t *info) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    float cmin[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, cmax[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    if (i < nt) {
+        const uint4 t = tris[i];
+        float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), hi = lo;
+        if (t.x >= nv || t.y >= nv || t.z >= nv) {
+            atomicOr(info + GB_ERR, GB_ERR_INDEX);
+        } else {
+            const float4 a = vpos[t.x], b = vpos[t.y], c = vpos[t.z];
+            lo = make_float4(fminf(fminf(a.x, b.x), c.x), fminf(fminf(a.y, b.y), c.y), fminf(fminf(a.z, b.z), c.z), 0.f);
+            hi = make_float4(fmaxf(fmaxf(a.x, b.x), c.x), fmaxf(fmaxf(a.y, b.y), c.y), fmaxf(fmaxf(a.z, b.z), c.z), 0.f);
+            const bool fin = isfinite(a.x) && isfinite(a.y) && isfinite(a.z) && isfinite(b.x) && isfinite(b.y) &&
+                             isfinite(b.z) && isfinite(c.x) && isfinite(c.y) && isfinite(c.z);
+            if (!fin) {
+                atomicAnd(info + GB_FINITE, 0);
+            } else {
+                const float cx = 0.5f * (lo.x + hi.x), cy = 0.5f * (lo.y + hi.y), cz = 0.5f * (lo.z + hi.z);
+                cmin[0] = cmax[0] = cx;
+                cmin[1] = cmax[1] = cy;
+                cmin[2] = cmax[2] = cz;
+            }
+        }
+        lo_out[i] = lo;
+        hi_out[i] = hi;
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            cmin[a] = fminf(cmin[a], __shfl_xor_sync(0xffffffffu, cmin[a], o));
+            cmax[a] = fmaxf(cmax[a], __shfl_xor_sync(0xffffffffu, cmax[a], o));
+        }
+    }
+    if ((threadIdx.x & 31u) == 0 && cmin[0] <= cmax[0]) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            atomicMin(cbounds + a, ordered(cmin[a]));
+            atomicMax(cbounds + 3 + a, ordered(cmax[a]));
+        }
+    }
+}
+
+// 2. Morton codes of the box centres
+__global__ void __launch_bounds__(kThreads) k_morton(const float4 *__restrict__ lo, const float4 *__restrict__ hi,
+                                                     uint32_t n, const uint32_t *__restrict__ cbounds, uint32_t *keys,
+                                                     uint32_t *vals) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 l = lo[i], h = hi[i];
+    const float c[3] = {0.5f * (l.x + h.x), 0.5f * (l.y + h.y), 0.5f * (l.z + h.z)};
+    uint32_t q[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float mn = unordered(cbounds[a]), mx = unordered(cbounds[3 + a]);
+        const float ext = mx - mn;
+        float u = ext > 0.f ? (c[a] - mn) / ext : 0.f;
+        u = fminf(fmaxf(u * 1024.f, 0.f), 1023.f);  // NaN -> 0
+        q[a] = (uint32_t)u;
+    }
+    keys[i] = (spread10(q[0]) << 2) | (spread10(q[1]) << 1) | spread10(q[2]);
+    vals[i] = i;
+}
+
+// length of the common prefix of the keys at positions i and j (positions break ties)
+__device__ __forceinline__ int prefix(const uint32_t *__restrict__ k, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    const uint32_t a = k[i], b = k[j];
+    return a != b ? __clz(a ^ b) : 32 + __clz((uint32_t)(i ^ j));
+}
+
+// 3. the radix tree: inner node i covers sorted positions [first, last]; children are inner
+// nodes (>= 0) or single positions (~pos)
+__global__ void __launch_bounds__(kThreads) k_radix_tree(const uint32_t *__restrict__ keys, int n, int2 *children,
+                                                         int2 *range, int32_t *parent_inner, int32_t *parent_leaf) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    const int d = prefix(keys, n, i, i + 1) - prefix(keys, n, i, i - 1) >= 0 ? 1 : -1;
+    const int dmin = prefix(keys, n, i, i - d);
+    int lmax = 2;
+    while (prefix(keys, n, i, i + lmax * d) > dmin) lmax <<= 1;
+    int l = 0;
+    for (int t = lmax >> 1; t >= 1; t >>= 1)
+        if (prefix(keys, n, i, i + (l + t) * d) > dmin) l += t;
+    const int j = i + l * d;
+    const int dnode = prefix(keys, n, i, j);
+    int s = 0;
+    for (int div = 2;; div <<= 1) {
+        const int t = (l + div - 1) / div;
+        if (prefix(keys, n, i, i + (s + t) * d) > dnode) s += t;
+        if (t <= 1) break;
+    }
+    const int split = i + s * d + (d < 0 ? -1 : 0);
+    const int first = min(i, j), last = max(i, j);
+    const int left = first == split ? ~split : split;
+    const int right = last == split + 1 ? ~(split + 1) : split + 1;
+    children[i] = make_int2(left, right);
+    range[i] = make_int2(first, last);
+    if (left >= 0)
+        parent_inner[left] = i;
+    else
+        parent_leaf[~left] = i;
+    if (right >= 0)
+        parent_inner[right] = i;
+    else
+        parent_leaf[~right] = i;
+    if (i == 0) parent_inner[0] = -1;
+}
+
+// What a child hands to its parent in the bottom-up pass (two per inner node).
+struct slot {
+    float4 lo;    // w: area-weighted cost S of the subtree
+    float4 hi;    // w: triangle count (as float, exact below 2^24)
+    int4 meta;    // x: child reference, y: height, z: 4-wide bound if inner else -1, w: M (see below)
+};
+
+__device__ __forceinline__ slot load_slot(const slot *p) {
+    slot s;
+    s.lo = __ldcg(&p->lo);
+    s.hi = __ldcg(&p->hi);
+    s.meta = __ldcg(&p->meta);
+    return s;
+}
+
+// 4. bottom-up fit, SAH collapse and binary node output. For the 4-wide stack bound every inner
+// node also carries B (the bound of a 4-wide node placed there: its wide children less one plus
+// the largest B among its inner grandchildren) and M (the largest B among its inner children).
+__global__ void __launch_bounds__(kThreads) k_bottom_up(const float4 *__restrict__ plo, const float4 *__restrict__ phi,
+                                                        const uint32_t *__restrict__ order, int n, int max_leaf,
+                                                        const int2 *__restrict__ children,
+                                                        const int2 *__restrict__ range,
+                                                        const int32_t *__restrict__ parent_inner,
+                                                        const int32_t *__restrict__ parent_leaf, slot *slots,
+                                                        uint32_t *visits, uint8_t *collapsed, float4 *nodes,
+                                                        int32_t *info) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const uint32_t prim = order[k];
+    slot me;
+    me.lo = plo[prim];
+    me.hi = phi[prim];
+    me.lo.w = half_area(me.lo, me.hi);
+    me.hi.w = 1.f;
+    me.meta = make_int4(~(k << 4), 0, -1, 0);
+    if (n == 1) {
+        info[GB_ROOT] = me.meta.x;
+        info[GB_DEPTH] = 0;
+        info[GB_ROOT4] = me.meta.x;
+        info[GB_BOUND4] = 0;
+        return;
+    }
+    int node = parent_leaf[k];
+    if (node < 0 || node >= n - 1) {
+        atomicOr(info + GB_ERR, GB_ERR_TREE);
+        return;
+    }
+    bool left = children[node].x == ~k;
+    for (int climb = 0; climb < kMaxClimb; ++climb) {
+        slots[2 * node + (left ? 0 : 1)] = me;
+        __threadfence();
+        if (atomicAdd(visits + node, 1u) == 0u) return;  // the sibling's thread continues
+        __threadfence();
+        const slot a = load_slot(slots + 2 * node), b = load_slot(slots + 2 * node + 1);
+        slot p;
+        p.lo = make_float4(fminf(a.lo.x, b.lo.x), fminf(a.lo.y, b.lo.y), fminf(a.lo.z, b.lo.z), 0.f);
+        p.hi = make_float4(fmaxf(a.hi.x, b.hi.x), fmaxf(a.hi.y, b.hi.y), fmaxf(a.hi.z, b.hi.z), 0.f);
+        const float area = half_area(p.lo, p.hi);
+        const float cnt = a.hi.w + b.hi.w;
+        const float keep = area + a.lo.w + b.lo.w;
+        const float as_leaf = area * cnt;
+        const bool leaf = cnt <= (float)max_leaf && !(as_leaf > keep);
+        collapsed[node] = leaf ? 1 : 0;
+        if (leaf) {
+            p.lo.w = as_leaf;
+            p.meta = make_int4(~((range[node].x << 4) | ((int)cnt - 1)), 0, -1, 0);
+        } else {
+            p.lo.w = keep;
+            const bool ai = a.meta.z >= 0, bi = b.meta.z >= 0;
+            const int wide_kids = (ai ? 2 : 1) + (bi ? 2 : 1);
+            const int bnd = wide_kids - 1 + max(ai ? a.meta.w : 0, bi ? b.meta.w : 0);
+            const int m = max(ai ? a.meta.z : 0, bi ? b.meta.z : 0);
+            p.meta = make_int4(node, 1 + max(a.meta.y, b.meta.y), bnd, m);
+            float4 *o = nodes + 4 * (size_t)node;
+            o[0] = make_float4(a.lo.x, a.lo.y, a.lo.z, __int_as_float(a.meta.x));
+            o[1] = make_float4(a.hi.x, a.hi.y, a.hi.z, 0.f);
+            o[2] = make_float4(b.lo.x, b.lo.y, b.lo.z, __int_as_float(b.meta.x));
+            o[3] = make_float4(b.hi.x, b.hi.y, b.hi.z, 0.f);
+        }
+        p.hi.w = cnt;
+        if (node == 0) {
+            info[GB_ROOT] = p.meta.x;
+            info[GB_DEPTH] = p.meta.y;
+            info[GB_ROOT4] = leaf ? p.meta.x : 0;
+            info[GB_BOUND4] = leaf ? 0 : p.meta.z;
+            return;
+        }
+        me = p;
+        const int up = parent_inner[node];
+        if (up < 0 || up >= n - 1) {
+            atomicOr(info + GB_ERR, GB_ERR_TREE);
+            return;
+        }
+        left = children[up].x == node;
+        node = up;
+    }
+    atomicOr(info + GB_ERR, GB_ERR_DEPTH);
+}
+
+// records in sorted order: v0 + original id, v0 - v1 + material, v0 - v2
+__global__ void __launch_bounds__(kThreads) k_records(const float4 *__restrict__ vpos, const uint4 *__restrict__ tris,
+                                                      const uint32_t *__restrict__ order, uint32_t n, uint32_t nv,
+                                                      float4 *records) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const uint32_t prim = order[k];
+    const uint4 t = tris[prim];
+    float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a, c = a;
+    if (t.x < nv && t.y < nv && t.z < nv) {
+        a = vpos[t.x];
+        b = vpos[t.y];
+        c = vpos[t.z];
+    }
+    float4 *r = records + 3 * (size_t)k;
+    r[0] = make_float4(a.x, a.y, a.z, __uint_as_float(prim));
+    r[1] = make_float4(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z), __uint_as_float(t.w));
+    r[2] = make_float4(__fsub_rn(a.x, c.x), __fsub_rn(a.y, c.y), __fsub_rn(a.z, c.z), 0.f);
+}
+
+// 5a. which inner nodes become 4-wide nodes: reachable (no collapsed ancestor) and at even depth
+__global__ void __launch_bounds__(kThreads) k_wide_flags(int n, const uint8_t *__restrict__ collapsed,
+                                                         const int32_t *__restrict__ parent_inner, int32_t *flag,
+                                                         int32_t *info) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int f = 0;
+    if (i < n - 1 && !collapsed[i]) {
+        int depth = 0, q = i;
+        bool reach = true;
+        while (q != 0 && depth < kMaxClimb) {
+            q = parent_inner[q];
+            ++depth;
+            if (q < 0 || q >= n - 1) {
+                atomicOr(info + GB_ERR, GB_ERR_TREE);
+                reach = false;
+                break;
+            }
+            if (collapsed[q]) {
+                reach = false;
+                break;
+            }
+        }
+        if (depth >= kMaxClimb) {
+            atomicOr(info + GB_ERR, GB_ERR_DEPTH);
+            reach = false;
+        }
+        if (reach) {
+            atomicAdd(info + GB_INNER, 1);
+            f = (depth & 1) == 0;
+        }
+    }
+    flag[i] = f;
+}
+
+// 5b. wide index of every flagged node (exclusive sum of the flags, -1 elsewhere) and the count
+__global__ void __launch_bounds__(kThreads) k_wide_index(int n, const int32_t *__restrict__ flag,
+                                                         const int32_t *__restrict__ excl, int32_t *wide_index,
+                                                         int32_t *info) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    wide_index[i] = flag[i] ? excl[i] : -1;
+    if (i == n - 1) info[GB_WIDE_NODES] = excl[i] + flag[i];
+}
+
+// 5c. the 4-wide nodes (structure of arrays per node, unused slots +inf / kEmptyWideChild)
+__global__ void __launch_bounds__(kThreads) k_wide_nodes(const float4 *__restrict__ nodes,
+                                                         const int32_t *__restrict__ wide_index, int n,
+                                                         float4 *nodes4) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const int w = wide_index[p];
+    if (w < 0) return;
+    float lo[3][4], hi[3][4];
+    int ref[4];
+    int k = 0;
+    const float4 *np = nodes + 4 * (size_t)p;
+    for (int side = 0; side < 2; ++side) {
+        const float4 bl = np[2 * side], bh = np[2 * side + 1];
+        const int c = __float_as_int(bl.w);
+        if (c >= n - 1) return;  // not a node of this tree (never for a tree of k_bottom_up)
+        if (c >= 0) {
+            const float4 *cp = nodes + 4 * (size_t)c;
+            for (int g = 0; g < 2; ++g) {
+                const float4 gl = cp[2 * g], gh = cp[2 * g + 1];
+                const int gc = __float_as_int(gl.w);
+                if (gc >= n - 1) return;
+                lo[0][k] = gl.x, lo[1][k] = gl.y, lo[2][k] = gl.z;
+                hi[0][k] = gh.x, hi[1][k] = gh.y, hi[2][k] = gh.z;
+                ref[k++] = gc >= 0 ? wide_index[gc] : gc;
+            }
+        } else {
+            lo[0][k] = bl.x, lo[1][k] = bl.y, lo[2][k] = bl.z;
+            hi[0][k] = bh.x, hi[1][k] = bh.y, hi[2][k] = bh.z;
+            ref[k++] = c;
+        }
+    }
+    const float inf = __int_as_float(0x7f800000);
+    for (; k < 4; ++k) {
+        for (int a = 0; a < 3; ++a) lo[a][k] = hi[a][k] = inf;
+        ref[k] = kEmptyWideChild;
+    }
+    float4 *o = nodes4 + 8 * (size_t)w;
+    for (int a = 0; a < 3; ++a) {
+        o[2 * a] = make_float4(lo[a][0], lo[a][1], lo[a][2], lo[a][3]);
+        o[2 * a + 1] = make_float4(hi[a][0], hi[a][1], hi[a][2], hi[a][3]);
+    }
+    o[6] = make_float4(__int_as_float(ref[0]), __int_as_float(ref[1]), __int_as_float(ref[2]), __int_as_float(ref[3]));
+    o[7] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+__global__ void k_init_info(int32_t *info, uint32_t *cbounds) {
+    if (threadIdx.x < 8) info[threadIdx.x] = threadIdx.x == GB_FINITE ? 1 : 0;
+    if (threadIdx.x < 3) cbounds[threadIdx.x] = 0xffffffffu;
+    else if (threadIdx.x < 6) cbounds[threadIdx.x] = 0u;
+}
+
+inline size_t up256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// scratch layout for up to n triangles
+struct arena {
+    float4 *lo, *hi;
+    uint32_t *keys_a, *keys_b, *vals_a, *vals_b, *cbounds, *visits;
+    int2 *children, *range;
+    int32_t *parent_inner, *parent_leaf, *flag, *excl;
+    slot *slots;
+    uint8_t *collapsed;
+    void *cub;
+    size_t cub_bytes, total;
+};
+
+size_t cub_bytes_for(uint32_t n) {
+    size_t a = 0, b = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, a, (const uint32_t *)nullptr, (uint32_t *)nullptr,
+                                    (const uint32_t *)nullptr, (uint32_t *)nullptr, (int)n, 0, 30);
+    cub::DeviceScan::ExclusiveSum(nullptr, b, (const int32_t *)nullptr, (int32_t *)nullptr, (int)n);
+    return a > b ? a : b;
+}
+
+arena carve(void *base, uint32_t n) {
+    arena A{};
+    char *p = (char *)base;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        void *r = p ? p + off : nullptr;
+        off += up256(bytes);
+        return r;
+    };
+    const size_t m = n > 0 ? n : 1;
+    A.lo = (float4 *)take(m * 16);
+    A.hi = (float4 *)take(m * 16);
+    A.keys_a = (uint32_t *)take(m * 4);
+    A.keys_b = (uint32_t *)take(m * 4);
+    A.vals_a = (uint32_t *)take(m * 4);
+    A.vals_b = (uint32_t *)take(m * 4);
+    A.cbounds = (uint32_t *)take(8 * 4);
+    A.visits = (uint32_t *)take(m * 4);
+    A.children = (int2 *)take(m * 8);
+    A.range = (int2 *)take(m * 8);
+    A.parent_inner = (int32_t *)take(m * 4);
+    A.parent_leaf = (int32_t *)take(m * 4);
+    A.flag = (int32_t *)take(m * 4);
+    A.excl = (int32_t *)take(m * 4);
+    A.slots = (slot *)take(m * 2 * sizeof(slot));
+    A.collapsed = (uint8_t *)take(m);
+    A.cub_bytes = cub_bytes_for((uint32_t)m);
+    A.cub = take(A.cub_bytes);
+    A.total = off;
+    return A;
+}
+
+inline unsigned blocks_for(uint32_t n) { return (n + kThreads - 1) / kThreads; }
+
+}  // namespace
+
+size_t gpu_build_scratch_bytes(uint32_t max_tris) { return carve(nullptr, max_tris).total; }
+
+cudaError_t gpu_build_binary(const float4 *vpos, uint32_t nv, const uint4 *tris, uint32_t nt, int max_leaf,
+                             void *scratch, size_t scratch_bytes, float4 *nodes, float4 *records,
+                             int32_t *wide_index, int32_t *info, cudaStream_t st) {
+    arena A = carve(scratch, nt);
+    if (A.total > scratch_bytes) return cudaErrorInvalidValue;
+    k_init_info<<<1, 32, 0, st>>>(info, A.cbounds);
+    if (nt == 0) return cudaGetLastError();
+    const unsigned nb = blocks_for(nt);
+    k_prims<<<nb, kThreads, 0, st>>>(vpos, nv, tris, nt, A.lo, A.hi, A.cbounds, info);
+    k_morton<<<nb, kThreads, 0, st>>>(A.lo, A.hi, nt, A.cbounds, A.keys_a, A.vals_a);
+    size_t cb = A.cub_bytes;
+    cudaError_t e = cub::DeviceRadixSort::SortPairs(A.cub, cb, A.keys_a, A.keys_b, A.vals_a, A.vals_b, (int)nt, 0,
+                                                    30, st);
+    if (e != cudaSuccess) return e;
+    // parents start at -1, so a position the tree misses is caught instead of read as an index
+    e = cudaMemsetAsync(A.visits, 0, (size_t)nt * 4, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(A.collapsed, 1, (size_t)nt, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(A.parent_inner, 0xff, (size_t)nt * 4, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(A.parent_leaf, 0xff, (size_t)nt * 4, st);
+    if (e != cudaSuccess) return e;
+    if (nt > 1)
+        k_radix_tree<<<blocks_for(nt - 1), kThreads, 0, st>>>(A.keys_b, (int)nt, A.children, A.range,
+                                                              A.parent_inner, A.parent_leaf);
+    k_bottom_up<<<nb, kThreads, 0, st>>>(A.lo, A.hi, A.vals_b, (int)nt, max_leaf, A.children, A.range,
+                                         A.parent_inner, A.parent_leaf, A.slots, A.visits, A.collapsed, nodes,
+                                         info);
+    k_records<<<nb, kThreads, 0, st>>>(vpos, tris, A.vals_b, nt, nv, records);
+    if (nt > 1) {
+        k_wide_flags<<<nb, kThreads, 0, st>>>((int)nt, A.collapsed, A.parent_inner, A.flag, info);
+        cb = A.cub_bytes;
+        e = cub::DeviceScan::ExclusiveSum(A.cub, cb, A.flag, A.excl, (int)nt, st);
+        if (e != cudaSuccess) return e;
+        k_wide_index<<<nb, kThreads, 0, st>>>((int)nt, A.flag, A.excl, wide_index, info);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t gpu_build_wide(const float4 *nodes, const int32_t *wide_index, uint32_t nt, float4 *nodes4,
+                           cudaStream_t st) {
+    if (nt < 2) return cudaSuccess;
+    k_wide_nodes<<<blocks_for(nt), kThreads, 0, st>>>(nodes, wide_index, (int)nt, nodes4);
+    return cudaGetLastError();
+}
+
+}  // namespace grt

@@ -1,0 +1,38 @@
+// BVH construction on the GPU (linear BVH with SAH leaf collapse), written in the device layout
+// of bvh_builder.hpp: 64-byte binary nodes, 48-byte triangle records and 128-byte 4-wide nodes.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+namespace grt {
+
+// Per-scene results, written by the device into an int32[8] array.
+enum gpu_build_info : int {
+    GB_ROOT = 0,        // child reference of the binary root (a leaf reference if the tree is one leaf)
+    GB_DEPTH = 1,       // edges from the root to the deepest leaf
+    GB_ROOT4 = 2,       // child reference of the 4-wide root
+    GB_BOUND4 = 3,      // most stack entries a 4-wide traversal can hold
+    GB_ERR = 4,         // error bits (GB_ERR_*)
+    GB_WIDE_NODES = 5,  // 4-wide nodes of the tree
+    GB_INNER = 6,       // binary inner nodes reachable from the root
+    GB_FINITE = 7,      // 1: every vertex coordinate of the scene is finite
+};
+enum : int { GB_ERR_INDEX = 1, GB_ERR_DEPTH = 2, GB_ERR_TREE = 4 };
+
+// Scratch bytes for scenes of up to `max_tris` triangles.
+size_t gpu_build_scratch_bytes(uint32_t max_tris);
+
+// Phase 1 of one scene: binary nodes (max(nt - 1, 1) x 64 B), records (nt x 48 B), and for every
+// binary node its 4-wide node index (wide_index, nt ints, -1 for none). `info` (int32[8], device)
+// receives the fields above. Stream-ordered; nothing is read back.
+cudaError_t gpu_build_binary(const float4 *vpos, uint32_t nv, const uint4 *tris, uint32_t nt, int max_leaf,
+                             void *scratch, size_t scratch_bytes, float4 *nodes, float4 *records,
+                             int32_t *wide_index, int32_t *info, cudaStream_t st);
+
+// Phase 2: the 4-wide nodes (info[GB_WIDE_NODES] x 128 B) from the binary nodes of phase 1.
+cudaError_t gpu_build_wide(const float4 *nodes, const int32_t *wide_index, uint32_t nt, float4 *nodes4,
+                           cudaStream_t st);
+
+}  // namespace grt

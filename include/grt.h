@@ -304,6 +304,26 @@ grt_status grt_adjoint(grt_ctx *ctx, const float *rays_dev, const grt_hit *hits_
                        uint32_t n, const float *vpos_dev, uint32_t vstride, float *grad_vpos_dev, float *grad_rays_dev,
                        grt_stream_t stream);
 
+/* ---- BVH construction on the GPU ----------------------------------------------------- */
+
+/* Builds the scene of grt_build on the GPU from DEVICE arrays in the same layouts (vertices
+ * float4, triangles uint4 with the material id in w). No counterpart in the reference, whose
+ * builds all run on the host (batch_rt::build, rt/cuda/base.cpp:88-117): a linear BVH over
+ * Morton codes of the triangle box centres, with subtrees of at most max_tris_per_node
+ * (1..16) triangles turned into leaves where the SAH cost says so, and its 4-wide collapse.
+ * The tree differs from the reference builder's, so closest hits equal the reference's except
+ * near-ties (any-hit answers are equal). Every tracer can trace it; grt_export_bvh has no
+ * reference tree to export and fails. The arrays are copied, so the caller may free them after
+ * the call. Ordered after earlier work on `stream`; returns when the build is done. At most
+ * 2^27 - 1 triangles. */
+grt_status grt_build_device(grt_ctx *ctx, const float *vpos4_dev, uint32_t nv, const uint32_t *tris4_dev,
+                            uint32_t nt, uint32_t max_tris_per_node, grt_stream_t stream);
+
+/* grt_build_scenes with the GPU builder: the vpos4 / tris4 pointers of `meshes` (a host array)
+ * are DEVICE pointers, read during the call only. grt_export_scene_bvh fails for such a set. */
+grt_status grt_build_scenes_device(grt_ctx *ctx, const grt_mesh *meshes, uint32_t count, uint32_t max_tris_per_node,
+                                   grt_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,160 @@
+"""GPU BVH construction (grt_build_device, grt_build_scenes_device): trees built on the GPU
+from device arrays, traced by every tracer, against the oracle on the reference's tree.
+Closest hits may differ from the reference only as near-ties (another tree visits triangles in
+another order); any-hit answers are equal. Also: degenerate inputs, errors, and the statistics
+of the trees."""
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_CASES, assert_hits_match
+
+pytestmark = pytest.mark.gpu
+
+TRACERS = ["while-while", "persistent-while-while", "if-if", "persistent-if-if", "speculative-while-while",
+           "persistent-speculative-while-while", "bvh4-speculative-while-while",
+           "persistent-bvh4-speculative-while-while"]
+
+
+@pytest.fixture(autouse=True)
+def _needs_cuda():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def _dev(a, dtype):
+    """A CUDA copy; uint32 arrays travel as int32 (same bits)."""
+    import torch
+    a = np.ascontiguousarray(a, dtype)
+    if a.dtype == np.uint32:
+        a = a.view(np.int32)
+    return torch.from_numpy(a).cuda()
+
+
+def _trace(rt, rays_np, any_hit):
+    import torch
+    rays = _dev(rays_np, np.float32)
+    hits = torch.zeros((rays.shape[0], 4), dtype=torch.float32, device="cuda")
+    rt.trace(rays, hits, any_hit, torch.cuda.current_stream().cuda_stream)
+    rt.check(torch.cuda.current_stream().cuda_stream, timeout_ms=60000)
+    return hits.cpu().numpy()
+
+
+def _occluded(h):
+    return (h.view(np.uint32)[:, 3] == 0xFFFFFFFF).astype(np.uint8)
+
+
+@pytest.fixture(scope="module")
+def oracles(orc, golden_scenes):
+    return {name: orc.OracleBVH(v, t) for name, (v, t, _, _) in golden_scenes.items()}
+
+
+@pytest.mark.parametrize("max_tris", [1, 4, 16])
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_gpu_tree_hits_match_oracle(gpu_tracer, golden_scenes, oracles, name, max_tris):
+    v, t, rays, any_rays = golden_scenes[name]
+    info = gpu_tracer.build_device(_dev(v, np.float32), _dev(t, np.uint32), max_tris=max_tris)
+    assert info["tri_records"] == t.shape[0] and info["depth"] <= 64
+    o = oracles[name]
+    want, _ = o.closest(rays)
+    want_any, _ = o.any(any_rays)
+    for tracer in TRACERS:
+        gpu_tracer.select(tracer)
+        assert_hits_match(_trace(gpu_tracer, rays, False), want, False, f"{name} {tracer} leaf<={max_tris}")
+        assert (_occluded(_trace(gpu_tracer, any_rays, True)) == want_any).all(), (name, tracer)
+    gpu_tracer.select("while-while")
+
+
+def test_gpu_tree_spheres_full_frame(gpu_tracer, wl, orc):
+    sc, rays = wl.spheres_primary(res=1024)
+    info = gpu_tracer.build_device(_dev(sc.vpos, np.float32), _dev(sc.tris, np.uint32), max_tris=4)
+    assert info["inner_nodes"] > 0
+    want, _ = orc.OracleBVH(sc.vpos, sc.tris).closest(rays)
+    for tracer in ("persistent-speculative-while-while", "while-while", "persistent-bvh4-speculative-while-while"):
+        gpu_tracer.select(tracer)
+        assert_hits_match(_trace(gpu_tracer, rays, False), want, False, f"spheres {tracer}")
+    gpu_tracer.select("while-while")
+
+
+def test_gpu_tree_degenerate_inputs(gpu_tracer, api):
+    import torch
+    ray = np.array([[0.2, 0.2, 1.0, 1e-4, 0.0, 0.0, -1.0, 3e38]], np.float32)
+    tri = np.array([[0, 1, 2, 7]], np.uint32)
+    v = np.array([[0, 0, 0, 0], [1, 0, 0, 0], [0, 1, 0, 0]], np.float32)
+    # one triangle: the root is a leaf
+    gpu_tracer.build_device(_dev(v, np.float32), _dev(tri, np.uint32))
+    for tracer in TRACERS:
+        gpu_tracer.select(tracer)
+        h = _trace(gpu_tracer, ray, False)
+        assert h[0, 0] == np.float32(1.0) and h.view(np.uint32)[0, 3] == 0
+    # no triangles: every ray misses
+    gpu_tracer.build_device(_dev(v, np.float32), torch.zeros((0, 4), dtype=torch.int32, device="cuda"))
+    for tracer in TRACERS:
+        gpu_tracer.select(tracer)
+        h = _trace(gpu_tracer, ray, False)
+        assert h[0, 0] == np.float32(3.4028234663852886e38)
+    # 5,000 copies of one triangle: equal Morton codes everywhere, equal t for every ray
+    many = np.tile(tri, (5000, 1))
+    gpu_tracer.build_device(_dev(v, np.float32), _dev(many, np.uint32), max_tris=3)
+    for tracer in TRACERS:
+        gpu_tracer.select(tracer)
+        h = _trace(gpu_tracer, ray, False)
+        assert h[0, 0] == np.float32(1.0) and h.view(np.uint32)[0, 3] < 5000
+    gpu_tracer.select("while-while")
+
+
+def test_gpu_tree_errors(gpu_tracer, api):
+    import torch
+    v = _dev(np.zeros((3, 4)), np.float32)
+    bad = _dev(np.array([[0, 1, 3, 0]]), np.uint32)
+    with pytest.raises(api.GRTError) as e:
+        gpu_tracer.build_device(v, bad)
+    assert e.value.status == 1  # invalid argument: index beyond the vertex count
+    with pytest.raises(api.GRTError):
+        gpu_tracer.build_device(v, _dev(np.array([[0, 1, 2, 0]]), np.uint32), max_tris=17)
+    gpu_tracer.build_device(v, _dev(np.array([[0, 1, 2, 0]]), np.uint32))
+    with pytest.raises(api.GRTError):
+        gpu_tracer.export_bvh()
+    with pytest.raises(ValueError):
+        gpu_tracer.build_device(torch.zeros((3, 3), device="cuda"), _dev(np.array([[0, 1, 2, 0]]), np.uint32))
+
+
+@pytest.mark.parametrize("tracer", ["persistent-while-while", "persistent-speculative-while-while",
+                                    "persistent-bvh4-speculative-while-while"])
+def test_gpu_scene_set_matches_oracle(api, orc, wl, tracer):
+    import torch
+    rt = api.BatchRayTracer(0)
+    scenes, rays, oracles = [], [], []
+    for i in range(10):
+        ntri = wl.log_uniform(93, 2 * i, 1024, 1 << 16)
+        nray = wl.log_uniform(93, 2 * i + 1, 4096, 1 << 15)
+        sc = wl.soup(300 + i, ntri, sigma=0.5)
+        lo, hi = sc.bounds()
+        scenes.append((_dev(sc.vpos, np.float32), _dev(sc.tris, np.uint32)))
+        r = wl.shell_rays(400 + i, lo, hi, nray)
+        r[: nray // 2, 7] = 1.5  # half the rays with a finite t_max
+        rays.append(r)
+        oracles.append(orc.OracleBVH(sc.vpos, sc.tris))
+    scenes.append((_dev(np.zeros((3, 4)), np.float32), torch.zeros((0, 4), dtype=torch.int32, device="cuda")))
+    rays.append(rays[0][:64].copy())
+    oracles.append(None)
+    stats = rt.build_scenes_device(scenes, max_tris=4)
+    assert [s["tri_records"] for s in stats] == [int(s[1].shape[0]) for s in scenes]
+    with pytest.raises(api.GRTError):
+        rt.export_scene_bvh(0, 1, 1)
+    rt.select(tracer)
+    stream = torch.cuda.current_stream().cuda_stream
+    for any_hit in (False, True):
+        d_rays = [_dev(r, np.float32) for r in rays]
+        outs = [torch.zeros((r.shape[0], 4), device="cuda") for r in rays]
+        rt.trace_multi([(s, d_rays[s], outs[s]) for s in range(len(rays))], any_hit=any_hit, stream=stream)
+        rt.check(stream, timeout_ms=60000)
+        for s, o in enumerate(oracles):
+            got = outs[s].cpu().numpy()
+            if o is None:
+                assert (got[:, 0] == np.float32(3.4028234663852886e38)).all()
+            elif any_hit:
+                assert (_occluded(got) == o.any(rays[s])[0]).all(), (tracer, s)
+            else:
+                assert_hits_match(got, o.closest(rays[s])[0], False, f"{tracer} scene {s}")
+    rt.close()
