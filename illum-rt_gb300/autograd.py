@@ -3,8 +3,10 @@
 ``closest_hits(tracer, vpos, tris, rays)`` returns (t, beta, gamma, ref) for every ray, with t,
 beta and gamma differentiable with respect to the vertex positions ``vpos`` [nv, 3] and the rays
 [n, 8] (origin in columns 0-2, direction in 4-6). The hit triangle of each ray is held fixed:
-the forward pass builds the BVH from the current vertices with the reference builder and
-traces with the selected tracer; the backward pass (grt_adjoint) recomputes each intersection
+the forward pass builds the BVH from the current vertices (with the reference builder on the
+host, or with builder="gpu" with the GPU builder straight from the device tensor, which avoids
+the round trip through host memory when the vertices change every step) and traces with the
+selected tracer; the backward pass (grt_adjoint) recomputes each intersection
 from the vertices and propagates dL/d(t, beta, gamma) to the three vertices and the ray.
 Misses (t = FLT_MAX) get no gradient; mask them out of the loss.
 """
@@ -16,13 +18,22 @@ import torch
 
 class _ClosestHits(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, vpos, rays, tracer, tris):
+    def forward(ctx, vpos, rays, tracer, tris, builder):
         with torch.no_grad():
-            v4 = np.ones((vpos.shape[0], 4), np.float32)
-            v4[:, :3] = vpos.detach().cpu().numpy()
-            tracer.build(v4, tris)
-            hits = torch.empty((rays.shape[0], 4), dtype=torch.float32, device=rays.device)
             stream = torch.cuda.current_stream(rays.device).cuda_stream
+            if builder == "gpu":
+                v4 = torch.ones((vpos.shape[0], 4), dtype=torch.float32, device=vpos.device)
+                v4[:, :3] = vpos.detach()
+                t4 = tris if isinstance(tris, torch.Tensor) else torch.from_numpy(
+                    np.ascontiguousarray(tris, np.uint32).view(np.int32))
+                tracer.build_device(v4, t4.to(vpos.device).contiguous(), stream=stream)
+            elif builder == "reference":
+                v4 = np.ones((vpos.shape[0], 4), np.float32)
+                v4[:, :3] = vpos.detach().cpu().numpy()
+                tracer.build(v4, tris)
+            else:
+                raise ValueError(f"unknown builder {builder!r}")
+            hits = torch.empty((rays.shape[0], 4), dtype=torch.float32, device=rays.device)
             tracer.trace(rays.detach(), hits, False, stream)
             tracer.check(stream)
         ctx.save_for_backward(vpos, rays, hits)
@@ -44,9 +55,11 @@ class _ClosestHits(torch.autograd.Function):
         ctx.tracer.adjoint(rays.detach().contiguous(), hits, grad3, grad_v, grad_r,
                            vpos=vpos.detach().contiguous(), stream=stream)
         return (grad_v if ctx.needs_input_grad[0] else None, grad_r if ctx.needs_input_grad[1] else None,
-                None, None)
+                None, None, None)
 
 
-def closest_hits(tracer, vpos: torch.Tensor, tris: np.ndarray, rays: torch.Tensor):
-    """(t, beta, gamma, ref) of each ray, differentiable in vpos [nv, 3] and rays [n, 8]."""
-    return _ClosestHits.apply(vpos, rays, tracer, tris)
+def closest_hits(tracer, vpos: torch.Tensor, tris, rays: torch.Tensor, builder: str = "reference"):
+    """(t, beta, gamma, ref) of each ray, differentiable in vpos [nv, 3] and rays [n, 8].
+    builder: "reference" (host build, hits bit-identical to the reference tracer with an exact
+    tracer) or "gpu" (GPU build; hits equal except near-ties)."""
+    return _ClosestHits.apply(vpos, rays, tracer, tris, builder)

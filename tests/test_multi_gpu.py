@@ -20,6 +20,8 @@ def _needs_cuda():
 @pytest.fixture(scope="module")
 def multi_case(api, orc, wl):
     import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
     scenes, rays, oracles = [], [], []
     for i in range(12):
         ntri = wl.log_uniform(91, 2 * i, 1024, 1 << 16)

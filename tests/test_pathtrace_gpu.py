@@ -24,6 +24,8 @@ def _needs_cuda():
 @pytest.fixture(scope="module")
 def spheres_setup(api, orc, wl):
     import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
     sc, rays = wl.spheres_primary(res=512)
     o = orc.OracleBVH(sc.vpos, sc.tris)
     rt = api.BatchRayTracer(0)
