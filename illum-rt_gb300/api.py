@@ -19,12 +19,13 @@ from . import _libs
 GRT_OK = 0
 STATUS_NAMES = {0: "GRT_OK", 1: "GRT_ERR_INVALID_ARG", 2: "GRT_ERR_OOM", 3: "GRT_ERR_CUDA", 4: "GRT_ERR_TIMEOUT",
                 5: "GRT_ERR_BVH_TOO_DEEP", 6: "GRT_ERR_NOT_BUILT", 7: "GRT_ERR_TRAVERSAL",
-                8: "GRT_ERR_UNKNOWN_TRACER", 9: "GRT_ERR_NO_DEVICE"}
+                8: "GRT_ERR_UNKNOWN_TRACER", 9: "GRT_ERR_NO_DEVICE", 10: "GRT_ERR_TOO_LARGE"}
 SPLIT = {"om": 0, "sm": 1, "sah": 2}
 TRACERS = ("while-while", "persistent-while-while", "if-if", "persistent-if-if", "speculative-while-while",
            "persistent-speculative-while-while", "bvh4-speculative-while-while",
            "persistent-bvh4-speculative-while-while")
 EXACT_TRACERS = TRACERS[:4]  # per-ray visit order of the reference: bit-identical results
+ALPHA_TRACERS = tuple(t + "-alpha" for t in TRACERS)  # alpha-aware variants (set_alpha)
 
 
 class GRTError(RuntimeError):
@@ -45,6 +46,10 @@ class BvhStats(ctypes.Structure):
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class AlphaTexture(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("alpha", ctypes.c_void_p)]
 
 
 class Tuning(ctypes.Structure):
@@ -106,6 +111,7 @@ _PROTOS = {
     "grt_scene_info": (I, [VP, U32, P(BvhStats)]),
     "grt_export_scene_bvh": (I, [VP, U32, VP, VP, P(U32)]),
     "grt_trace_multi": (I, [VP, VP, U32, I, VP]),
+    "grt_set_alpha": (I, [VP, VP, U32, VP, U32, VP, U32]),
     "grt_build_device": (I, [VP, VP, U32, VP, U32, U32, VP]),
     "grt_build_scenes_device": (I, [VP, VP, U32, U32, VP]),
 }
@@ -256,6 +262,19 @@ class BatchRayTracer:
         self._check(lib().grt_build_device(self.ctx, _ptr(vpos), int(vpos.shape[0]), _ptr(tris), int(tris.shape[0]),
                                            int(max_tris or self.bvh_max_tris_per_node), VP(stream or 0)))
         return self.info()
+
+    def set_alpha(self, tc, mat_tex, textures):
+        """Texture data of the alpha-aware tracers (grt_set_alpha): tc float32 [nv, 2] per vertex
+        of the built scene, mat_tex int32 [n_materials] (texture index or -1), textures: list of
+        float32 [height, width] alpha arrays. set_alpha(None, None, None) clears it."""
+        if mat_tex is None:
+            self._check(lib().grt_set_alpha(self.ctx, None, 0, None, 0, None, 0))
+            return
+        tc = np.ascontiguousarray(tc, np.float32)
+        mt = np.ascontiguousarray(mat_tex, np.int32)
+        tex = [np.ascontiguousarray(t, np.float32) for t in textures]
+        arr = (AlphaTexture * max(1, len(tex)))(*[AlphaTexture(t.shape[1], t.shape[0], t.ctypes.data) for t in tex])
+        self._check(lib().grt_set_alpha(self.ctx, _ptr(tc), tc.shape[0], _ptr(mt), mt.shape[0], arr, len(tex)))
 
     def use(self, rd: RayData):
         self.rd = rd

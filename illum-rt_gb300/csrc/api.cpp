@@ -154,6 +154,64 @@ grt_status grt_build(grt_ctx *c, const float *vpos4, uint32_t nv, const uint32_t
     return GRT_OK;
 }
 
+grt_status grt_set_alpha(grt_ctx *c, const float *tc2, uint32_t nv, const int32_t *mat_tex, uint32_t n_mat,
+                         const grt_alpha_texture *tex, uint32_t n_tex) {
+    if (!c) return GRT_ERR_INVALID_ARG;
+    device_guard g(c->device);
+    if (c->d_alpha) cudaFree(c->d_alpha);
+    c->d_alpha = nullptr;
+    ++c->scene_generation;  // captured path-tracing graphs hold the old scene
+    if (!mat_tex) return GRT_OK;
+    if (!c->built) return fail(c, GRT_ERR_NOT_BUILT, "grt_set_alpha before a successful build");
+    if (nv != c->nv || (nv && !tc2) || (n_tex && !tex))
+        return fail(c, GRT_ERR_INVALID_ARG, "texture coordinates must cover the built scene's vertices");
+    size_t texels = 0;
+    for (uint32_t k = 0; k < n_tex; ++k) {
+        if (!tex[k].alpha || tex[k].width == 0 || tex[k].height == 0 || tex[k].width > (1u << 24) ||
+            tex[k].height > (1u << 24))
+            return fail(c, GRT_ERR_INVALID_ARG, "texture " + std::to_string(k) + ": empty or oversized");
+        texels += (size_t)tex[k].width * tex[k].height;
+    }
+    if (texels >= (1ull << 32)) return fail(c, GRT_ERR_INVALID_ARG, "more than 2^32 texels");
+    for (uint32_t m = 0; m < n_mat; ++m)
+        if (mat_tex[m] < -1 || mat_tex[m] >= (int32_t)n_tex)
+            return fail(c, GRT_ERR_INVALID_ARG, "material " + std::to_string(m) + " names no texture");
+    // one allocation: descriptor, texture coordinates, material table, texture table, texels
+    auto a16 = [](size_t b) { return (b + 15) & ~(size_t)15; };
+    const size_t o_tc = a16(sizeof(alpha_data)), o_mat = o_tc + a16((size_t)nv * 8),
+                 o_tex = o_mat + a16((size_t)n_mat * 4), o_texels = o_tex + a16((size_t)n_tex * 16),
+                 total = o_texels + std::max<size_t>(texels * 4, 4);
+    std::vector<char> host(total, 0);
+    std::vector<uint4> table(n_tex);
+    size_t first = 0;
+    for (uint32_t k = 0; k < n_tex; ++k) {
+        table[k] = make_uint4(tex[k].width, tex[k].height, (uint32_t)first, 0u);
+        std::memcpy(host.data() + o_texels + first * 4, tex[k].alpha, (size_t)tex[k].width * tex[k].height * 4);
+        first += (size_t)tex[k].width * tex[k].height;
+    }
+    if (nv) std::memcpy(host.data() + o_tc, tc2, (size_t)nv * 8);
+    if (n_mat) std::memcpy(host.data() + o_mat, mat_tex, (size_t)n_mat * 4);
+    if (n_tex) std::memcpy(host.data() + o_tex, table.data(), (size_t)n_tex * 16);
+    char *dev = nullptr;
+    cudaError_t e = cudaMalloc(&dev, total);
+    if (e != cudaSuccess) return cuda_fail(c, e, "allocating the texture data");
+    alpha_data d;
+    d.tris = (const uint4 *)c->d_tris;
+    d.tc = (const float2 *)(dev + o_tc);
+    d.mat_tex = (const int32_t *)(dev + o_mat);
+    d.tex = (const uint4 *)(dev + o_tex);
+    d.texels = (const float *)(dev + o_texels);
+    d.n_mat = n_mat;
+    std::memcpy(host.data(), &d, sizeof(d));
+    e = cudaMemcpy(dev, host.data(), total, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(dev);
+        return cuda_fail(c, e, "uploading the texture data");
+    }
+    c->d_alpha = dev;
+    return GRT_OK;
+}
+
 grt_status grt_bvh_info(grt_ctx *c, grt_bvh_stats *out) {
     if (!c || !out) return GRT_ERR_INVALID_ARG;
     if (!c->built) return fail(c, GRT_ERR_NOT_BUILT, "no scene has been built");
@@ -249,10 +307,10 @@ grt_status grt_trace(grt_ctx *c, const float *rays_dev, grt_hit *hits_dev, uint3
     grt::launch_params lp = params_for(c, any_hit != 0);
     cudaError_t e;
     if (kTracers[c->tracer].persistent)
-        e = grt::launch_trace_persistent(c->sc, (const float4 *)rays_dev, hits_dev, n, any_hit != 0, lp, c->d_err,
+        e = grt::launch_trace_persistent(scene_for(c), (const float4 *)rays_dev, hits_dev, n, any_hit != 0, lp, c->d_err,
                                          c->d_counter, (cudaStream_t)stream);
     else
-        e = grt::launch_trace_plain(c->sc, (const float4 *)rays_dev, hits_dev, n, any_hit != 0, lp, c->d_err,
+        e = grt::launch_trace_plain(scene_for(c), (const float4 *)rays_dev, hits_dev, n, any_hit != 0, lp, c->d_err,
                                     (cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "launching the traversal kernel");
     return GRT_OK;

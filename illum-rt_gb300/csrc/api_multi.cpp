@@ -159,6 +159,8 @@ grt_status grt_trace_multi(grt_ctx *c, const grt_ray_batch *batches, uint32_t co
         total += x.n;
     }
     if (total > (1ull << 31)) return fail(c, GRT_ERR_INVALID_ARG, "more than 2^31 rays in one call");
+    if (kTracers[c->tracer].alpha)
+        return fail(c, GRT_ERR_INVALID_ARG, "alpha-aware tracing of scene sets is not supported");
     const int order = kTracers[c->tracer].order;
     const int needed = order == WIDE_SPECULATIVE ? (int)c->ms.max_bound4 : (int)c->ms.max_depth;
     if (needed > kStackLarge)

@@ -79,7 +79,7 @@ cudaError_t enqueue_pathtrace(grt_ctx *c, const grt_pt_params &p, const pt_param
         e = launch_compact_hits(prim_hits, n_primary, hit_list, n_list, at<uint32_t>(c, L.compact), st);
     if (e != cudaSuccess) return e;
     if (p.mode == GRT_PT_FUSED)
-        return launch_fused(c->sc, ps, pp, (const float4 *)prim_rays, prim_hits, hit_list, n_list, n_paths, results,
+        return launch_fused(scene_for(c), ps, pp, (const float4 *)prim_rays, prim_hits, hit_list, n_list, n_paths, results,
                             bounce_hits, lp, c->d_err, counters + 63, st);
     uint32_t *queue[2] = {at<uint32_t>(c, L.queue0), at<uint32_t>(c, L.queue1)};
     float4 *rays[2] = {at<float4>(c, L.rays0), at<float4>(c, L.rays1)};
@@ -89,7 +89,7 @@ cudaError_t enqueue_pathtrace(grt_ctx *c, const grt_pt_params &p, const pt_param
                               rays[0], results, counters + 1, st);
     for (uint32_t b = 1; b <= p.max_bounces && e == cudaSuccess; ++b) {
         const int cur = (b - 1) & 1, nxt = b & 1;
-        e = launch_trace_plain(c->sc, rays[cur], hits, n_paths, false, lp_trace, c->d_err, st, counters + b);
+        e = launch_trace_plain(scene_for(c), rays[cur], hits, n_paths, false, lp_trace, c->d_err, st, counters + b);
         if (e == cudaSuccess)
             e = launch_wavefront_shade(ps, pp, n_paths, counters + b, queue[cur], rays[cur], hits, states,
                                        counters + b + 1, queue[nxt], rays[nxt], results, bounce_hits, st);
@@ -190,7 +190,7 @@ grt_status grt_pathtrace(grt_ctx *c, const grt_pt_params *params, const float *p
     launch_params lp_trace = params_for(c, false);  // one-thread-per-ray kernel of the wavefront form
     launch_params lp = lp_trace;
     lp.grid_blocks = (c->tuning.blocks_per_sm > 0 ? c->tuning.blocks_per_sm
-                                                  : fused_blocks_per_sm(lp.block_threads, lp.stack_entries, lp.order)) *
+                                                  : fused_blocks_per_sm(lp.block_threads, lp.stack_entries, lp.order, scene_for(c).alpha != nullptr)) *
                      c->num_sms;
     cudaStream_t st = (cudaStream_t)stream;
     if (!p.use_graph) {
@@ -205,7 +205,7 @@ grt_status grt_pathtrace(grt_ctx *c, const grt_pt_params *params, const float *p
         (uint64_t)(uintptr_t)c->d_albedo, c->n_albedo, (uint64_t)(uintptr_t)st, (uint64_t)lp.block_threads,
         (uint64_t)lp.grid_blocks, (uint64_t)lp.refill_threshold, (uint64_t)lp.refill_period,
         (uint64_t)lp.stack_entries, (uint64_t)lp.order, (uint64_t)lp_trace.block_threads,
-        (uint64_t)(uintptr_t)lp_trace.counters};
+        (uint64_t)(uintptr_t)lp_trace.counters, (uint64_t)(uintptr_t)scene_for(c).alpha};
     if (!c->pt_graph.exec || c->pt_graph.key != key) {
         if (c->pt_graph.exec) cudaGraphExecDestroy(c->pt_graph.exec);
         c->pt_graph.exec = nullptr;

@@ -32,6 +32,8 @@ struct grt_ctx {
     cudaStream_t stream = nullptr;  // grt_trace_host stream
     unsigned long long *d_trav_counters = nullptr;  // grt_set_traversal_counters (caller's memory)
     uint64_t scene_generation = 0;  // bumped by every build (invalidates captured graphs)
+    // texture data of the alpha-aware tracers (grt_set_alpha): one device allocation
+    void *d_alpha = nullptr;
     // shading data of the path tracer
     float *d_albedo = nullptr;
     uint32_t n_albedo = 0;
@@ -83,7 +85,7 @@ inline grt_status cuda_fail(grt_ctx *c, cudaError_t e, const char *what) {
 }
 
 inline void free_scene(grt_ctx *c) {
-    for (void **p : {&c->d_nodes, &c->d_recs, &c->d_vpos, &c->d_tris, &c->d_nodes4}) {
+    for (void **p : {&c->d_nodes, &c->d_recs, &c->d_vpos, &c->d_tris, &c->d_nodes4, &c->d_alpha}) {
         if (*p) cudaFree(*p);
         *p = nullptr;
     }
@@ -97,20 +99,40 @@ inline double ms_since(std::chrono::steady_clock::time_point t0) {
 
 // The tracers a context can select (the reference's `raytracer` names for the same loop
 // shapes, rt/cuda/platform.cpp:34-56).
+// Every loop shape also comes as "<name>-alpha", the alpha-aware variant (the reference
+// registers the same pairs, rt/cuda/platform.cpp:34-51).
 struct tracer_kind {
     const char *name;
     bool persistent;
     int order;
+    bool alpha;
 };
-inline const tracer_kind kTracers[] = {{"while-while", false, WHILE_WHILE},
-                                       {"persistent-while-while", true, WHILE_WHILE},
-                                       {"if-if", false, IF_IF},
-                                       {"persistent-if-if", true, IF_IF},
-                                       {"speculative-while-while", false, SPECULATIVE},
-                                       {"persistent-speculative-while-while", true, SPECULATIVE},
-                                       {"bvh4-speculative-while-while", false, WIDE_SPECULATIVE},
-                                       {"persistent-bvh4-speculative-while-while", true, WIDE_SPECULATIVE}};
-inline const int kNumTracers = 8;
+inline const tracer_kind kTracers[] = {
+    {"while-while", false, WHILE_WHILE, false},
+    {"persistent-while-while", true, WHILE_WHILE, false},
+    {"if-if", false, IF_IF, false},
+    {"persistent-if-if", true, IF_IF, false},
+    {"speculative-while-while", false, SPECULATIVE, false},
+    {"persistent-speculative-while-while", true, SPECULATIVE, false},
+    {"bvh4-speculative-while-while", false, WIDE_SPECULATIVE, false},
+    {"persistent-bvh4-speculative-while-while", true, WIDE_SPECULATIVE, false},
+    {"while-while-alpha", false, WHILE_WHILE, true},
+    {"persistent-while-while-alpha", true, WHILE_WHILE, true},
+    {"if-if-alpha", false, IF_IF, true},
+    {"persistent-if-if-alpha", true, IF_IF, true},
+    {"speculative-while-while-alpha", false, SPECULATIVE, true},
+    {"persistent-speculative-while-while-alpha", true, SPECULATIVE, true},
+    {"bvh4-speculative-while-while-alpha", false, WIDE_SPECULATIVE, true},
+    {"persistent-bvh4-speculative-while-while-alpha", true, WIDE_SPECULATIVE, true}};
+inline const int kNumTracers = 16;
+
+// The scene a launch traces: the built scene, with the texture data attached when an
+// alpha-aware tracer is selected and grt_set_alpha has supplied it.
+inline dev_scene scene_for(const grt_ctx *c) {
+    dev_scene s = c->sc;
+    s.alpha = kTracers[c->tracer].alpha ? (const alpha_data *)c->d_alpha : nullptr;
+    return s;
+}
 
 // Stack entries the selected tracer needs on the current scene.
 inline int needed_stack(const grt_ctx *c) {
@@ -131,7 +153,7 @@ inline launch_params params_for(grt_ctx *c, bool any_hit) {
     if (kTracers[c->tracer].persistent) {
         int per_sm = t.blocks_per_sm > 0 ? t.blocks_per_sm
                                          : grt::persistent_blocks_per_sm(lp.block_threads, lp.stack_entries, any_hit,
-                                                                         lp.order);
+                                                                         lp.order, scene_for(c).alpha != nullptr);
         lp.grid_blocks = per_sm * c->num_sms;
     }
     return lp;

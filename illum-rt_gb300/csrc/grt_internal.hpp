@@ -9,6 +9,16 @@
 namespace grt {
 
 // Everything a traversal kernel needs about one scene; passed by value as a kernel argument.
+// Texture data of the alpha-aware tracers (device memory, one allocation).
+struct alpha_data {
+    const uint4 *tris;       // the scene's triangles: vertex indices, material id
+    const float2 *tc;        // texture coordinate per vertex
+    const int32_t *mat_tex;  // texture per material, -1 for none
+    const uint4 *tex;        // per texture: width, height, first texel, 0
+    const float *texels;     // alpha values, texture after texture, row by row
+    uint32_t n_mat;
+};
+
 struct dev_scene {
     const float4 *nodes;    // 4 float4 per inner node (layout in bvh_builder.hpp)
     const float4 *records;  // 3 float4 per triangle record
@@ -17,6 +27,7 @@ struct dev_scene {
     int32_t root4;          // child reference of the 4-wide root
     int32_t empty;          // 1: no triangles, every ray misses
     int32_t finite;         // 1: every vertex coordinate is finite (enables the min/max slab test)
+    const alpha_data *alpha;  // alpha-aware tracing, or nullptr
 };
 
 // Bits a kernel ORs into the context's error word.
@@ -62,6 +73,6 @@ cudaError_t launch_trace_persistent(const dev_scene &sc, const float4 *rays, grt
 cudaError_t prepare_trace_kernels();
 
 // Occupancy of the persistent kernel for a block size and stack variant (blocks per SM).
-int persistent_blocks_per_sm(int block_threads, int stack_entries, bool any_hit, int order);
+int persistent_blocks_per_sm(int block_threads, int stack_entries, bool any_hit, int order, bool alpha);
 
 }  // namespace grt

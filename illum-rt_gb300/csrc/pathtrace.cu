@@ -395,7 +395,7 @@ __global__ void k_wf_shade(pt_scene ps, pt_params_dev pp, const uint32_t *__rest
 // lanes shade their hit together (Russian roulette, next bounce direction) and go back to
 // traversal, or finish their path and take a new one from the global path counter. Shading and
 // path set-up therefore run warp-coherently instead of one lane at a time.
-template <int ORDER, int STACK>
+template <int ORDER, int STACK, bool ALPHA>
 __global__ void __launch_bounds__(256) k_pt_fused(dev_scene sc, pt_scene ps, pt_params_dev pp,
                                                   const float4 *__restrict__ prim_rays,
                                                   const grt_hit *__restrict__ prim_hits,
@@ -474,11 +474,11 @@ __global__ void __launch_bounds__(256) k_pt_fused(dev_scene sc, pt_scene ps, pt_
         // traversal phase
         for (int it = 1;; ++it) {
             if (SPEC)
-                trav_spec_iter<STACK, false, false, WIDE>(s, tracing, plain, sc, r, stk, stride, err);
+                trav_spec_iter<STACK, false, false, WIDE, ALPHA>(s, tracing, plain, sc, r, stk, stride, err);
             else if (tracing && plain)
-                trav_advance<ORDER, STACK, false, false, true>(s, sc, r, stk, stride, err);
+                trav_advance<ORDER, STACK, false, false, true, ALPHA>(s, sc, r, stk, stride, err);
             else if (tracing)
-                trav_advance<ORDER, STACK, false, false, false>(s, sc, r, stk, stride, err);
+                trav_advance<ORDER, STACK, false, false, false, ALPHA>(s, sc, r, stk, stride, err);
             if (tracing && s.done) {
                 tracing = false;
                 waiting = true;
@@ -497,7 +497,7 @@ cudaError_t fused_launch(const dev_scene &sc, const pt_scene &ps, const pt_param
                          grt_path_result *results, grt_hit *bounce_hits, const launch_params &lp, unsigned *err,
                          unsigned *counter, cudaStream_t st) {
     const size_t smem = (size_t)(STACK * sizeof(int) + kPathSlotBytes) * lp.block_threads;
-    auto kern = k_pt_fused<ORDER, STACK>;
+    auto kern = sc.alpha ? k_pt_fused<ORDER, STACK, true> : k_pt_fused<ORDER, STACK, false>;
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
     kern<<<lp.grid_blocks, lp.block_threads, smem, st>>>(sc, ps, pp, prim_rays, prim_hits, hit_list, n_list, n_paths,
@@ -571,33 +571,42 @@ cudaError_t launch_fused(const dev_scene &sc, const pt_scene &ps, const pt_param
 
 cudaError_t prepare_pt_kernels() {
     const int bytes = (kStackLarge * (int)sizeof(int) + kPathSlotBytes) * 256;
-    for (const void *f : {(const void *)k_pt_fused<IF_IF, kStackSmall>, (const void *)k_pt_fused<IF_IF, kStackLarge>,
-                          (const void *)k_pt_fused<WHILE_WHILE, kStackSmall>,
-                          (const void *)k_pt_fused<WHILE_WHILE, kStackLarge>,
-                          (const void *)k_pt_fused<SPECULATIVE, kStackSmall>,
-                          (const void *)k_pt_fused<SPECULATIVE, kStackLarge>,
-                          (const void *)k_pt_fused<WIDE_SPECULATIVE, kStackSmall>,
-                          (const void *)k_pt_fused<WIDE_SPECULATIVE, kStackLarge>}) {
+    for (const void *f : {(const void *)k_pt_fused<IF_IF, kStackSmall, false>, (const void *)k_pt_fused<IF_IF, kStackLarge, false>,
+                          (const void *)k_pt_fused<WHILE_WHILE, kStackSmall, false>,
+                          (const void *)k_pt_fused<WHILE_WHILE, kStackLarge, false>,
+                          (const void *)k_pt_fused<SPECULATIVE, kStackSmall, false>,
+                          (const void *)k_pt_fused<SPECULATIVE, kStackLarge, false>,
+                          (const void *)k_pt_fused<WIDE_SPECULATIVE, kStackSmall, false>,
+                          (const void *)k_pt_fused<WIDE_SPECULATIVE, kStackLarge, false>,
+                          (const void *)k_pt_fused<IF_IF, kStackSmall, true>, (const void *)k_pt_fused<IF_IF, kStackLarge, true>,
+                          (const void *)k_pt_fused<WHILE_WHILE, kStackSmall, true>,
+                          (const void *)k_pt_fused<WHILE_WHILE, kStackLarge, true>,
+                          (const void *)k_pt_fused<SPECULATIVE, kStackSmall, true>,
+                          (const void *)k_pt_fused<SPECULATIVE, kStackLarge, true>,
+                          (const void *)k_pt_fused<WIDE_SPECULATIVE, kStackSmall, true>,
+                          (const void *)k_pt_fused<WIDE_SPECULATIVE, kStackLarge, true>}) {
         cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
 }
 
-int fused_blocks_per_sm(int block_threads, int stack_entries, int order) {
+template <bool ALPHA> const void *fused_fn(int order, bool small) {
+    return order == WHILE_WHILE      ? (small ? (const void *)k_pt_fused<WHILE_WHILE, kStackSmall, ALPHA>
+                                              : (const void *)k_pt_fused<WHILE_WHILE, kStackLarge, ALPHA>)
+           : order == SPECULATIVE      ? (small ? (const void *)k_pt_fused<SPECULATIVE, kStackSmall, ALPHA>
+                                                : (const void *)k_pt_fused<SPECULATIVE, kStackLarge, ALPHA>)
+           : order == WIDE_SPECULATIVE ? (small ? (const void *)k_pt_fused<WIDE_SPECULATIVE, kStackSmall, ALPHA>
+                                                : (const void *)k_pt_fused<WIDE_SPECULATIVE, kStackLarge, ALPHA>)
+                                       : (small ? (const void *)k_pt_fused<IF_IF, kStackSmall, ALPHA>
+                                                : (const void *)k_pt_fused<IF_IF, kStackLarge, ALPHA>);
+}
+
+int fused_blocks_per_sm(int block_threads, int stack_entries, int order, bool alpha) {
     int blocks = 0;
     const bool small = stack_entries <= kStackSmall;
     const size_t smem = (size_t)((small ? kStackSmall : kStackLarge) * sizeof(int) + kPathSlotBytes) * block_threads;
-    const void *fn = order == WHILE_WHILE
-                         ? (small ? (const void *)k_pt_fused<WHILE_WHILE, kStackSmall>
-                                  : (const void *)k_pt_fused<WHILE_WHILE, kStackLarge>)
-                     : order == SPECULATIVE
-                         ? (small ? (const void *)k_pt_fused<SPECULATIVE, kStackSmall>
-                                  : (const void *)k_pt_fused<SPECULATIVE, kStackLarge>)
-                     : order == WIDE_SPECULATIVE
-                         ? (small ? (const void *)k_pt_fused<WIDE_SPECULATIVE, kStackSmall>
-                                  : (const void *)k_pt_fused<WIDE_SPECULATIVE, kStackLarge>)
-                         : (small ? (const void *)k_pt_fused<IF_IF, kStackSmall> : (const void *)k_pt_fused<IF_IF, kStackLarge>);
+    const void *fn = alpha ? fused_fn<true>(order, small) : fused_fn<false>(order, small);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, block_threads, smem) != cudaSuccess) return 1;
     return blocks > 0 ? blocks : 1;
 }

@@ -20,7 +20,7 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 
-template <int ORDER, int STACK, bool ANY, bool COUNT>
+template <int ORDER, int STACK, bool ANY, bool COUNT, bool ALPHA>
 __global__ void __launch_bounds__(256) k_trace_plain(const float4 *__restrict__ rays, grt_hit *__restrict__ hits,
                                                      uint32_t n, const uint32_t *__restrict__ n_dev, dev_scene sc,
                                                      unsigned *err, unsigned long long *counters) {
@@ -40,12 +40,12 @@ __global__ void __launch_bounds__(256) k_trace_plain(const float4 *__restrict__ 
     const bool plain = active && sc.finite && ray_is_plain(r);
     if (SPEC) {  // the whole warp stays in the loop until its last ray ends
         while (__any_sync(kFull, active && !s.done))
-            trav_spec_iter<STACK, ANY, COUNT, WIDE>(s, active, plain, sc, r, stk, stride, err);
+            trav_spec_iter<STACK, ANY, COUNT, WIDE, ALPHA>(s, active, plain, sc, r, stk, stride, err);
         if (!active) return;
     } else if (plain) {  // one loop per slab variant: the choice is made once per ray
-        while (!s.done) trav_advance<ORDER, STACK, ANY, COUNT, true>(s, sc, r, stk, stride, err);
+        while (!s.done) trav_advance<ORDER, STACK, ANY, COUNT, true, ALPHA>(s, sc, r, stk, stride, err);
     } else {
-        while (!s.done) trav_advance<ORDER, STACK, ANY, COUNT, false>(s, sc, r, stk, stride, err);
+        while (!s.done) trav_advance<ORDER, STACK, ANY, COUNT, false, ALPHA>(s, sc, r, stk, stride, err);
     }
     store_hit<ANY>(hits, i, s);
     if (COUNT) {
@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(256) k_trace_plain(const float4 *__restrict__ 
     }
 }
 
-template <int ORDER, int STACK, bool ANY>
+template <int ORDER, int STACK, bool ANY, bool ALPHA>
 __global__ void __launch_bounds__(256) k_trace_persistent(const float4 *__restrict__ rays, grt_hit *__restrict__ hits,
                                                           uint32_t n, dev_scene sc, unsigned *err,
                                                           unsigned *counter, int refill_threshold, int refill_period) {
@@ -103,11 +103,11 @@ __global__ void __launch_bounds__(256) k_trace_persistent(const float4 *__restri
         // traverse; every `refill_period` iterations the warp counts its busy lanes
         for (int it = 1;; ++it) {
             if (SPEC)
-                trav_spec_iter<STACK, ANY, false, WIDE>(s, have, plain, sc, r, stk, stride, err);
+                trav_spec_iter<STACK, ANY, false, WIDE, ALPHA>(s, have, plain, sc, r, stk, stride, err);
             else if (have && plain)
-                trav_advance<ORDER, STACK, ANY, false, true>(s, sc, r, stk, stride, err);
+                trav_advance<ORDER, STACK, ANY, false, true, ALPHA>(s, sc, r, stk, stride, err);
             else if (have)
-                trav_advance<ORDER, STACK, ANY, false, false>(s, sc, r, stk, stride, err);
+                trav_advance<ORDER, STACK, ANY, false, false, ALPHA>(s, sc, r, stk, stride, err);
             if (have && s.done) {
                 store_hit<ANY>(hits, idx, s);
                 have = false;
@@ -126,10 +126,16 @@ cudaError_t plain_launch(const dev_scene &sc, const float4 *rays, grt_hit *hits,
     const int bt = lp.block_threads;
     const size_t smem = (size_t)STACK * bt * sizeof(int);
     const uint32_t blocks = (n + bt - 1) / bt;
-    if (lp.counters)
-        k_trace_plain<ORDER, STACK, ANY, true><<<blocks, bt, smem, st>>>(rays, hits, n, n_dev, sc, err, lp.counters);
+    // the alpha-aware instances only when the scene carries texture data (the test costs
+    // registers even when it never runs)
+    if (lp.counters && sc.alpha)
+        k_trace_plain<ORDER, STACK, ANY, true, true><<<blocks, bt, smem, st>>>(rays, hits, n, n_dev, sc, err, lp.counters);
+    else if (lp.counters)
+        k_trace_plain<ORDER, STACK, ANY, true, false><<<blocks, bt, smem, st>>>(rays, hits, n, n_dev, sc, err, lp.counters);
+    else if (sc.alpha)
+        k_trace_plain<ORDER, STACK, ANY, false, true><<<blocks, bt, smem, st>>>(rays, hits, n, n_dev, sc, err, nullptr);
     else
-        k_trace_plain<ORDER, STACK, ANY, false><<<blocks, bt, smem, st>>>(rays, hits, n, n_dev, sc, err, nullptr);
+        k_trace_plain<ORDER, STACK, ANY, false, false><<<blocks, bt, smem, st>>>(rays, hits, n, n_dev, sc, err, nullptr);
     return cudaGetLastError();
 }
 
@@ -140,8 +146,12 @@ cudaError_t persistent_launch(const dev_scene &sc, const float4 *rays, grt_hit *
     const size_t smem = (size_t)STACK * bt * sizeof(int);
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
-    k_trace_persistent<ORDER, STACK, ANY><<<lp.grid_blocks, bt, smem, st>>>(rays, hits, n, sc, err, counter,
-                                                                            lp.refill_threshold, lp.refill_period);
+    if (sc.alpha)
+        k_trace_persistent<ORDER, STACK, ANY, true><<<lp.grid_blocks, bt, smem, st>>>(
+            rays, hits, n, sc, err, counter, lp.refill_threshold, lp.refill_period);
+    else
+        k_trace_persistent<ORDER, STACK, ANY, false><<<lp.grid_blocks, bt, smem, st>>>(
+            rays, hits, n, sc, err, counter, lp.refill_threshold, lp.refill_period);
     return cudaGetLastError();
 }
 
@@ -179,16 +189,22 @@ template <int O, int S, bool A> struct persistent_f {
 template <int O, int S, bool A> struct attr_f {
     static cudaError_t run(int bytes) {
         const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
-        cudaError_t e = cudaFuncSetAttribute(k_trace_plain<O, S, A, false>, a, bytes);
-        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_plain<O, S, A, true>, a, bytes);
-        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_persistent<O, S, A>, a, bytes);
+        cudaError_t e = cudaFuncSetAttribute(k_trace_plain<O, S, A, false, false>, a, bytes);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_plain<O, S, A, true, false>, a, bytes);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_plain<O, S, A, false, true>, a, bytes);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_plain<O, S, A, true, true>, a, bytes);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_persistent<O, S, A, false>, a, bytes);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_persistent<O, S, A, true>, a, bytes);
         return e;
     }
 };
 template <int O, int S, bool A> struct occupancy_f {
-    static cudaError_t run(int block_threads, int *blocks) {
-        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_trace_persistent<O, S, A>, block_threads,
-                                                             (size_t)S * block_threads * sizeof(int));
+    static cudaError_t run(int block_threads, bool alpha, int *blocks) {
+        const size_t smem = (size_t)S * block_threads * sizeof(int);
+        return alpha ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_trace_persistent<O, S, A, true>,
+                                                                     block_threads, smem)
+                     : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_trace_persistent<O, S, A, false>,
+                                                                     block_threads, smem);
     }
 };
 
@@ -217,9 +233,9 @@ cudaError_t prepare_trace_kernels() {
     return cudaSuccess;
 }
 
-int persistent_blocks_per_sm(int block_threads, int stack_entries, bool any_hit, int order) {
+int persistent_blocks_per_sm(int block_threads, int stack_entries, bool any_hit, int order, bool alpha) {
     int blocks = 0;
-    if (dispatch<occupancy_f>(order, stack_entries, any_hit, block_threads, &blocks) != cudaSuccess) return 1;
+    if (dispatch<occupancy_f>(order, stack_entries, any_hit, block_threads, alpha, &blocks) != cudaSuccess) return 1;
     return blocks > 0 ? blocks : 1;
 }
 

@@ -133,6 +133,33 @@ __device__ __forceinline__ bool tri_test(const float4 &p0, const float4 &p1, con
     return false;
 }
 
+// The alpha test of the alpha-aware tracers (rt/cpu/bvh2.cpp:109-117, 168-174): a hit on
+// triangle `tri` with material `mat` counts only if diff_geom::opacity() > 0.5
+// (libgi/rt.cpp:32-36). The texture coordinate is (1 - beta - gamma) a + beta b + gamma c,
+// rounded as diff_geom's constructor rounds it (libgi/rt.cpp:7-14), and the texel is
+// texture2d::sample's (libgi/scene.h:28-36): wrap to [0, 1), nearest texel (int)(u w + 0.5),
+// index w wrapping to 0. No texture, or a material id beyond the table: opaque. A texel index
+// that is not finite (non-finite texture coordinates, undefined in the reference) reads texel 0.
+static __device__ __forceinline__ bool alpha_opaque(const alpha_data *A, uint32_t tri, uint32_t mat, float b, float g) {
+    if (mat >= A->n_mat) return true;
+    const int32_t k = __ldg(A->mat_tex + mat);
+    if (k < 0) return true;
+    const uint4 t = __ldg(A->tris + tri);
+    const float2 ta = __ldg(A->tc + t.x), tb = __ldg(A->tc + t.y), tc = __ldg(A->tc + t.z);
+    const float w = __fsub_rn(__fsub_rn(1.0f, b), g);
+    float u = __fadd_rn(__fadd_rn(__fmul_rn(w, ta.x), __fmul_rn(b, tb.x)), __fmul_rn(g, tc.x));
+    float v = __fadd_rn(__fadd_rn(__fmul_rn(w, ta.y), __fmul_rn(b, tb.y)), __fmul_rn(g, tc.y));
+    u = __fsub_rn(u, floorf(u));
+    v = __fsub_rn(v, floorf(v));
+    const uint4 tx = __ldg(A->tex + k);
+    const float fx = __fadd_rn(__fmul_rn(u, (float)tx.x), 0.5f), fy = __fadd_rn(__fmul_rn(v, (float)tx.y), 0.5f);
+    int x = isfinite(fx) ? (int)fx : 0, y = isfinite(fy) ? (int)fy : 0;
+    if (x == (int)tx.x) x = 0;
+    if (y == (int)tx.y) y = 0;
+    if (x < 0 || y < 0 || x >= (int)tx.x || y >= (int)tx.y) x = y = 0;
+    return __ldg(A->texels + tx.z + (size_t)y * tx.x + x) > 0.5f;
+}
+
 // One 256-bit read-only load (two float4) from a 32-byte-aligned address: a 64-byte binary
 // node is two such loads (each half is one child's box and reference), four fewer L1 requests
 // per node than 128-bit loads.
@@ -186,7 +213,7 @@ __device__ __forceinline__ void trav_init(trav_t &s, const dev_scene &sc, bool w
 // `cur` instead of being pushed and popped straight back, and a leaf is tested when it would
 // be popped. Grouping a warp's node visits in one loop and its leaf tests after it keeps the
 // lanes on the same code path far more often than one node-or-leaf per iteration would.
-template <int STACK, bool ANY, bool PLAIN, bool COUNT = false>
+template <int STACK, bool ANY, bool PLAIN, bool COUNT = false, bool ALPHA = false>
 __device__ __forceinline__ void trav_iter(trav_t &s, const dev_scene &sc, const ray_t &r, int *stk, int stride,
                                           unsigned *err) {
     while (s.cur >= 0) {
@@ -241,7 +268,8 @@ __device__ __forceinline__ void trav_iter(trav_t &s, const dev_scene &sc, const 
         if (COUNT) ++s.n_tri;
         const float4 p0 = __ldg(rp + 3 * k), p1 = __ldg(rp + 3 * k + 1), p2 = __ldg(rp + 3 * k + 2);
         float t, b, g;
-        if (tri_test(p0, p1, p2, r, ANY ? r.tmax : fminf(r.tmax, s.hit.t), t, b, g) && (ANY || t < s.hit.t)) {
+        if (tri_test(p0, p1, p2, r, ANY ? r.tmax : fminf(r.tmax, s.hit.t), t, b, g) && (ANY || t < s.hit.t) &&
+                (!ALPHA || alpha_opaque(sc.alpha, __float_as_uint(p0.w), __float_as_uint(p1.w), b, g))) {
             s.hit.t = t;
             s.hit.b = b;
             s.hit.g = g;
@@ -265,7 +293,7 @@ __device__ __forceinline__ void trav_iter(trav_t &s, const dev_scene &sc, const 
 // The if-if order: one inner node or one leaf per call (the reference's if-if tracer,
 // rt/cuda/trace-kernels.cu:1058-1149, visits in the same per-ray order as while-while). Lanes of
 // a warp at nodes and lanes at leaves take different branches in the same call.
-template <int STACK, bool ANY, bool PLAIN, bool COUNT = false>
+template <int STACK, bool ANY, bool PLAIN, bool COUNT = false, bool ALPHA = false>
 __device__ __forceinline__ void trav_step(trav_t &s, const dev_scene &sc, const ray_t &r, int *stk, int stride,
                                           unsigned *err) {
     if (++s.steps > kStepLimit) {
@@ -311,7 +339,8 @@ __device__ __forceinline__ void trav_step(trav_t &s, const dev_scene &sc, const 
             if (COUNT) ++s.n_tri;
             const float4 p0 = __ldg(rp + 3 * k), p1 = __ldg(rp + 3 * k + 1), p2 = __ldg(rp + 3 * k + 2);
             float t, b, g;
-            if (tri_test(p0, p1, p2, r, ANY ? r.tmax : fminf(r.tmax, s.hit.t), t, b, g) && (ANY || t < s.hit.t)) {
+            if (tri_test(p0, p1, p2, r, ANY ? r.tmax : fminf(r.tmax, s.hit.t), t, b, g) && (ANY || t < s.hit.t) &&
+                (!ALPHA || alpha_opaque(sc.alpha, __float_as_uint(p0.w), __float_as_uint(p1.w), b, g))) {
                 s.hit.t = t;
                 s.hit.b = b;
                 s.hit.g = g;
@@ -453,7 +482,7 @@ __device__ __forceinline__ void spec_node4(trav_t &s, const dev_scene &sc, const
 // postponed leaf use the closest hit from before that leaf, so the ray may visit nodes the
 // reference would have culled. A triangle found there can replace the reference's answer only
 // if its t lies within rounding of the culled box's entry distance: a near-tie.
-template <int STACK, bool ANY, bool COUNT, bool WIDE = false>
+template <int STACK, bool ANY, bool COUNT, bool WIDE = false, bool ALPHA = false>
 __device__ __forceinline__ void trav_spec_iter(trav_t &s, bool active, bool plain, const dev_scene &sc,
                                                const ray_t &r, int *stk, int stride, unsigned *err) {
     const bool mine = active && !s.done;
@@ -500,7 +529,8 @@ __device__ __forceinline__ void trav_spec_iter(trav_t &s, bool active, bool plai
                 if (COUNT) ++s.n_tri;
                 const float4 p0 = __ldg(rp + 3 * k), p1 = __ldg(rp + 3 * k + 1), p2 = __ldg(rp + 3 * k + 2);
                 float t, b, g;
-                if (tri_test(p0, p1, p2, r, ANY ? r.tmax : fminf(r.tmax, s.hit.t), t, b, g) && (ANY || t < s.hit.t)) {
+                if (tri_test(p0, p1, p2, r, ANY ? r.tmax : fminf(r.tmax, s.hit.t), t, b, g) && (ANY || t < s.hit.t) &&
+                (!ALPHA || alpha_opaque(sc.alpha, __float_as_uint(p0.w), __float_as_uint(p1.w), b, g))) {
                     s.hit.t = t;
                     s.hit.b = b;
                     s.hit.g = g;
@@ -520,13 +550,13 @@ __device__ __forceinline__ void trav_spec_iter(trav_t &s, bool active, bool plai
 
 // One iteration of a non-speculative loop order for this lane's ray (PLAIN: min/max slab test,
 // see ray_is_plain). The speculative order is trav_spec_iter, which the whole warp calls together.
-template <int ORDER, int STACK, bool ANY, bool COUNT, bool PLAIN>
+template <int ORDER, int STACK, bool ANY, bool COUNT, bool PLAIN, bool ALPHA = false>
 __device__ __forceinline__ void trav_advance(trav_t &s, const dev_scene &sc, const ray_t &r, int *stk, int stride,
                                              unsigned *err) {
     if (ORDER == WHILE_WHILE)
-        trav_iter<STACK, ANY, PLAIN, COUNT>(s, sc, r, stk, stride, err);
+        trav_iter<STACK, ANY, PLAIN, COUNT, ALPHA>(s, sc, r, stk, stride, err);
     else
-        trav_step<STACK, ANY, PLAIN, COUNT>(s, sc, r, stk, stride, err);
+        trav_step<STACK, ANY, PLAIN, COUNT, ALPHA>(s, sc, r, stk, stride, err);
 }
 
 // Writes one result in the reference's encodings (see include/grt.h).

@@ -304,6 +304,27 @@ grt_status grt_adjoint(grt_ctx *ctx, const float *rays_dev, const grt_hit *hits_
                        uint32_t n, const float *vpos_dev, uint32_t vstride, float *grad_vpos_dev, float *grad_rays_dev,
                        grt_stream_t stream);
 
+/* ---- alpha-aware tracing ---------------------------------------------------------------- */
+
+/* One single-channel texture: width x height alpha values, row by row. */
+typedef struct grt_alpha_texture {
+    uint32_t width, height;
+    const float *alpha;
+} grt_alpha_texture;
+
+/* Texture data of the alpha-aware tracers, the "<tracer>-alpha" names (the reference registers
+ * an alpha variant of each tracer, rt/cuda/platform.cpp:34-51). With one of them selected, a
+ * triangle hit counts only where the alpha of its material's texture at the hit's interpolated
+ * texture coordinate is > 0.5, as in the reference CPU tracer (rt/cpu/bvh2.cpp:109-117, 168-174;
+ * libgi/rt.cpp:7-14, 32-36; nearest texel with wrap-around, libgi/scene.h:28-36). Host arrays,
+ * copied: texcoords2 (2 floats per vertex of the built scene, nv = its vertex count),
+ * material_texture (per material id: a texture index, or -1 for an opaque material), textures.
+ * Triangles whose material id is beyond the table are opaque. Applies to grt_trace,
+ * grt_trace_host and grt_pathtrace (not to scene sets); a new build drops it; a NULL
+ * material_texture clears it. */
+grt_status grt_set_alpha(grt_ctx *ctx, const float *texcoords2, uint32_t nv, const int32_t *material_texture,
+                         uint32_t n_materials, const grt_alpha_texture *textures, uint32_t n_textures);
+
 /* ---- BVH construction on the GPU ----------------------------------------------------- */
 
 /* Builds the scene of grt_build on the GPU from DEVICE arrays in the same layouts (vertices

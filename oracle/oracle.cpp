@@ -332,6 +332,16 @@ struct builder {
     }
 };
 
+// Texture data of the alpha-aware tracers: a texture coordinate per vertex, a texture per
+// material (or none) and single-channel alpha textures of w x h texels, row by row.
+struct alpha_set {
+    bool on = false;
+    std::vector<float> tc;          // 2 per vertex
+    std::vector<int32_t> mat_tex;   // texture index per material, -1 for none
+    std::vector<uint32_t> w, h, off;
+    std::vector<float> texels;
+};
+
 struct bvh {
     scene sc;
     std::vector<float> v4;
@@ -340,6 +350,7 @@ struct bvh {
     std::vector<node> nodes;
     std::vector<uint32_t> index;
     bool failed = false;
+    alpha_set alpha;
 };
 
 struct ray {
@@ -422,6 +433,33 @@ struct counters {
     uint32_t inner = 0, tris = 0, max_sp = 0;
 };
 
+// The alpha test of the alpha-aware tracers (rt/cpu/bvh2.cpp:109-117, 168-174): a hit counts only
+// if diff_geom::opacity() > 0.5 (libgi/rt.cpp:32-36). The texture coordinate is interpolated as in
+// diff_geom's constructor, (1 - beta - gamma) a + beta b + gamma c (libgi/rt.cpp:7-14), and
+// looked up by texture2d::sample (libgi/scene.h:28-36): wrap to [0, 1), nearest texel by
+// (int)(u w + 0.5), index w wrapping to 0. A material without a texture is opaque. Material ids
+// beyond the table, and texture coordinates whose texel index is not finite, are outside what
+// the reference defines; here they count as opaque and as texel 0.
+inline bool opaque(const bvh &h, uint32_t tri, const hit &is) {
+    const alpha_set &A = h.alpha;
+    const uint32_t *t = h.sc.t4 + 4 * tri;
+    const uint32_t m = t[3];
+    if (m >= A.mat_tex.size() || A.mat_tex[m] < 0) return true;
+    const uint32_t k = (uint32_t)A.mat_tex[m];
+    const float w = 1.0f - is.beta - is.gamma;
+    const float *a = A.tc.data() + 2 * t[0], *b = A.tc.data() + 2 * t[1], *c = A.tc.data() + 2 * t[2];
+    float u = w * a[0] + is.beta * b[0] + is.gamma * c[0];
+    float v = w * a[1] + is.beta * b[1] + is.gamma * c[1];
+    u = u - std::floor(u);
+    v = v - std::floor(v);
+    const float fx = u * (float)A.w[k] + 0.5f, fy = v * (float)A.h[k] + 0.5f;
+    int x = std::isfinite(fx) ? (int)fx : 0, y = std::isfinite(fy) ? (int)fy : 0;
+    if (x == (int)A.w[k]) x = 0;
+    if (y == (int)A.h[k]) y = 0;
+    if (x < 0 || y < 0 || x >= (int)A.w[k] || y >= (int)A.h[k]) x = y = 0;
+    return A.texels[A.off[k] + (size_t)y * A.w[k] + x] > 0.5f;
+}
+
 // binary_bvh_tracer::closest_hit (rt/cpu/bvh2.cpp:71-137), non-alpha, indexed layout.
 inline hit closest_hit(const bvh &h, const ray &r, counters *cnt) {
     hit closest, is;
@@ -469,6 +507,7 @@ inline hit closest_hit(const bvh &h, const ray &r, counters *cnt) {
                 uint32_t tri = h.index[off + i];
                 ++n_tri;
                 if (intersect_tri(h.sc, tri, r, is)) {
+                    if (h.alpha.on && !opaque(h, tri, is)) continue;
                     if (is.t < closest.t) {
                         closest = is;
                         closest.ref = tri;
@@ -519,6 +558,7 @@ inline bool any_hit(const bvh &h, const ray &r, counters *cnt) {
             for (int32_t i = 0; i < count; ++i) {
                 ++n_tri;
                 if (intersect_tri(h.sc, h.index[off + i], r, is)) {
+                    if (h.alpha.on && !opaque(h, h.index[off + i], is)) continue;
                     result = true;
                     break;
                 }
@@ -652,6 +692,27 @@ void *orc_build(const float *vpos4, uint32_t nv, const uint32_t *tris4, uint32_t
     h->index.swap(b.index);
     h->failed = b.failed;
     return h;
+}
+
+// Texture data for the alpha-aware tracing of orc_closest / orc_any (tc2: 2 floats per vertex;
+// mat_tex: texture per material or -1; tex_wh: width and height per texture; texels: the
+// textures' alpha values one after another). n_tex = 0 and mat_tex = NULL switch alpha off.
+void orc_set_alpha(void *hp, const float *tc2, uint32_t nv, const int32_t *mat_tex, uint32_t n_mat,
+                   const uint32_t *tex_wh, const float *texels, uint32_t n_tex) {
+    alpha_set &A = ((bvh *)hp)->alpha;
+    A = alpha_set();
+    if (!mat_tex) return;
+    A.on = true;
+    A.tc.assign(tc2, tc2 + 2 * (size_t)nv);
+    A.mat_tex.assign(mat_tex, mat_tex + n_mat);
+    size_t total = 0;
+    for (uint32_t k = 0; k < n_tex; ++k) {
+        A.w.push_back(tex_wh[2 * k]);
+        A.h.push_back(tex_wh[2 * k + 1]);
+        A.off.push_back((uint32_t)total);
+        total += (size_t)tex_wh[2 * k] * tex_wh[2 * k + 1];
+    }
+    A.texels.assign(texels, texels + total);
 }
 
 int orc_failed(void *hp) { return ((bvh *)hp)->failed ? 1 : 0; }

@@ -149,6 +149,32 @@ class OracleBVH(_BVHBase):
         self.lib.orc_any(self.h, _p(rays), n, _p(occ), _p(cnt) if counts else None, threads)
         return occ, cnt
 
+    def set_alpha(self, alpha):
+        """Alpha-aware tracing from now on (alpha: an AlphaSet), or off with None."""
+        f = self.lib.orc_set_alpha
+        f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint32,
+                      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32]
+        if alpha is None:
+            f(self.h, None, 0, None, 0, None, None, 0)
+            return
+        self._alpha = alpha  # keeps the arrays alive for the call
+        f(self.h, _p(alpha.tc), alpha.tc.shape[0], _p(alpha.mat_tex), alpha.mat_tex.shape[0], _p(alpha.tex_wh),
+          _p(alpha.texels), alpha.tex_wh.shape[0])
+
+
+class AlphaSet:
+    """Texture data of the alpha-aware tracers: tc float32 [nv, 2], mat_tex int32 [n_materials]
+    (texture index or -1), textures: list of float32 [h, w] alpha arrays."""
+
+    def __init__(self, tc, mat_tex, textures):
+        self.tc = np.ascontiguousarray(tc, np.float32)
+        self.mat_tex = np.ascontiguousarray(mat_tex, np.int32)
+        self.textures = [np.ascontiguousarray(t, np.float32) for t in textures]
+        self.tex_wh = np.ascontiguousarray([[t.shape[1], t.shape[0]] for t in self.textures] or np.zeros((0, 2)),
+                                           np.uint32).reshape(-1, 2)
+        self.texels = np.ascontiguousarray(np.concatenate([t.ravel() for t in self.textures])
+                                           if self.textures else np.zeros(1), np.float32)
+
 
 class ReferenceBVH(_BVHBase):
     """The reference's own binary_bvh_tracer, compiled from its sources into oracle/_ref."""
@@ -171,6 +197,26 @@ class ReferenceBVH(_BVHBase):
         occ = np.zeros(rays.shape[0], np.uint8)
         self.lib.ref_any(self.h, _p(rays), rays.shape[0], _p(occ), threads)
         return occ
+
+
+class ReferenceAlphaBVH(ReferenceBVH):
+    """The reference's alpha-aware tracer (binary_bvh_tracer<indexed, esc on, true>, SAH)."""
+
+    def __init__(self, vpos, tris, alpha: AlphaSet, max_tris=4, planes=16):
+        lib = _load(REF_SO, "ref_")
+        lib.ref_closest.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_int]
+        lib.ref_any.argtypes = lib.ref_closest.argtypes
+        f = lib.ref_build_alpha
+        f.restype = ctypes.c_void_p
+        f.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p,
+                      ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
+                      ctypes.c_int, ctypes.c_int]
+        self.lib = lib
+        self._v = np.ascontiguousarray(vpos, np.float32)
+        self._t = np.ascontiguousarray(tris, np.uint32)
+        self._alpha = alpha
+        self.h = f(_p(self._v), self._v.shape[0], _p(self._t), self._t.shape[0], _p(alpha.tc), _p(alpha.mat_tex),
+                   alpha.mat_tex.shape[0], _p(alpha.tex_wh), _p(alpha.texels), alpha.tex_wh.shape[0], max_tris, planes)
 
 
 def max_threads() -> int:

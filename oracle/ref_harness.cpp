@@ -24,11 +24,14 @@ namespace {
 
 typedef binary_bvh_tracer<bbvh_triangle_layout::indexed, bbvh_esc_mode::on> tracer_esc;
 typedef binary_bvh_tracer<bbvh_triangle_layout::indexed, bbvh_esc_mode::off> tracer_noesc;
+// the alpha-aware variant the reference instantiates (rt/cpu/bvh2.cpp:324)
+typedef binary_bvh_tracer<bbvh_triangle_layout::indexed, bbvh_esc_mode::on, true> tracer_alpha;
 
 struct handle {
     ::scene sc;
     individual_ray_tracer *rt = nullptr;
     ::bvh *bvh = nullptr;
+    std::vector<texture2d<vec4> *> owned;  // textures of the alpha-aware scene
 };
 
 template <typename T> void configure_and_build(handle *h, int split, int max_tris, int planes) {
@@ -73,6 +76,44 @@ void *ref_build(const float *vpos4, uint32_t nv, const uint32_t *tris4, uint32_t
         configure_and_build<tracer_esc>(h, split, max_tris, planes);
     else
         configure_and_build<tracer_noesc>(h, split, max_tris, planes);
+    return h;
+}
+
+// The alpha-aware tracer (ESC on, SAH) over a scene with texture coordinates (tc2: 2 per
+// vertex), a texture per material (mat_tex, -1 for none; the material table has n_mat entries)
+// and alpha textures (tex_wh: width, height per texture; texels: alpha values one texture after
+// another, stored as the w channel of the reference's vec4 texels).
+void *ref_build_alpha(const float *vpos4, uint32_t nv, const uint32_t *tris4, uint32_t nt, const float *tc2,
+                      const int32_t *mat_tex, uint32_t n_mat, const uint32_t *tex_wh, const float *texels,
+                      uint32_t n_tex, int max_tris, int planes) {
+    handle *h = new handle();
+    h->sc.vertices.resize(nv);
+    for (uint32_t i = 0; i < nv; ++i) {
+        h->sc.vertices[i].pos = vec3(vpos4[4 * i + 0], vpos4[4 * i + 1], vpos4[4 * i + 2]);
+        h->sc.vertices[i].norm = vec3(0, 0, 1);
+        h->sc.vertices[i].tc = vec2(tc2[2 * i], tc2[2 * i + 1]);
+    }
+    h->sc.triangles.resize(nt);
+    for (uint32_t i = 0; i < nt; ++i) {
+        h->sc.triangles[i].a = tris4[4 * i + 0];
+        h->sc.triangles[i].b = tris4[4 * i + 1];
+        h->sc.triangles[i].c = tris4[4 * i + 2];
+        h->sc.triangles[i].material_id = tris4[4 * i + 3];
+    }
+    size_t off = 0;
+    for (uint32_t k = 0; k < n_tex; ++k) {
+        texture2d<vec4> *t = new texture2d<vec4>();
+        t->w = tex_wh[2 * k];
+        t->h = tex_wh[2 * k + 1];
+        t->texel = new vec4[(size_t)t->w * t->h];
+        for (size_t q = 0; q < (size_t)t->w * t->h; ++q) t->texel[q] = vec4(0, 0, 0, texels[off + q]);
+        off += (size_t)t->w * t->h;
+        h->owned.push_back(t);
+    }
+    h->sc.materials.resize(n_mat);
+    for (uint32_t m = 0; m < n_mat; ++m)
+        h->sc.materials[m].albedo_tex = mat_tex[m] >= 0 ? h->owned[mat_tex[m]] : nullptr;
+    configure_and_build<tracer_alpha>(h, 2, max_tris, planes);
     return h;
 }
 
@@ -127,6 +168,7 @@ void ref_any(void *hp, const float *rays8, uint32_t n, uint8_t *occluded, int th
 void ref_free(void *hp) {
     handle *h = (handle *)hp;
     delete h->rt;
+    for (texture2d<vec4> *t : h->owned) delete t;
     delete h;
 }
 

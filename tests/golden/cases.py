@@ -115,3 +115,58 @@ BUILDERS = [
     ("sm_4_esc", dict(split="sm", max_tris=4, planes=1, esc=True)),
     ("om_2", dict(split="om", max_tris=2, planes=1, esc=False)),
 ]
+
+
+def alpha_scene():
+    """Alpha-aware case: two stacked 33x33-vertex grids over [0,1]^2 (z = 0 and z = 0.1, the upper
+    one with a height ripple), 4,096 triangles, texture coordinates spanning [-1.5, 2.5] (several
+    wraps, negative values), and four materials by triangle index mod 4: no texture (opaque), an
+    8x8 checker of alpha 0 / 1, a 16x4 ramp whose texels include exactly 0.5 (the threshold is
+    strict), and a fully transparent 3x5 texture.
+    Returns (vpos, tris, tc [nv, 2], mat_tex [4], textures)."""
+    n = 33
+    xs = np.linspace(0.0, 1.0, n, dtype=np.float32)
+    X, Y = np.meshgrid(xs, xs)
+    layers = []
+    for z0, amp in ((0.0, 0.0), (0.1, 0.03)):
+        Z = z0 + amp * np.sin(9.0 * X) * np.cos(7.0 * Y)
+        layers.append(np.stack([X, Y, Z.astype(np.float32)], -1).reshape(-1, 3))
+    v3 = np.concatenate(layers)
+    vpos = np.ones((v3.shape[0], 4), np.float32)
+    vpos[:, :3] = v3
+    t = []
+    for layer in range(2):
+        base = layer * n * n
+        for j in range(n - 1):
+            for i in range(n - 1):
+                a = base + j * n + i
+                t.append((a, a + 1, a + n + 1))
+                t.append((a, a + n + 1, a + n))
+    tris = np.zeros((len(t), 4), np.uint32)
+    tris[:, :3] = np.asarray(t, np.uint32)
+    tris[:, 3] = np.arange(len(t)) % 4
+    tc = (v3[:, :2] * 4.0 - 1.5).astype(np.float32)
+    tc[n * n:] = (tc[n * n:] * 0.75 + 0.3).astype(np.float32)
+    checker = ((np.arange(8)[:, None] + np.arange(8)[None, :]) % 2).astype(np.float32)
+    ramp = np.tile(np.linspace(0.2, 0.8, 16, dtype=np.float32), (4, 1))
+    ramp[:, 5] = 0.5
+    ramp[1, :] = 0.5
+    clear = np.zeros((5, 3), np.float32)
+    return vpos, tris, tc, np.array([-1, 0, 1, 2], np.int32), [checker, ramp, clear]
+
+
+def alpha_rays():
+    """Closest-hit rays: a 96x96 pinhole frame looking down at the grids plus 4,096 random rays;
+    any-hit rays: 4,096 random rays with finite t_max."""
+    o = np.array([0.5, -0.4, 1.2], np.float32)
+    u, w = np.meshgrid(np.linspace(0.05, 0.95, 96), np.linspace(0.05, 0.95, 96))
+    target = np.stack([u, w, np.zeros_like(u)], -1).reshape(-1, 3)
+    d = target - o
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    cam = np.zeros((d.shape[0], 8), np.float32)
+    cam[:, 0:3] = o
+    cam[:, 3] = 1e-4
+    cam[:, 4:7] = d
+    cam[:, 7] = FLT_MAX
+    rnd = random_rays(106, 4096, (0.0, 0.0, -0.2), (1.0, 1.0, 0.3))
+    return np.concatenate([cam, rnd]), random_rays(107, 4096, (0.0, 0.0, -0.2), (1.0, 1.0, 0.3), tmax_scale=0.6)

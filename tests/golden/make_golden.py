@@ -7,7 +7,10 @@ stores, per builder configuration of cases.BUILDERS, the SHA-256 of the referenc
 4 triangles per leaf, early split clipping), the reference's closest hits of the scene's rays
 and its any-hit answers for a set of rays with finite t_max.
 
-Run from the repository root:  python tests/golden/make_golden.py
+The alpha-aware case (cases.alpha_scene) is stored the same way from the reference's
+alpha-aware tracer (binary_bvh_tracer<indexed, esc on, true>).
+
+Run from the repository root:  python tests/golden/make_golden.py  (or ... make_golden.py alpha)
 """
 from __future__ import annotations
 
@@ -92,5 +95,27 @@ def main():
               f"of {any_rays.shape[0]}, {os.path.getsize(path)} bytes")
 
 
+def main_alpha():
+    """The alpha-aware case: the reference's binary_bvh_tracer<indexed, esc on, true>."""
+    orc = ge.load_oracle()
+    v, t, tc, mat_tex, textures = cases.alpha_scene()
+    rays, any_rays = cases.alpha_rays()
+    alpha = orc.AlphaSet(tc, mat_tex, textures)
+    ref = orc.ReferenceAlphaBVH(v, t, alpha)
+    data = {"vpos_digest": array_digest(v), "tris_digest": array_digest(t), "tc_digest": array_digest(tc),
+            "texels_digest": array_digest(alpha.texels), "rays_digest": array_digest(rays),
+            "any_rays_digest": array_digest(any_rays),
+            "closest": ref.closest(rays), "any_occluded": ref.any(any_rays)}
+    path = os.path.join(HERE, "golden_alpha.npz")
+    np.savez_compressed(path, **data)
+    hits = int((data["closest"][:, 0] < cases.FLT_MAX).sum())
+    print(f"alpha: {rays.shape[0]} rays, {hits} hits, {int(data['any_occluded'].sum())} occluded "
+          f"of {any_rays.shape[0]}, {os.path.getsize(path)} bytes")
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["alpha"]:
+        main_alpha()
+    else:
+        main()
+        main_alpha()
