@@ -48,6 +48,11 @@ class BvhStats(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class LeafStats(ctypes.Structure):
+    _fields_ = [("leaves", ctypes.c_uint32), ("min_tris", ctypes.c_int32), ("max_tris", ctypes.c_int32),
+                ("avg_tris", ctypes.c_uint32), ("median_tris", ctypes.c_int32)]
+
+
 class AlphaTexture(ctypes.Structure):
     _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("alpha", ctypes.c_void_p)]
 
@@ -112,6 +117,12 @@ _PROTOS = {
     "grt_export_scene_bvh": (I, [VP, U32, VP, VP, P(U32)]),
     "grt_trace_multi": (I, [VP, VP, U32, I, VP]),
     "grt_set_alpha": (I, [VP, VP, U32, VP, U32, VP, U32]),
+    "grt_set_bvh_cache": (I, [VP, ctypes.c_char_p]),
+    "grt_bvh_cache_stats": (I, [VP, P(ctypes.c_uint64), P(ctypes.c_uint64)]),
+    "grt_export_bvh_obj": (I, [VP, I, ctypes.c_char_p]),
+    "grt_bvh_leaf_stats": (I, [VP, P(LeafStats)]),
+    "grt_host_bvh_export_obj": (I, [VP, I, ctypes.c_char_p]),
+    "grt_host_bvh_leaf_stats": (I, [VP, P(LeafStats)]),
     "grt_build_device": (I, [VP, VP, U32, VP, U32, U32, VP]),
     "grt_build_scenes_device": (I, [VP, VP, U32, U32, VP]),
 }
@@ -171,6 +182,18 @@ class HostBVH:
         lib().grt_host_bvh_export(self.h, _ptr(nodes), _ptr(index), ctypes.byref(root))
         return nodes, index, int(root.value)
 
+    def export_obj(self, max_depth: int, path: str):
+        st = lib().grt_host_bvh_export_obj(self.h, int(max_depth), str(path).encode())
+        if st != GRT_OK:
+            raise GRTError(st, f"cannot write {path}")
+
+    def leaf_stats(self) -> dict:
+        s = LeafStats()
+        st = lib().grt_host_bvh_leaf_stats(self.h, ctypes.byref(s))
+        if st != GRT_OK:
+            raise GRTError(st, "no leaf statistics for this tree")
+        return {k: getattr(s, k) for k, _ in s._fields_}
+
     def __del__(self):
         try:
             lib().grt_host_bvh_free(self.h)
@@ -206,6 +229,7 @@ class BatchRayTracer:
         self.device = device
         self.bvh_type = "sah"         # `bvh type`
         self.bvh_max_tris_per_node = 4  # `bvh max_tris`
+        self.bvh_planes = 16            # `bvh sah <planes>` of the CPU tracer
         self.rd: RayData | None = None
         self.tracer = TRACERS[0]
 
@@ -228,7 +252,10 @@ class BatchRayTracer:
 
     # -- wf::batch_ray_tracer surface -----------------------------------------------------
     def interprete(self, command: str) -> bool:
-        """Script commands of the CUDA tracer and platform; returns False for unknown ones."""
+        """Script commands of the CUDA tracer and platform (`bvh type`, `bvh max_tris`,
+        rt/cuda/base.cpp:134-153; `raytracer`, rt/cuda/platform.cpp:102-131) and of the CPU
+        tracer (`bvh om|sm|sah <planes>|triangles single|multiple <n>|statistics|export
+        <depth> <file>`, rt/cpu/bvh2.cpp:192-241); returns False for unknown ones."""
         words = command.split()
         if len(words) == 3 and words[:2] == ["bvh", "type"]:
             if words[2] not in SPLIT:
@@ -241,16 +268,61 @@ class BatchRayTracer:
         if len(words) == 2 and words[0] == "raytracer":
             self.select(words[1])
             return True
+        if len(words) >= 2 and words[0] == "bvh":
+            sub = words[1:]
+            if sub in (["om"], ["sm"]):
+                self.bvh_type = sub[0]
+                return True
+            if len(sub) == 2 and sub[0] == "sah":
+                self.bvh_type, self.bvh_planes = "sah", int(sub[1])
+                return True
+            if sub == ["triangles", "single"]:
+                self.bvh_max_tris_per_node = 1
+                return True
+            if len(sub) == 3 and sub[:2] == ["triangles", "multiple"]:
+                self.bvh_max_tris_per_node = int(sub[2])
+                return True
+            if sub == ["statistics"]:
+                st = self.leaf_stats()
+                print(f"number of leaf nodes: {st['leaves']}")
+                print(f"minimum triangles per node: {st['min_tris']}")
+                print(f"maximum triangles per node: {st['max_tris']}")
+                print(f"average triangles per node: {st['avg_tris']}")
+                print(f"median of triangles per node: {st['median_tris']}")
+                return True
+            if len(sub) == 3 and sub[0] == "export":
+                self.export_obj(int(sub[1]), sub[2])
+                print(f"bvh exported to {sub[2]}")
+                return True
         return False
+
+    def set_bvh_cache(self, directory):
+        """On-disk cache of built trees (grt_set_bvh_cache); None switches it off."""
+        self._check(lib().grt_set_bvh_cache(self.ctx, directory.encode() if directory else None))
+
+    def cache_stats(self):
+        hits, misses = ctypes.c_uint64(), ctypes.c_uint64()
+        self._check(lib().grt_bvh_cache_stats(self.ctx, ctypes.byref(hits), ctypes.byref(misses)))
+        return int(hits.value), int(misses.value)
+
+    def export_obj(self, max_depth: int, path: str):
+        """The tree's boxes above max_depth as OBJ (the reference's `bvh export`)."""
+        self._check(lib().grt_export_bvh_obj(self.ctx, int(max_depth), str(path).encode()))
+
+    def leaf_stats(self) -> dict:
+        """The reference's `bvh statistics` figures of the current tree."""
+        st = LeafStats()
+        self._check(lib().grt_bvh_leaf_stats(self.ctx, ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in st._fields_}
 
     def select(self, name: str):
         self._check(lib().grt_select_tracer(self.ctx, name.encode()))
         self.tracer = name
 
-    def build(self, vpos, tris, split=None, max_tris=None, planes=16, esc=True) -> dict:
+    def build(self, vpos, tris, split=None, max_tris=None, planes=None, esc=True) -> dict:
         v = np.ascontiguousarray(vpos, np.float32)
         t = np.ascontiguousarray(tris, np.uint32)
-        o = make_opts(split or self.bvh_type, max_tris or self.bvh_max_tris_per_node, planes, esc)
+        o = make_opts(split or self.bvh_type, max_tris or self.bvh_max_tris_per_node, planes or self.bvh_planes, esc)
         self._check(lib().grt_build(self.ctx, _ptr(v), v.shape[0], _ptr(t), t.shape[0], ctypes.byref(o)))
         return self.info()
 

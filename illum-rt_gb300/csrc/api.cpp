@@ -95,7 +95,7 @@ grt_status grt_build(grt_ctx *c, const float *vpos4, uint32_t nv, const uint32_t
     auto t0 = std::chrono::steady_clock::now();
     std::string msg;
     grt::ref_tree tree;
-    if (!grt::build_reference_bvh(vpos4, nv, tris4, nt, bo, tree, msg)) return fail(c, GRT_ERR_INVALID_ARG, msg);
+    if (!grt::build_or_load(c, vpos4, nv, tris4, nt, bo, tree, msg)) return fail(c, GRT_ERR_INVALID_ARG, msg);
     c->stats.build_ms = ms_since(t0);
 
     t0 = std::chrono::steady_clock::now();
@@ -231,6 +231,12 @@ struct grt_host_bvh {
     grt::ref_tree tree;
     grt_bvh_stats stats{};
 };
+
+}  // extern "C"
+
+const grt::ref_tree &host_tree(const grt_host_bvh *h) { return h->tree; }
+
+extern "C" {
 
 grt_status grt_host_bvh_build(const float *vpos4, uint32_t nv, const uint32_t *tris4, uint32_t nt,
                               const grt_bvh_opts *opts, grt_host_bvh **out) {

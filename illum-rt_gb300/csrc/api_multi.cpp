@@ -49,7 +49,7 @@ grt_status grt_build_scenes(grt_ctx *c, const grt_mesh *meshes, uint32_t count, 
         for (uint32_t k; (k = next++) < count;) {
             const uint32_t i = order[k];
             const grt_mesh &m = meshes[i];
-            ok[i] = build_reference_bvh(m.vpos4, m.nv, m.tris4, m.nt, bo, trees[i], errs[i]) &&
+            ok[i] = build_or_load(c, m.vpos4, m.nv, m.tris4, m.nt, bo, trees[i], errs[i]) &&
                     flatten_bvh(trees[i], m.vpos4, m.tris4, flats[i], errs[i]) &&
                     flatten_bvh4(trees[i], flats[i], wides[i], errs[i]);
         }

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <array>
+#include <atomic>
 #include <chrono>
 #include <cstring>
 #include <string>
@@ -32,6 +33,9 @@ struct grt_ctx {
     cudaStream_t stream = nullptr;  // grt_trace_host stream
     unsigned long long *d_trav_counters = nullptr;  // grt_set_traversal_counters (caller's memory)
     uint64_t scene_generation = 0;  // bumped by every build (invalidates captured graphs)
+    // on-disk cache of reference trees (grt_set_bvh_cache); empty: off
+    std::string cache_dir;
+    std::atomic<uint64_t> cache_hits{0}, cache_misses{0};
     // texture data of the alpha-aware tracers (grt_set_alpha): one device allocation
     void *d_alpha = nullptr;
     // shading data of the path tracer
@@ -59,8 +63,14 @@ struct grt_ctx {
 };
 
 void grt_free_multi(grt_ctx *c);
+const grt::ref_tree &host_tree(const grt_host_bvh *h);
 
 namespace grt {
+
+// The reference build (build_reference_bvh), through the context's on-disk cache when one is
+// set (bvh_cache.cpp). Safe to call from several threads at once.
+bool build_or_load(grt_ctx *c, const float *vpos4, uint32_t nv, const uint32_t *tris4, uint32_t nt,
+                   const build_opts &bo, ref_tree &tree, std::string &err);
 
 struct device_guard {
     int prev = -1;

@@ -141,6 +141,36 @@ grt_status grt_host_bvh_build(const float *vpos4, uint32_t nv, const uint32_t *t
                               const grt_bvh_opts *opts, grt_host_bvh **out);
 /* ref_nodes, tri_records and depth of the host BVH; build_ms of its construction. */
 grt_status grt_host_bvh_info(const grt_host_bvh *bvh, grt_bvh_stats *out);
+
+/* On-disk cache of built trees. No counterpart in the reference, which builds every scene
+ * again on each start (its tracer can only export boxes, rt/cpu/bvh2.cpp:228-285). With a
+ * directory set, grt_build and grt_build_scenes first look for a file named by a 128-bit hash
+ * of the vertex and triangle arrays and the builder options; a file that is missing, from
+ * other inputs or damaged costs one build, after which the tree is written there (under a
+ * temporary name, then renamed). The cached tree is the reference builder's, so results are
+ * unchanged. NULL or "" switches the cache off. */
+grt_status grt_set_bvh_cache(grt_ctx *ctx, const char *directory);
+/* Builds served from the cache (hits) and built and stored (misses) since the context was made. */
+grt_status grt_bvh_cache_stats(const grt_ctx *ctx, uint64_t *hits, uint64_t *misses);
+
+/* The reference tracer's `bvh export <depth> <file.obj>` (rt/cpu/bvh2.cpp:228-283): the child
+ * boxes of the inner nodes above `max_depth` as OBJ quads, grouped by level, in the reference's
+ * order and number format. */
+grt_status grt_export_bvh_obj(grt_ctx *ctx, int max_depth, const char *path);
+
+/* The reference tracer's `bvh statistics` (rt/cpu/bvh2.cpp:286-317), computed the same way
+ * (the maximum is only updated by a leaf that is not a new minimum; the median of an even
+ * number of leaves averages positions n/2 and n/2 + 1, so two leaves are an error). */
+typedef struct grt_leaf_stats {
+    uint32_t leaves;
+    int32_t min_tris, max_tris;
+    uint32_t avg_tris;   /* integer division, as printed by the reference */
+    int32_t median_tris;
+} grt_leaf_stats;
+grt_status grt_bvh_leaf_stats(grt_ctx *ctx, grt_leaf_stats *out);
+/* The same two for a host-only BVH (no device needed). */
+grt_status grt_host_bvh_export_obj(const grt_host_bvh *bvh, int max_depth, const char *path);
+grt_status grt_host_bvh_leaf_stats(const grt_host_bvh *bvh, grt_leaf_stats *out);
 grt_status grt_host_bvh_export(const grt_host_bvh *bvh, uint32_t *nodes14, uint32_t *index, uint32_t *root);
 void grt_host_bvh_free(grt_host_bvh *bvh);
 

@@ -199,6 +199,17 @@ class ReferenceBVH(_BVHBase):
         return occ
 
 
+def ref_bvh_command(ref: "ReferenceBVH", args: str) -> str:
+    """Runs the reference tracer's `bvh <args>` command on `ref` and returns its stdout."""
+    f = ref.lib.ref_bvh_command
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int]
+    buf = ctypes.create_string_buffer(1 << 16)
+    if not f(ref.h, args.encode(), buf, len(buf)):
+        raise RuntimeError(f"the reference did not take 'bvh {args}'")
+    return buf.value.decode()
+
+
 class ReferenceAlphaBVH(ReferenceBVH):
     """The reference's alpha-aware tracer (binary_bvh_tracer<indexed, esc on, true>, SAH)."""
 

@@ -14,7 +14,9 @@
 
 #include <cstdint>
 #include <cstring>
+#include <iostream>
 #include <omp.h>
+#include <sstream>
 
 // The harness needs no scene teardown beyond the member vectors (libgi/scene.cpp is not built:
 // it needs assimp and ImageMagick).
@@ -163,6 +165,24 @@ void ref_any(void *hp, const float *rays8, uint32_t n, uint8_t *occluded, int th
     if (threads > 0) omp_set_num_threads(threads);
 #pragma omp parallel for schedule(dynamic, 256)
     for (int64_t i = 0; i < (int64_t)n; ++i) occluded[i] = h->rt->any_hit(make_ray(rays8 + 8 * i)) ? 1 : 0;
+}
+
+// Runs the reference tracer's own script command `bvh <args>` (binary_bvh_tracer::interprete,
+// rt/cpu/bvh2.cpp:192-241) and returns what it printed on stdout (at most cap - 1 bytes).
+int ref_bvh_command(void *hp, const char *args, char *out, int cap) {
+    handle *h = (handle *)hp;
+    std::ostringstream captured;
+    std::streambuf *old = std::cout.rdbuf(captured.rdbuf());
+    std::istringstream in(args);
+    const bool ok = h->rt->interprete("bvh", in);
+    std::cout.rdbuf(old);
+    const std::string s = captured.str();
+    const int n = (int)std::min<size_t>(s.size(), cap > 0 ? (size_t)cap - 1 : 0);
+    if (cap > 0) {
+        std::memcpy(out, s.data(), n);
+        out[n] = 0;
+    }
+    return ok ? 1 : 0;
 }
 
 void ref_free(void *hp) {

@@ -113,9 +113,39 @@ def main_alpha():
           f"of {any_rays.shape[0]}, {os.path.getsize(path)} bytes")
 
 
+TOOL_DEPTHS = (1, 4, 9)
+
+
+def main_tools():
+    """The reference tracer's `bvh export <depth> <file>` and `bvh statistics` outputs for every
+    golden scene (default CUDA build): SHA-256 of each exported OBJ text and the printed lines."""
+    import tempfile
+    orc = ge.load_oracle()
+    data = {}
+    for name, (v, t, _, _, _) in scenes().items():
+        ref = orc.ReferenceBVH(v, t, **dict(cases.BUILDERS[0][1]))
+        for d in TOOL_DEPTHS:
+            with tempfile.TemporaryDirectory() as tmp:
+                path = os.path.join(tmp, "bvh.obj")
+                orc.ref_bvh_command(ref, f"export {d} {path}")
+                with open(path, "rb") as f:
+                    data[f"obj_{name}_{d}"] = array_digest(np.frombuffer(f.read(), np.uint8))
+        try:
+            text = orc.ref_bvh_command(ref, "statistics")
+        except Exception:  # the reference's median reads past the end for two leaves
+            text = ""
+        data[f"stats_{name}"] = np.frombuffer(text.encode(), np.uint8).copy()
+    path = os.path.join(HERE, "golden_bvh_tools.npz")
+    np.savez_compressed(path, **data)
+    print(f"bvh tools: {len(data)} entries, {os.path.getsize(path)} bytes")
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["alpha"]:
         main_alpha()
+    elif sys.argv[1:] == ["tools"]:
+        main_tools()
     else:
         main()
         main_alpha()
+        main_tools()
