@@ -47,7 +47,7 @@ struct hasher {
 };
 
 constexpr char kMagic[8] = {'G', 'R', 'T', 'B', 'V', 'H', 0, 1};
-constexpr uint32_t kFormat = 1;
+constexpr uint32_t kFormat = 2;
 
 struct file_header {
     char magic[8];
@@ -55,7 +55,15 @@ struct file_header {
     uint64_t key_a, key_b;
     int32_t split, max_tris, planes, esc;
     uint64_t n_nodes, n_index;
+    uint64_t body_a, body_b;  // hash of the node and index arrays that follow
 };
+
+hasher body_hash(const ref_tree &t) {
+    hasher h;
+    h.bytes(t.nodes.data(), t.nodes.size() * sizeof(ref_node));
+    h.bytes(t.index.data(), t.index.size() * 4);
+    return h;
+}
 
 std::string cache_path(const std::string &dir, const hasher &h) {
     char name[64];
@@ -74,8 +82,9 @@ hasher key_of(const float *vpos4, uint32_t nv, const uint32_t *tris4, uint32_t n
     return h;
 }
 
-// A cached tree is used only if every link stays inside its arrays and every index names a
-// triangle, so a damaged or foreign file can cost a rebuild but never a bad access.
+// A cached tree is used only if its arrays hash to the value stored with them and every link
+// stays inside its arrays and every index names a triangle, so a damaged or foreign file can
+// cost a rebuild but never a wrong tree or a bad access.
 bool tree_is_sane(const ref_tree &t, uint32_t nt) {
     const size_t nn = t.nodes.size(), ni = t.index.size();
     if (nn == 0 || t.root >= nn) return false;
@@ -106,6 +115,10 @@ bool load_tree(const std::string &path, const hasher &h, uint32_t nv, uint32_t n
         out.index.resize(hd.n_index);
         ok = std::fread(out.nodes.data(), sizeof(ref_node), hd.n_nodes, f) == hd.n_nodes &&
              std::fread(out.index.data(), 4, hd.n_index, f) == hd.n_index && std::fgetc(f) == EOF;
+        if (ok) {
+            const hasher b = body_hash(out);
+            ok = b.a == hd.body_a && b.b == hd.body_b;
+        }
     }
     std::fclose(f);
     return ok && tree_is_sane(out, nt);
@@ -132,6 +145,9 @@ void store_tree(const std::string &path, const hasher &h, uint32_t nv, uint32_t 
     hd.esc = o.esc ? 1 : 0;
     hd.n_nodes = t.nodes.size();
     hd.n_index = t.index.size();
+    const hasher body = body_hash(t);
+    hd.body_a = body.a;
+    hd.body_b = body.b;
     bool ok = std::fwrite(&hd, sizeof(hd), 1, f) == 1 &&
               std::fwrite(t.nodes.data(), sizeof(ref_node), t.nodes.size(), f) == t.nodes.size() &&
               std::fwrite(t.index.data(), 4, t.index.size(), f) == t.index.size();
