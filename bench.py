@@ -52,8 +52,9 @@ def parse_args():
     ap.add_argument("--profile-case", action="store_true",
                     help="run one tuned and one plain step (no graphs) and exit (for ncu captures)")
     ap.add_argument("--profile-paths", type=int, default=1 << 20, help="paths of the --profile-case step")
-    ap.add_argument("--workload", default="spheres", choices=["spheres", "soups64"],
-                    help="soups64: 64 uneven triangle soups traced in one launch, host vs GPU BVH builds")
+    ap.add_argument("--workload", default="spheres", choices=["spheres", "soups64", "direct"],
+                    help="soups64: 64 uneven triangle soups traced in one launch, host vs GPU BVH builds; "
+                         "direct: light-source sampling, fused persistent kernel vs wavefront steps")
     return ap.parse_args()
 
 
@@ -533,6 +534,60 @@ def run_soups64(args):
     print(json.dumps(out), flush=True)
 
 
+def run_direct(args, samples: int = 8):
+    """Direct lighting on the 256 spheres with a floor and two area lights, 1024x1024 camera
+    rays, `samples` light samples per pixel: the fused persistent kernel against the wavefront
+    steps (camera trace, then per sample: light sampling, shadow trace, integration) in the
+    fastest exact loop order for each. Value: light samples per second of the fused form."""
+    import torch
+    import __graft_entry__ as ge
+    ge.load_package()
+    from illum_rt_gb300 import api, workloads as wl
+    sc, mats, rays_np = wl.lit_spheres(count=256, res=RES)
+    n = rays_np.shape[0]
+    rays = torch.from_numpy(rays_np).cuda()
+    fb = torch.zeros((n, 4), device="cuda")
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    rt = api.BatchRayTracer(0)
+    rt.build(sc.vpos, sc.tris)
+    rt.set_material_table(mats)
+
+    def timed(mode, tracer):
+        rt.select(tracer)
+        for _ in range(max(3, args.warmup)):
+            rt.direct(rays, fb, samples, mode=mode, seed=3, stream=sp)
+        rt.check(sp)
+        times = []
+        for _ in range(args.steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            rt.direct(rays, fb, samples, mode=mode, seed=3, stream=sp)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        rt.check(sp)
+        return statistics.median(times)
+
+    res = {}
+    for tracer in ("while-while", "if-if", "speculative-while-while", "bvh4-speculative-while-while"):
+        res["fused/" + tracer] = timed(api.DL_FUSED, tracer)
+    for tracer in ("while-while", "if-if", "speculative-while-while", "persistent-speculative-while-while"):
+        res["wavefront/" + tracer] = timed(api.DL_WAVEFRONT, tracer)
+    best_f = min((v, k) for k, v in res.items() if k.startswith("fused"))
+    best_w = min((v, k) for k, v in res.items() if k.startswith("wavefront"))
+    line = {"metric": "Msamples/s direct lighting (light-source sampling), fused vs wavefront", "unit": "Msamples/s",
+            "value": round(n * samples / best_f[0] / 1e3, 1), "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": "lit_spheres-262150: 256 spheres, floor, 2 area lights, 1024x1024 camera rays",
+                       "samples_per_pixel": samples},
+            "fused_ms": round(best_f[0], 4), "fused_form": best_f[1], "wavefront_ms": round(best_w[0], 4),
+            "wavefront_form": best_w[1], "speedup_fused_vs_wavefront": round(best_w[0] / best_f[0], 3),
+            "all_ms": {k: round(v, 4) for k, v in res.items()}}
+    print(json.dumps(line), flush=True)
+    rt.close()
+
+
 def run_profile_case(paths: int):
     """One tuned step, then one plain step (no graphs; 1,048,576 paths unless asked otherwise):
     a case whose launches ncu can capture one by one."""
@@ -560,6 +615,8 @@ def main():
         run_reference(args)
     elif args.workload == "soups64":
         run_soups64(args)
+    elif args.workload == "direct":
+        run_direct(args)
     else:
         run_gb300(args)
 

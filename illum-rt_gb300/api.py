@@ -70,6 +70,13 @@ class PtParams(ctypes.Structure):
 PT_WAVEFRONT, PT_FUSED = 0, 1
 
 
+class DirectParams(ctypes.Structure):
+    _fields_ = [("samples", ctypes.c_uint32), ("mode", ctypes.c_uint32), ("seed", ctypes.c_uint64)]
+
+
+DL_WAVEFRONT, DL_FUSED = 0, 1
+
+
 class Mesh(ctypes.Structure):
     _fields_ = [("vpos4", ctypes.c_void_p), ("nv", ctypes.c_uint32), ("tris4", ctypes.c_void_p), ("nt", ctypes.c_uint32)]
 
@@ -117,6 +124,8 @@ _PROTOS = {
     "grt_export_scene_bvh": (I, [VP, U32, VP, VP, P(U32)]),
     "grt_trace_multi": (I, [VP, VP, U32, I, VP]),
     "grt_set_alpha": (I, [VP, VP, U32, VP, U32, VP, U32]),
+    "grt_set_material_table": (I, [VP, VP, U32]),
+    "grt_direct": (I, [VP, P(DirectParams), VP, U32, VP, VP]),
     "grt_set_bvh_cache": (I, [VP, ctypes.c_char_p]),
     "grt_bvh_cache_stats": (I, [VP, P(ctypes.c_uint64), P(ctypes.c_uint64)]),
     "grt_export_bvh_obj": (I, [VP, I, ctypes.c_char_p]),
@@ -334,6 +343,19 @@ class BatchRayTracer:
         self._check(lib().grt_build_device(self.ctx, _ptr(vpos), int(vpos.shape[0]), _ptr(tris), int(tris.shape[0]),
                                            int(max_tris or self.bvh_max_tris_per_node), VP(stream or 0)))
         return self.info()
+
+    def set_material_table(self, mats):
+        """Materials for direct lighting (grt_set_material_table): float32 [m, 8] = albedo rgb,
+        emission rgb, ior, roughness. Triangles with an emitting material are the lights."""
+        m = np.ascontiguousarray(mats, np.float32).reshape(-1, 8)
+        self._check(lib().grt_set_material_table(self.ctx, _ptr(m), m.shape[0]))
+
+    def direct(self, rays, framebuffer, samples, mode=DL_FUSED, seed=0, stream=None):
+        """Direct lighting (grt_direct) of CUDA rays [n, 8], accumulated into the CUDA frame
+        buffer [n, 4] (radiance sum, sample count)."""
+        p = DirectParams(int(samples), int(mode), int(seed))
+        self._check(lib().grt_direct(self.ctx, ctypes.byref(p), _ptr(rays), int(rays.shape[0]), _ptr(framebuffer),
+                                     VP(stream or 0)))
 
     def set_alpha(self, tc, mat_tex, textures):
         """Texture data of the alpha-aware tracers (grt_set_alpha): tc float32 [nv, 2] per vertex

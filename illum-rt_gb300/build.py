@@ -54,7 +54,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> dict:
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".hpp", ".cuh", ".h"))]
     headers.append(os.path.join(HERE, "..", "include", "grt.h"))
     cu = sorted(f for f in os.listdir(CSRC) if f.endswith(".cu"))
-    cpp = ["api.cpp", "api_pt.cpp", "api_multi.cpp", "api_gpu_build.cpp", "bvh_builder.cpp", "bvh_cache.cpp"]
+    cpp = ["api.cpp", "api_pt.cpp", "api_multi.cpp", "api_gpu_build.cpp", "api_direct.cpp", "bvh_builder.cpp", "bvh_cache.cpp"]
     hostflags = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-Wall", "-Wno-unused-function"]
     jobs = []
     for f in cu:

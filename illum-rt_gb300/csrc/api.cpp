@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "ctx.hpp"
+#include "direct.hpp"
 #include "multi.hpp"
 #include "pathtrace.hpp"
 
@@ -53,6 +54,7 @@ grt_status grt_create(const grt_config *cfg, grt_ctx **out) {
     if (e == cudaSuccess) e = grt::prepare_trace_kernels();
     if (e == cudaSuccess) e = grt::prepare_pt_kernels();
     if (e == cudaSuccess) e = grt::prepare_multi_kernels();
+    if (e == cudaSuccess) e = grt::prepare_dl_kernels();
     if (e != cudaSuccess) {
         cudaGetLastError();
         if (c->d_err) cudaFree(c->d_err);
@@ -72,6 +74,7 @@ grt_status grt_destroy(grt_ctx *c) {
         if (c->d_stage) cudaFree(c->d_stage);
         if (c->d_scratch) cudaFree(c->d_scratch);
         if (c->d_albedo) cudaFree(c->d_albedo);
+        if (c->d_dl_scratch) cudaFree(c->d_dl_scratch);
         if (c->pt_graph.exec) cudaGraphExecDestroy(c->pt_graph.exec);
         if (c->d_err) cudaFree(c->d_err);
         if (c->stream) cudaStreamDestroy(c->stream);

@@ -38,6 +38,14 @@ struct grt_ctx {
     std::atomic<uint64_t> cache_hits{0}, cache_misses{0};
     // texture data of the alpha-aware tracers (grt_set_alpha): one device allocation
     void *d_alpha = nullptr;
+    // direct lighting (grt_set_material_table, grt_direct): materials and light distribution in
+    // one allocation, per-pixel buffers of the wavefront form in another
+    void *d_dl = nullptr;
+    uint32_t dl_n_mat = 0, dl_n_lights = 0;
+    float dl_integral = 0.f;
+    size_t dl_off_lights = 0, dl_off_f = 0, dl_off_cdf = 0;
+    void *d_dl_scratch = nullptr;
+    size_t dl_scratch_bytes = 0;
     // shading data of the path tracer
     float *d_albedo = nullptr;
     uint32_t n_albedo = 0;
@@ -95,7 +103,7 @@ inline grt_status cuda_fail(grt_ctx *c, cudaError_t e, const char *what) {
 }
 
 inline void free_scene(grt_ctx *c) {
-    for (void **p : {&c->d_nodes, &c->d_recs, &c->d_vpos, &c->d_tris, &c->d_nodes4, &c->d_alpha}) {
+    for (void **p : {&c->d_nodes, &c->d_recs, &c->d_vpos, &c->d_tris, &c->d_nodes4, &c->d_alpha, &c->d_dl}) {
         if (*p) cudaFree(*p);
         *p = nullptr;
     }

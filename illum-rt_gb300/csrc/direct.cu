@@ -1,0 +1,267 @@
+// Direct lighting kernels: the wavefront steps of the reference's direct-wf algorithm
+// (k::sample_light, the shadow-ray trace, k::integrate_light; rt/cuda/bounce.cu:210-250,
+// 380-410) and one fused persistent kernel doing all of them per pixel.
+#include "direct.hpp"
+#include "traverse.cuh"
+
+namespace grt {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+using dl::f3;
+
+// Materials beyond the table get the reference's default material (libgi/material.h:144-151).
+__device__ __forceinline__ dl::material material_of(const dl_scene &ds, uint32_t id) {
+    if (id < ds.n_mat) return ds.mats[id];
+    dl::material m = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, 1.3f, 0.1f};
+    return m;
+}
+
+__device__ __forceinline__ f3 vert(const dl_scene &ds, uint32_t i) {
+    const float4 v = __ldg(ds.vpos + i);
+    return {v.x, v.y, v.z};
+}
+
+// What the sampling step decides for one sample of one pixel.
+struct dl_prep {
+    bool emissive;  // the camera ray hit a light: its emission is added, no shadow ray
+    f3 emis;
+    f3 org, dir;
+    float tmax;     // -FLT_MAX: no shadow ray
+    f3 lcol;
+    float pdf;
+};
+
+// k::sample_light (rt/cuda/bounce.cu:210-250) for sample `s` of pixel `pixel`; random numbers
+// from the PCG32 stream seed + s * n + pixel.
+__device__ dl_prep prepare(const dl_scene &ds, f3 o, f3 d, float t, uint32_t ref, uint32_t pixel, uint32_t s,
+                           uint32_t n, uint64_t seed) {
+    dl_prep p;
+    p.emissive = false;
+    p.emis = p.org = p.dir = p.lcol = {0.f, 0.f, 0.f};
+    p.tmax = -FLT_MAX;
+    p.pdf = 0.f;
+    if (t == FLT_MAX) return p;
+    const uint4 tri = __ldg(ds.tris + ref);
+    const dl::material m = material_of(ds, tri.w);
+    const f3 em = {m.emissive[0], m.emissive[1], m.emissive[2]};
+    if (dl::not_black(em)) {
+        p.emissive = true;
+        p.emis = em;
+        return p;
+    }
+    if (ds.n_lights == 0) return p;
+    pm::pcg32 rng;
+    rng.set_sequence(seed + (uint64_t)s * n + pixel);
+    const float x0 = rng.uniform(), x1 = rng.uniform(), x2 = rng.uniform();
+    float pdf_l;
+    const uint32_t id = dl::sample_light_index(ds.n_lights, ds.lf, ds.lcdf, ds.integral, x2, pdf_l);
+    const uint4 L = __ldg(ds.lights + id);
+    const dl::material lm = material_of(ds, L.w);
+    const f3 from = {pm::add(o.x, pm::mul(t, d.x)), pm::add(o.y, pm::mul(t, d.y)), pm::add(o.z, pm::mul(t, d.z))};
+    const dl::light_sample ls =
+        dl::sample_li(from, vert(ds, L.x), vert(ds, L.y), vert(ds, L.z), {lm.emissive[0], lm.emissive[1], lm.emissive[2]},
+                      x0, x1);
+    p.lcol = ls.lcol;
+    p.pdf = pm::mul(pdf_l, ls.pdf);
+    if (dl::not_black(ls.lcol)) {
+        p.org = ls.org;
+        p.dir = ls.dir;
+        p.tmax = ls.tmax;
+    }
+    return p;
+}
+
+// k::integrate_light (rt/cuda/bounce.cu:380-410): the radiance of one sample.
+__device__ f3 radiance(const dl_scene &ds, f3 d, float t, uint32_t ref, f3 w_i, float tmax, f3 lcol, float pdf,
+                       bool occluded) {
+    if (t == FLT_MAX || !(tmax > 0.f) || occluded) return {0.f, 0.f, 0.f};
+    const uint4 tri = __ldg(ds.tris + ref);
+    const dl::material m = material_of(ds, tri.w);
+    const f3 ns = pm::facing_normal(vert(ds, tri.x), vert(ds, tri.y), vert(ds, tri.z), d);
+    return dl::integrate(lcol, {-d.x, -d.y, -d.z}, w_i, ns, m, pdf);
+}
+
+__device__ __forceinline__ float4 plus(float4 a, f3 b, float w) {
+    return make_float4(pm::add(a.x, b.x), pm::add(a.y, b.y), pm::add(a.z, b.z), pm::add(a.w, w));
+}
+
+__device__ __forceinline__ ray_t shadow_ray(f3 o, f3 d, float tmax) {
+    ray_t r;
+    r.ox = o.x;
+    r.oy = o.y;
+    r.oz = o.z;
+    r.tmin = dl::kEps;  // the shadow ray's t_min (bounce.cu:246)
+    r.dx = d.x;
+    r.dy = d.y;
+    r.dz = d.z;
+    r.tmax = tmax;
+    r.ix = __fdiv_rn(1.0f, d.x);
+    r.iy = __fdiv_rn(1.0f, d.y);
+    r.iz = __fdiv_rn(1.0f, d.z);
+    return r;
+}
+
+__global__ void __launch_bounds__(256) k_dl_sample(dl_scene ds, const float4 *__restrict__ rays,
+                                                   const grt_hit *__restrict__ hits, uint32_t n, uint32_t s,
+                                                   uint64_t seed, float4 *shadow_rays, float4 *lsample, float4 *fb) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 ro = rays[2 * (size_t)i], rd = rays[2 * (size_t)i + 1];
+    const grt_hit h = hits[i];
+    const dl_prep p = prepare(ds, {ro.x, ro.y, ro.z}, {rd.x, rd.y, rd.z}, h.t, h.ref, i, s, n, seed);
+    if (p.emissive) fb[i] = plus(fb[i], p.emis, 0.f);
+    shadow_rays[2 * (size_t)i] = make_float4(p.org.x, p.org.y, p.org.z, dl::kEps);
+    shadow_rays[2 * (size_t)i + 1] = make_float4(p.dir.x, p.dir.y, p.dir.z, p.tmax);
+    lsample[i] = make_float4(p.lcol.x, p.lcol.y, p.lcol.z, p.pdf);
+}
+
+__global__ void __launch_bounds__(256) k_dl_integrate(dl_scene ds, const float4 *__restrict__ rays,
+                                                      const grt_hit *__restrict__ hits,
+                                                      const float4 *__restrict__ shadow_rays,
+                                                      const grt_hit *__restrict__ shadow_hits,
+                                                      const float4 *__restrict__ lsample, uint32_t n, float4 *fb) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 rd = rays[2 * (size_t)i + 1];
+    const grt_hit h = hits[i];
+    const float4 sd = shadow_rays[2 * (size_t)i + 1];
+    const float4 l = lsample[i];
+    const bool occluded = shadow_hits[i].ref == 0xFFFFFFFFu;
+    const f3 rad = radiance(ds, {rd.x, rd.y, rd.z}, h.t, h.ref, {sd.x, sd.y, sd.z}, sd.w, {l.x, l.y, l.z}, l.w, occluded);
+    fb[i] = plus(fb[i], rad, 1.0f);
+}
+
+// Fused form, warp-synchronous: a warp takes 32 consecutive pixels from the global counter,
+// traverses their camera rays together (closest hit), then for each sample prepares the light
+// samples, traverses the shadow rays together (any hit) and integrates into registers, in the
+// order the wavefront steps add to the frame buffer. All lanes of a warp are always in the same
+// phase, so every loop order works, the speculative ones included, and the shadow rays of one
+// sample stay as coherent as in the wavefront form.
+template <int ORDER, int STACK, bool ANY>
+__device__ __forceinline__ void trace_all(trav_t &s, bool active, bool plain, const dev_scene &sc, const ray_t &r,
+                                          int *stk, int stride, unsigned *err) {
+    constexpr bool SPEC = ORDER == SPECULATIVE || ORDER == WIDE_SPECULATIVE;
+    constexpr bool WIDE = ORDER == WIDE_SPECULATIVE;
+    while (__any_sync(kFull, active && !s.done)) {
+        if (SPEC)
+            trav_spec_iter<STACK, ANY, false, WIDE>(s, active, plain, sc, r, stk, stride, err);
+        else if (active && !s.done && plain)
+            trav_advance<ORDER, STACK, ANY, false, true>(s, sc, r, stk, stride, err);
+        else if (active && !s.done)
+            trav_advance<ORDER, STACK, ANY, false, false>(s, sc, r, stk, stride, err);
+    }
+}
+
+template <int ORDER, int STACK>
+__global__ void __launch_bounds__(256) k_dl_fused(dev_scene sc, dl_scene ds, const float4 *__restrict__ rays,
+                                                  uint32_t n, uint32_t samples, uint64_t seed, float4 *fb,
+                                                  unsigned *err, unsigned *counter) {
+    extern __shared__ int s_stack[];
+    constexpr bool WIDE = ORDER == WIDE_SPECULATIVE;
+    const unsigned lane = threadIdx.x & 31u;
+    int *stk = s_stack + threadIdx.x;
+    const int stride = blockDim.x;
+    for (;;) {
+        unsigned base = 0;
+        if (lane == 0) base = atomicAdd(counter, 32u);
+        base = __shfl_sync(kFull, base, 0);
+        if (base >= n) break;
+        const uint32_t pix = base + lane;
+        const bool active = pix < n;
+        ray_t r = {};
+        trav_t s;
+        if (active) r = load_ray(rays, pix);
+        const f3 o = {r.ox, r.oy, r.oz}, d = {r.dx, r.dy, r.dz};
+        float4 acc = active ? fb[pix] : make_float4(0.f, 0.f, 0.f, 0.f);
+        trav_init(s, sc, WIDE);
+        bool plain = active && sc.finite && ray_is_plain(r);
+        trace_all<ORDER, STACK, false>(s, active, plain, sc, r, stk, stride, err);
+        const float ht = active ? s.hit.t : FLT_MAX;
+        const uint32_t href = s.hit.ref;
+        for (uint32_t smp = 0; smp < samples; ++smp) {
+            dl_prep p;
+            if (active) {
+                p = prepare(ds, o, d, ht, href, pix, smp, n, seed);
+                if (p.emissive) acc = plus(acc, p.emis, 0.f);
+            }
+            const bool shoot = active && p.tmax > 0.f;  // a shadow ray that can find an occluder
+            if (shoot) r = shadow_ray(p.org, p.dir, p.tmax);
+            trav_init(s, sc, WIDE);
+            plain = shoot && sc.finite && ray_is_plain(r);
+            trace_all<ORDER, STACK, true>(s, shoot, plain, sc, r, stk, stride, err);
+            if (active) {
+                const f3 rad = shoot ? radiance(ds, d, ht, href, p.dir, p.tmax, p.lcol, p.pdf, s.found)
+                                     : f3{0.f, 0.f, 0.f};
+                acc = plus(acc, rad, 1.0f);
+            }
+        }
+        if (active) fb[pix] = acc;
+    }
+}
+
+template <int ORDER, int STACK> const void *fused_ptr() { return (const void *)k_dl_fused<ORDER, STACK>; }
+
+template <int ORDER, int STACK>
+cudaError_t fused_run(const dev_scene &sc, const dl_scene &ds, const float4 *rays, uint32_t n, uint32_t samples,
+                      uint64_t seed, float4 *fb, int bt, int num_sms, unsigned *err, unsigned *counter,
+                      cudaStream_t st) {
+    const size_t smem = (size_t)STACK * bt * sizeof(int);
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dl_fused<ORDER, STACK>, bt, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    e = cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
+    if (e != cudaSuccess) return e;
+    k_dl_fused<ORDER, STACK><<<per_sm * num_sms, bt, smem, st>>>(sc, ds, rays, n, samples, seed, fb, err, counter);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_dl_sample(const dl_scene &ds, const float4 *rays, const grt_hit *hits, uint32_t n, uint32_t s,
+                             uint64_t seed, float4 *shadow_rays, float4 *lsample, float4 *fb, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    k_dl_sample<<<(n + 255) / 256, 256, 0, st>>>(ds, rays, hits, n, s, seed, shadow_rays, lsample, fb);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dl_integrate(const dl_scene &ds, const float4 *rays, const grt_hit *hits, const float4 *shadow_rays,
+                                const grt_hit *shadow_hits, const float4 *lsample, uint32_t n, float4 *fb,
+                                cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    k_dl_integrate<<<(n + 255) / 256, 256, 0, st>>>(ds, rays, hits, shadow_rays, shadow_hits, lsample, n, fb);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dl_fused(const dev_scene &sc, const dl_scene &ds, const float4 *rays, uint32_t n, uint32_t samples,
+                            uint64_t seed, float4 *fb, int order, int stack_entries, int bt, int num_sms, unsigned *err,
+                            unsigned *counter, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    const bool small = stack_entries <= kStackSmall;
+#define GRT_DL_RUN(O)                                                                                            \
+    return small ? fused_run<O, kStackSmall>(sc, ds, rays, n, samples, seed, fb, bt, num_sms, err, counter, st) \
+                 : fused_run<O, kStackLarge>(sc, ds, rays, n, samples, seed, fb, bt, num_sms, err, counter, st)
+    switch (order) {
+        case IF_IF: GRT_DL_RUN(IF_IF);
+        case SPECULATIVE: GRT_DL_RUN(SPECULATIVE);
+        case WIDE_SPECULATIVE: GRT_DL_RUN(WIDE_SPECULATIVE);
+        default: GRT_DL_RUN(WHILE_WHILE);
+    }
+#undef GRT_DL_RUN
+}
+
+cudaError_t prepare_dl_kernels() {
+    const int bytes = kStackLarge * 256 * (int)sizeof(int);
+    for (const void *f : {fused_ptr<IF_IF, kStackSmall>(), fused_ptr<IF_IF, kStackLarge>(),
+                          fused_ptr<WHILE_WHILE, kStackSmall>(), fused_ptr<WHILE_WHILE, kStackLarge>(),
+                          fused_ptr<SPECULATIVE, kStackSmall>(), fused_ptr<SPECULATIVE, kStackLarge>(),
+                          fused_ptr<WIDE_SPECULATIVE, kStackSmall>(), fused_ptr<WIDE_SPECULATIVE, kStackLarge>()}) {
+        cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+}  // namespace grt

@@ -137,6 +137,37 @@ def spheres_primary(res: int = 1024):
     return sc, rays
 
 
+def lit_spheres(count: int = 256, res: int = 1024):
+    """Direct-lighting scene: `count` UV spheres (materials 0-3 by sphere), a floor at y = -12
+    (material 4) and two emissive quads at y = 14 facing down (material 5), with its material
+    table float32 [6, 8] (albedo rgb, emission rgb, ior, roughness) and res x res camera rays."""
+    sc = spheres(count=count)
+    per_sphere = 2 * 32 * 16
+    tris = sc.tris.copy()
+    tris[:, 3] = (np.arange(tris.shape[0]) // per_sphere) % 4
+    quads = [((-30.0, -12.0, -30.0), (60.0, 60.0), 4, True),   # floor, normal up
+             ((-6.0, 14.0, -3.0), (5.0, 6.0), 5, False),      # lights, normal down
+             ((2.0, 14.0, -4.0), (5.0, 5.0), 5, False)]
+    v = [sc.vpos]
+    t = [tris]
+    base = sc.vpos.shape[0]
+    for (x0, y, z0), (dx, dz), mat, up in quads:
+        q = np.array([[x0, y, z0, 1], [x0 + dx, y, z0, 1], [x0 + dx, y, z0 + dz, 1], [x0, y, z0 + dz, 1]], np.float32)
+        v.append(q)
+        tri = [(0, 2, 1), (0, 3, 2)] if up else [(0, 1, 2), (0, 2, 3)]
+        t.append(np.array([[base + a, base + b, base + c, mat] for a, b, c in tri], np.uint32))
+        base += 4
+    mats = np.array([[0.8, 0.3, 0.3, 0, 0, 0, 1.3, 0.1],
+                     [0.3, 0.8, 0.3, 0, 0, 0, 1.5, 0.3],
+                     [0.3, 0.3, 0.8, 0, 0, 0, 1.2, 0.05],
+                     [0.7, 0.7, 0.7, 0, 0, 0, 1.8, 0.6],
+                     [0.5, 0.5, 0.5, 0, 0, 0, 1.3, 0.9],
+                     [0.0, 0.0, 0.0, 12, 11, 9, 1.3, 0.1]], np.float32)
+    scene = Scene("lit_spheres", np.concatenate(v), np.concatenate(t))
+    rays = camera_rays((0.0, 0.0, 35.0), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 65.0, res, res)
+    return scene, mats, rays
+
+
 def multi_scene_sizes(seed: int = 4, count: int = 64):
     """Triangle and ray counts of the uneven multi-scene batch (log-uniform)."""
     tris = [log_uniform(seed, 2 * i, 1024, 1 << 20) for i in range(count)]

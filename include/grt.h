@@ -334,6 +334,43 @@ grt_status grt_adjoint(grt_ctx *ctx, const float *rays_dev, const grt_hit *hits_
                        uint32_t n, const float *vpos_dev, uint32_t vstride, float *grad_vpos_dev, float *grad_rays_dev,
                        grt_stream_t stream);
 
+/* ---- direct lighting ------------------------------------------------------------------ */
+
+/* One material: the fields of the reference's material that shading reads
+ * (libgi/material.h:144-151): albedo, emission, index of refraction, roughness. */
+typedef struct grt_material {
+    float albedo[3];
+    float emissive[3];
+    float ior;
+    float roughness;
+} grt_material;
+
+/* Material table of the built scene for grt_direct, indexed by the triangles' material ids
+ * (ids beyond the table get the reference's default material). The lights are the triangles
+ * whose material emits, chosen by power, luma(emission * area * pi), as the reference's CUDA
+ * platform prepares them (rt/cuda/preprocessing.cpp:17-35). Host array, copied; must follow
+ * the build; a new build drops it. */
+grt_status grt_set_material_table(grt_ctx *ctx, const grt_material *materials, uint32_t n);
+
+enum { GRT_DL_WAVEFRONT = 0, GRT_DL_FUSED = 1 };
+typedef struct grt_direct_params {
+    uint32_t samples;  /* light samples per pixel */
+    uint32_t mode;     /* GRT_DL_WAVEFRONT or GRT_DL_FUSED */
+    uint64_t seed;     /* sample s of pixel i draws from the PCG32 stream seed + s * n + i */
+} grt_direct_params;
+
+/* Direct lighting by light-source sampling, the reference's direct-wf steps (rt/cuda/bounce.cu:
+ * k::sample_light 210-250, the shadow-ray trace, k::integrate_light 380-410 with its layered
+ * GGX-coat BRDF): for every camera ray (DEVICE rays_dev, the grt_trace layout) the closest hit,
+ * then `samples` times: a light chosen by power, a point on it, an any-hit shadow ray, and
+ * framebuffer[i] += (radiance, 1) (a hit on an emitter first adds its emission). framebuffer_dev
+ * is n float4, accumulated into. GRT_DL_WAVEFRONT runs the steps as separate launches with the
+ * selected tracer; GRT_DL_FUSED runs everything in one persistent kernel in the selected
+ * tracer's loop order, a warp tracing 32 pixels' rays together phase by phase. Both forms give
+ * the same bits (for the speculative orders, up to the near-ties of their camera-ray hits). */
+grt_status grt_direct(grt_ctx *ctx, const grt_direct_params *params, const float *rays_dev, uint32_t n,
+                      float *framebuffer_dev, grt_stream_t stream);
+
 /* ---- alpha-aware tracing ---------------------------------------------------------------- */
 
 /* One single-channel texture: width x height alpha values, row by row. */

@@ -908,6 +908,219 @@ void orc_pathtrace(void *hp, const float *prim_rays8, const float *prim_hits4, u
     }
 }
 
+// ---- direct lighting by light-source sampling ------------------------------------------
+//
+// The reference's CUDA direct-wf steps: k::sample_light with k::sample_index and k::sample_Li
+// (rt/cuda/bounce.cu:148-250), the any-hit shadow ray, and k::integrate_light with layered_gtr2
+// (bounce.cu:291-339, 380-410; fresnel_dielectric libgi/util.h:91-106, tan2_theta
+// libgi/util.h:141-160), over the light distribution of compute_light_distribution
+// (rt/cuda/preprocessing.cpp:17-35: luma(trianglelight::power()), libgi/scene.cpp:518-527;
+// distribution_1d::build_cdf, libgi/discrete_distributions.cpp:33-45). Geometric normals (the
+// shading normal facing the camera ray, a light's normal by its winding), normalize as
+// v * (1 / sqrt(v . v)), and the three random numbers of sample s of pixel i from the PCG32
+// stream seed + s * n + i.
+
+struct dl_mat {
+    float albedo[3], emissive[3], ior, roughness;
+};
+
+struct dl_set {
+    std::vector<dl_mat> mats;
+    std::vector<uint32_t> lights;  // 4 per light: a, b, c, material
+    std::vector<float> f, cdf;
+    float integral = 0.f;
+    const dl_mat &mat(uint32_t id) const {
+        static const dl_mat def = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, 1.3f, 0.1f};  // libgi/material.h:144-151
+        return id < mats.size() ? mats[id] : def;
+    }
+};
+
+static bool emits(const dl_mat &m) { return m.emissive[0] != 0.f || m.emissive[1] != 0.f || m.emissive[2] != 0.f; }
+
+static dl_set make_dl_set(const scene &sc, const float *mats8, uint32_t n_mat) {
+    dl_set L;
+    L.mats.resize(n_mat);
+    std::memcpy(L.mats.data(), mats8, (size_t)n_mat * sizeof(dl_mat));
+    for (uint32_t i = 0; i < sc.nt; ++i) {
+        const uint32_t *t = sc.t4 + 4 * (size_t)i;
+        if (t[3] >= n_mat || !emits(L.mats[t[3]])) continue;
+        const v3 a = sc.vert(t[0]), b = sc.vert(t[1]), c = sc.vert(t[2]);
+        const v3 e1 = vsub(b, a), e2 = vsub(c, a);
+        const v3 x = {e1.y * e2.z - e1.z * e2.y, e1.z * e2.x - e1.x * e2.z, e1.x * e2.y - e1.y * e2.x};
+        const float len = std::sqrt(x.x * x.x + x.y * x.y + x.z * x.z);
+        const float pi = 3.14159265358979323846f;
+        const float *em = L.mats[t[3]].emissive;
+        const float p0 = em[0] * 0.5f * len * pi, p1 = em[1] * 0.5f * len * pi, p2 = em[2] * 0.5f * len * pi;
+        L.f.push_back(0.212671f * p0 + 0.715160f * p1 + 0.072169f * p2);
+        L.lights.insert(L.lights.end(), {t[0], t[1], t[2], t[3]});
+    }
+    const size_t N = L.f.size();
+    L.cdf.assign(N + 1, 0.f);
+    for (size_t i = 1; i <= N; ++i) L.cdf[i] = L.cdf[i - 1] + L.f[i - 1];
+    L.integral = L.cdf[N];
+    for (size_t i = 1; i <= N; ++i) L.cdf[i] = L.integral > 0.f ? L.cdf[i] / L.integral : (float)i / (float)N;
+    return L;
+}
+
+static float dl_fresnel(float cos_wi, float ior_medium, float ior_material) {
+    const float ei = cos_wi < 0.0f ? ior_material : ior_medium;
+    const float et = cos_wi < 0.0f ? ior_medium : ior_material;
+    cos_wi = std::fabs(cos_wi);
+    cos_wi = cos_wi < 0.0f ? 0.0f : (cos_wi > 1.0f ? 1.0f : cos_wi);
+    const float sin_t = (ei / et) * std::sqrt(1.0f - cos_wi * cos_wi);
+    if (sin_t >= 1.0f) return 1.0f;
+    const float rev = 1.f - sin_t * sin_t;
+    const float cos_t = std::sqrt(rev > 0.0f ? rev : 0.0f);
+    const float rparl = ((et * cos_wi) - (ei * cos_t)) / ((et * cos_wi) + (ei * cos_t));
+    const float rperp = ((ei * cos_wi) - (et * cos_t)) / ((ei * cos_wi) + (et * cos_t));
+    return (rparl * rparl + rperp * rperp) / 2;
+}
+
+static float dl_tan2(float c) {
+    float s2 = 1.0f - c * c;
+    s2 = s2 < 0.0f ? 0.0f : s2;
+    return s2 / (c * c);
+}
+
+static float dl_ggx_d(float nh, float rough) {
+    if (nh <= 0) return 0.f;
+    const float t2 = dl_tan2(nh);
+    if (!std::isfinite(t2)) return 0.f;
+    const float a2 = rough * rough;
+    const float pi = 3.14159265358979323846f;
+    return a2 / (pi * ((nh * nh) * (nh * nh)) * ((a2 + t2) * (a2 + t2)));
+}
+
+static float dl_ggx_g1(float nv, float rough) {
+    if (nv <= 0) return 0.f;
+    const float t2 = dl_tan2(nv);
+    if (!std::isfinite(t2)) return 0.f;
+    return 2.f / (1.f + std::sqrt(1.f + (rough * rough) * t2));
+}
+
+static float cdot3(v3 a, v3 b) {
+    const float x = vdot(a, b);
+    return x < 0.0f ? 0.0f : x;
+}
+
+// layered_gtr2: (1 - F) lambert + F coat
+static v3 dl_brdf(v3 w_o, v3 w_i, v3 ns, const dl_mat &m) {
+    const float dwo = vdot(ns, w_o);
+    const float F = dl_fresnel(dwo < 0.0f ? -dwo : dwo, 1.0f, m.ior);
+    const float one_over_pi = (float)(1.0 / 3.14159265358979323846);
+    v3 diff = {0.f, 0.f, 0.f};
+    if (vdot(w_i, ns) > 0) diff = {one_over_pi * m.albedo[0], one_over_pi * m.albedo[1], one_over_pi * m.albedo[2]};
+    float spec = 0.f;
+    if (vdot(ns, w_i) > 0) {
+        const float nv = cdot3(ns, w_o), nl = cdot3(ns, w_i);
+        if (nv != 0.f) {
+            v3 h = {w_o.x + w_i.x, w_o.y + w_i.y, w_o.z + w_i.z};
+            const float inv = 1.0f / std::sqrt(vdot(h, h));
+            h = {h.x * inv, h.y * inv, h.z * inv};
+            const float nh = cdot3(ns, h), hl = cdot3(h, w_i);
+            const float Fh = dl_fresnel(hl, 1.f, m.ior);
+            const float D = dl_ggx_d(nh, m.roughness);
+            const float G = dl_ggx_g1(nv, m.roughness) * dl_ggx_g1(nl, m.roughness);
+            spec = (Fh * D * G) / (4 * std::fabs(nv) * std::fabs(nl));
+        }
+    }
+    const float k = 1.0f - F;
+    return {k * diff.x + F * spec, k * diff.y + F * spec, k * diff.z + F * spec};
+}
+
+// one pixel: closest hit, then `samples` light samples accumulated into fb (4 floats)
+static void dl_pixel(const bvh &h, const dl_set &L, const float *ray8, uint32_t pixel, uint32_t n, uint32_t samples,
+                     uint64_t seed, float *fb) {
+    const ray r = load_ray(ray8);
+    const hit ph = closest_hit(h, r, nullptr);
+    const v3 o = {ray8[0], ray8[1], ray8[2]}, d = {ray8[4], ray8[5], ray8[6]};
+    for (uint32_t s = 0; s < samples; ++s) {
+        v3 rad = {0.f, 0.f, 0.f};
+        if (ph.t != FLT_MAX) {
+            const uint32_t *t = h.sc.t4 + 4 * (size_t)ph.ref;
+            const dl_mat &m = L.mat(t[3]);
+            if (emits(m)) {
+                fb[0] += m.emissive[0];
+                fb[1] += m.emissive[1];
+                fb[2] += m.emissive[2];
+                fb[3] += 0.0f;
+            } else if (!L.f.empty()) {
+                rng32 g;
+                g.seq(seed + (uint64_t)s * n + pixel);
+                const float x0 = g.uniform(), x1 = g.uniform(), x2 = g.uniform();
+                // sample_index: lower_bound over the first N cdf entries
+                int count = (int)L.f.size(), first = 0, i = 0;
+                while (count > 0) {
+                    i = first;
+                    const int step = count / 2;
+                    i += step;
+                    if (L.cdf[i] < x2) {
+                        first = ++i;
+                        count -= step + 1;
+                    } else {
+                        count = step;
+                    }
+                }
+                const int id = i > 0 ? i - 1 : i;
+                const float pdf_l = L.f[id] / L.integral;
+                const uint32_t *lt = L.lights.data() + 4 * (size_t)id;
+                const v3 a = h.sc.vert(lt[0]), b = h.sc.vert(lt[1]), c = h.sc.vert(lt[2]);
+                const float *em = L.mat(lt[3]).emissive;
+                // sample_Li
+                const v3 from = {o.x + ph.t * d.x, o.y + ph.t * d.y, o.z + ph.t * d.z};
+                const float su0 = std::sqrt(x0);
+                const float bb = 1.0f - su0, bg = x1 * su0;
+                const float w = 1.0f - bb - bg;
+                const v3 target = {w * a.x + bb * b.x + bg * c.x, w * a.y + bb * b.y + bg * c.y,
+                                   w * a.z + bb * b.z + bg * c.z};
+                const v3 e1 = vsub(b, a), e2 = vsub(c, a);
+                const v3 x = {e1.y * e2.z - e1.z * e2.y, e1.z * e2.x - e1.x * e2.z, e1.x * e2.y - e1.y * e2.x};
+                const float inv = 1.0f / std::sqrt(vdot(x, x));
+                const v3 ln = {x.x * inv, x.y * inv, x.z * inv};
+                v3 wi = vsub(target, from);
+                const float area = 0.5f * std::sqrt(vdot(x, x));
+                float tmax = std::sqrt(vdot(wi, wi));
+                wi = {wi.x / tmax, wi.y / tmax, wi.z / tmax};
+                tmax -= 1e-4f;
+                const float cos_l = vdot(ln, {-wi.x, -wi.y, -wi.z});
+                v3 lcol = {0.f, 0.f, 0.f};
+                float a_pdf = 0.f;
+                if (cos_l > 0.0f) {
+                    lcol = {em[0], em[1], em[2]};
+                    a_pdf = tmax * tmax / (cos_l * area);
+                }
+                const float pdf = pdf_l * a_pdf;
+                if ((lcol.x != 0.f || lcol.y != 0.f || lcol.z != 0.f) && tmax > 0.f) {
+                    float sr[8] = {from.x, from.y, from.z, 1e-4f, wi.x, wi.y, wi.z, tmax};
+                    if (!any_hit(h, load_ray(sr), nullptr)) {
+                        uint32_t mat_id;
+                        const v3 ns = facing_normal(h.sc, ph.ref, d, mat_id);
+                        const v3 f = dl_brdf({-d.x, -d.y, -d.z}, wi, ns, m);
+                        const float cos_t = cdot3(wi, ns);
+                        rad = {lcol.x * f.x * cos_t / pdf, lcol.y * f.y * cos_t / pdf, lcol.z * f.z * cos_t / pdf};
+                    }
+                }
+            }
+        }
+        fb[0] += rad.x;
+        fb[1] += rad.y;
+        fb[2] += rad.z;
+        fb[3] += 1.0f;
+    }
+}
+
+// Direct lighting of n camera rays (8 floats each) into fb (4 floats per ray, accumulated);
+// mats8: 8 floats per material (albedo rgb, emission rgb, ior, roughness).
+void orc_direct(void *hp, const float *rays8, uint64_t n, const float *mats8, uint32_t n_mat, uint32_t samples,
+                uint64_t seed, float *fb, int threads) {
+    bvh *h = (bvh *)hp;
+    const dl_set L = make_dl_set(h->sc, mats8, n_mat);
+    set_threads(threads);
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t i = 0; i < (int64_t)n; ++i)
+        dl_pixel(*h, L, rays8 + 8 * i, (uint32_t)i, (uint32_t)n, samples, seed, fb + 4 * i);
+}
+
 int orc_max_threads() { return omp_get_max_threads(); }
 
 void orc_free(void *hp) { delete (bvh *)hp; }
