@@ -19,7 +19,8 @@ from . import _libs
 GRT_OK = 0
 STATUS_NAMES = {0: "GRT_OK", 1: "GRT_ERR_INVALID_ARG", 2: "GRT_ERR_OOM", 3: "GRT_ERR_CUDA", 4: "GRT_ERR_TIMEOUT",
                 5: "GRT_ERR_BVH_TOO_DEEP", 6: "GRT_ERR_NOT_BUILT", 7: "GRT_ERR_TRAVERSAL",
-                8: "GRT_ERR_UNKNOWN_TRACER", 9: "GRT_ERR_NO_DEVICE", 10: "GRT_ERR_TOO_LARGE"}
+                8: "GRT_ERR_UNKNOWN_TRACER", 9: "GRT_ERR_NO_DEVICE", 10: "GRT_ERR_TOO_LARGE",
+                11: "GRT_ERR_ABORTED"}
 SPLIT = {"om": 0, "sm": 1, "sah": 2}
 TRACERS = ("while-while", "persistent-while-while", "if-if", "persistent-if-if", "speculative-while-while",
            "persistent-speculative-while-while", "bvh4-speculative-while-while",
@@ -112,6 +113,7 @@ _PROTOS = {
     "grt_trace": (I, [VP, VP, VP, U32, I, VP]),
     "grt_trace_host": (I, [VP, VP, VP, U32, I]),
     "grt_check": (I, [VP, VP, U32]),
+    "grt_abort": (I, [VP]),
     "grt_set_traversal_counters": (I, [VP, VP]),
     "grt_compact_hits": (I, [VP, VP, U32, VP, VP, VP]),
     "grt_shadow_rays": (I, [VP, VP, VP, U32, P(ctypes.c_float), ctypes.c_float, VP, VP, VP]),
@@ -398,6 +400,11 @@ class BatchRayTracer:
 
     def check(self, stream=None, timeout_ms: int = 0):
         self._check(lib().grt_check(self.ctx, VP(stream or 0), timeout_ms))
+
+    def abort(self):
+        """grt_abort: the context's persistent kernels stop taking work until the next check();
+        callable from another thread while this one waits in check()."""
+        self._check(lib().grt_abort(self.ctx))
 
     def trace_host(self, rays: np.ndarray, any_hit=False, hits: np.ndarray | None = None) -> np.ndarray:
         r = np.ascontiguousarray(rays, np.float32)

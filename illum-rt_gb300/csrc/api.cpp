@@ -5,6 +5,7 @@
 // pointers, sizes and status codes.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -45,10 +46,17 @@ grt_status grt_create(const grt_config *cfg, grt_ctx **out) {
     c->device = dev;
     device_guard g(dev);
     cudaError_t e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e == cudaSuccess) e = cudaMalloc(&c->d_err, 2 * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_err, grt::kStatusWords * sizeof(unsigned));
     if (e == cudaSuccess) {
-        c->d_counter = c->d_err + 1;
-        e = cudaMemset(c->d_err, 0, 2 * sizeof(unsigned));
+        c->d_counter = c->d_err + grt::kStatusCounter;
+        e = cudaMemset(c->d_err, 0, grt::kStatusWords * sizeof(unsigned));
+    }
+    if (e == cudaSuccess) e = cudaHostAlloc((void **)&c->h_flag, 3 * sizeof(unsigned), cudaHostAllocDefault);
+    if (e == cudaSuccess) {
+        c->h_flag[0] = 1u;
+        c->h_flag[1] = 0u;
+        c->h_flag[2] = grt::kAbortCounter;
+        e = cudaStreamCreateWithFlags(&c->abort_stream, cudaStreamNonBlocking);
     }
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = grt::prepare_trace_kernels();
@@ -58,6 +66,8 @@ grt_status grt_create(const grt_config *cfg, grt_ctx **out) {
     if (e != cudaSuccess) {
         cudaGetLastError();
         if (c->d_err) cudaFree(c->d_err);
+        if (c->h_flag) cudaFreeHost(c->h_flag);
+        if (c->abort_stream) cudaStreamDestroy(c->abort_stream);
         delete c;
         return e == cudaErrorMemoryAllocation ? GRT_ERR_OOM : GRT_ERR_CUDA;
     }
@@ -77,6 +87,8 @@ grt_status grt_destroy(grt_ctx *c) {
         if (c->d_dl_scratch) cudaFree(c->d_dl_scratch);
         if (c->pt_graph.exec) cudaGraphExecDestroy(c->pt_graph.exec);
         if (c->d_err) cudaFree(c->d_err);
+        if (c->h_flag) cudaFreeHost(c->h_flag);
+        if (c->abort_stream) cudaStreamDestroy(c->abort_stream);
         if (c->stream) cudaStreamDestroy(c->stream);
     }
     delete c;
@@ -332,29 +344,85 @@ grt_status grt_set_traversal_counters(grt_ctx *c, unsigned long long *counters_d
     return GRT_OK;
 }
 
+namespace {
+
+// Raises (raise = true) or clears the abort request, on the abort stream. Raising also moves the
+// persistent kernels' work counter far past any ray count, so that a running persistent kernel
+// finds no more work at its next fetch.
+cudaError_t set_abort(grt_ctx *c, bool raise) {
+    cudaError_t e = cudaMemcpyAsync(c->d_err + grt::kStatusAbort, c->h_flag + (raise ? 0 : 1), sizeof(unsigned),
+                                    cudaMemcpyHostToDevice, c->abort_stream);
+    if (e == cudaSuccess && raise)
+        e = cudaMemcpyAsync(c->d_err + grt::kStatusCounter, c->h_flag + 2, sizeof(unsigned), cudaMemcpyHostToDevice,
+                            c->abort_stream);
+    return e == cudaSuccess ? cudaStreamSynchronize(c->abort_stream) : e;
+}
+
+// Polls the stream until it is idle or `limit_ms` passes (0: no limit); true when idle.
+bool wait_stream(cudaStream_t st, uint32_t limit_ms, cudaError_t &err) {
+    const auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        const cudaError_t q = cudaStreamQuery(st);
+        if (q == cudaSuccess) return true;
+        if (q != cudaErrorNotReady) {
+            err = q;
+            return false;
+        }
+        if (limit_ms && ms_since(t0) > limit_ms) return false;
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+}
+
+}  // namespace
+
+grt_status grt_abort(grt_ctx *c) {
+    if (!c) return GRT_ERR_INVALID_ARG;
+    device_guard g(c->device);
+    const cudaError_t e = set_abort(c, true);
+    return e == cudaSuccess ? GRT_OK : cuda_fail(c, e, "raising the abort request");
+}
+
 grt_status grt_check(grt_ctx *c, grt_stream_t stream, uint32_t timeout_ms) {
     if (!c) return GRT_ERR_INVALID_ARG;
     device_guard g(c->device);
     cudaStream_t st = (cudaStream_t)stream;
-    auto t0 = std::chrono::steady_clock::now();
-    for (;;) {
-        cudaError_t q = cudaStreamQuery(st);
-        if (q == cudaSuccess) break;
-        if (q != cudaErrorNotReady) return cuda_fail(c, q, "waiting for the stream");
-        if (timeout_ms && ms_since(t0) > timeout_ms)
-            return fail(c, GRT_ERR_TIMEOUT, "stream did not finish within " + std::to_string(timeout_ms) + " ms");
-        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    cudaError_t e = cudaSuccess;
+    bool timed_out = false;
+    if (!wait_stream(st, timeout_ms, e)) {
+        if (e != cudaSuccess) return cuda_fail(c, e, "waiting for the stream");
+        // stop the work in flight: persistent kernels finish the rays they hold and take no more
+        timed_out = true;
+        e = set_abort(c, true);
+        if (e != cudaSuccess) return cuda_fail(c, e, "raising the abort request");
+        const uint32_t drain_ms = std::max<uint32_t>(2000u, timeout_ms);
+        if (!wait_stream(st, drain_ms, e)) {
+            if (e != cudaSuccess) return cuda_fail(c, e, "waiting for the aborted stream");
+            return fail(c, GRT_ERR_TIMEOUT, "stream did not finish within " + std::to_string(timeout_ms) +
+                                                " ms and had not stopped " + std::to_string(drain_ms) +
+                                                " ms after the abort request, which stays raised");
+        }
     }
-    unsigned bits = 0;
-    cudaError_t e = cudaMemcpy(&bits, c->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) return cuda_fail(c, e, "reading the kernel error word");
-    if (bits) {
-        cudaMemset(c->d_err, 0, sizeof(unsigned));
+    unsigned status[grt::kStatusWords] = {0};
+    e = cudaMemcpy(status, c->d_err, sizeof(status), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(c, e, "reading the kernel status");
+    const unsigned bits = status[grt::kStatusErr];
+    const bool raised = status[grt::kStatusAbort] != 0u;
+    if (raised) {
+        e = set_abort(c, false);  // the stream is idle: later launches run normally again
+        if (e != cudaSuccess) return cuda_fail(c, e, "clearing the abort request");
+    }
+    if (bits) cudaMemset(c->d_err, 0, sizeof(unsigned));
+    if (timed_out)
+        return fail(c, GRT_ERR_TIMEOUT, "stream did not finish within " + std::to_string(timeout_ms) +
+                                            " ms; the work in flight was aborted and its outputs are incomplete");
+    if (bits & (grt::ERR_STACK_OVERFLOW | grt::ERR_STEP_LIMIT)) {
         std::string m = "traversal kernel reported:";
         if (bits & grt::ERR_STACK_OVERFLOW) m += " stack overflow";
         if (bits & grt::ERR_STEP_LIMIT) m += " step limit";
         return fail(c, GRT_ERR_TRAVERSAL, m);
     }
+    if (raised || (bits & grt::ERR_ABORTED))
+        return fail(c, GRT_ERR_ABORTED, "work stopped early after grt_abort; its outputs are incomplete");
     return GRT_OK;
 }
 

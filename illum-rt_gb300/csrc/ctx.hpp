@@ -26,8 +26,10 @@ struct grt_ctx {
     grt_bvh_stats stats{};
     int tracer = 0;  // index into kTracers
     grt_tuning tuning{};
-    unsigned *d_err = nullptr;      // error bits ORed in by kernels
-    unsigned *d_counter = nullptr;  // ray counter of the persistent kernel
+    unsigned *d_err = nullptr;      // status block (grt_internal.hpp): error bits, counter, abort request
+    unsigned *d_counter = nullptr;  // work counter of the persistent kernels (d_err + 1)
+    unsigned *h_flag = nullptr;     // pinned {1, 0, kAbortCounter}: the words grt_abort / grt_check write
+    cudaStream_t abort_stream = nullptr;  // non-blocking stream of those writes
     void *d_stage = nullptr;        // grt_trace_host staging: rays then hits
     size_t stage_bytes = 0;
     cudaStream_t stream = nullptr;  // grt_trace_host stream

@@ -159,6 +159,7 @@ __global__ void __launch_bounds__(256) k_dl_fused(dev_scene sc, dl_scene ds, con
                                                   uint32_t n, uint32_t samples, uint64_t seed, float4 *fb,
                                                   unsigned *err, unsigned *counter) {
     extern __shared__ int s_stack[];
+    if (stop_requested_at_entry(err)) return;  // the host asked the context to stop
     constexpr bool WIDE = ORDER == WIDE_SPECULATIVE;
     const unsigned lane = threadIdx.x & 31u;
     int *stk = s_stack + threadIdx.x;

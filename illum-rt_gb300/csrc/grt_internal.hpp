@@ -31,7 +31,31 @@ struct dev_scene {
 };
 
 // Bits a kernel ORs into the context's error word.
-enum : unsigned { ERR_STACK_OVERFLOW = 1u, ERR_STEP_LIMIT = 2u };
+enum : unsigned { ERR_STACK_OVERFLOW = 1u, ERR_STEP_LIMIT = 2u, ERR_ABORTED = 4u };
+
+// The context's status block in device memory: [0] error bits, [1] work counter of the
+// persistent kernels, [32] abort request (alone in its 128-byte line, away from the counter's
+// atomics). Kernels receive a pointer to word 0 (`err`). To stop work, the host writes the
+// abort request and a huge value into the counter, both with copy-engine writes on a stream of
+// their own so that they land while kernels run: a running persistent kernel then finds its
+// counter exhausted at its next fetch and ends, with no extra work in its loop, and a
+// persistent kernel that starts later reads the request once per warp on entry and does
+// nothing. One-thread-per-ray kernels are not stopped: each is bounded by its ray count.
+enum : int { kStatusErr = 0, kStatusCounter = 1, kStatusAbort = 32, kStatusWords = 64 };
+static const unsigned kAbortCounter = 0xC0000000u;  // far beyond any ray count, far below 2^32
+
+#ifdef __CUDACC__
+// Warp-uniform entry check: true (and ERR_ABORTED recorded) when the host has asked the
+// context's kernels to stop. All 32 lanes must call it before any lane leaves.
+__device__ __forceinline__ bool stop_requested_at_entry(unsigned *err) {
+    unsigned stop = 0;
+    if ((threadIdx.x & 31u) == 0) {
+        stop = *((const volatile unsigned *)(err + kStatusAbort)) != 0u ? 1u : 0u;
+        if (stop) atomicOr(err, ERR_ABORTED);
+    }
+    return __shfl_sync(0xffffffffu, stop, 0) != 0u;
+}
+#endif
 
 // Stack variants compiled into the library (entries per thread, shared memory).
 static const int kStackSmall = 32;

@@ -404,6 +404,7 @@ __global__ void __launch_bounds__(256) k_pt_fused(dev_scene sc, pt_scene ps, pt_
                                                   grt_path_result *results, grt_hit *bounce_hits, unsigned *err,
                                                   unsigned *counter, int refill_threshold, int refill_period) {
     extern __shared__ int s_stack[];
+    if (stop_requested_at_entry(err)) return;  // the host asked the context to stop
     const unsigned lane = threadIdx.x & 31u;
     const unsigned lanes_below = (1u << lane) - 1u;
     int *stk = s_stack + threadIdx.x;

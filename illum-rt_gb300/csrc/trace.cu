@@ -60,6 +60,7 @@ __global__ void __launch_bounds__(256) k_trace_persistent(const float4 *__restri
                                                           uint32_t n, dev_scene sc, unsigned *err,
                                                           unsigned *counter, int refill_threshold, int refill_period) {
     extern __shared__ int s_stack[];
+    if (stop_requested_at_entry(err)) return;  // the host asked the context to stop
     constexpr bool SPEC = ORDER == SPECULATIVE || ORDER == WIDE_SPECULATIVE;
     constexpr bool WIDE = ORDER == WIDE_SPECULATIVE;
     const unsigned lane = threadIdx.x & 31u;

@@ -56,7 +56,8 @@ typedef enum grt_status {
     GRT_ERR_TRAVERSAL = 7,      /* a kernel flagged a stack overflow or hit its step limit */
     GRT_ERR_UNKNOWN_TRACER = 8, /* grt_select_tracer: no tracer of that name */
     GRT_ERR_NO_DEVICE = 9,      /* no CUDA device of the requested ordinal */
-    GRT_ERR_TOO_LARGE = 10      /* input exceeds the fixed capacity of grt_compact_hits_static */
+    GRT_ERR_TOO_LARGE = 10,     /* input exceeds the fixed capacity of grt_compact_hits_static */
+    GRT_ERR_ABORTED = 11        /* work stopped early after grt_abort; its outputs are incomplete */
 } grt_status;
 
 /* One hit record, 16 bytes, the layout of wf::cuda::tri_is (rt/cuda/base.h:32-41).
@@ -206,8 +207,23 @@ grt_status grt_trace_host(grt_ctx *ctx, const float *rays_host, grt_hit *hits_ho
 grt_status grt_set_traversal_counters(grt_ctx *ctx, unsigned long long *counters_dev);
 
 /* Waits for `stream` (at most timeout_ms milliseconds; 0 = no limit) and returns the first
- * error flagged by a kernel since the previous check. */
+ * error flagged by a kernel since the previous check. When the limit passes, it raises the
+ * abort request (grt_abort), waits for the work in flight to stop, clears the request and
+ * returns GRT_ERR_TIMEOUT: the context stays usable, the outputs of the aborted launches are
+ * incomplete. A request raised by grt_abort is cleared once the stream has finished, and the
+ * result is then GRT_ERR_ABORTED. */
 grt_status grt_check(grt_ctx *ctx, grt_stream_t stream, uint32_t timeout_ms);
+
+/* Asks the context's kernels to stop: a running persistent kernel (the persistent tracers, the
+ * fused path tracer, scene sets, fused direct lighting) takes no further rays, paths or pixels
+ * (those in flight finish), and persistent launches that start later do nothing, until
+ * grt_check clears the request; one-thread-per-ray launches run to the end, each bounded by its
+ * ray count. The request is a pair of copy-engine writes on a stream of its own, so it reaches
+ * kernels that are running and costs them nothing while it is not raised; grt_abort may be
+ * called from another host thread while the context's owner waits in grt_check. The reference
+ * has no way to stop a launch (its error path resets the device,
+ * rt/cuda/cuda-helpers.cpp:5-12). */
+grt_status grt_abort(grt_ctx *ctx);
 
 /* ---- ray generation steps around the traversal ---------------------------------------- */
 
