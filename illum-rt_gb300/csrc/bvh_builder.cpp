@@ -400,12 +400,18 @@ bool flatten_bvh(const ref_tree &tree, const float *vpos4, const uint32_t *tris4
         const ref_node &n = N[i];
         float *d = out.nodes.data() + (size_t)inner_id[i] * 16;
         int32_t cl = child_ref(n.link_l, ok), cr = child_ref(n.link_r, ok);
-        std::memcpy(d + 0, n.lmin, 12);
-        std::memcpy(d + 3, &cl, 4);
-        std::memcpy(d + 4, n.lmax, 12);
-        std::memcpy(d + 8, n.rmin, 12);
-        std::memcpy(d + 11, &cr, 4);
-        std::memcpy(d + 12, n.rmax, 12);
+        const float *lo[2] = {n.lmin, n.rmin}, *hi[2] = {n.lmax, n.rmax};
+        const int32_t ref[2] = {cl, cr};
+        for (int side = 0; side < 2; ++side) {
+            float *e = d + 8 * side;
+            e[0] = lo[side][0];
+            e[1] = lo[side][1];
+            e[2] = hi[side][0];
+            e[3] = hi[side][1];
+            e[4] = lo[side][2];
+            e[5] = hi[side][2];
+            std::memcpy(e + 6, &ref[side], 4);
+        }
     }
     const ref_node &root = N[tree.root];
     if (root.inner()) {

@@ -35,11 +35,10 @@ bool build_reference_bvh(const float *vpos4, uint32_t nv, const uint32_t *tris4,
 
 // Device layout produced from a reference tree.
 //
-// Node (64 bytes, four float4):
-//   [0] left  box min xyz, w = left child reference (int bits)
-//   [1] left  box max xyz, w = 0
-//   [2] right box min xyz, w = right child reference (int bits)
-//   [3] right box max xyz, w = 0
+// Node (64 bytes): two 32-byte child records, left then right, each
+//   (min.x, min.y, max.x, max.y, min.z, max.z, child reference as int bits, 0)
+// so that the slab test's x/y bounds pair with the ray's (o.x, o.y) and the z bounds with
+// (o.z, o.z) as packed f32x2 operands (traverse.cuh).
 // A child reference c >= 0 is an inner node index; c < 0 is a leaf with ~c = (first << 4) |
 // (count - 1), `first` indexing the triangle records, so leaves never need a fetch of their own.
 // Triangle record (48 bytes, three float4), in leaf order:

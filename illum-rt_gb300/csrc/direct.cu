@@ -88,19 +88,7 @@ __device__ __forceinline__ float4 plus(float4 a, f3 b, float w) {
 }
 
 __device__ __forceinline__ ray_t shadow_ray(f3 o, f3 d, float tmax) {
-    ray_t r;
-    r.ox = o.x;
-    r.oy = o.y;
-    r.oz = o.z;
-    r.tmin = dl::kEps;  // the shadow ray's t_min (bounce.cu:246)
-    r.dx = d.x;
-    r.dy = d.y;
-    r.dz = d.z;
-    r.tmax = tmax;
-    r.ix = __fdiv_rn(1.0f, d.x);
-    r.iy = __fdiv_rn(1.0f, d.y);
-    r.iz = __fdiv_rn(1.0f, d.z);
-    return r;
+    return make_ray(o.x, o.y, o.z, d.x, d.y, d.z, dl::kEps, tmax);  // the shadow ray's t_min (bounce.cu:246)
 }
 
 __global__ void __launch_bounds__(256) k_dl_sample(dl_scene ds, const float4 *__restrict__ rays,
@@ -174,9 +162,9 @@ __global__ void __launch_bounds__(256) k_dl_fused(dev_scene sc, dl_scene ds, con
         ray_t r = {};
         trav_t s;
         if (active) r = load_ray(rays, pix);
-        const f3 o = {r.ox, r.oy, r.oz}, d = {r.dx, r.dy, r.dz};
+        const f3 o = {r.ox(), r.oy(), r.oz()}, d = {r.dx, r.dy, r.dz};
         float4 acc = active ? fb[pix] : make_float4(0.f, 0.f, 0.f, 0.f);
-        trav_init(s, sc, WIDE);
+        trav_init(s, sc, r, WIDE);
         bool plain = active && sc.finite && ray_is_plain(r);
         trace_all<ORDER, STACK, false>(s, active, plain, sc, r, stk, stride, err);
         const float ht = active ? s.hit.t : FLT_MAX;
@@ -189,7 +177,7 @@ __global__ void __launch_bounds__(256) k_dl_fused(dev_scene sc, dl_scene ds, con
             }
             const bool shoot = active && p.tmax > 0.f;  // a shadow ray that can find an occluder
             if (shoot) r = shadow_ray(p.org, p.dir, p.tmax);
-            trav_init(s, sc, WIDE);
+            trav_init(s, sc, r, WIDE);
             plain = shoot && sc.finite && ray_is_plain(r);
             trace_all<ORDER, STACK, true>(s, shoot, plain, sc, r, stk, stride, err);
             if (active) {

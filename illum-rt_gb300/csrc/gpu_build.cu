@@ -242,10 +242,10 @@ __global__ void __launch_bounds__(kThreads) k_bottom_up(const float4 *__restrict
             const int m = max(ai ? a.meta.z : 0, bi ? b.meta.z : 0);
             p.meta = make_int4(node, 1 + max(a.meta.y, b.meta.y), bnd, m);
             float4 *o = nodes + 4 * (size_t)node;
-            o[0] = make_float4(a.lo.x, a.lo.y, a.lo.z, __int_as_float(a.meta.x));
-            o[1] = make_float4(a.hi.x, a.hi.y, a.hi.z, 0.f);
-            o[2] = make_float4(b.lo.x, b.lo.y, b.lo.z, __int_as_float(b.meta.x));
-            o[3] = make_float4(b.hi.x, b.hi.y, b.hi.z, 0.f);
+            o[0] = make_float4(a.lo.x, a.lo.y, a.hi.x, a.hi.y);
+            o[1] = make_float4(a.lo.z, a.hi.z, __int_as_float(a.meta.x), 0.f);
+            o[2] = make_float4(b.lo.x, b.lo.y, b.hi.x, b.hi.y);
+            o[3] = make_float4(b.lo.z, b.hi.z, __int_as_float(b.meta.x), 0.f);
         }
         p.hi.w = cnt;
         if (node == 0) {
@@ -345,22 +345,22 @@ __global__ void __launch_bounds__(kThreads) k_wide_nodes(const float4 *__restric
     int k = 0;
     const float4 *np = nodes + 4 * (size_t)p;
     for (int side = 0; side < 2; ++side) {
-        const float4 bl = np[2 * side], bh = np[2 * side + 1];
-        const int c = __float_as_int(bl.w);
+        const float4 bxy = np[2 * side], bz = np[2 * side + 1];  // (lo.x, lo.y, hi.x, hi.y), (lo.z, hi.z, ref, 0)
+        const int c = __float_as_int(bz.z);
         if (c >= n - 1) return;  // not a node of this tree (never for a tree of k_bottom_up)
         if (c >= 0) {
             const float4 *cp = nodes + 4 * (size_t)c;
             for (int g = 0; g < 2; ++g) {
-                const float4 gl = cp[2 * g], gh = cp[2 * g + 1];
-                const int gc = __float_as_int(gl.w);
+                const float4 gxy = cp[2 * g], gz = cp[2 * g + 1];
+                const int gc = __float_as_int(gz.z);
                 if (gc >= n - 1) return;
-                lo[0][k] = gl.x, lo[1][k] = gl.y, lo[2][k] = gl.z;
-                hi[0][k] = gh.x, hi[1][k] = gh.y, hi[2][k] = gh.z;
+                lo[0][k] = gxy.x, lo[1][k] = gxy.y, lo[2][k] = gz.x;
+                hi[0][k] = gxy.z, hi[1][k] = gxy.w, hi[2][k] = gz.y;
                 ref[k++] = gc >= 0 ? wide_index[gc] : gc;
             }
         } else {
-            lo[0][k] = bl.x, lo[1][k] = bl.y, lo[2][k] = bl.z;
-            hi[0][k] = bh.x, hi[1][k] = bh.y, hi[2][k] = bh.z;
+            lo[0][k] = bxy.x, lo[1][k] = bxy.y, lo[2][k] = bz.x;
+            hi[0][k] = bxy.z, hi[1][k] = bxy.w, hi[2][k] = bz.y;
             ref[k++] = c;
         }
     }

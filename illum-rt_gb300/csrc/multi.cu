@@ -65,7 +65,7 @@ __global__ void __launch_bounds__(256) k_trace_multi(const dev_scene *__restrict
                         sc = scenes[mb.scene];
                         hits = mb.hits;
                         r = load_ray(mb.rays, idx);
-                        trav_init(s, sc, WIDE);
+                        trav_init(s, sc, r, WIDE);
                         plain = sc.finite && ray_is_plain(r);
                         have = true;
                         if (s.done) {  // empty scene

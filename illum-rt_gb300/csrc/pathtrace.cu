@@ -287,19 +287,7 @@ __device__ __forceinline__ void clear_unused(grt_hit *bounce_hits, const pt_para
 }
 
 __device__ __forceinline__ ray_t make_ray(pm::f3 o, pm::f3 d, float tmin, float tmax) {
-    ray_t r;
-    r.ox = o.x;
-    r.oy = o.y;
-    r.oz = o.z;
-    r.tmin = tmin;
-    r.dx = d.x;
-    r.dy = d.y;
-    r.dz = d.z;
-    r.tmax = tmax;
-    r.ix = __fdiv_rn(1.0f, d.x);
-    r.iy = __fdiv_rn(1.0f, d.y);
-    r.iz = __fdiv_rn(1.0f, d.z);
-    return r;
+    return grt::make_ray(o.x, o.y, o.z, d.x, d.y, d.z, tmin, tmax);
 }
 
 // ---- wavefront form -----------------------------------------------------------------------
@@ -426,12 +414,12 @@ __global__ void __launch_bounds__(256) k_pt_fused(dev_scene sc, pt_scene ps, pt_
             path_t st;
             const uint32_t p = path_load(slots, me, pp.seed, st);
             record_bounce(bounce_hits, pp, p, st.bounce, s.hit);
-            pm::f3 o = {r.ox, r.oy, r.oz}, d = {r.dx, r.dy, r.dz};
+            pm::f3 o = {r.ox(), r.oy(), r.oz()}, d = {r.dx, r.dy, r.dz};
             grt_path_result res;
             if (path_bounce<true>(ps, sc.records, pp, st, s.hit, o, d, res)) {
                 path_save(slots, me, p, st);
                 r = make_ray(o, d, pp.eps, FLT_MAX);
-                trav_init(s, sc, WIDE);
+                trav_init(s, sc, r, WIDE);
                 plain = sc.finite && ray_is_plain(r);
                 tracing = true;
             } else {
@@ -460,7 +448,7 @@ __global__ void __launch_bounds__(256) k_pt_fused(dev_scene sc, pt_scene ps, pt_
                             path_start(ps, pp, my, prim_rays, prim_hits, hit_list, nl, st, ro, rd);
                             path_save(slots, me, my, st);
                             r = make_ray({ro.x, ro.y, ro.z}, {rd.x, rd.y, rd.z}, ro.w, rd.w);
-                            trav_init(s, sc, WIDE);
+                            trav_init(s, sc, r, WIDE);
                             plain = sc.finite && ray_is_plain(r);
                             tracing = true;
                         }

@@ -34,7 +34,7 @@ __global__ void __launch_bounds__(256) k_trace_plain(const float4 *__restrict__ 
     ray_t r = {};
     if (active) r = load_ray(rays, i);
     trav_t s;
-    trav_init(s, sc, WIDE);
+    trav_init(s, sc, r, WIDE);
     int *stk = s_stack + threadIdx.x;
     const int stride = blockDim.x;
     const bool plain = active && sc.finite && ray_is_plain(r);
@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(256) k_trace_persistent(const float4 *__restri
                     if (my < n) {
                         idx = my;
                         r = load_ray(rays, my);
-                        trav_init(s, sc, WIDE);
+                        trav_init(s, sc, r, WIDE);
                         plain = sc.finite && ray_is_plain(r);
                         have = true;
                         if (s.done) {  // empty scene

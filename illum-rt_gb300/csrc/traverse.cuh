@@ -18,9 +18,93 @@
 
 namespace grt {
 
+// A ray: origin and 1/d (libgi/rt.h:24-31) in packed f32x2 pairs, the operands of the slab
+// test (low word first): (o.x, o.y), (o.z, o.z), (1/d.x, 1/d.y), (1/d.z, 1/d.z).
 struct ray_t {
-    float ox, oy, oz, dx, dy, dz, ix, iy, iz, tmin, tmax;
+    uint64_t oxy, ozz, ixy, izz;
+    float dx, dy, dz, tmin, tmax;
+    __device__ __forceinline__ float ox() const;
+    __device__ __forceinline__ float oy() const;
+    __device__ __forceinline__ float oz() const;
+    __device__ __forceinline__ float ix() const;
+    __device__ __forceinline__ float iy() const;
+    __device__ __forceinline__ float iz() const;
 };
+
+// Two f32 values in one 64-bit register, `lo` in the low word (the lower address in memory).
+__device__ __forceinline__ uint64_t pk2(float lo, float hi) {
+    uint64_t v;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(v) : "f"(lo), "f"(hi));
+    return v;
+}
+__device__ __forceinline__ void upk2(uint64_t v, float &lo, float &hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+// Packed subtraction and product (sm_100 and later): each of the two lanes is rounded to
+// nearest as the scalar sub.rn.f32 / mul.rn.f32 would round it, so results keep their bits.
+__device__ __forceinline__ uint64_t sub2(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t mul2(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+// Three-input minimum and maximum (sm_100 and later), used on operands that are never NaN.
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
+__device__ __forceinline__ float lo2(uint64_t v) {
+    float a, b;
+    upk2(v, a, b);
+    return a;
+}
+__device__ __forceinline__ float hi2(uint64_t v) {
+    float a, b;
+    upk2(v, a, b);
+    return b;
+}
+__device__ __forceinline__ float ray_t::ox() const { return lo2(oxy); }
+__device__ __forceinline__ float ray_t::oy() const { return hi2(oxy); }
+__device__ __forceinline__ float ray_t::oz() const { return lo2(ozz); }
+__device__ __forceinline__ float ray_t::ix() const { return lo2(ixy); }
+__device__ __forceinline__ float ray_t::iy() const { return hi2(ixy); }
+__device__ __forceinline__ float ray_t::iz() const { return lo2(izz); }
+
+// A ray from its origin, direction and [t_min, t_max]; ray::ray computes id = 1/d in IEEE
+// float (libgi/rt.h:28).
+__device__ __forceinline__ ray_t make_ray(float ox, float oy, float oz, float dx, float dy, float dz, float tmin,
+                                          float tmax) {
+    ray_t r;
+    const float ix = __fdiv_rn(1.0f, dx), iy = __fdiv_rn(1.0f, dy), iz = __fdiv_rn(1.0f, dz);
+    r.oxy = pk2(ox, oy);
+    r.ozz = pk2(oz, oz);
+    r.ixy = pk2(ix, iy);
+    r.izz = pk2(iz, iz);
+    r.dx = dx;
+    r.dy = dy;
+    r.dz = dz;
+    r.tmin = tmin;
+    r.tmax = tmax;
+    return r;
+}
+
+// The largest float below x (x not NaN): t < x exactly when t <= below(x), for any t that is
+// not NaN.
+__device__ __forceinline__ float below(float x) {
+    const uint32_t u = __float_as_uint(x);
+    return __uint_as_float(x > 0.f ? u - 1u : (x == 0.f ? 0x80000001u : u + 1u));
+}
 
 struct hit_t {
     float t, b, g;
@@ -30,20 +114,7 @@ struct hit_t {
 
 __device__ __forceinline__ ray_t load_ray(const float4 *__restrict__ rays, uint32_t i) {
     const float4 a = __ldg(rays + 2 * (size_t)i), d = __ldg(rays + 2 * (size_t)i + 1);
-    ray_t r;
-    r.ox = a.x;
-    r.oy = a.y;
-    r.oz = a.z;
-    r.tmin = a.w;
-    r.dx = d.x;
-    r.dy = d.y;
-    r.dz = d.z;
-    r.tmax = d.w;
-    // ray::ray computes id = 1/d in IEEE float (libgi/rt.h:28)
-    r.ix = __fdiv_rn(1.0f, d.x);
-    r.iy = __fdiv_rn(1.0f, d.y);
-    r.iz = __fdiv_rn(1.0f, d.z);
-    return r;
+    return make_ray(a.x, a.y, a.z, d.x, d.y, d.z, a.w, d.w);
 }
 
 __device__ __forceinline__ bool finite_nonzero(float x) { return isfinite(x) && x != 0.f; }
@@ -52,16 +123,16 @@ __device__ __forceinline__ bool finite_nonzero(float x) { return isfinite(x) && 
 // 1/d finite and non-zero. Then min/max instructions give exactly the reference's selects
 // (they differ only on NaN operands, and on the sign of zero, which no comparison sees).
 __device__ __forceinline__ bool ray_is_plain(const ray_t &r) {
-    return finite_nonzero(r.ix) && finite_nonzero(r.iy) && finite_nonzero(r.iz) && isfinite(r.ox) &&
-           isfinite(r.oy) && isfinite(r.oz);
+    return finite_nonzero(r.ix()) && finite_nonzero(r.iy()) && finite_nonzero(r.iz()) && isfinite(r.ox()) &&
+           isfinite(r.oy()) && isfinite(r.oz());
 }
 
 template <bool PLAIN>
 __device__ __forceinline__ bool slab(float lx, float ly, float lz, float hx, float hy, float hz, const ray_t &r,
                                      float &tnear) {
-    const float ax = __fmul_rn(__fsub_rn(lx, r.ox), r.ix), bx = __fmul_rn(__fsub_rn(hx, r.ox), r.ix);
-    const float ay = __fmul_rn(__fsub_rn(ly, r.oy), r.iy), by = __fmul_rn(__fsub_rn(hy, r.oy), r.iy);
-    const float az = __fmul_rn(__fsub_rn(lz, r.oz), r.iz), bz = __fmul_rn(__fsub_rn(hz, r.oz), r.iz);
+    const float ax = __fmul_rn(__fsub_rn(lx, r.ox()), r.ix()), bx = __fmul_rn(__fsub_rn(hx, r.ox()), r.ix());
+    const float ay = __fmul_rn(__fsub_rn(ly, r.oy()), r.iy()), by = __fmul_rn(__fsub_rn(hy, r.oy()), r.iy());
+    const float az = __fmul_rn(__fsub_rn(lz, r.oz()), r.iz()), bz = __fmul_rn(__fsub_rn(hz, r.oz()), r.iz());
     float t1, t2;
     if (PLAIN) {
         t1 = fmaxf(fmaxf(fminf(ax, bx), fminf(ay, by)), fminf(az, bz));
@@ -77,6 +148,24 @@ __device__ __forceinline__ bool slab(float lx, float ly, float lz, float hx, flo
     }
     tnear = t1;
     return !(t1 > t2) && !(t2 < r.tmin) && !(t1 > r.tmax);
+}
+
+// The slab test of a plain ray (ray_is_plain) against one child record of a binary node,
+// (lo.x, lo.y, hi.x, hi.y) in `xy` pairs and (lo.z, hi.z) in `z`: the six differences and six
+// products of slab() as three packed operations each, the same bits. With no NaN among the
+// products, slab()'s !(t1 > t2) && !(t1 > t_max), and the closest-hit cull t1 < t_closest, are
+// together t1 <= min(t2, lim) for lim = t_max (any hit) or min(t_max, below(t_closest)), a
+// NaN t_max dropping out of the minimum as it drops out of slab()'s comparison.
+__device__ __forceinline__ bool slab2(uint64_t xy_lo, uint64_t xy_hi, uint64_t z, const ray_t &r, float lim,
+                                      float &tnear) {
+    float ax, ay, bx, by, az, bz;
+    upk2(mul2(sub2(xy_lo, r.oxy), r.ixy), ax, ay);
+    upk2(mul2(sub2(xy_hi, r.oxy), r.ixy), bx, by);
+    upk2(mul2(sub2(z, r.ozz), r.izz), az, bz);
+    const float t1 = max3f(fminf(ax, bx), fminf(ay, by), fminf(az, bz));
+    const float t2 = min3f(fmaxf(ax, bx), fmaxf(ay, by), fmaxf(az, bz));
+    tnear = t1;
+    return t1 <= fminf(t2, lim) && !(t2 < r.tmin);
 }
 
 // Cramer's rule test of the reference (libgi/intersect.h:36-67) on a triangle record
@@ -97,7 +186,7 @@ __device__ __forceinline__ bool tri_test(const float4 &p0, const float4 &p1, con
     const float a = p1.x, b = p1.y, c = p1.z;
     const float d = p2.x, e = p2.y, f = p2.z;
     const float g = r.dx, h = r.dy, i = r.dz;
-    const float j = __fsub_rn(p0.x, r.ox), k = __fsub_rn(p0.y, r.oy), l = __fsub_rn(p0.z, r.oz);
+    const float j = __fsub_rn(p0.x, r.ox()), k = __fsub_rn(p0.y, r.oy()), l = __fsub_rn(p0.z, r.oz());
     float c1 = __fsub_rn(__fmul_rn(e, i), __fmul_rn(h, f));
     float c2 = __fsub_rn(__fmul_rn(g, f), __fmul_rn(d, i));
     float c3 = __fsub_rn(__fmul_rn(d, h), __fmul_rn(e, g));
@@ -169,6 +258,11 @@ __device__ __forceinline__ void ldg256(const float4 *p, float4 &a, float4 &b) {
         : "l"(p));
 }
 
+// One 256-bit read-only load as four 64-bit words: one child record of a binary node.
+__device__ __forceinline__ void ldg256_b64(const float4 *p, uint64_t &a, uint64_t &b, uint64_t &c, uint64_t &d) {
+    asm("ld.global.nc.v4.b64 {%0, %1, %2, %3}, [%4];" : "=l"(a), "=l"(b), "=l"(c), "=l"(d) : "l"(p));
+}
+
 // Decoding of a leaf child reference: ~ref = (first << 4) | (count - 1).
 __device__ __forceinline__ void leaf_range(int32_t ref, uint32_t &first, uint32_t &count) {
     const uint32_t v = ~(uint32_t)ref;
@@ -187,10 +281,11 @@ struct trav_t {
     bool more;     // speculative order: `cur` holds a node or leaf still to visit
     int32_t pend;  // speculative order: postponed leaf (0 = none; leaf references are negative)
     uint32_t n_inner, n_tri;  // inner nodes visited and triangles tested (counting kernels only)
+    float lim;                // min(t_max, below(hit.t)): a plain ray's closest-hit box limit
     hit_t hit;
 };
 
-__device__ __forceinline__ void trav_init(trav_t &s, const dev_scene &sc, bool wide = false) {
+__device__ __forceinline__ void trav_init(trav_t &s, const dev_scene &sc, const ray_t &r, bool wide = false) {
     s.cur = wide ? sc.root4 : sc.root;
     s.sp = 0;
     s.steps = 0;
@@ -201,10 +296,44 @@ __device__ __forceinline__ void trav_init(trav_t &s, const dev_scene &sc, bool w
     s.n_inner = 0;
     s.n_tri = 0;
     s.hit.t = FLT_MAX;
+    s.lim = fminf(r.tmax, below(FLT_MAX));
     s.hit.b = 0.f;
     s.hit.g = 0.f;
     s.hit.ref = 0u;
     s.hit.rec = 0u;
+}
+
+// Both child tests of the binary node at `np` (layout in bvh_builder.hpp): whether each child
+// is entered (its box meets the ray inside [t_min, t_max] and, for closest hits, starts before
+// the closest hit so far), its entry distance and its reference. Plain rays take slab2 with
+// the cull folded in; the others the reference's compare-and-select form.
+template <bool ANY, bool PLAIN>
+__device__ __forceinline__ void node_test(const float4 *np, const trav_t &s, const ray_t &r, bool &hl, bool &hr,
+                                          float &dl, float &dr, int32_t &cl, int32_t &cr) {
+    uint64_t l0, l1, l2, l3, r0, r1, r2, r3;
+    ldg256_b64(np, l0, l1, l2, l3);
+    ldg256_b64(np + 2, r0, r1, r2, r3);
+    cl = (int32_t)(uint32_t)l3;
+    cr = (int32_t)(uint32_t)r3;
+    if (PLAIN) {
+        const float lim = ANY ? r.tmax : s.lim;
+        hl = slab2(l0, l1, l2, r, lim, dl);
+        hr = slab2(r0, r1, r2, r, lim, dr);
+    } else {
+        float lx, ly, hx, hy, lz, hz;
+        upk2(l0, lx, ly);
+        upk2(l1, hx, hy);
+        upk2(l2, lz, hz);
+        hl = slab<false>(lx, ly, lz, hx, hy, hz, r, dl);
+        upk2(r0, lx, ly);
+        upk2(r1, hx, hy);
+        upk2(r2, lz, hz);
+        hr = slab<false>(lx, ly, lz, hx, hy, hz, r, dr);
+        if (!ANY) {
+            hl = hl && dl < s.hit.t;
+            hr = hr && dr < s.hit.t;
+        }
+    }
 }
 
 // One traversal iteration in the while-while order: inner nodes (two box tests each) until the
@@ -223,18 +352,10 @@ __device__ __forceinline__ void trav_iter(trav_t &s, const dev_scene &sc, const 
             return;
         }
         if (COUNT) ++s.n_inner;
-        const float4 *np = sc.nodes + 4 * (size_t)s.cur;
-        float4 n0, n1, n2, n3;
-        ldg256(np, n0, n1);
-        ldg256(np + 2, n2, n3);
         float dl, dr;
-        bool hl = slab<PLAIN>(n0.x, n0.y, n0.z, n1.x, n1.y, n1.z, r, dl);
-        bool hr = slab<PLAIN>(n2.x, n2.y, n2.z, n3.x, n3.y, n3.z, r, dr);
-        if (!ANY) {
-            hl = hl && dl < s.hit.t;
-            hr = hr && dr < s.hit.t;
-        }
-        const int32_t cl = __float_as_int(n0.w), cr = __float_as_int(n2.w);
+        bool hl, hr;
+        int32_t cl, cr;
+        node_test<ANY, PLAIN>(sc.nodes + 4 * (size_t)s.cur, s, r, hl, hr, dl, dr, cl, cr);
         if (hl && hr) {
             const bool left_first = dl < dr;
             if (s.sp >= STACK) {
@@ -271,6 +392,7 @@ __device__ __forceinline__ void trav_iter(trav_t &s, const dev_scene &sc, const 
         if (tri_test(p0, p1, p2, r, ANY ? r.tmax : fminf(r.tmax, s.hit.t), t, b, g) && (ANY || t < s.hit.t) &&
                 (!ALPHA || alpha_opaque(sc.alpha, __float_as_uint(p0.w), __float_as_uint(p1.w), b, g))) {
             s.hit.t = t;
+            if (!ANY) s.lim = fminf(r.tmax, below(t));
             s.hit.b = b;
             s.hit.g = g;
             s.hit.ref = __float_as_uint(p0.w);
@@ -303,18 +425,10 @@ __device__ __forceinline__ void trav_step(trav_t &s, const dev_scene &sc, const 
     }
     if (s.cur >= 0) {
         if (COUNT) ++s.n_inner;
-        const float4 *np = sc.nodes + 4 * (size_t)s.cur;
-        float4 n0, n1, n2, n3;
-        ldg256(np, n0, n1);
-        ldg256(np + 2, n2, n3);
         float dl, dr;
-        bool hl = slab<PLAIN>(n0.x, n0.y, n0.z, n1.x, n1.y, n1.z, r, dl);
-        bool hr = slab<PLAIN>(n2.x, n2.y, n2.z, n3.x, n3.y, n3.z, r, dr);
-        if (!ANY) {
-            hl = hl && dl < s.hit.t;
-            hr = hr && dr < s.hit.t;
-        }
-        const int32_t cl = __float_as_int(n0.w), cr = __float_as_int(n2.w);
+        bool hl, hr;
+        int32_t cl, cr;
+        node_test<ANY, PLAIN>(sc.nodes + 4 * (size_t)s.cur, s, r, hl, hr, dl, dr, cl, cr);
         if (hl && hr) {
             const bool left_first = dl < dr;
             if (s.sp >= STACK) {
@@ -342,6 +456,7 @@ __device__ __forceinline__ void trav_step(trav_t &s, const dev_scene &sc, const 
             if (tri_test(p0, p1, p2, r, ANY ? r.tmax : fminf(r.tmax, s.hit.t), t, b, g) && (ANY || t < s.hit.t) &&
                 (!ALPHA || alpha_opaque(sc.alpha, __float_as_uint(p0.w), __float_as_uint(p1.w), b, g))) {
                 s.hit.t = t;
+                if (!ANY) s.lim = fminf(r.tmax, below(t));
                 s.hit.b = b;
                 s.hit.g = g;
                 s.hit.ref = __float_as_uint(p0.w);
@@ -367,18 +482,10 @@ __device__ __forceinline__ void trav_step(trav_t &s, const dev_scene &sc, const 
 template <int STACK, bool ANY, bool PLAIN>
 __device__ __forceinline__ void spec_node(trav_t &s, const dev_scene &sc, const ray_t &r, int *stk, int stride,
                                           unsigned *err) {
-    const float4 *np = sc.nodes + 4 * (size_t)s.cur;
-    float4 n0, n1, n2, n3;
-        ldg256(np, n0, n1);
-        ldg256(np + 2, n2, n3);
     float dl, dr;
-    bool hl = slab<PLAIN>(n0.x, n0.y, n0.z, n1.x, n1.y, n1.z, r, dl);
-    bool hr = slab<PLAIN>(n2.x, n2.y, n2.z, n3.x, n3.y, n3.z, r, dr);
-    if (!ANY) {
-        hl = hl && dl < s.hit.t;
-        hr = hr && dr < s.hit.t;
-    }
-    const int32_t cl = __float_as_int(n0.w), cr = __float_as_int(n2.w);
+    bool hl, hr;
+    int32_t cl, cr;
+    node_test<ANY, PLAIN>(sc.nodes + 4 * (size_t)s.cur, s, r, hl, hr, dl, dr, cl, cr);
     if (hl && hr) {
         const bool left_first = dl < dr;
         if (s.sp >= STACK) {
@@ -544,6 +651,7 @@ __device__ __forceinline__ void trav_spec_iter(trav_t &s, bool active, bool plai
                 if (tri_test(p0, p1, p2, r, ANY ? r.tmax : fminf(r.tmax, s.hit.t), t, b, g) && (ANY || t < s.hit.t) &&
                 (!ALPHA || alpha_opaque(sc.alpha, __float_as_uint(p0.w), __float_as_uint(p1.w), b, g))) {
                     s.hit.t = t;
+                    if (!ANY) s.lim = fminf(r.tmax, below(t));
                     s.hit.b = b;
                     s.hit.g = g;
                     s.hit.ref = __float_as_uint(p0.w);
