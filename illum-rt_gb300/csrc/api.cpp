@@ -290,6 +290,17 @@ grt_status grt_select_tracer(grt_ctx *c, const char *name) {
     if (!c || !name) return GRT_ERR_INVALID_ARG;
     std::string n(name);
     if (n == "default") n = kTracers[0].name;
+    // The reference's two other loop shapes, by what they compute per ray: `simple`
+    // (rt/cuda/trace-kernels.cu:67-235) is one thread per ray taking one node or leaf per
+    // iteration, which is the if-if loop; `dynamic-while-while` (:702-1054) is the while-while
+    // loop with lanes refilled when fewer than 20 are active, which is the persistent
+    // while-while tracer at its default refill threshold.
+    static const char *const aliases[][2] = {{"simple", "if-if"},
+                                             {"simple-alpha", "if-if-alpha"},
+                                             {"dynamic-while-while", "persistent-while-while"},
+                                             {"dynamic-while-while-alpha", "persistent-while-while-alpha"}};
+    for (const auto &a : aliases)
+        if (n == a[0]) n = a[1];
     for (int i = 0; i < kNumTracers; ++i)
         if (n == kTracers[i].name) {
             c->tracer = i;

@@ -183,7 +183,10 @@ void grt_host_bvh_free(grt_host_bvh *bvh);
  * "persistent-": persistent warps with dynamic ray fetch. The loop order of the selected tracer
  * is also the one grt_pathtrace uses. The if-if and while-while orders give results identical
  * to the reference CPU tracer; the speculative orders may differ from it in near-ties only (a
- * different triangle whose t is within a few ulps of the reference's). Unknown name:
+ * different triangle whose t is within a few ulps of the reference's). Every name also comes
+ * with the suffix "-alpha" (alpha-aware, grt_set_alpha). The reference's "simple" and
+ * "dynamic-while-while" (and their "-alpha" forms) are accepted too and select "if-if" and
+ * "persistent-while-while", the loops that compute what they compute. Unknown name:
  * GRT_ERR_UNKNOWN_TRACER. */
 grt_status grt_select_tracer(grt_ctx *ctx, const char *name);
 grt_status grt_set_tuning(grt_ctx *ctx, const grt_tuning *tuning);

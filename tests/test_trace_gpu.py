@@ -110,6 +110,25 @@ def test_errors_are_status_codes(api, wl):
     rt.close()
 
 
+@pytest.mark.parametrize("alias,same", [("simple", "if-if"), ("dynamic-while-while", "persistent-while-while"),
+                                        ("simple-alpha", "if-if-alpha"),
+                                        ("dynamic-while-while-alpha", "persistent-while-while-alpha")])
+def test_reference_tracer_names(gpu_tracer, golden_scenes, alias, same):
+    """Every `raytracer` name of the reference's CUDA platform (rt/cuda/platform.cpp:102-131)
+    selects a tracer; `simple` and `dynamic-while-while` give the reference's hits exactly."""
+    name = GOLDEN_CASES[0]
+    g = load_golden(name)
+    v, t, rays, any_rays = golden_scenes[name]
+    gpu_tracer.build(v, t)
+    assert gpu_tracer.interprete(f"raytracer {alias}")
+    got = _trace(gpu_tracer, rays, False)
+    assert_hits_match(got, g["closest"], True, f"{alias} closest hits")
+    assert (occluded(_trace(gpu_tracer, any_rays, True)) == g["any_occluded"]).all()
+    gpu_tracer.select(same)
+    assert same_bits(_trace(gpu_tracer, rays, False), got).all()
+    gpu_tracer.select("while-while")
+
+
 def test_empty_scene_misses(gpu_tracer):
     v = np.zeros((3, 4), np.float32)
     gpu_tracer.build(v, np.zeros((0, 4), np.uint32), esc=False)
