@@ -525,11 +525,14 @@ bool flatten_bvh4(const ref_tree &tree, const flat_bvh &flat, flat_bvh4 &out, st
         for (int i = 0; i < 4; ++i) {
             const bool used = i < k;
             const float inf = __builtin_inff();
-            for (int a = 0; a < 3; ++a) {
-                d[4 * (2 * a) + i] = used ? ch[i].lo[a] : inf;
-                d[4 * (2 * a + 1) + i] = used ? ch[i].hi[a] : inf;
-            }
-            std::memcpy(d + 24 + i, &ref[i], 4);
+            float *e = d + 8 * i;
+            e[0] = used ? ch[i].lo[0] : inf;
+            e[1] = used ? ch[i].lo[1] : inf;
+            e[2] = used ? ch[i].hi[0] : inf;
+            e[3] = used ? ch[i].hi[1] : inf;
+            e[4] = used ? ch[i].lo[2] : inf;
+            e[5] = used ? ch[i].hi[2] : inf;
+            std::memcpy(e + 6, &ref[i], 4);
         }
         uint32_t sub = 0;
         for (uint32_t cw : kids[w]) sub = std::max(sub, bound[cw]);

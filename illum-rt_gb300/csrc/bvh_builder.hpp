@@ -62,11 +62,10 @@ bool flatten_bvh(const ref_tree &tree, const float *vpos4, const uint32_t *tris4
 
 // 4-wide device layout: the reference tree collapsed two levels at a time. A wide node holds
 // the children of a binary node's inner children (the grandchildren) and its leaf children,
-// 2 to 4 of them, with their boxes as the reference stores them. 128 bytes, eight float4:
-//   [0] lo.x of children 0..3   [1] hi.x   [2] lo.y   [3] hi.y   [4] lo.z   [5] hi.z
-//   [6] child references (int bits): >= 0 wide node, < 0 leaf (same encoding and the same
-//       triangle records as the binary layout), kEmptyChild for an unused slot
-//   [7] unused
+// 2 to 4 of them, with their boxes as the reference stores them. 128 bytes: four 32-byte child
+// records in the binary node's format, (lo.x, lo.y, hi.x, hi.y, lo.z, hi.z, reference, 0); a
+// reference >= 0 is a wide node, < 0 a leaf (same encoding and the same triangle records as the
+// binary layout), kEmptyChild an unused slot (its box all +inf).
 // Children appear in the reference's left-to-right order; wide nodes are in preorder.
 static const int32_t kEmptyChild = 0x7fffffff;
 struct flat_bvh4 {

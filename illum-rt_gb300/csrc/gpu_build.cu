@@ -332,7 +332,7 @@ __global__ void __launch_bounds__(kThreads) k_wide_index(int n, const int32_t *_
     if (i == n - 1) info[GB_WIDE_NODES] = excl[i] + flag[i];
 }
 
-// 5c. the 4-wide nodes (structure of arrays per node, unused slots +inf / kEmptyWideChild)
+// 5c. the 4-wide nodes (four child records, unused slots +inf / kEmptyWideChild)
 __global__ void __launch_bounds__(kThreads) k_wide_nodes(const float4 *__restrict__ nodes,
                                                          const int32_t *__restrict__ wide_index, int n,
                                                          float4 *nodes4) {
@@ -370,12 +370,10 @@ __global__ void __launch_bounds__(kThreads) k_wide_nodes(const float4 *__restric
         ref[k] = kEmptyWideChild;
     }
     float4 *o = nodes4 + 8 * (size_t)w;
-    for (int a = 0; a < 3; ++a) {
-        o[2 * a] = make_float4(lo[a][0], lo[a][1], lo[a][2], lo[a][3]);
-        o[2 * a + 1] = make_float4(hi[a][0], hi[a][1], hi[a][2], hi[a][3]);
+    for (int i = 0; i < 4; ++i) {  // child records as in the binary layout
+        o[2 * i] = make_float4(lo[0][i], lo[1][i], hi[0][i], hi[1][i]);
+        o[2 * i + 1] = make_float4(lo[2][i], hi[2][i], __int_as_float(ref[i]), 0.f);
     }
-    o[6] = make_float4(__int_as_float(ref[0]), __int_as_float(ref[1]), __int_as_float(ref[2]), __int_as_float(ref[3]));
-    o[7] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
 __global__ void k_init_info(int32_t *info, uint32_t *cbounds) {

@@ -121,31 +121,27 @@ __device__ __forceinline__ bool finite_nonzero(float x) { return isfinite(x) && 
 
 // A ray is "plain" when no slab product (box - o) * (1/d) can be NaN: o finite and every
 // 1/d finite and non-zero. Then min/max instructions give exactly the reference's selects
-// (they differ only on NaN operands, and on the sign of zero, which no comparison sees).
+// (they differ only on NaN operands, and on the sign of zero, which no comparison sees), and
+// the traversal takes slab2 instead of slab.
 __device__ __forceinline__ bool ray_is_plain(const ray_t &r) {
     return finite_nonzero(r.ix()) && finite_nonzero(r.iy()) && finite_nonzero(r.iz()) && isfinite(r.ox()) &&
            isfinite(r.oy()) && isfinite(r.oz());
 }
 
-template <bool PLAIN>
+// The reference's slab test, intersect4 (libgi/intersect.h:230-267), with glm's min / max as the
+// selects (y < x) ? y : x and (x < y) ? y : x, for rays that are not plain.
 __device__ __forceinline__ bool slab(float lx, float ly, float lz, float hx, float hy, float hz, const ray_t &r,
                                      float &tnear) {
     const float ax = __fmul_rn(__fsub_rn(lx, r.ox()), r.ix()), bx = __fmul_rn(__fsub_rn(hx, r.ox()), r.ix());
     const float ay = __fmul_rn(__fsub_rn(ly, r.oy()), r.iy()), by = __fmul_rn(__fsub_rn(hy, r.oy()), r.iy());
     const float az = __fmul_rn(__fsub_rn(lz, r.oz()), r.iz()), bz = __fmul_rn(__fsub_rn(hz, r.oz()), r.iz());
-    float t1, t2;
-    if (PLAIN) {
-        t1 = fmaxf(fmaxf(fminf(ax, bx), fminf(ay, by)), fminf(az, bz));
-        t2 = fminf(fminf(fmaxf(ax, bx), fmaxf(ay, by)), fmaxf(az, bz));
-    } else {
-        const float t1x = (ax < bx) ? ax : bx, t2x = (bx < ax) ? ax : bx;
-        const float t1y = (ay < by) ? ay : by, t2y = (by < ay) ? ay : by;
-        const float t1z = (az < bz) ? az : bz, t2z = (bz < az) ? az : bz;
-        t1 = (t1x < t1y) ? t1y : t1x;
-        t1 = (t1z < t1) ? t1 : t1z;
-        t2 = (t2x < t2y) ? t2x : t2y;
-        t2 = (t2z < t2) ? t2z : t2;
-    }
+    const float t1x = (ax < bx) ? ax : bx, t2x = (bx < ax) ? ax : bx;
+    const float t1y = (ay < by) ? ay : by, t2y = (by < ay) ? ay : by;
+    const float t1z = (az < bz) ? az : bz, t2z = (bz < az) ? az : bz;
+    float t1 = (t1x < t1y) ? t1y : t1x;
+    t1 = (t1z < t1) ? t1 : t1z;
+    float t2 = (t2x < t2y) ? t2x : t2y;
+    t2 = (t2z < t2) ? t2z : t2;
     tnear = t1;
     return !(t1 > t2) && !(t2 < r.tmin) && !(t1 > r.tmax);
 }
@@ -249,15 +245,6 @@ static __device__ __forceinline__ bool alpha_opaque(const alpha_data *A, uint32_
     return __ldg(A->texels + tx.z + (size_t)y * tx.x + x) > 0.5f;
 }
 
-// One 256-bit read-only load (two float4) from a 32-byte-aligned address: a 64-byte binary
-// node is two such loads (each half is one child's box and reference), four fewer L1 requests
-// per node than 128-bit loads.
-__device__ __forceinline__ void ldg256(const float4 *p, float4 &a, float4 &b) {
-    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
-        : "l"(p));
-}
-
 // One 256-bit read-only load as four 64-bit words: one child record of a binary node.
 __device__ __forceinline__ void ldg256_b64(const float4 *p, uint64_t &a, uint64_t &b, uint64_t &c, uint64_t &d) {
     asm("ld.global.nc.v4.b64 {%0, %1, %2, %3}, [%4];" : "=l"(a), "=l"(b), "=l"(c), "=l"(d) : "l"(p));
@@ -303,10 +290,23 @@ __device__ __forceinline__ void trav_init(trav_t &s, const dev_scene &sc, const 
     s.hit.rec = 0u;
 }
 
-// Both child tests of the binary node at `np` (layout in bvh_builder.hpp): whether each child
-// is entered (its box meets the ray inside [t_min, t_max] and, for closest hits, starts before
-// the closest hit so far), its entry distance and its reference. Plain rays take slab2 with
-// the cull folded in; the others the reference's compare-and-select form.
+// The test of one child record (layout in bvh_builder.hpp): whether the child is entered (its
+// box meets the ray inside [t_min, t_max] and, for closest hits, starts before the closest hit
+// so far) and its entry distance. Plain rays take slab2 with the cull folded in; the others the
+// reference's compare-and-select form.
+template <bool ANY, bool PLAIN>
+__device__ __forceinline__ bool child_test(uint64_t xy_lo, uint64_t xy_hi, uint64_t z, const trav_t &s,
+                                           const ray_t &r, float &tnear) {
+    if (PLAIN) return slab2(xy_lo, xy_hi, z, r, ANY ? r.tmax : s.lim, tnear);
+    float lx, ly, hx, hy, lz, hz;
+    upk2(xy_lo, lx, ly);
+    upk2(xy_hi, hx, hy);
+    upk2(z, lz, hz);
+    const bool h = slab(lx, ly, lz, hx, hy, hz, r, tnear);
+    return ANY ? h : h && tnear < s.hit.t;
+}
+
+// Both child tests of the binary node at `np`: entered or not, entry distances, references.
 template <bool ANY, bool PLAIN>
 __device__ __forceinline__ void node_test(const float4 *np, const trav_t &s, const ray_t &r, bool &hl, bool &hr,
                                           float &dl, float &dr, int32_t &cl, int32_t &cr) {
@@ -315,25 +315,8 @@ __device__ __forceinline__ void node_test(const float4 *np, const trav_t &s, con
     ldg256_b64(np + 2, r0, r1, r2, r3);
     cl = (int32_t)(uint32_t)l3;
     cr = (int32_t)(uint32_t)r3;
-    if (PLAIN) {
-        const float lim = ANY ? r.tmax : s.lim;
-        hl = slab2(l0, l1, l2, r, lim, dl);
-        hr = slab2(r0, r1, r2, r, lim, dr);
-    } else {
-        float lx, ly, hx, hy, lz, hz;
-        upk2(l0, lx, ly);
-        upk2(l1, hx, hy);
-        upk2(l2, lz, hz);
-        hl = slab<false>(lx, ly, lz, hx, hy, hz, r, dl);
-        upk2(r0, lx, ly);
-        upk2(r1, hx, hy);
-        upk2(r2, lz, hz);
-        hr = slab<false>(lx, ly, lz, hx, hy, hz, r, dr);
-        if (!ANY) {
-            hl = hl && dl < s.hit.t;
-            hr = hr && dr < s.hit.t;
-        }
-    }
+    hl = child_test<ANY, PLAIN>(l0, l1, l2, s, r, dl);
+    hr = child_test<ANY, PLAIN>(r0, r1, r2, s, r, dr);
 }
 
 // One traversal iteration in the while-while order: inner nodes (two box tests each) until the
@@ -514,25 +497,16 @@ template <int STACK, bool ANY, bool PLAIN>
 __device__ __forceinline__ void spec_node4(trav_t &s, const dev_scene &sc, const ray_t &r, int *stk, int stride,
                                            unsigned *err) {
     const float4 *np = sc.nodes4 + 8 * (size_t)s.cur;
-    float4 lx, hx, ly, hy, lz, hz, crf, unused;
-    ldg256(np, lx, hx);
-    ldg256(np + 2, ly, hy);
-    ldg256(np + 4, lz, hz);
-    ldg256(np + 6, crf, unused);
-    const int4 cr = make_int4(__float_as_int(crf.x), __float_as_int(crf.y), __float_as_int(crf.z), __float_as_int(crf.w));
     float k[4];
-    int c[4] = {cr.x, cr.y, cr.z, cr.w};
-    bool h0 = slab<PLAIN>(lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, r, k[0]);
-    bool h1 = slab<PLAIN>(lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, r, k[1]);
-    bool h2 = slab<PLAIN>(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, r, k[2]);
-    bool h3 = slab<PLAIN>(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, r, k[3]);
-    if (!ANY) {
-        h0 = h0 && k[0] < s.hit.t;
-        h1 = h1 && k[1] < s.hit.t;
-        h2 = h2 && k[2] < s.hit.t;
-        h3 = h3 && k[3] < s.hit.t;
+    int c[4];
+    bool hit[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        uint64_t xy_lo, xy_hi, z, ref;
+        ldg256_b64(np + 2 * i, xy_lo, xy_hi, z, ref);
+        c[i] = (int32_t)(uint32_t)ref;
+        hit[i] = child_test<ANY, PLAIN>(xy_lo, xy_hi, z, s, r, k[i]);
     }
-    const bool hit[4] = {h0, h1, h2, h3};
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         if (!hit[i] || c[i] == kEmptyWideChild) {
