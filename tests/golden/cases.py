@@ -85,6 +85,17 @@ def kat_rays():
     r.append(_ray((0.5, 0.5, 0.3), (1.0, 0.0, -0.1)))   # towards the steep triangle
     r.append(_ray((10.2, 10.2, 20.0), down))            # far triangle
     r.append(_ray((0.3, 0.3, 0.0), (0.0, 0.0, -1.0)))   # origin on the surface
+    # the same boundaries for a direction with no zero component (the packed slab test's rays)
+    tilt = (0.01, 0.02, -1.0)
+    r.append(_ray((0.4, 0.1, 1.0), tilt, np.float32(0.0), NAN))                # NaN t_max
+    r.append(_ray((0.4, 0.1, 1.0), tilt, NAN, FLT_MAX))                        # NaN t_min
+    r.append(_ray((0.4, 0.1, 1.0), tilt, np.float32(2.0), np.float32(1.0)))   # t_min > t_max
+    r.append(_ray((0.4, 0.1, 1.0), tilt, np.float32(0.0), np.float32(0.0)))   # t_max = 0
+    r.append(_ray((0.4, 0.1, 1.0), tilt, -INF, INF))                           # unbounded both ways
+    r.append(_ray((0.35, 0.15, -1.0), tilt, np.float32(-10.0), FLT_MAX))       # hits behind the origin
+    r.append(_ray((0.3, 0.3, 0.0), tilt, np.float32(-1.0), FLT_MAX))           # hit at t = 0
+    r.append(_ray((0.3, 0.3, 1e-7), tilt, np.float32(-1.0), FLT_MAX))          # hit just below t = 0
+    r.append(_ray((0.35, 0.15, 1.0), tilt, np.float32(1.0), FLT_MAX))          # t near t_min
     for y in np.arange(-0.25, 1.3, 0.125):
         for x in np.arange(-0.25, 1.3, 0.125):
             r.append(_ray((x, y, 1.0), down))
