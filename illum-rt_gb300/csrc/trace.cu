@@ -40,7 +40,7 @@ __global__ void __launch_bounds__(256) k_trace_plain(const float4 *__restrict__ 
     const bool plain = active && sc.finite && ray_is_plain(r);
     if (SPEC) {  // the whole warp stays in the loop until its last ray ends
         while (__any_sync(kFull, active && !s.done))
-            trav_spec_iter<STACK, ANY, COUNT, WIDE, ALPHA>(s, active, plain, sc, r, stk, stride, err);
+            trav_spec_iter<STACK, ANY, COUNT, WIDE, ALPHA, kPendTrace>(s, active, plain, sc, r, stk, stride, err);
         if (!active) return;
     } else if (plain) {  // one loop per slab variant: the choice is made once per ray
         while (!s.done) trav_advance<ORDER, STACK, ANY, COUNT, true, ALPHA>(s, sc, r, stk, stride, err);
@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(256) k_trace_persistent(const float4 *__restri
         // traverse; every `refill_period` iterations the warp counts its busy lanes
         for (int it = 1;; ++it) {
             if (SPEC)
-                trav_spec_iter<STACK, ANY, false, WIDE, ALPHA>(s, have, plain, sc, r, stk, stride, err);
+                trav_spec_iter<STACK, ANY, false, WIDE, ALPHA, kPendTrace>(s, have, plain, sc, r, stk, stride, err);
             else if (have && plain)
                 trav_advance<ORDER, STACK, ANY, false, true, ALPHA>(s, sc, r, stk, stride, err);
             else if (have)
