@@ -134,7 +134,7 @@ __device__ __forceinline__ void trace_all(trav_t &s, bool active, bool plain, co
     constexpr bool WIDE = ORDER == WIDE_SPECULATIVE;
     while (__any_sync(kFull, active && !s.done)) {
         if (SPEC)
-            trav_spec_iter<STACK, ANY, false, WIDE, false, kPendDirect>(s, active, plain, sc, r, stk, stride, err);
+            trav_spec_iter<STACK, ANY, false, WIDE, false, kPendDirect, kExitDirect>(s, active, plain, sc, r, stk, stride, err);
         else if (active && !s.done && plain)
             trav_advance<ORDER, STACK, ANY, false, true>(s, sc, r, stk, stride, err);
         else if (active && !s.done)

@@ -61,12 +61,13 @@ __device__ __forceinline__ bool stop_requested_at_entry(unsigned *err) {
 static const int kStackSmall = 32;
 static const int kStackLarge = 64;
 
-// Leaves a lane of the speculative loop order may postpone before its warp's leaf phase
-// (traverse.cuh), per kernel family, as measured on GB300: diffuse bounce rays gain most from
-// two, camera and shadow rays from three.
-static const int kPendPaths = 2;   // fused path tracer
-static const int kPendDirect = 3;  // fused direct lighting
-static const int kPendTrace = 3;   // batch traces (one scene or a scene set)
+// The speculative loop order's two warp-level parameters (traverse.cuh), per kernel family, as
+// measured on GB300: how many leaves a lane may postpone before the warp's leaf phase, and with
+// how many lanes still searching for their first leaf the warp stops visiting nodes.
+static const int kPendPaths = 2, kExitPaths = 4;                // fused path tracer
+static const int kPendDirect = 3, kExitDirect = 2;              // fused direct lighting
+static const int kPendTrace = 3, kExitTrace = 1;                // one-thread-per-ray batch traces
+static const int kPendPersistent = 3, kExitPersistent = 4;      // persistent batch traces, scene sets
 
 // Upper bound on traversal steps (inner nodes + leaves) of one ray. A DFS over a tree visits
 // each node at most once per ray, so a correct BVH never reaches it; it bounds the work of a

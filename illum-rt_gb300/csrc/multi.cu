@@ -82,7 +82,7 @@ __global__ void __launch_bounds__(256) k_trace_multi(const dev_scene *__restrict
         }
         for (int it = 1;; ++it) {
             if (SPEC)
-                trav_spec_iter<STACK, ANY, false, WIDE, false, kPendTrace>(s, have, plain, sc, r, stk, stride, err);
+                trav_spec_iter<STACK, ANY, false, WIDE, false, kPendPersistent, kExitPersistent>(s, have, plain, sc, r, stk, stride, err);
             else if (have && plain)
                 trav_advance<ORDER, STACK, ANY, false, true>(s, sc, r, stk, stride, err);
             else if (have)

@@ -20,8 +20,18 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 
+// Resident blocks of 256 threads asked of the compiler per loop order, as measured on GB300
+// (plain bounce traces of the sphere scene): left to itself the compiler holds the speculative
+// loop to 48 registers and spills; at 4 blocks (64 registers at most) the while-while and
+// speculative loops run 4 % / 1 % faster, the if-if loop is fastest at 5 and the 4-wide loop
+// with no bound (72 registers).
+template <int ORDER>
+constexpr int plain_min_blocks() {
+    return ORDER == IF_IF ? 5 : ORDER == WIDE_SPECULATIVE ? 1 : 4;
+}
+
 template <int ORDER, int STACK, bool ANY, bool COUNT, bool ALPHA>
-__global__ void __launch_bounds__(256) k_trace_plain(const float4 *__restrict__ rays, grt_hit *__restrict__ hits,
+__global__ void __launch_bounds__(256, plain_min_blocks<ORDER>()) k_trace_plain(const float4 *__restrict__ rays, grt_hit *__restrict__ hits,
                                                      uint32_t n, const uint32_t *__restrict__ n_dev, dev_scene sc,
                                                      unsigned *err, unsigned long long *counters) {
     extern __shared__ int s_stack[];
@@ -40,7 +50,7 @@ __global__ void __launch_bounds__(256) k_trace_plain(const float4 *__restrict__ 
     const bool plain = active && sc.finite && ray_is_plain(r);
     if (SPEC) {  // the whole warp stays in the loop until its last ray ends
         while (__any_sync(kFull, active && !s.done))
-            trav_spec_iter<STACK, ANY, COUNT, WIDE, ALPHA, kPendTrace>(s, active, plain, sc, r, stk, stride, err);
+            trav_spec_iter<STACK, ANY, COUNT, WIDE, ALPHA, kPendTrace, kExitTrace>(s, active, plain, sc, r, stk, stride, err);
         if (!active) return;
     } else if (plain) {  // one loop per slab variant: the choice is made once per ray
         while (!s.done) trav_advance<ORDER, STACK, ANY, COUNT, true, ALPHA>(s, sc, r, stk, stride, err);
@@ -104,7 +114,7 @@ __global__ void __launch_bounds__(256) k_trace_persistent(const float4 *__restri
         // traverse; every `refill_period` iterations the warp counts its busy lanes
         for (int it = 1;; ++it) {
             if (SPEC)
-                trav_spec_iter<STACK, ANY, false, WIDE, ALPHA, kPendTrace>(s, have, plain, sc, r, stk, stride, err);
+                trav_spec_iter<STACK, ANY, false, WIDE, ALPHA, kPendPersistent, kExitPersistent>(s, have, plain, sc, r, stk, stride, err);
             else if (have && plain)
                 trav_advance<ORDER, STACK, ANY, false, true, ALPHA>(s, sc, r, stk, stride, err);
             else if (have)

@@ -561,13 +561,16 @@ __device__ __forceinline__ void spec_node4(trav_t &s, const dev_scene &sc, const
 // for their first leaf; then all postponed leaves are tested together. The reference postpones
 // one leaf; here a lane may postpone up to PEND (1 to 3) before the leaf phase, so that lanes
 // already holding a leaf do useful work instead of idling while the warp searches (on GB300 two
-// took 9 % off the fused path step and three 14 % off fused direct lighting). Every lane of the
-// warp must call this together (it ballots over the full warp); `active` marks lanes with a ray.
+// took 9 % off the fused path step and three 14 % off fused direct lighting). The warp leaves
+// the node phase once at most EXIT lanes are still searching for their first leaf; those lanes
+// resume where they stopped in the next call, so this changes when leaves are tested, not which
+// (4 of 32 took another 4 % off the fused path step). Every lane of the warp must call this
+// together (it ballots over the full warp); `active` marks lanes with a ray.
 // Each ray's leaves are still tested in the reference's order, but node tests after a
 // postponed leaf use the closest hit from before that leaf, so the ray may visit nodes the
 // reference would have culled. A triangle found there can replace the reference's answer only
 // if its t lies within rounding of the culled box's entry distance: a near-tie.
-template <int STACK, bool ANY, bool COUNT, bool WIDE = false, bool ALPHA = false, int PEND = 1>
+template <int STACK, bool ANY, bool COUNT, bool WIDE = false, bool ALPHA = false, int PEND = 1, int EXIT = 0>
 __device__ __forceinline__ void trav_spec_iter(trav_t &s, bool active, bool plain, const dev_scene &sc,
                                                const ray_t &r, int *stk, int stride, unsigned *err) {
     const bool mine = active && !s.done;
@@ -607,20 +610,24 @@ __device__ __forceinline__ void trav_spec_iter(trav_t &s, bool active, bool plai
     // Three visits per warp vote (measured on GB300: 4.4 % faster than one visit per vote, and
     // 1.2 % faster than two); a lane that has stopped searching may make up to two more
     // speculative node visits before the leaf phase, which leaves its hit within the near-tie
-    // class. The loop count bounds the work of a malformed tree.
-    for (uint32_t guard = 0;; guard += 3) {
-        if (guard >= kStepLimit) {
-            if (mine && !s.done) {
-                atomicOr(err, ERR_STEP_LIMIT);
-                s.done = true;
-            }
-            break;
-        }
+    // class. The warp's visit slots of this call are added to every live lane's step count (an
+    // upper bound of its own visits), so the work of a ray on a malformed tree stays bounded
+    // across calls, without a per-visit count.
+    uint32_t slots = 0;
+    for (;;) {
         visit();
         visit();
         visit();
+        slots += 3;
         const bool searching = mine && !s.done && s.more && s.pend == 0;
-        if (!__any_sync(0xffffffffu, searching)) break;
+        if (__popc(__ballot_sync(0xffffffffu, searching)) <= EXIT || slots >= kStepLimit) break;
+    }
+    if (mine && !s.done) {
+        s.steps += slots;
+        if (s.steps > kStepLimit) {
+            atomicOr(err, ERR_STEP_LIMIT);
+            s.done = true;
+        }
     }
     if (mine && !s.done) {
         while (s.pend != 0 && !s.done) {
