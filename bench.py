@@ -179,6 +179,10 @@ class Step:
         self.rt_plain.build(sc.vpos, sc.tris)
         self.rt_plain.select("while-while")
         self.plain_order = "while-while"
+        # the plain kernels on the tuned step's tree (its leaf size): the counting pass of the
+        # roofline figure and the plain form on the same tree
+        self.rt_tt = api.BatchRayTracer(device)
+        self.rt_tt.build(sc.vpos, sc.tris, max_tris=tuning.get("max_tris", 4))
         self.rt.select(tuning.get("tracer", "persistent-while-while"))
         kw = {k: v for k, v in tuning.items() if k in ("block_threads", "blocks_per_sm", "refill_threshold",
                                                          "refill_period", "stack_entries")}
@@ -210,6 +214,10 @@ class Step:
     def plain(self):
         self.rt_plain.trace(self.rays, self.hits, False, self.sp)
         self.rt_plain.pathtrace(self.p_plain, self.rays, self.hits, N_PATHS, self.results, None, self.sp)
+
+    def plain_tuned_tree(self):
+        self.rt_tt.trace(self.rays, self.hits, False, self.sp)
+        self.rt_tt.pathtrace(self.p_plain, self.rays, self.hits, N_PATHS, self.results, None, self.sp)
 
     def e2e(self):
         with self.torch.cuda.stream(self.stream):
@@ -271,22 +279,25 @@ class Step:
 
     def algorithmic_bytes(self):
         """(bytes per step of the pathtrace part, bytes of the primary part) from the counting
-        kernel: 32 B ray + 16 B hit + 64 B per inner node + 48 B per triangle test."""
+        kernel on the tuned step's tree: 32 B ray + 16 B hit + 64 B per inner node + 48 B per
+        triangle test."""
         torch = self.torch
         cnt = torch.zeros(3, dtype=torch.int64, device=self.dev)
         # the exact reference order, so that the counts are the reference traversal's own
-        self.rt_plain.select("while-while")
-        self.rt_plain.set_traversal_counters(cnt)
-        self.rt_plain.trace(self.rays, self.hits, False, self.sp)
-        self.rt_plain.check(self.sp)
+        rt = self.rt_tt
+        order = rt.tracer
+        rt.select("while-while")
+        rt.set_traversal_counters(cnt)
+        rt.trace(self.rays, self.hits, False, self.sp)
+        rt.check(self.sp)
         prim = [int(x) for x in cnt.cpu()]
         cnt.zero_()
         p = self.api.BatchRayTracer.pt_params(mode=self.api.PT_WAVEFRONT)
-        self.rt_plain.pathtrace(p, self.rays, self.hits, N_PATHS, self.results, None, self.sp)
-        self.rt_plain.check(self.sp)
+        rt.pathtrace(p, self.rays, self.hits, N_PATHS, self.results, None, self.sp)
+        rt.check(self.sp)
         bounce = [int(x) for x in cnt.cpu()]
-        self.rt_plain.set_traversal_counters(None)
-        self.rt_plain.select(self.plain_order)
+        rt.set_traversal_counters(None)
+        rt.select(order)
         to_bytes = lambda c: 48 * c[0] + 64 * c[1] + 48 * c[2]
         return to_bytes(bounce), to_bytes(prim), bounce, prim
 
@@ -387,6 +398,15 @@ def run_gb300(args):
         step.plain()
     plain_bvh4_ms = statistics.median(time_steps(step, step.plain, 3)[0])
     step.rt_plain.select(plain_order)
+    # the plain form in its best order on the tuned step's tree
+    tt_times = {}
+    for order in ("while-while", "if-if", "speculative-while-while"):
+        step.rt_tt.select(order)
+        for _ in range(2):
+            step.plain_tuned_tree()
+        tt_times[order] = statistics.median(time_steps(step, step.plain_tuned_tree, 3)[0])
+    tt_order = min(tt_times, key=tt_times.get)
+    step.rt_tt.select(tt_order)
 
     # rays per step of each form (identical work: same paths, same bounces)
     step.plain()
@@ -446,8 +466,9 @@ def run_gb300(args):
                 "bytes_per_launch": pt_bytes, "bounce_rays": bounce_cnt[0],
                 "inner_nodes_per_ray": round(bounce_cnt[1] / max(1, bounce_cnt[0]), 2),
                 "tri_tests_per_ray": round(bounce_cnt[2] / max(1, bounce_cnt[0]), 2),
-                "note": "B_ray = 32 + 16 + 64 n_node + 48 n_tri; the BVH (26 MB) stays L2-resident, "
-                        "so these bytes are mostly served from L2"}
+                "note": "B_ray = 32 + 16 + 64 n_node + 48 n_tri, counted in the exact while-while order on the "
+                        "tuned step's tree; the BVH (%.0f MB) stays L2-resident, so these bytes are mostly served "
+                        "from L2" % (step.build_info["device_bytes"] / 1e6)}
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(statistics.mean(tuned_ms), 4), "higher_is_better": True,
@@ -461,8 +482,12 @@ def run_gb300(args):
         "plain_wavefront": {"value": round(plain_value, 1), "ms_per_step": round(statistics.mean(plain_ms), 4),
                             "rays_per_step": rays_plain, "loop_order": plain_order,
                             "order_ms": {k: round(v, 4) for k, v in plain_times.items()},
-                            "bvh4_speculative_ms": round(plain_bvh4_ms, 4)},
+                            "bvh4_speculative_ms": round(plain_bvh4_ms, 4),
+                            "tuned_tree": {"bvh": "SAH 16 planes, ESC, leaf<=%d" % tuning.get("max_tris", 4),
+                                           "loop_order": tt_order,
+                                           "order_ms": {k: round(v, 4) for k, v in tt_times.items()}}},
         "speedup_vs_plain": round(value / plain_value, 3),
+        "speedup_vs_plain_same_tree": round(tt_times[tt_order] / statistics.mean(tuned_ms), 3),
         "speedup_vs_plain_while_while": round(plain_times["while-while"] / statistics.mean(tuned_ms), 3),
         "e2e": {"value": round(job_value(rays_tuned, args.steps, t_e2e_pipe, world), 1), "unit": "Mrays/s",
                 "ms_per_step": round(e2e_pipe_ms / args.steps, 4), "h2d_bytes_per_step": int(step.n_primary * 32),
