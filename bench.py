@@ -632,16 +632,16 @@ def run_direct(args, samples: int = 8):
     rt.build(sc.vpos, sc.tris)
     rt.set_material_table(mats)
 
-    def timed(mode, tracer):
+    def timed(mode, tracer, sampling="light"):
         rt.select(tracer)
         for _ in range(max(3, args.warmup)):
-            rt.direct(rays, fb, samples, mode=mode, seed=3, stream=sp)
+            rt.direct(rays, fb, samples, mode=mode, seed=3, stream=sp, sampling=sampling)
         rt.check(sp)
         times = []
         for _ in range(args.steps):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            rt.direct(rays, fb, samples, mode=mode, seed=3, stream=sp)
+            rt.direct(rays, fb, samples, mode=mode, seed=3, stream=sp, sampling=sampling)
             e1.record(stream)
             e1.synchronize()
             times.append(e0.elapsed_time(e1))
@@ -655,6 +655,14 @@ def run_direct(args, samples: int = 8):
         res["wavefront/" + tracer] = timed(api.DL_WAVEFRONT, tracer)
     best_f = min((v, k) for k, v in res.items() if k.startswith("fused"))
     best_w = min((v, k) for k, v in res.items() if k.startswith("wavefront"))
+    # the direction strategies of direct-wf (closest-hit rays instead of shadow rays), in the
+    # loop orders that are fastest for light sampling
+    directions = {}
+    for smp in ("uniform", "cosine"):
+        f_ms = timed(api.DL_FUSED, best_f[1].split("/", 1)[1], smp)
+        w_ms = timed(api.DL_WAVEFRONT, best_w[1].split("/", 1)[1], smp)
+        directions[smp] = {"fused_ms": round(f_ms, 4), "wavefront_ms": round(w_ms, 4),
+                           "speedup_fused_vs_wavefront": round(w_ms / f_ms, 3)}
     line = {"metric": "Msamples/s direct lighting (light-source sampling), fused vs wavefront", "unit": "Msamples/s",
             "value": round(n * samples / best_f[0] / 1e3, 1), "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded)",
@@ -662,7 +670,7 @@ def run_direct(args, samples: int = 8):
                        "samples_per_pixel": samples},
             "fused_ms": round(best_f[0], 4), "fused_form": best_f[1], "wavefront_ms": round(best_w[0], 4),
             "wavefront_form": best_w[1], "speedup_fused_vs_wavefront": round(best_w[0] / best_f[0], 3),
-            "all_ms": {k: round(v, 4) for k, v in res.items()}}
+            "all_ms": {k: round(v, 4) for k, v in res.items()}, "direction_sampling": directions}
     print(json.dumps(line), flush=True)
     rt.close()
 

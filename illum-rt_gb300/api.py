@@ -72,10 +72,12 @@ PT_WAVEFRONT, PT_FUSED = 0, 1
 
 
 class DirectParams(ctypes.Structure):
-    _fields_ = [("samples", ctypes.c_uint32), ("mode", ctypes.c_uint32), ("seed", ctypes.c_uint64)]
+    _fields_ = [("samples", ctypes.c_uint32), ("mode", ctypes.c_uint32), ("seed", ctypes.c_uint64),
+                ("sampling", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
 DL_WAVEFRONT, DL_FUSED = 0, 1
+DL_SAMPLING = {"light": 0, "uniform": 1, "cosine": 2}  # GRT_DL_SAMPLE_*
 
 
 class Mesh(ctypes.Structure):
@@ -352,10 +354,11 @@ class BatchRayTracer:
         m = np.ascontiguousarray(mats, np.float32).reshape(-1, 8)
         self._check(lib().grt_set_material_table(self.ctx, _ptr(m), m.shape[0]))
 
-    def direct(self, rays, framebuffer, samples, mode=DL_FUSED, seed=0, stream=None):
+    def direct(self, rays, framebuffer, samples, mode=DL_FUSED, seed=0, stream=None, sampling="light"):
         """Direct lighting (grt_direct) of CUDA rays [n, 8], accumulated into the CUDA frame
-        buffer [n, 4] (radiance sum, sample count)."""
-        p = DirectParams(int(samples), int(mode), int(seed))
+        buffer [n, 4] (radiance sum, sample count); sampling "light", "uniform" or "cosine"
+        (the reference direct-wf's `sampling` setting)."""
+        p = DirectParams(int(samples), int(mode), int(seed), DL_SAMPLING[sampling], 0)
         self._check(lib().grt_direct(self.ctx, ctypes.byref(p), _ptr(rays), int(rays.shape[0]), _ptr(framebuffer),
                                      VP(stream or 0)))
 

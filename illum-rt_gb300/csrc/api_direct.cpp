@@ -1,6 +1,6 @@
 // C-ABI of direct lighting (include/grt.h): the material table with the light distribution
 // (the reference's compute_light_distribution, rt/cuda/preprocessing.cpp:17-35) and the
-// wavefront and fused forms of the direct-wf steps (direct.cu).
+// wavefront and fused forms of the direct-wf steps (direct.cu), light or direction sampling.
 #include <algorithm>
 #include <cmath>
 #include <string>
@@ -77,6 +77,9 @@ grt_status grt_set_material_table(grt_ctx *c, const grt_material *mats, uint32_t
                  o_c = o_f + a256((size_t)std::max(nl, 1u) * 4), total = o_c + (size_t)(nl + 1) * 4;
     std::vector<char> host(total, 0);
     static_assert(sizeof(dl::material) == sizeof(grt_material), "material layouts differ");
+    static_assert(dl::kSampleLight == GRT_DL_SAMPLE_LIGHT && dl::kSampleUniform == GRT_DL_SAMPLE_UNIFORM &&
+                      dl::kSampleCosine == GRT_DL_SAMPLE_COSINE,
+                  "sampling strategies differ");
     if (n) std::memcpy(host.data(), mats, (size_t)n * sizeof(grt_material));
     if (nl) {
         std::memcpy(host.data() + o_l, lights.data(), (size_t)nl * 16);
@@ -110,6 +113,8 @@ grt_status grt_direct(grt_ctx *c, const grt_direct_params *p, const float *rays_
     if (!rays_dev || !fb_dev || !aligned16(rays_dev) || !aligned16(fb_dev))
         return fail(c, GRT_ERR_INVALID_ARG, "null or misaligned ray / frame buffer");
     if (p->mode > GRT_DL_FUSED) return fail(c, GRT_ERR_INVALID_ARG, "unknown direct-lighting mode");
+    if (p->sampling > GRT_DL_SAMPLE_COSINE || p->reserved != 0)
+        return fail(c, GRT_ERR_INVALID_ARG, "unknown direct-lighting sampling strategy");
     if (kTracers[c->tracer].alpha) return fail(c, GRT_ERR_INVALID_ARG, "direct lighting has no alpha-aware form");
     if (needed_stack(c) > kStackLarge) return fail(c, GRT_ERR_BVH_TOO_DEEP, "the BVH needs a deeper stack");
     device_guard g(c->device);
@@ -121,8 +126,9 @@ grt_status grt_direct(grt_ctx *c, const grt_direct_params *p, const float *rays_
     if (p->mode == GRT_DL_FUSED) {
         const grt_tuning &t = c->tuning;
         const int stack = std::max(needed_stack(c), t.stack_entries);
-        e = launch_dl_fused(scene_for(c), ds, rays, n, p->samples, p->seed, fb, kTracers[c->tracer].order, stack,
-                            t.block_threads > 0 ? t.block_threads : 128, c->num_sms, c->d_err, c->d_counter, st);
+        e = launch_dl_fused(scene_for(c), ds, rays, n, p->samples, p->seed, p->sampling, fb, kTracers[c->tracer].order,
+                            stack, t.block_threads > 0 ? t.block_threads : 128, c->num_sms, c->d_err, c->d_counter,
+                            st);
         return e == cudaSuccess ? GRT_OK : cuda_fail(c, e, "launching the fused direct-lighting kernel");
     }
     // wavefront: hits (16 B), shadow rays (32 B), shadow hits (16 B), light colour + pdf (16 B)
@@ -147,11 +153,12 @@ grt_status grt_direct(grt_ctx *c, const grt_direct_params *p, const float *rays_
         return persistent ? launch_trace_persistent(sc, r, h, n, any, lp, c->d_err, c->d_counter, st)
                           : launch_trace_plain(sc, r, h, n, any, lp, c->d_err, st);
     };
+    const bool light = p->sampling == GRT_DL_SAMPLE_LIGHT;  // shadow rays: any hit; directions: closest
     e = trace(rays, hits, false);
     for (uint32_t s = 0; s < p->samples && e == cudaSuccess; ++s) {
-        e = launch_dl_sample(ds, rays, hits, n, s, p->seed, srays, ls, fb, st);
-        if (e == cudaSuccess) e = trace(srays, shits, true);
-        if (e == cudaSuccess) e = launch_dl_integrate(ds, rays, hits, srays, shits, ls, n, fb, st);
+        e = launch_dl_sample(ds, rays, hits, n, s, p->seed, p->sampling, srays, ls, fb, st);
+        if (e == cudaSuccess) e = trace(srays, shits, light);
+        if (e == cudaSuccess) e = launch_dl_integrate(ds, rays, hits, srays, shits, ls, n, p->sampling, fb, st);
     }
     return e == cudaSuccess ? GRT_OK : cuda_fail(c, e, "launching the direct-lighting steps");
 }

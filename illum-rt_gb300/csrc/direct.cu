@@ -1,6 +1,8 @@
 // Direct lighting kernels: the wavefront steps of the reference's direct-wf algorithm
 // (k::sample_light, the shadow-ray trace, k::integrate_light; rt/cuda/bounce.cu:210-250,
-// 380-410) and one fused persistent kernel doing all of them per pixel.
+// 380-410; or k::sample_uniform_dir / k::sample_cos_dir, the closest-hit trace,
+// k::integrate_dir; bounce.cu:33-142, 341-375) and one fused persistent kernel doing all of them
+// per pixel.
 #include "direct.hpp"
 #include "traverse.cuh"
 
@@ -29,14 +31,15 @@ struct dl_prep {
     f3 emis;
     f3 org, dir;
     float tmax;     // -FLT_MAX: no shadow ray
-    f3 lcol;
+    f3 lcol;        // light sampling: the light's emission
     float pdf;
 };
 
-// k::sample_light (rt/cuda/bounce.cu:210-250) for sample `s` of pixel `pixel`; random numbers
-// from the PCG32 stream seed + s * n + pixel.
+// k::sample_light (rt/cuda/bounce.cu:210-250), or k::sample_uniform_dir / k::sample_cos_dir
+// (bounce.cu:33-142) for the direction strategies, for sample `s` of pixel `pixel`; random
+// numbers from the PCG32 stream seed + s * n + pixel.
 __device__ dl_prep prepare(const dl_scene &ds, f3 o, f3 d, float t, uint32_t ref, uint32_t pixel, uint32_t s,
-                           uint32_t n, uint64_t seed) {
+                           uint32_t n, uint64_t seed, uint32_t sampling) {
     dl_prep p;
     p.emissive = false;
     p.emis = p.org = p.dir = p.lcol = {0.f, 0.f, 0.f};
@@ -49,6 +52,16 @@ __device__ dl_prep prepare(const dl_scene &ds, f3 o, f3 d, float t, uint32_t ref
     if (dl::not_black(em)) {
         p.emissive = true;
         p.emis = em;
+        return p;
+    }
+    if (sampling != dl::kSampleLight) {
+        pm::pcg32 rng;
+        rng.set_sequence(seed + (uint64_t)s * n + pixel);
+        const float x0 = rng.uniform(), x1 = rng.uniform();
+        const f3 ns = pm::facing_normal(vert(ds, tri.x), vert(ds, tri.y), vert(ds, tri.z), d);
+        p.org = {pm::add(o.x, pm::mul(t, d.x)), pm::add(o.y, pm::mul(t, d.y)), pm::add(o.z, pm::mul(t, d.z))};
+        p.dir = dl::sample_dir(sampling, ns, x0, x1, p.pdf);
+        p.tmax = FLT_MAX;
         return p;
     }
     if (ds.n_lights == 0) return p;
@@ -83,6 +96,18 @@ __device__ f3 radiance(const dl_scene &ds, f3 d, float t, uint32_t ref, f3 w_i, 
     return dl::integrate(lcol, {-d.x, -d.y, -d.z}, w_i, ns, m, pdf);
 }
 
+// k::integrate_dir (rt/cuda/bounce.cu:341-375): the radiance of one direction sample whose ray
+// hit (sec_t, sec_ref): the emission of that triangle's material.
+__device__ f3 radiance_dir(const dl_scene &ds, f3 d, float t, uint32_t ref, f3 w_i, float pdf, float sec_t,
+                           uint32_t sec_ref) {
+    if (t == FLT_MAX || sec_t == FLT_MAX) return {0.f, 0.f, 0.f};
+    const uint4 tri = __ldg(ds.tris + ref);
+    const dl::material m = material_of(ds, tri.w);
+    const dl::material lm = material_of(ds, __ldg(ds.tris + sec_ref).w);
+    const f3 ns = pm::facing_normal(vert(ds, tri.x), vert(ds, tri.y), vert(ds, tri.z), d);
+    return dl::integrate({lm.emissive[0], lm.emissive[1], lm.emissive[2]}, {-d.x, -d.y, -d.z}, w_i, ns, m, pdf);
+}
+
 __device__ __forceinline__ float4 plus(float4 a, f3 b, float w) {
     return make_float4(pm::add(a.x, b.x), pm::add(a.y, b.y), pm::add(a.z, b.z), pm::add(a.w, w));
 }
@@ -93,12 +118,13 @@ __device__ __forceinline__ ray_t shadow_ray(f3 o, f3 d, float tmax) {
 
 __global__ void __launch_bounds__(256) k_dl_sample(dl_scene ds, const float4 *__restrict__ rays,
                                                    const grt_hit *__restrict__ hits, uint32_t n, uint32_t s,
-                                                   uint64_t seed, float4 *shadow_rays, float4 *lsample, float4 *fb) {
+                                                   uint64_t seed, uint32_t sampling, float4 *shadow_rays,
+                                                   float4 *lsample, float4 *fb) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4 ro = rays[2 * (size_t)i], rd = rays[2 * (size_t)i + 1];
     const grt_hit h = hits[i];
-    const dl_prep p = prepare(ds, {ro.x, ro.y, ro.z}, {rd.x, rd.y, rd.z}, h.t, h.ref, i, s, n, seed);
+    const dl_prep p = prepare(ds, {ro.x, ro.y, ro.z}, {rd.x, rd.y, rd.z}, h.t, h.ref, i, s, n, seed, sampling);
     if (p.emissive) fb[i] = plus(fb[i], p.emis, 0.f);
     shadow_rays[2 * (size_t)i] = make_float4(p.org.x, p.org.y, p.org.z, dl::kEps);
     shadow_rays[2 * (size_t)i + 1] = make_float4(p.dir.x, p.dir.y, p.dir.z, p.tmax);
@@ -109,15 +135,19 @@ __global__ void __launch_bounds__(256) k_dl_integrate(dl_scene ds, const float4 
                                                       const grt_hit *__restrict__ hits,
                                                       const float4 *__restrict__ shadow_rays,
                                                       const grt_hit *__restrict__ shadow_hits,
-                                                      const float4 *__restrict__ lsample, uint32_t n, float4 *fb) {
+                                                      const float4 *__restrict__ lsample, uint32_t n,
+                                                      uint32_t sampling, float4 *fb) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4 rd = rays[2 * (size_t)i + 1];
     const grt_hit h = hits[i];
     const float4 sd = shadow_rays[2 * (size_t)i + 1];
     const float4 l = lsample[i];
-    const bool occluded = shadow_hits[i].ref == 0xFFFFFFFFu;
-    const f3 rad = radiance(ds, {rd.x, rd.y, rd.z}, h.t, h.ref, {sd.x, sd.y, sd.z}, sd.w, {l.x, l.y, l.z}, l.w, occluded);
+    const grt_hit sh = shadow_hits[i];
+    const f3 d = {rd.x, rd.y, rd.z}, w_i = {sd.x, sd.y, sd.z};
+    const f3 rad = sampling == dl::kSampleLight
+                       ? radiance(ds, d, h.t, h.ref, w_i, sd.w, {l.x, l.y, l.z}, l.w, sh.ref == 0xFFFFFFFFu)
+                       : radiance_dir(ds, d, h.t, h.ref, w_i, l.w, sh.t, sh.ref);
     fb[i] = plus(fb[i], rad, 1.0f);
 }
 
@@ -142,10 +172,12 @@ __device__ __forceinline__ void trace_all(trav_t &s, bool active, bool plain, co
     }
 }
 
-template <int ORDER, int STACK>
+// DIR: a direction strategy (closest-hit rays, k::integrate_dir) instead of light sampling
+// (any-hit shadow rays, k::integrate_light).
+template <int ORDER, int STACK, bool DIR>
 __global__ void __launch_bounds__(256) k_dl_fused(dev_scene sc, dl_scene ds, const float4 *__restrict__ rays,
-                                                  uint32_t n, uint32_t samples, uint64_t seed, float4 *fb,
-                                                  unsigned *err, unsigned *counter) {
+                                                  uint32_t n, uint32_t samples, uint64_t seed, uint32_t sampling,
+                                                  float4 *fb, unsigned *err, unsigned *counter) {
     extern __shared__ int s_stack[];
     if (stop_requested_at_entry(err)) return;  // the host asked the context to stop
     constexpr bool WIDE = ORDER == WIDE_SPECULATIVE;
@@ -172,17 +204,19 @@ __global__ void __launch_bounds__(256) k_dl_fused(dev_scene sc, dl_scene ds, con
         for (uint32_t smp = 0; smp < samples; ++smp) {
             dl_prep p;
             if (active) {
-                p = prepare(ds, o, d, ht, href, pix, smp, n, seed);
+                p = prepare(ds, o, d, ht, href, pix, smp, n, seed, DIR ? sampling : dl::kSampleLight);
                 if (p.emissive) acc = plus(acc, p.emis, 0.f);
             }
-            const bool shoot = active && p.tmax > 0.f;  // a shadow ray that can find an occluder
+            const bool shoot = active && p.tmax > 0.f;  // a ray that can find an occluder / a light
             if (shoot) r = shadow_ray(p.org, p.dir, p.tmax);
             trav_init(s, sc, r, WIDE);
             plain = shoot && sc.finite && ray_is_plain(r);
-            trace_all<ORDER, STACK, true>(s, shoot, plain, sc, r, stk, stride, err);
+            trace_all<ORDER, STACK, !DIR>(s, shoot, plain, sc, r, stk, stride, err);
             if (active) {
-                const f3 rad = shoot ? radiance(ds, d, ht, href, p.dir, p.tmax, p.lcol, p.pdf, s.found)
-                                     : f3{0.f, 0.f, 0.f};
+                f3 rad = {0.f, 0.f, 0.f};
+                if (shoot)
+                    rad = DIR ? radiance_dir(ds, d, ht, href, p.dir, p.pdf, s.hit.t, s.hit.ref)
+                              : radiance(ds, d, ht, href, p.dir, p.tmax, p.lcol, p.pdf, s.found);
                 acc = plus(acc, rad, 1.0f);
             }
         }
@@ -190,48 +224,64 @@ __global__ void __launch_bounds__(256) k_dl_fused(dev_scene sc, dl_scene ds, con
     }
 }
 
-template <int ORDER, int STACK> const void *fused_ptr() { return (const void *)k_dl_fused<ORDER, STACK>; }
+template <int ORDER, int STACK, bool DIR> const void *fused_ptr() { return (const void *)k_dl_fused<ORDER, STACK, DIR>; }
 
-template <int ORDER, int STACK>
+template <int ORDER, int STACK, bool DIR>
 cudaError_t fused_run(const dev_scene &sc, const dl_scene &ds, const float4 *rays, uint32_t n, uint32_t samples,
-                      uint64_t seed, float4 *fb, int bt, int num_sms, unsigned *err, unsigned *counter,
-                      cudaStream_t st) {
+                      uint64_t seed, uint32_t sampling, float4 *fb, int bt, int num_sms, unsigned *err,
+                      unsigned *counter, cudaStream_t st) {
     const size_t smem = (size_t)STACK * bt * sizeof(int);
     int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dl_fused<ORDER, STACK>, bt, smem);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dl_fused<ORDER, STACK, DIR>, bt, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) per_sm = 1;
     e = cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
-    k_dl_fused<ORDER, STACK><<<per_sm * num_sms, bt, smem, st>>>(sc, ds, rays, n, samples, seed, fb, err, counter);
+    k_dl_fused<ORDER, STACK, DIR><<<per_sm * num_sms, bt, smem, st>>>(sc, ds, rays, n, samples, seed, sampling, fb,
+                                                                       err, counter);
     return cudaGetLastError();
+}
+
+template <int ORDER, bool DIR>
+cudaError_t fused_run(const dev_scene &sc, const dl_scene &ds, const float4 *rays, uint32_t n, uint32_t samples,
+                      uint64_t seed, uint32_t sampling, float4 *fb, int stack_entries, int bt, int num_sms,
+                      unsigned *err, unsigned *counter, cudaStream_t st) {
+    return stack_entries <= kStackSmall
+               ? fused_run<ORDER, kStackSmall, DIR>(sc, ds, rays, n, samples, seed, sampling, fb, bt, num_sms, err,
+                                                    counter, st)
+               : fused_run<ORDER, kStackLarge, DIR>(sc, ds, rays, n, samples, seed, sampling, fb, bt, num_sms, err,
+                                                    counter, st);
 }
 
 }  // namespace
 
 cudaError_t launch_dl_sample(const dl_scene &ds, const float4 *rays, const grt_hit *hits, uint32_t n, uint32_t s,
-                             uint64_t seed, float4 *shadow_rays, float4 *lsample, float4 *fb, cudaStream_t st) {
+                             uint64_t seed, uint32_t sampling, float4 *shadow_rays, float4 *lsample, float4 *fb,
+                             cudaStream_t st) {
     if (n == 0) return cudaSuccess;
-    k_dl_sample<<<(n + 255) / 256, 256, 0, st>>>(ds, rays, hits, n, s, seed, shadow_rays, lsample, fb);
+    k_dl_sample<<<(n + 255) / 256, 256, 0, st>>>(ds, rays, hits, n, s, seed, sampling, shadow_rays, lsample, fb);
     return cudaGetLastError();
 }
 
 cudaError_t launch_dl_integrate(const dl_scene &ds, const float4 *rays, const grt_hit *hits, const float4 *shadow_rays,
-                                const grt_hit *shadow_hits, const float4 *lsample, uint32_t n, float4 *fb,
-                                cudaStream_t st) {
+                                const grt_hit *shadow_hits, const float4 *lsample, uint32_t n, uint32_t sampling,
+                                float4 *fb, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
-    k_dl_integrate<<<(n + 255) / 256, 256, 0, st>>>(ds, rays, hits, shadow_rays, shadow_hits, lsample, n, fb);
+    k_dl_integrate<<<(n + 255) / 256, 256, 0, st>>>(ds, rays, hits, shadow_rays, shadow_hits, lsample, n, sampling,
+                                                    fb);
     return cudaGetLastError();
 }
 
 cudaError_t launch_dl_fused(const dev_scene &sc, const dl_scene &ds, const float4 *rays, uint32_t n, uint32_t samples,
-                            uint64_t seed, float4 *fb, int order, int stack_entries, int bt, int num_sms, unsigned *err,
-                            unsigned *counter, cudaStream_t st) {
+                            uint64_t seed, uint32_t sampling, float4 *fb, int order, int stack_entries, int bt,
+                            int num_sms, unsigned *err, unsigned *counter, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
-    const bool small = stack_entries <= kStackSmall;
-#define GRT_DL_RUN(O)                                                                                            \
-    return small ? fused_run<O, kStackSmall>(sc, ds, rays, n, samples, seed, fb, bt, num_sms, err, counter, st) \
-                 : fused_run<O, kStackLarge>(sc, ds, rays, n, samples, seed, fb, bt, num_sms, err, counter, st)
+#define GRT_DL_RUN(O)                                                                                             \
+    return sampling == dl::kSampleLight                                                                          \
+               ? fused_run<O, false>(sc, ds, rays, n, samples, seed, sampling, fb, stack_entries, bt, num_sms, err, \
+                                     counter, st)                                                                 \
+               : fused_run<O, true>(sc, ds, rays, n, samples, seed, sampling, fb, stack_entries, bt, num_sms, err,  \
+                                    counter, st)
     switch (order) {
         case IF_IF: GRT_DL_RUN(IF_IF);
         case SPECULATIVE: GRT_DL_RUN(SPECULATIVE);
@@ -243,10 +293,15 @@ cudaError_t launch_dl_fused(const dev_scene &sc, const dl_scene &ds, const float
 
 cudaError_t prepare_dl_kernels() {
     const int bytes = kStackLarge * 256 * (int)sizeof(int);
-    for (const void *f : {fused_ptr<IF_IF, kStackSmall>(), fused_ptr<IF_IF, kStackLarge>(),
-                          fused_ptr<WHILE_WHILE, kStackSmall>(), fused_ptr<WHILE_WHILE, kStackLarge>(),
-                          fused_ptr<SPECULATIVE, kStackSmall>(), fused_ptr<SPECULATIVE, kStackLarge>(),
-                          fused_ptr<WIDE_SPECULATIVE, kStackSmall>(), fused_ptr<WIDE_SPECULATIVE, kStackLarge>()}) {
+    for (const void *f :
+         {fused_ptr<IF_IF, kStackSmall, false>(), fused_ptr<IF_IF, kStackLarge, false>(),
+          fused_ptr<WHILE_WHILE, kStackSmall, false>(), fused_ptr<WHILE_WHILE, kStackLarge, false>(),
+          fused_ptr<SPECULATIVE, kStackSmall, false>(), fused_ptr<SPECULATIVE, kStackLarge, false>(),
+          fused_ptr<WIDE_SPECULATIVE, kStackSmall, false>(), fused_ptr<WIDE_SPECULATIVE, kStackLarge, false>(),
+          fused_ptr<IF_IF, kStackSmall, true>(), fused_ptr<IF_IF, kStackLarge, true>(),
+          fused_ptr<WHILE_WHILE, kStackSmall, true>(), fused_ptr<WHILE_WHILE, kStackLarge, true>(),
+          fused_ptr<SPECULATIVE, kStackSmall, true>(), fused_ptr<SPECULATIVE, kStackLarge, true>(),
+          fused_ptr<WIDE_SPECULATIVE, kStackSmall, true>(), fused_ptr<WIDE_SPECULATIVE, kStackLarge, true>()}) {
         cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
         if (e != cudaSuccess) return e;
     }

@@ -1,5 +1,5 @@
-// Direct lighting by light-source sampling: the sampling and integration steps of the
-// reference's CUDA "direct-wf" algorithm, usable on host and device.
+// Direct lighting: the sampling and integration steps of the reference's CUDA "direct-wf"
+// algorithm, usable on host and device.
 //
 // Restated from rt/cuda/bounce.cu and the libgi helpers it calls:
 //   * light choice by power: distribution_1d (libgi/discrete_distributions.cpp:33-60) over
@@ -9,6 +9,10 @@
 //     (bounce.cu:178-208): shadow ray from the hit point, t_max = distance - eps, pdf =
 //     t_max^2 / (cos_light * area), zero for a light facing away;
 //   * k::sample_light (bounce.cu:210-250): an emissive hit adds its emission and casts no ray;
+//   * direction sampling instead of light sampling: k::sample_uniform_dir (bounce.cu:33-73) with
+//     uniform_sample_hemisphere (libgi/sampling.h:20-28), k::sample_cos_dir (bounce.cu:91-129)
+//     with cosine_sample_hemisphere, both aligned to the normal facing the camera ray, and
+//     k::integrate_dir (bounce.cu:341-375): the emission of whatever the ray hits;
 //   * k::integrate_light (bounce.cu:380-410) with layered_gtr2 (bounce.cu:333-339): the
 //     Fresnel-weighted mix of lambertian_reflection (bounce.cu:291-295) and gtr_coat_reflection
 //     (bounce.cu:316-331, GGX ggx_d / ggx_g1 at bounce.cu:298-313, fresnel_dielectric at
@@ -20,8 +24,9 @@
 //   * normals are the triangles' geometric normals (the synthetic scenes carry no vertex
 //     normals); the shading normal faces the camera ray (flip_normals_to_ray), a light's normal
 //     follows its winding (lights are one-sided, as in sample_Li);
-//   * the three random numbers of a sample come from a PCG32 stream per (pixel, sample) instead
-//     of the reference's per-frame uniform buffer.
+//   * the random numbers of a sample (three for a light sample, two for a direction) come from
+//     a PCG32 stream per (pixel, sample) instead of the reference's per-frame uniform buffer;
+//   * sin and cos of 2 pi u come from pm::sincos_turns instead of sinf / cosf.
 #pragma once
 #include "pt_math.cuh"
 
@@ -37,7 +42,11 @@ using pm::sub;
 
 constexpr float kPi = 3.14159265358979323846f;                       // pi (libgi/rt.h:15)
 constexpr float kOneOverPi = (float)(1.0 / 3.14159265358979323846);  // one_over_pi (libgi/rt.h:16)
+constexpr float kOneOver2Pi = (float)(1.0 / (2.0 * 3.14159265358979323846));  // one_over_2pi (libgi/rt.h:17)
 constexpr float kEps = 1e-4f;  // ray::eps (libgi/rt.h:25)
+
+// The sampling strategies (grt_direct_params::sampling).
+enum : uint32_t { kSampleLight = 0, kSampleUniform = 1, kSampleCosine = 2 };
 
 // One material of the table: albedo, emission, index of refraction, roughness.
 struct material {
@@ -187,7 +196,30 @@ GRT_HD light_sample sample_li(f3 from, f3 a, f3 b, f3 c, f3 emissive, float x0, 
     return s;
 }
 
-// k::integrate_light (rt/cuda/bounce.cu:380-410): brightness * f * cos(theta) / pdf
+// uniform_sample_hemisphere (libgi/sampling.h:20-26): z = u0, r = sqrt|1 - z^2|, phi = 2 pi u1.
+GRT_HD f3 uniform_sample_hemisphere(float u0, float u1) {
+    const float r0 = sub(1.0f, mul(u0, u0));
+    const float r = sqrt_rn(r0 < 0.0f ? -r0 : r0);
+    float sn, cs;
+    pm::sincos_turns(u1, sn, cs);
+    return {mul(r, cs), mul(r, sn), u0};
+}
+
+// The direction of a direction sample around the normal ns facing the camera ray and its pdf:
+// k::sample_uniform_dir (bounce.cu:33-73: pdf one_over_2pi) and k::sample_cos_dir
+// (bounce.cu:91-129: pdf one_over_pi * cdot(w_i, n)).
+GRT_HD f3 sample_dir(uint32_t sampling, f3 ns, float x0, float x1, float &pdf) {
+    if (sampling == kSampleCosine) {
+        const f3 w = pm::align(pm::cosine_sample_hemisphere(x0, x1), ns);
+        pdf = mul(kOneOverPi, cdot(w, ns));
+        return w;
+    }
+    pdf = kOneOver2Pi;
+    return pm::align(uniform_sample_hemisphere(x0, x1), ns);
+}
+
+// k::integrate_light (rt/cuda/bounce.cu:380-410) and k::integrate_dir (bounce.cu:341-375, with
+// lcol the emission of the triangle the direction ray hit): brightness * f * cos(theta) / pdf
 GRT_HD f3 integrate(f3 lcol, f3 w_o, f3 w_i, f3 ns, const material &m, float pdf) {
     const f3 f = layered_gtr2(w_o, w_i, ns, m);
     const float cos_t = cdot(w_i, ns);

@@ -372,21 +372,32 @@ typedef struct grt_material {
 grt_status grt_set_material_table(grt_ctx *ctx, const grt_material *materials, uint32_t n);
 
 enum { GRT_DL_WAVEFRONT = 0, GRT_DL_FUSED = 1 };
+/* The sampling strategies of the reference's direct-wf algorithm (its `sampling` setting,
+ * gi/direct.cpp:503-541): a light chosen by power, or a direction on the hemisphere of the hit,
+ * uniform or cosine-weighted. */
+enum { GRT_DL_SAMPLE_LIGHT = 0, GRT_DL_SAMPLE_UNIFORM = 1, GRT_DL_SAMPLE_COSINE = 2 };
 typedef struct grt_direct_params {
-    uint32_t samples;  /* light samples per pixel */
-    uint32_t mode;     /* GRT_DL_WAVEFRONT or GRT_DL_FUSED */
-    uint64_t seed;     /* sample s of pixel i draws from the PCG32 stream seed + s * n + i */
+    uint32_t samples;   /* samples per pixel */
+    uint32_t mode;      /* GRT_DL_WAVEFRONT or GRT_DL_FUSED */
+    uint64_t seed;      /* sample s of pixel i draws from the PCG32 stream seed + s * n + i */
+    uint32_t sampling;  /* GRT_DL_SAMPLE_LIGHT (0), GRT_DL_SAMPLE_UNIFORM or GRT_DL_SAMPLE_COSINE */
+    uint32_t reserved;  /* must be 0 */
 } grt_direct_params;
 
-/* Direct lighting by light-source sampling, the reference's direct-wf steps (rt/cuda/bounce.cu:
- * k::sample_light 210-250, the shadow-ray trace, k::integrate_light 380-410 with its layered
- * GGX-coat BRDF): for every camera ray (DEVICE rays_dev, the grt_trace layout) the closest hit,
- * then `samples` times: a light chosen by power, a point on it, an any-hit shadow ray, and
- * framebuffer[i] += (radiance, 1) (a hit on an emitter first adds its emission). framebuffer_dev
- * is n float4, accumulated into. GRT_DL_WAVEFRONT runs the steps as separate launches with the
+/* Direct lighting, the reference's direct-wf steps (rt/cuda/bounce.cu): for every camera ray
+ * (DEVICE rays_dev, the grt_trace layout) the closest hit, then `samples` times a sample of the
+ * chosen strategy and framebuffer[i] += (radiance, 1) (a hit on an emitter first adds its
+ * emission and casts no ray):
+ *   GRT_DL_SAMPLE_LIGHT: a light chosen by power, a point on it, an any-hit shadow ray and the
+ *     light's emission (k::sample_light 210-250, k::integrate_light 380-410);
+ *   GRT_DL_SAMPLE_UNIFORM / _COSINE: a direction on the hemisphere around the normal (pdf
+ *     1 / 2pi, or cos / pi), a closest-hit ray and the emission of the triangle it hits
+ *     (k::sample_uniform_dir 33-73, k::sample_cos_dir 91-129, k::integrate_dir 341-375);
+ * each weighted by the layered GGX-coat BRDF times cos over the pdf. framebuffer_dev is n
+ * float4, accumulated into. GRT_DL_WAVEFRONT runs the steps as separate launches with the
  * selected tracer; GRT_DL_FUSED runs everything in one persistent kernel in the selected
  * tracer's loop order, a warp tracing 32 pixels' rays together phase by phase. Both forms give
- * the same bits (for the speculative orders, up to the near-ties of their camera-ray hits). */
+ * the same bits (for the speculative orders, up to the near-ties of their hits). */
 grt_status grt_direct(grt_ctx *ctx, const grt_direct_params *params, const float *rays_dev, uint32_t n,
                       float *framebuffer_dev, grt_stream_t stream);
 

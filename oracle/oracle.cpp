@@ -908,7 +908,7 @@ void orc_pathtrace(void *hp, const float *prim_rays8, const float *prim_hits4, u
     }
 }
 
-// ---- direct lighting by light-source sampling ------------------------------------------
+// ---- direct lighting ----------------------------------------------------------------------
 //
 // The reference's CUDA direct-wf steps: k::sample_light with k::sample_index and k::sample_Li
 // (rt/cuda/bounce.cu:148-250), the any-hit shadow ray, and k::integrate_light with layered_gtr2
@@ -918,7 +918,12 @@ void orc_pathtrace(void *hp, const float *prim_rays8, const float *prim_hits4, u
 // distribution_1d::build_cdf, libgi/discrete_distributions.cpp:33-45). Geometric normals (the
 // shading normal facing the camera ray, a light's normal by its winding), normalize as
 // v * (1 / sqrt(v . v)), and the three random numbers of sample s of pixel i from the PCG32
-// stream seed + s * n + i.
+// stream seed + s * n + i. The direction strategies instead draw two numbers from that stream,
+// sample uniform_sample_hemisphere (libgi/sampling.h:20-26; pdf one_over_2pi) or
+// cosine_sample_hemisphere (pdf one_over_pi * cdot(w_i, n)) around the normal facing the camera
+// ray (k::sample_uniform_dir / k::sample_cos_dir, rt/cuda/bounce.cu:33-142), trace a closest-hit
+// ray from the hit point (t_min 1e-4) and weight the emission of the triangle it hits
+// (k::integrate_dir, bounce.cu:341-375).
 
 struct dl_mat {
     float albedo[3], emissive[3], ior, roughness;
@@ -1028,9 +1033,19 @@ static v3 dl_brdf(v3 w_o, v3 w_i, v3 ns, const dl_mat &m) {
     return {k * diff.x + F * spec, k * diff.y + F * spec, k * diff.z + F * spec};
 }
 
-// one pixel: closest hit, then `samples` light samples accumulated into fb (4 floats)
+// a tangent-space sample rotated to the frame of n (align, libgi/util.h:212-218)
+static v3 align_to(v3 v, v3 n) {
+    const float s = std::signbit(n.z) ? -1.0f : 1.0f;
+    const v3 w = {v.x, v.y, v.z * s};
+    const v3 hh = {n.x, n.y, n.z + s};
+    const float k = vdot(w, hh) / (1.0f + (n.z < 0.f ? -n.z : n.z));
+    return {k * hh.x - w.x, k * hh.y - w.y, k * hh.z - w.z};
+}
+
+// one pixel: closest hit, then `samples` samples (sampling 0: light, 1: uniform direction,
+// 2: cosine-weighted direction) accumulated into fb (4 floats)
 static void dl_pixel(const bvh &h, const dl_set &L, const float *ray8, uint32_t pixel, uint32_t n, uint32_t samples,
-                     uint64_t seed, float *fb) {
+                     uint64_t seed, uint32_t sampling, float *fb) {
     const ray r = load_ray(ray8);
     const hit ph = closest_hit(h, r, nullptr);
     const v3 o = {ray8[0], ray8[1], ray8[2]}, d = {ray8[4], ray8[5], ray8[6]};
@@ -1044,6 +1059,34 @@ static void dl_pixel(const bvh &h, const dl_set &L, const float *ray8, uint32_t 
                 fb[1] += m.emissive[1];
                 fb[2] += m.emissive[2];
                 fb[3] += 0.0f;
+            } else if (sampling != 0) {
+                rng32 g;
+                g.seq(seed + (uint64_t)s * n + pixel);
+                const float x0 = g.uniform(), x1 = g.uniform();
+                uint32_t mat_id;
+                const v3 ns = facing_normal(h.sc, ph.ref, d, mat_id);
+                const v3 from = {o.x + ph.t * d.x, o.y + ph.t * d.y, o.z + ph.t * d.z};
+                v3 wi;
+                float pdf;
+                if (sampling == 2) {
+                    wi = cosine_dir(x0, x1, ns);
+                    pdf = (float)(1.0 / 3.14159265358979323846) * cdot3(wi, ns);
+                } else {
+                    const float r0 = 1.0f - x0 * x0;
+                    const float rr = std::sqrt(r0 < 0.0f ? -r0 : r0);
+                    float sn, cs;
+                    turn_sincos(x1, sn, cs);
+                    wi = align_to({rr * cs, rr * sn, x0}, ns);
+                    pdf = (float)(1.0 / (2.0 * 3.14159265358979323846));
+                }
+                float sr[8] = {from.x, from.y, from.z, 1e-4f, wi.x, wi.y, wi.z, FLT_MAX};
+                const hit lh = closest_hit(h, load_ray(sr), nullptr);
+                if (lh.t != FLT_MAX) {
+                    const float *em = L.mat(h.sc.t4[4 * (size_t)lh.ref + 3]).emissive;
+                    const v3 f = dl_brdf({-d.x, -d.y, -d.z}, wi, ns, m);
+                    const float cos_t = cdot3(wi, ns);
+                    rad = {em[0] * f.x * cos_t / pdf, em[1] * f.y * cos_t / pdf, em[2] * f.z * cos_t / pdf};
+                }
             } else if (!L.f.empty()) {
                 rng32 g;
                 g.seq(seed + (uint64_t)s * n + pixel);
@@ -1112,13 +1155,13 @@ static void dl_pixel(const bvh &h, const dl_set &L, const float *ray8, uint32_t 
 // Direct lighting of n camera rays (8 floats each) into fb (4 floats per ray, accumulated);
 // mats8: 8 floats per material (albedo rgb, emission rgb, ior, roughness).
 void orc_direct(void *hp, const float *rays8, uint64_t n, const float *mats8, uint32_t n_mat, uint32_t samples,
-                uint64_t seed, float *fb, int threads) {
+                uint64_t seed, uint32_t sampling, float *fb, int threads) {
     bvh *h = (bvh *)hp;
     const dl_set L = make_dl_set(h->sc, mats8, n_mat);
     set_threads(threads);
 #pragma omp parallel for schedule(dynamic, 256)
     for (int64_t i = 0; i < (int64_t)n; ++i)
-        dl_pixel(*h, L, rays8 + 8 * i, (uint32_t)i, (uint32_t)n, samples, seed, fb + 4 * i);
+        dl_pixel(*h, L, rays8 + 8 * i, (uint32_t)i, (uint32_t)n, samples, seed, sampling, fb + 4 * i);
 }
 
 int orc_max_threads() { return omp_get_max_threads(); }

@@ -44,6 +44,9 @@ def ref_available() -> bool:
     return os.path.exists(REF_SO)
 
 
+SAMPLING = {"light": 0, "uniform": 1, "cosine": 2}  # grt_direct_params::sampling
+
+
 class _BVHBase:
     prefix = ""
 
@@ -149,17 +152,18 @@ class OracleBVH(_BVHBase):
         self.lib.orc_any(self.h, _p(rays), n, _p(occ), _p(cnt) if counts else None, threads)
         return occ, cnt
 
-    def direct(self, rays, mats, samples, seed=0, threads=0):
+    def direct(self, rays, mats, samples, seed=0, threads=0, sampling="light"):
         """Direct lighting as grt_direct defines it: float32 [n, 4] frame buffer (radiance sum,
         sample count) for camera rays [n, 8] and materials [m, 8] (albedo rgb, emission rgb,
-        ior, roughness)."""
+        ior, roughness); sampling "light", "uniform" or "cosine"."""
         rays = np.ascontiguousarray(rays, np.float32)
         mats = np.ascontiguousarray(mats, np.float32)
         fb = np.zeros((rays.shape[0], 4), np.float32)
         f = self.lib.orc_direct
         f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_uint32,
-                      ctypes.c_uint32, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_int]
-        f(self.h, _p(rays), rays.shape[0], _p(mats), mats.shape[0], samples, seed, _p(fb), threads)
+                      ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_int]
+        f(self.h, _p(rays), rays.shape[0], _p(mats), mats.shape[0], samples, seed, SAMPLING[sampling], _p(fb),
+          threads)
         return fb
 
     def set_alpha(self, alpha):

@@ -1,6 +1,9 @@
-"""Direct lighting by light-source sampling (grt_direct: the reference's direct-wf steps) in
-the wavefront and the fused persistent form: both equal the oracle's restatement in every bit of
-the frame buffer for the exact loop orders, on spheres with a floor and two area lights."""
+"""Direct lighting (grt_direct: the reference's direct-wf steps) by light-source sampling and by
+uniform or cosine-weighted direction sampling, in the wavefront and the fused persistent form:
+both equal the oracle's restatement in every bit of the frame buffer for the exact loop orders,
+on spheres with a floor and two area lights; the three strategies estimate the same light."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -44,6 +47,76 @@ def test_direct_matches_oracle(api, lit_case, tracer, mode):
     got = fb.cpu().numpy()
     bad = (got.view(np.uint32) != want.view(np.uint32)).any(1)
     assert not bad.any(), f"{bad.sum()} pixels differ, first {np.nonzero(bad)[0][:5]}"
+    rt.close()
+
+
+@pytest.fixture(scope="module")
+def dir_cases(orc, lit_case):
+    sc, mats, rays, _ = lit_case
+    o = orc.OracleBVH(sc.vpos, sc.tris)
+    return {smp: o.direct(rays, mats, samples=3, seed=11, sampling=smp) for smp in ("uniform", "cosine")}
+
+
+@pytest.mark.parametrize("sampling", ["uniform", "cosine"])
+@pytest.mark.parametrize("tracer", ["while-while", "persistent-while-while", "if-if", "persistent-if-if"])
+@pytest.mark.parametrize("mode", ["wavefront", "fused"])
+def test_direct_direction_sampling_matches_oracle(api, lit_case, dir_cases, tracer, mode, sampling):
+    """k::sample_uniform_dir / k::sample_cos_dir, a closest-hit trace, k::integrate_dir."""
+    import torch
+    sc, mats, rays, _ = lit_case
+    want = dir_cases[sampling]
+    assert (want[:, :3].sum(1) > 0).mean() > 0.01 and np.isfinite(want).all()
+    rt = api.BatchRayTracer(0)
+    rt.build(sc.vpos, sc.tris)
+    rt.set_material_table(mats)
+    rt.select(tracer)
+    r = torch.from_numpy(rays).cuda()
+    fb = torch.zeros((rays.shape[0], 4), device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    rt.direct(r, fb, samples=3, mode=api.DL_FUSED if mode == "fused" else api.DL_WAVEFRONT, seed=11, stream=stream,
+              sampling=sampling)
+    rt.check(stream, timeout_ms=60000)
+    bad = (fb.cpu().numpy().view(np.uint32) != want.view(np.uint32)).any(1)
+    assert not bad.any(), f"{bad.sum()} pixels differ, first {np.nonzero(bad)[0][:5]}"
+    rt.close()
+
+
+def test_direct_strategies_estimate_the_same_light(api, lit_case):
+    """Light, uniform and cosine sampling are estimators of the same direct light: at 256 samples
+    per pixel their means over the pixels that see a non-emitting surface agree within a few
+    percent (the one-sidedness of light sampling and the noise of uniform sampling allowed for)."""
+    import torch
+    sc, mats, rays, _ = lit_case
+    rt = api.BatchRayTracer(0)
+    rt.build(sc.vpos, sc.tris)
+    rt.set_material_table(mats)
+    rt.select("persistent-speculative-while-while")
+    r = torch.from_numpy(rays).cuda()
+    stream = torch.cuda.Stream()
+    hits = torch.zeros((rays.shape[0], 4), device="cuda")
+    rt.trace(r, hits, False, stream.cuda_stream)
+    means = {}
+    for smp in ("light", "uniform", "cosine"):
+        fb = torch.zeros((rays.shape[0], 4), device="cuda")
+        rt.direct(r, fb, samples=256, mode=api.DL_FUSED, seed=5, stream=stream.cuda_stream, sampling=smp)
+        rt.check(stream.cuda_stream, timeout_ms=60000)
+        means[smp] = fb.cpu().numpy()
+    h = hits.cpu().numpy()
+    hit = h[:, 0] < 3e38
+    ref = h[:, 3].view(np.uint32)
+    emits = np.zeros(len(h), bool)
+    emits[hit] = mats[sc.tris[ref[hit], 3], 3:6].sum(1) > 0
+    sel = hit & ~emits
+    assert sel.mean() > 0.3
+    m = {k: v[sel, :3].mean() for k, v in means.items()}
+    assert all((v[:, 3] == 256).all() for v in means.values())
+    assert abs(m["uniform"] / m["light"] - 1) < 0.05 and abs(m["cosine"] / m["light"] - 1) < 0.05, m
+    bad = api.DirectParams(1, api.DL_FUSED, 0, 3, 0)  # no such strategy
+    fb = torch.zeros((rays.shape[0], 4), device="cuda")
+    with pytest.raises(api.GRTError) as e:
+        rt._check(api.lib().grt_direct(rt.ctx, ctypes.byref(bad), r.data_ptr(), int(r.shape[0]), fb.data_ptr(),
+                                       stream.cuda_stream))
+    assert e.value.status == 1
     rt.close()
 
 
