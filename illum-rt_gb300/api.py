@@ -130,6 +130,7 @@ _PROTOS = {
     "grt_set_alpha": (I, [VP, VP, U32, VP, U32, VP, U32]),
     "grt_set_material_table": (I, [VP, VP, U32]),
     "grt_direct": (I, [VP, P(DirectParams), VP, U32, VP, VP]),
+    "grt_hit_albedo": (I, [VP, U32, VP, U32, VP, VP]),
     "grt_set_bvh_cache": (I, [VP, ctypes.c_char_p]),
     "grt_bvh_cache_stats": (I, [VP, P(ctypes.c_uint64), P(ctypes.c_uint64)]),
     "grt_export_bvh_obj": (I, [VP, I, ctypes.c_char_p]),
@@ -361,6 +362,12 @@ class BatchRayTracer:
         p = DirectParams(int(samples), int(mode), int(seed), DL_SAMPLING[sampling], 0)
         self._check(lib().grt_direct(self.ctx, ctypes.byref(p), _ptr(rays), int(rays.shape[0]), _ptr(framebuffer),
                                      VP(stream or 0)))
+
+    def hit_albedo(self, rays, framebuffer, mode=DL_FUSED, stream=None):
+        """primary-wf's shading (grt_hit_albedo): framebuffer [n, 4] += (albedo of the closest
+        hit's material, 1) for CUDA rays [n, 8]."""
+        self._check(lib().grt_hit_albedo(self.ctx, int(mode), _ptr(rays), int(rays.shape[0]), _ptr(framebuffer),
+                                         VP(stream or 0)))
 
     def set_alpha(self, tc, mat_tex, textures):
         """Texture data of the alpha-aware tracers (grt_set_alpha): tc float32 [nv, 2] per vertex

@@ -126,9 +126,9 @@ grt_status grt_direct(grt_ctx *c, const grt_direct_params *p, const float *rays_
     if (p->mode == GRT_DL_FUSED) {
         const grt_tuning &t = c->tuning;
         const int stack = std::max(needed_stack(c), t.stack_entries);
-        e = launch_dl_fused(scene_for(c), ds, rays, n, p->samples, p->seed, p->sampling, fb, kTracers[c->tracer].order,
-                            stack, t.block_threads > 0 ? t.block_threads : 128, c->num_sms, c->d_err, c->d_counter,
-                            st);
+        e = launch_dl_fused(scene_for(c), ds, rays, n, p->samples, p->seed, p->sampling, 0u, fb,
+                            kTracers[c->tracer].order, stack, t.block_threads > 0 ? t.block_threads : 128, c->num_sms,
+                            c->d_err, c->d_counter, st);
         return e == cudaSuccess ? GRT_OK : cuda_fail(c, e, "launching the fused direct-lighting kernel");
     }
     // wavefront: hits (16 B), shadow rays (32 B), shadow hits (16 B), light colour + pdf (16 B)
@@ -161,6 +161,49 @@ grt_status grt_direct(grt_ctx *c, const grt_direct_params *p, const float *rays_
         if (e == cudaSuccess) e = launch_dl_integrate(ds, rays, hits, srays, shits, ls, n, p->sampling, fb, st);
     }
     return e == cudaSuccess ? GRT_OK : cuda_fail(c, e, "launching the direct-lighting steps");
+}
+
+grt_status grt_hit_albedo(grt_ctx *c, uint32_t mode, const float *rays_dev, uint32_t n, float *fb_dev,
+                          grt_stream_t stream) {
+    if (!c) return GRT_ERR_INVALID_ARG;
+    if (!c->built) return fail(c, GRT_ERR_NOT_BUILT, "grt_hit_albedo before a successful build");
+    if (!c->d_dl) return fail(c, GRT_ERR_INVALID_ARG, "grt_hit_albedo needs grt_set_material_table first");
+    if (n == 0) return GRT_OK;
+    if (!rays_dev || !fb_dev || !aligned16(rays_dev) || !aligned16(fb_dev))
+        return fail(c, GRT_ERR_INVALID_ARG, "null or misaligned ray / frame buffer");
+    if (mode > GRT_DL_FUSED) return fail(c, GRT_ERR_INVALID_ARG, "unknown mode");
+    if (kTracers[c->tracer].alpha) return fail(c, GRT_ERR_INVALID_ARG, "albedo shading has no alpha-aware form");
+    if (needed_stack(c) > kStackLarge) return fail(c, GRT_ERR_BVH_TOO_DEEP, "the BVH needs a deeper stack");
+    device_guard g(c->device);
+    const cudaStream_t st = (cudaStream_t)stream;
+    const dl_scene ds = dl_scene_of(c);
+    const float4 *rays = (const float4 *)rays_dev;
+    float4 *fb = (float4 *)fb_dev;
+    cudaError_t e = cudaSuccess;
+    if (mode == GRT_DL_FUSED) {
+        const grt_tuning &t = c->tuning;
+        const int stack = std::max(needed_stack(c), t.stack_entries);
+        e = launch_dl_fused(scene_for(c), ds, rays, n, 0u, 0u, GRT_DL_SAMPLE_LIGHT, 1u, fb, kTracers[c->tracer].order,
+                            stack, t.block_threads > 0 ? t.block_threads : 128, c->num_sms, c->d_err, c->d_counter,
+                            st);
+        return e == cudaSuccess ? GRT_OK : cuda_fail(c, e, "launching the fused albedo kernel");
+    }
+    const size_t need = (size_t)n * 80;  // the direct-lighting scratch; its first n * 16 bytes hold the hits
+    if (c->dl_scratch_bytes < need) {
+        if (c->d_dl_scratch) cudaFree(c->d_dl_scratch);
+        c->d_dl_scratch = nullptr;
+        c->dl_scratch_bytes = 0;
+        e = cudaMalloc(&c->d_dl_scratch, need);
+        if (e != cudaSuccess) return cuda_fail(c, e, "allocating the albedo buffers");
+        c->dl_scratch_bytes = need;
+    }
+    grt_hit *hits = (grt_hit *)c->d_dl_scratch;
+    const launch_params lp = params_for(c, false);
+    const dev_scene sc = scene_for(c);
+    e = kTracers[c->tracer].persistent ? launch_trace_persistent(sc, rays, hits, n, false, lp, c->d_err, c->d_counter, st)
+                                       : launch_trace_plain(sc, rays, hits, n, false, lp, c->d_err, st);
+    if (e == cudaSuccess) e = launch_add_albedo(ds, hits, n, fb, st);
+    return e == cudaSuccess ? GRT_OK : cuda_fail(c, e, "launching the albedo steps");
 }
 
 }  // extern "C"

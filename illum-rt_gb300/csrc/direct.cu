@@ -151,6 +151,26 @@ __global__ void __launch_bounds__(256) k_dl_integrate(dl_scene ds, const float4 
     fb[i] = plus(fb[i], rad, 1.0f);
 }
 
+// add_hitpoint_albedo (rt/cuda/kernels.cu:170-197), untextured: fb += (albedo, 1) of the hit
+// triangle's material, (0, 0, 0, 1) for a miss.
+__device__ __forceinline__ float4 albedo_of(const dl_scene &ds, float t, uint32_t ref) {
+    if (t == FLT_MAX) return make_float4(0.f, 0.f, 0.f, 1.f);
+    const dl::material m = material_of(ds, __ldg(ds.tris + ref).w);
+    return make_float4(m.albedo[0], m.albedo[1], m.albedo[2], 1.f);
+}
+
+__device__ __forceinline__ float4 plus4(float4 a, float4 b) {
+    return make_float4(pm::add(a.x, b.x), pm::add(a.y, b.y), pm::add(a.z, b.z), pm::add(a.w, b.w));
+}
+
+__global__ void __launch_bounds__(256) k_add_albedo(dl_scene ds, const grt_hit *__restrict__ hits, uint32_t n,
+                                                    float4 *fb) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const grt_hit h = hits[i];
+    fb[i] = plus4(fb[i], albedo_of(ds, h.t, h.ref));
+}
+
 // Fused form, warp-synchronous: a warp takes 32 consecutive pixels from the global counter,
 // traverses their camera rays together (closest hit), then for each sample prepares the light
 // samples, traverses the shadow rays together (any hit) and integrates into registers, in the
@@ -177,7 +197,7 @@ __device__ __forceinline__ void trace_all(trav_t &s, bool active, bool plain, co
 template <int ORDER, int STACK, bool DIR>
 __global__ void __launch_bounds__(256) k_dl_fused(dev_scene sc, dl_scene ds, const float4 *__restrict__ rays,
                                                   uint32_t n, uint32_t samples, uint64_t seed, uint32_t sampling,
-                                                  float4 *fb, unsigned *err, unsigned *counter) {
+                                                  uint32_t albedo, float4 *fb, unsigned *err, unsigned *counter) {
     extern __shared__ int s_stack[];
     if (stop_requested_at_entry(err)) return;  // the host asked the context to stop
     constexpr bool WIDE = ORDER == WIDE_SPECULATIVE;
@@ -201,6 +221,7 @@ __global__ void __launch_bounds__(256) k_dl_fused(dev_scene sc, dl_scene ds, con
         trace_all<ORDER, STACK, false>(s, active, plain, sc, r, stk, stride, err);
         const float ht = active ? s.hit.t : FLT_MAX;
         const uint32_t href = s.hit.ref;
+        if (albedo && active) acc = plus4(acc, albedo_of(ds, ht, href));  // primary-wf's shading
         for (uint32_t smp = 0; smp < samples; ++smp) {
             dl_prep p;
             if (active) {
@@ -228,8 +249,8 @@ template <int ORDER, int STACK, bool DIR> const void *fused_ptr() { return (cons
 
 template <int ORDER, int STACK, bool DIR>
 cudaError_t fused_run(const dev_scene &sc, const dl_scene &ds, const float4 *rays, uint32_t n, uint32_t samples,
-                      uint64_t seed, uint32_t sampling, float4 *fb, int bt, int num_sms, unsigned *err,
-                      unsigned *counter, cudaStream_t st) {
+                      uint64_t seed, uint32_t sampling, uint32_t albedo, float4 *fb, int bt, int num_sms,
+                      unsigned *err, unsigned *counter, cudaStream_t st) {
     const size_t smem = (size_t)STACK * bt * sizeof(int);
     int per_sm = 0;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dl_fused<ORDER, STACK, DIR>, bt, smem);
@@ -237,20 +258,20 @@ cudaError_t fused_run(const dev_scene &sc, const dl_scene &ds, const float4 *ray
     if (per_sm < 1) per_sm = 1;
     e = cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
-    k_dl_fused<ORDER, STACK, DIR><<<per_sm * num_sms, bt, smem, st>>>(sc, ds, rays, n, samples, seed, sampling, fb,
-                                                                       err, counter);
+    k_dl_fused<ORDER, STACK, DIR><<<per_sm * num_sms, bt, smem, st>>>(sc, ds, rays, n, samples, seed, sampling,
+                                                                       albedo, fb, err, counter);
     return cudaGetLastError();
 }
 
 template <int ORDER, bool DIR>
 cudaError_t fused_run(const dev_scene &sc, const dl_scene &ds, const float4 *rays, uint32_t n, uint32_t samples,
-                      uint64_t seed, uint32_t sampling, float4 *fb, int stack_entries, int bt, int num_sms,
-                      unsigned *err, unsigned *counter, cudaStream_t st) {
+                      uint64_t seed, uint32_t sampling, uint32_t albedo, float4 *fb, int stack_entries, int bt,
+                      int num_sms, unsigned *err, unsigned *counter, cudaStream_t st) {
     return stack_entries <= kStackSmall
-               ? fused_run<ORDER, kStackSmall, DIR>(sc, ds, rays, n, samples, seed, sampling, fb, bt, num_sms, err,
-                                                    counter, st)
-               : fused_run<ORDER, kStackLarge, DIR>(sc, ds, rays, n, samples, seed, sampling, fb, bt, num_sms, err,
-                                                    counter, st);
+               ? fused_run<ORDER, kStackSmall, DIR>(sc, ds, rays, n, samples, seed, sampling, albedo, fb, bt, num_sms,
+                                                    err, counter, st)
+               : fused_run<ORDER, kStackLarge, DIR>(sc, ds, rays, n, samples, seed, sampling, albedo, fb, bt, num_sms,
+                                                    err, counter, st);
 }
 
 }  // namespace
@@ -272,16 +293,23 @@ cudaError_t launch_dl_integrate(const dl_scene &ds, const float4 *rays, const gr
     return cudaGetLastError();
 }
 
+cudaError_t launch_add_albedo(const dl_scene &ds, const grt_hit *hits, uint32_t n, float4 *fb, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    k_add_albedo<<<(n + 255) / 256, 256, 0, st>>>(ds, hits, n, fb);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_dl_fused(const dev_scene &sc, const dl_scene &ds, const float4 *rays, uint32_t n, uint32_t samples,
-                            uint64_t seed, uint32_t sampling, float4 *fb, int order, int stack_entries, int bt,
-                            int num_sms, unsigned *err, unsigned *counter, cudaStream_t st) {
+                            uint64_t seed, uint32_t sampling, uint32_t albedo, float4 *fb, int order,
+                            int stack_entries, int bt, int num_sms, unsigned *err, unsigned *counter,
+                            cudaStream_t st) {
     if (n == 0) return cudaSuccess;
 #define GRT_DL_RUN(O)                                                                                             \
     return sampling == dl::kSampleLight                                                                          \
-               ? fused_run<O, false>(sc, ds, rays, n, samples, seed, sampling, fb, stack_entries, bt, num_sms, err, \
-                                     counter, st)                                                                 \
-               : fused_run<O, true>(sc, ds, rays, n, samples, seed, sampling, fb, stack_entries, bt, num_sms, err,  \
-                                    counter, st)
+               ? fused_run<O, false>(sc, ds, rays, n, samples, seed, sampling, albedo, fb, stack_entries, bt,     \
+                                     num_sms, err, counter, st)                                                   \
+               : fused_run<O, true>(sc, ds, rays, n, samples, seed, sampling, albedo, fb, stack_entries, bt,      \
+                                    num_sms, err, counter, st)
     switch (order) {
         case IF_IF: GRT_DL_RUN(IF_IF);
         case SPECULATIVE: GRT_DL_RUN(SPECULATIVE);

@@ -32,11 +32,15 @@ cudaError_t launch_dl_sample(const dl_scene &ds, const float4 *rays, const grt_h
 cudaError_t launch_dl_integrate(const dl_scene &ds, const float4 *rays, const grt_hit *hits, const float4 *shadow_rays,
                                 const grt_hit *shadow_hits, const float4 *lsample, uint32_t n, uint32_t sampling,
                                 float4 *fb, cudaStream_t st);
+// fb += (albedo, 1) of every hit (add_hitpoint_albedo), the wavefront form's shading launch.
+cudaError_t launch_add_albedo(const dl_scene &ds, const grt_hit *hits, uint32_t n, float4 *fb, cudaStream_t st);
 // The fused form: camera-ray traversal, `samples` samples with their ray traversals, and the
-// integration, in one persistent launch, in any loop order.
+// integration, in one persistent launch, in any loop order. `albedo` != 0 adds
+// add_hitpoint_albedo's (albedo, 1) of every camera ray before the samples.
 cudaError_t launch_dl_fused(const dev_scene &sc, const dl_scene &ds, const float4 *rays, uint32_t n, uint32_t samples,
-                            uint64_t seed, uint32_t sampling, float4 *fb, int order, int stack_entries,
-                            int block_threads, int num_sms, unsigned *err, unsigned *counter, cudaStream_t st);
+                            uint64_t seed, uint32_t sampling, uint32_t albedo, float4 *fb, int order,
+                            int stack_entries, int block_threads, int num_sms, unsigned *err, unsigned *counter,
+                            cudaStream_t st);
 cudaError_t prepare_dl_kernels();
 
 }  // namespace grt

@@ -401,6 +401,15 @@ typedef struct grt_direct_params {
 grt_status grt_direct(grt_ctx *ctx, const grt_direct_params *params, const float *rays_dev, uint32_t n,
                       float *framebuffer_dev, grt_stream_t stream);
 
+/* The shading step of the reference's primary-wf algorithm, add_hitpoint_albedo
+ * (rt/cuda/kernels.cu:170-197): for every camera ray (DEVICE rays_dev) the closest hit, and
+ * framebuffer[i] += (albedo of the hit triangle's material, 1), or (0, 0, 0, 1) for a miss,
+ * with the materials of grt_set_material_table (untextured). mode GRT_DL_WAVEFRONT traces with
+ * the selected tracer and shades in a second launch; GRT_DL_FUSED does both in one persistent
+ * kernel in the selected tracer's loop order. */
+grt_status grt_hit_albedo(grt_ctx *ctx, uint32_t mode, const float *rays_dev, uint32_t n, float *framebuffer_dev,
+                          grt_stream_t stream);
+
 /* ---- alpha-aware tracing ---------------------------------------------------------------- */
 
 /* One single-channel texture: width x height alpha values, row by row. */

@@ -166,6 +166,23 @@ class OracleBVH(_BVHBase):
           threads)
         return fb
 
+    def hit_albedo(self, rays, mats, fb=None):
+        """add_hitpoint_albedo (rt/cuda/kernels.cu:170-197), untextured: fb + (albedo of the
+        closest hit's material, 1), (0, 0, 0, 1) for a miss; materials beyond the table have the
+        reference's default material (albedo 0)."""
+        mats = np.ascontiguousarray(mats, np.float32).reshape(-1, 8)
+        h, _ = self.closest(rays)
+        add = np.zeros((h.shape[0], 4), np.float32)
+        add[:, 3] = 1.0
+        hit = h[:, 0] != np.float32(3.4028234663852886e38)
+        mat = self._t[h[hit, 3].view(np.uint32), 3]
+        known = mat < mats.shape[0]
+        alb = np.zeros((mat.shape[0], 3), np.float32)
+        alb[known] = mats[mat[known], 0:3]
+        add[hit, 0:3] = alb
+        base = np.zeros_like(add) if fb is None else np.asarray(fb, np.float32)
+        return (base + add).astype(np.float32)
+
     def set_alpha(self, alpha):
         """Alpha-aware tracing from now on (alpha: an AlphaSet), or off with None."""
         f = self.lib.orc_set_alpha

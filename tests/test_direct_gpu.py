@@ -1,7 +1,8 @@
 """Direct lighting (grt_direct: the reference's direct-wf steps) by light-source sampling and by
 uniform or cosine-weighted direction sampling, in the wavefront and the fused persistent form:
 both equal the oracle's restatement in every bit of the frame buffer for the exact loop orders,
-on spheres with a floor and two area lights; the three strategies estimate the same light."""
+on spheres with a floor and two area lights; the three strategies estimate the same light.
+Also primary-wf's albedo shading (grt_hit_albedo) in both forms."""
 import ctypes
 
 import numpy as np
@@ -117,6 +118,37 @@ def test_direct_strategies_estimate_the_same_light(api, lit_case):
         rt._check(api.lib().grt_direct(rt.ctx, ctypes.byref(bad), r.data_ptr(), int(r.shape[0]), fb.data_ptr(),
                                        stream.cuda_stream))
     assert e.value.status == 1
+    rt.close()
+
+
+@pytest.mark.parametrize("tracer", ["while-while", "persistent-while-while", "if-if", "persistent-speculative-while-while"])
+@pytest.mark.parametrize("mode", ["wavefront", "fused"])
+def test_hit_albedo_matches_oracle(api, orc, lit_case, tracer, mode):
+    """primary-wf's shading step, add_hitpoint_albedo: fb += (albedo of the hit, 1), accumulated
+    onto what the frame buffer held; one material id beyond the table gets the default (0)."""
+    import torch
+    sc, mats, rays, _ = lit_case
+    tris = sc.tris.copy()
+    tris[::97, 3] = mats.shape[0] + 5  # a few triangles with an unknown material
+    o = orc.OracleBVH(sc.vpos, tris)
+    fb0 = np.random.default_rng(7).random((rays.shape[0], 4), dtype=np.float32)
+    want = o.hit_albedo(rays, mats, fb0)
+    rt = api.BatchRayTracer(0)
+    rt.build(sc.vpos, tris)
+    rt.set_material_table(mats)
+    rt.select(tracer)
+    r = torch.from_numpy(rays).cuda()
+    fb = torch.from_numpy(fb0.copy()).cuda()
+    stream = torch.cuda.current_stream().cuda_stream
+    rt.hit_albedo(r, fb, mode=api.DL_FUSED if mode == "fused" else api.DL_WAVEFRONT, stream=stream)
+    rt.check(stream, timeout_ms=60000)
+    got = fb.cpu().numpy()
+    bad = (got.view(np.uint32) != want.view(np.uint32)).any(1)
+    if "speculative" in tracer:  # the other triangle of a near-tie may carry another albedo
+        assert bad.mean() < 1e-3, int(bad.sum())
+    else:
+        assert not bad.any(), f"{bad.sum()} pixels differ, first {np.nonzero(bad)[0][:5]}"
+    assert (got[:, 3] == fb0[:, 3] + 1).all()
     rt.close()
 
 
