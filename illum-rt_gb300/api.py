@@ -139,6 +139,7 @@ _PROTOS = {
     "grt_host_bvh_leaf_stats": (I, [VP, P(LeafStats)]),
     "grt_build_device": (I, [VP, VP, U32, VP, U32, U32, VP]),
     "grt_build_scenes_device": (I, [VP, VP, U32, U32, VP]),
+    "grt_refit": (I, [VP, VP, U32, VP]),
 }
 
 
@@ -334,6 +335,7 @@ class BatchRayTracer:
         self.tracer = name
 
     def build(self, vpos, tris, split=None, max_tris=None, planes=None, esc=True) -> dict:
+        self._refit_key = None  # autograd.closest_hits(builder="refit") builds anew
         v = np.ascontiguousarray(vpos, np.float32)
         t = np.ascontiguousarray(tris, np.uint32)
         o = make_opts(split or self.bvh_type, max_tris or self.bvh_max_tris_per_node, planes or self.bvh_planes, esc)
@@ -343,11 +345,18 @@ class BatchRayTracer:
     def build_device(self, vpos, tris, max_tris=None, stream=None) -> dict:
         """The GPU builder (grt_build_device) on CUDA tensors: vpos float32 [nv, 4], tris
         int32/uint32 [nt, 4]. Returns the build statistics."""
+        self._refit_key = None  # autograd.closest_hits(builder="refit") builds anew
         _check_cuda_tensor(vpos, "vpos", 4)
         _check_cuda_tensor(tris, "tris", 4)
         self._check(lib().grt_build_device(self.ctx, _ptr(vpos), int(vpos.shape[0]), _ptr(tris), int(tris.shape[0]),
                                            int(max_tris or self.bvh_max_tris_per_node), VP(stream or 0)))
         return self.info()
+
+    def refit(self, vpos, stream=None):
+        """grt_refit: the built tree refitted to new vertex positions, a CUDA tensor float32
+        [nv, 4] of the built scene's vertex count."""
+        _check_cuda_tensor(vpos, "vpos", 4)
+        self._check(lib().grt_refit(self.ctx, _ptr(vpos), int(vpos.shape[0]), VP(stream or 0)))
 
     def set_material_table(self, mats):
         """Materials for direct lighting (grt_set_material_table): float32 [m, 8] = albedo rgb,
@@ -487,6 +496,7 @@ class BatchRayTracer:
     # -- many scenes in one launch ----------------------------------------------------------
     def build_scenes(self, scenes, **opts) -> list:
         """scenes: list of (vpos float32 [nv, 4], tris uint32 [nt, 4]). Returns per-scene stats."""
+        self._refit_key = None  # autograd.closest_hits(builder="refit") builds anew
         keep = [(np.ascontiguousarray(v, np.float32), np.ascontiguousarray(t, np.uint32)) for v, t in scenes]
         arr = (Mesh * len(keep))(*[Mesh(_ptr(v), v.shape[0], _ptr(t), t.shape[0]) for v, t in keep])
         o = make_opts(**{"split": self.bvh_type, "max_tris": self.bvh_max_tris_per_node, **opts})
@@ -501,6 +511,7 @@ class BatchRayTracer:
     def build_scenes_device(self, scenes, max_tris=None, stream=None) -> list:
         """The GPU builder over a scene set (grt_build_scenes_device): scenes is a list of
         (vpos CUDA float32 [nv, 4], tris CUDA int32/uint32 [nt, 4]). Returns per-scene stats."""
+        self._refit_key = None  # autograd.closest_hits(builder="refit") builds anew
         for v, t in scenes:
             _check_cuda_tensor(v, "vpos", 4)
             _check_cuda_tensor(t, "tris", 4)

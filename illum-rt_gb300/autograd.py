@@ -5,8 +5,9 @@ beta and gamma differentiable with respect to the vertex positions ``vpos`` [nv,
 [n, 8] (origin in columns 0-2, direction in 4-6). The hit triangle of each ray is held fixed:
 the forward pass builds the BVH from the current vertices (with the reference builder on the
 host, or with builder="gpu" with the GPU builder straight from the device tensor, which avoids
-the round trip through host memory when the vertices change every step) and traces with the
-selected tracer; the backward pass (grt_adjoint) recomputes each intersection
+the round trip through host memory when the vertices change every step, or with
+builder="refit", which refits the tree the tracer already holds for this mesh to the current
+vertices and builds on the GPU only the first time) and traces with the selected tracer; the backward pass (grt_adjoint) recomputes each intersection
 from the vertices and propagates dL/d(t, beta, gamma) to the three vertices and the ray.
 Misses (t = FLT_MAX) get no gradient; mask them out of the loss.
 """
@@ -21,12 +22,17 @@ class _ClosestHits(torch.autograd.Function):
     def forward(ctx, vpos, rays, tracer, tris, builder):
         with torch.no_grad():
             stream = torch.cuda.current_stream(rays.device).cuda_stream
-            if builder == "gpu":
+            if builder in ("gpu", "refit"):
                 v4 = torch.ones((vpos.shape[0], 4), dtype=torch.float32, device=vpos.device)
                 v4[:, :3] = vpos.detach()
                 t4 = tris if isinstance(tris, torch.Tensor) else torch.from_numpy(
                     np.ascontiguousarray(tris, np.uint32).view(np.int32))
-                tracer.build_device(v4, t4.to(vpos.device).contiguous(), stream=stream)
+                key = (int(vpos.shape[0]), id(tris))
+                if builder == "refit" and getattr(tracer, "_refit_key", None) == key:
+                    tracer.refit(v4, stream=stream)
+                else:
+                    tracer.build_device(v4, t4.to(vpos.device).contiguous(), stream=stream)
+                    tracer._refit_key = key if builder == "refit" else None
             elif builder == "reference":
                 v4 = np.ones((vpos.shape[0], 4), np.float32)
                 v4[:, :3] = vpos.detach().cpu().numpy()
@@ -61,5 +67,6 @@ class _ClosestHits(torch.autograd.Function):
 def closest_hits(tracer, vpos: torch.Tensor, tris, rays: torch.Tensor, builder: str = "reference"):
     """(t, beta, gamma, ref) of each ray, differentiable in vpos [nv, 3] and rays [n, 8].
     builder: "reference" (host build, hits bit-identical to the reference tracer with an exact
-    tracer) or "gpu" (GPU build; hits equal except near-ties)."""
+    tracer), "gpu" (GPU build; hits equal except near-ties) or "refit" (the tracer's tree for
+    the same `tris` object refitted to the current vertices; hits equal except near-ties)."""
     return _ClosestHits.apply(vpos, rays, tracer, tris, builder)

@@ -142,10 +142,14 @@ grt_status grt_build(grt_ctx *c, const float *vpos4, uint32_t nv, const uint32_t
     up(&c->d_recs, flat.records.data(), rb);
     up(&c->d_vpos, vpos4, vb);
     up(&c->d_tris, tris4, tb);
+    up(&c->d_parent, flat.parent.data(), flat.parent.size() * 4);
+    up(&c->d_wide_index, wide.wide_index.data(), wide.wide_index.size() * 4);
     if (e != cudaSuccess) {
         free_scene(c);
         return cuda_fail(c, e, "uploading the BVH");
     }
+    c->n_links = flat.inner;
+    c->n_records = (uint32_t)(flat.records.size() / 12);
     c->stats.upload_ms = ms_since(t0);
 
     c->sc.nodes = (const float4 *)c->d_nodes;

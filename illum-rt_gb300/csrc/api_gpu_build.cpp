@@ -10,6 +10,7 @@
 
 #include "ctx.hpp"
 #include "gpu_build.hpp"
+#include "refit.hpp"
 
 using namespace grt;
 
@@ -70,11 +71,13 @@ grt_status grt_build_device(grt_ctx *c, const float *vpos4_dev, uint32_t nv, con
     if (e == cudaSuccess) e = cudaMalloc(&tmp.scratch, scratch);
     if (e == cudaSuccess) e = cudaMalloc(&tmp.wide_index, (size_t)std::max(nt, 1u) * 4);
     if (e == cudaSuccess) e = cudaMalloc(&tmp.info, 8 * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_parent, (size_t)std::max(nt, 1u) * 4);
     if (e == cudaSuccess && nv) e = cudaMemcpyAsync(c->d_vpos, vpos4_dev, (size_t)nv * 16, cudaMemcpyDeviceToDevice, st);
     if (e == cudaSuccess && nt) e = cudaMemcpyAsync(c->d_tris, tris4_dev, (size_t)nt * 16, cudaMemcpyDeviceToDevice, st);
     if (e == cudaSuccess)
         e = gpu_build_binary((const float4 *)c->d_vpos, nv, (const uint4 *)c->d_tris, nt, (int)max_tris, tmp.scratch,
-                             scratch, (float4 *)c->d_nodes, (float4 *)c->d_recs, tmp.wide_index, tmp.info, st);
+                             scratch, (float4 *)c->d_nodes, (float4 *)c->d_recs, tmp.wide_index,
+                             (int32_t *)c->d_parent, tmp.info, st);
     int32_t info[8] = {0};
     if (e == cudaSuccess) e = cudaMemcpyAsync(info, tmp.info, sizeof(info), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -111,8 +114,56 @@ grt_status grt_build_device(grt_ctx *c, const float *vpos4_dev, uint32_t nv, con
     c->stats.tri_records = nt;
     c->stats.depth = c->depth;
     c->stats.device_bytes = nb + rb + wb + (size_t)nv * 16 + (size_t)nt * 16;
+    c->d_wide_index = tmp.wide_index;  // kept for refits
+    tmp.wide_index = nullptr;
+    c->n_links = nt > 1 ? nt - 1 : 0;
+    c->n_records = nt;
     c->gpu_tree = true;
     c->built = true;
+    return GRT_OK;
+}
+
+grt_status grt_refit(grt_ctx *c, const float *vpos4_dev, uint32_t nv, grt_stream_t stream) {
+    if (!c) return GRT_ERR_INVALID_ARG;
+    if (!c->built) return fail(c, GRT_ERR_NOT_BUILT, "grt_refit before a successful build");
+    if (nv != c->nv) return fail(c, GRT_ERR_INVALID_ARG, "grt_refit needs the built scene's vertex count");
+    if (nv && (!vpos4_dev || !aligned16(vpos4_dev)))
+        return fail(c, GRT_ERR_INVALID_ARG, "null or misaligned vertex array");
+    if (c->n_links && !c->d_parent) return fail(c, GRT_ERR_INVALID_ARG, "this scene has no refit links");
+    device_guard g(c->device);
+    const cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = cudaSuccess;
+    if (!c->d_refit) e = cudaMalloc(&c->d_refit, 256 + (size_t)std::max(c->n_links, 1u) * 4);
+    if (e == cudaSuccess && nv)
+        e = cudaMemcpyAsync(c->d_vpos, vpos4_dev, (size_t)nv * 16, cudaMemcpyDeviceToDevice, st);
+    refit_args a;
+    a.vpos = (const float4 *)c->d_vpos;
+    a.tris = (const uint4 *)c->d_tris;
+    a.nv = nv;
+    a.nt = c->nt;
+    a.records = (float4 *)c->d_recs;
+    a.n_records = c->sc.empty ? 0 : c->n_records;
+    a.nodes = (float4 *)c->d_nodes;
+    a.links = (const int32_t *)c->d_parent;
+    a.n_nodes = c->sc.empty ? 0 : c->n_links;
+    a.root = c->sc.root;
+    a.flags = (unsigned *)c->d_refit;
+    a.arrive = (unsigned *)((char *)c->d_refit + 256);
+    if (e == cudaSuccess) e = launch_refit(a, st);
+    // the 4-wide nodes take their children's records from the refitted binary nodes
+    if (e == cudaSuccess && a.n_nodes && c->d_wide_index && c->d_nodes4)
+        e = gpu_build_wide((const float4 *)c->d_nodes, (const int32_t *)c->d_wide_index, c->n_links + 1,
+                           (float4 *)c->d_nodes4, st);
+    unsigned flags = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&flags, a.flags, sizeof(flags), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(c, e, "refitting the BVH");
+    ++c->scene_generation;  // captured path-tracing graphs hold the scene's flags
+    c->sc.finite = (flags & kRefitNonFinite) ? 0 : 1;
+    // the device tree is no longer the reference builder's: nothing to export
+    c->tree = ref_tree();
+    c->gpu_tree = true;
+    if (flags & kRefitBadTree) return fail(c, GRT_ERR_TRAVERSAL, "refit found a malformed tree");
     return GRT_OK;
 }
 
@@ -159,7 +210,7 @@ grt_status grt_build_scenes_device(grt_ctx *c, const grt_mesh *meshes, uint32_t 
         e = gpu_build_binary((const float4 *)m.vpos4, m.nv, (const uint4 *)m.tris4, m.nt, (int)max_tris, tmp.scratch,
                              scratch, (float4 *)((char *)c->ms.d_nodes + off[i][0]),
                              (float4 *)((char *)c->ms.d_recs + off[i][1]), (int32_t *)((char *)wide_pool + off[i][2]),
-                             tmp.info + 8 * (size_t)i, st);
+                             nullptr, tmp.info + 8 * (size_t)i, st);
     }
     std::vector<int32_t> info((size_t)count * 8, 0);
     if (e == cudaSuccess) e = cudaMemcpyAsync(info.data(), tmp.info, info.size() * 4, cudaMemcpyDeviceToHost, st);

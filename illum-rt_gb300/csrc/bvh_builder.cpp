@@ -394,12 +394,15 @@ bool flatten_bvh(const ref_tree &tree, const float *vpos4, const uint32_t *tris4
     };
     out.inner = inner;
     out.nodes.assign((size_t)inner * 16, 0.f);
+    out.parent.assign(inner, -1);
     bool ok = true;
     for (size_t i = 0; i < N.size(); ++i) {
         if (!N[i].inner()) continue;
         const ref_node &n = N[i];
         float *d = out.nodes.data() + (size_t)inner_id[i] * 16;
         int32_t cl = child_ref(n.link_l, ok), cr = child_ref(n.link_r, ok);
+        if (cl >= 0) out.parent[cl] = inner_id[i] * 2;
+        if (cr >= 0) out.parent[cr] = inner_id[i] * 2 + 1;
         const float *lo[2] = {n.lmin, n.rmin}, *hi[2] = {n.lmax, n.rmax};
         const int32_t ref[2] = {cl, cr};
         for (int side = 0; side < 2; ++side) {
@@ -413,9 +416,10 @@ bool flatten_bvh(const ref_tree &tree, const float *vpos4, const uint32_t *tris4
             std::memcpy(e + 6, &ref[side], 4);
         }
     }
+    out.inner_id = std::move(inner_id);
     const ref_node &root = N[tree.root];
     if (root.inner()) {
-        out.root = inner_id[tree.root];
+        out.root = out.inner_id[tree.root];
     } else if (root.link_r == 0) {
         out.empty = true;
         out.root = 0;
@@ -486,8 +490,10 @@ bool flatten_bvh4(const ref_tree &tree, const flat_bvh &flat, flat_bvh4 &out, st
         return (uint32_t)(out.nodes.size() / 32 - 1);
     };
     // recursive lambda via explicit function object (depth is at most the reference depth)
+    out.wide_index.assign(flat.inner + 1, -1);  // one entry past the last node, as the GPU builder's
     std::function<uint32_t(uint32_t)> build = [&](uint32_t bin) -> uint32_t {
         const uint32_t w = new_node();
+        out.wide_index[flat.inner_id[bin]] = (int32_t)w;
         const ref_node &n = N[bin];
         child ch[4];
         int k = 0;

@@ -49,6 +49,8 @@ bool build_reference_bvh(const float *vpos4, uint32_t nv, const uint32_t *tris4,
 struct flat_bvh {
     std::vector<float> nodes;    // 16 floats per inner node
     std::vector<float> records;  // 12 floats per record
+    std::vector<int32_t> parent;    // per inner node: (parent << 1) | side, -1 for the root (refit)
+    std::vector<int32_t> inner_id;  // per reference node: its inner node index, -1 for a leaf
     int32_t root = 0;            // child reference of the root (a leaf reference if the tree is one leaf)
     uint32_t depth = 0;          // edges from the root to the deepest leaf
     uint32_t inner = 0;
@@ -70,6 +72,7 @@ bool flatten_bvh(const ref_tree &tree, const float *vpos4, const uint32_t *tris4
 static const int32_t kEmptyChild = 0x7fffffff;
 struct flat_bvh4 {
     std::vector<float> nodes;  // 32 floats per wide node
+    std::vector<int32_t> wide_index;  // per binary inner node and one more: the wide node it heads, -1 for none
     int32_t root = 0;          // wide node 0, or a leaf reference if the tree is one leaf
     uint32_t count = 0;
     uint32_t stack_bound = 0;  // most stack entries a traversal can hold

@@ -22,6 +22,11 @@ struct grt_ctx {
     grt::ref_tree tree;
     grt::dev_scene sc{};
     void *d_nodes = nullptr, *d_recs = nullptr, *d_vpos = nullptr, *d_tris = nullptr, *d_nodes4 = nullptr;
+    // refit links: per binary node (parent << 1) | side (-1: root or not in the tree), and the
+    // 4-wide node each binary node heads (-1: none); n_links entries each
+    void *d_parent = nullptr, *d_wide_index = nullptr;
+    void *d_refit = nullptr;  // refit scratch: flags, then one arrival counter per node
+    uint32_t n_links = 0, n_records = 0;
     uint32_t nv = 0, nt = 0, depth = 0, stack_bound4 = 0;
     grt_bvh_stats stats{};
     int tracer = 0;  // index into kTracers
@@ -105,12 +110,14 @@ inline grt_status cuda_fail(grt_ctx *c, cudaError_t e, const char *what) {
 }
 
 inline void free_scene(grt_ctx *c) {
-    for (void **p : {&c->d_nodes, &c->d_recs, &c->d_vpos, &c->d_tris, &c->d_nodes4, &c->d_alpha, &c->d_dl}) {
+    for (void **p : {&c->d_nodes, &c->d_recs, &c->d_vpos, &c->d_tris, &c->d_nodes4, &c->d_alpha, &c->d_dl,
+                     &c->d_parent, &c->d_wide_index, &c->d_refit}) {
         if (*p) cudaFree(*p);
         *p = nullptr;
     }
     c->built = false;
     c->gpu_tree = false;
+    c->n_links = c->n_records = 0;
 }
 
 inline double ms_since(std::chrono::steady_clock::time_point t0) {

@@ -289,8 +289,9 @@ __global__ void __launch_bounds__(kThreads) k_records(const float4 *__restrict__
 
 // 5a. which inner nodes become 4-wide nodes: reachable (no collapsed ancestor) and at even depth
 __global__ void __launch_bounds__(kThreads) k_wide_flags(int n, const uint8_t *__restrict__ collapsed,
-                                                         const int32_t *__restrict__ parent_inner, int32_t *flag,
-                                                         int32_t *info) {
+                                                         const int32_t *__restrict__ parent_inner,
+                                                         const float4 *__restrict__ nodes, int32_t *flag,
+                                                         int32_t *links, int32_t *info) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int f = 0;
@@ -317,6 +318,11 @@ __global__ void __launch_bounds__(kThreads) k_wide_flags(int n, const uint8_t *_
         if (reach) {
             atomicAdd(info + GB_INNER, 1);
             f = (depth & 1) == 0;
+            if (links) {  // refit links of the node's inner children: (parent << 1) | side
+                const int cl = __float_as_int(nodes[4 * (size_t)i + 1].z), cr = __float_as_int(nodes[4 * (size_t)i + 3].z);
+                if (cl >= 0 && cl < n - 1) links[cl] = 2 * i;
+                if (cr >= 0 && cr < n - 1) links[cr] = 2 * i + 1;
+            }
         }
     }
     flag[i] = f;
@@ -444,7 +450,7 @@ size_t gpu_build_scratch_bytes(uint32_t max_tris) { return carve(nullptr, max_tr
 
 cudaError_t gpu_build_binary(const float4 *vpos, uint32_t nv, const uint4 *tris, uint32_t nt, int max_leaf,
                              void *scratch, size_t scratch_bytes, float4 *nodes, float4 *records,
-                             int32_t *wide_index, int32_t *info, cudaStream_t st) {
+                             int32_t *wide_index, int32_t *links, int32_t *info, cudaStream_t st) {
     arena A = carve(scratch, nt);
     if (A.total > scratch_bytes) return cudaErrorInvalidValue;
     k_init_info<<<1, 32, 0, st>>>(info, A.cbounds);
@@ -461,6 +467,7 @@ cudaError_t gpu_build_binary(const float4 *vpos, uint32_t nv, const uint4 *tris,
     if (e == cudaSuccess) e = cudaMemsetAsync(A.collapsed, 1, (size_t)nt, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(A.parent_inner, 0xff, (size_t)nt * 4, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(A.parent_leaf, 0xff, (size_t)nt * 4, st);
+    if (e == cudaSuccess && links) e = cudaMemsetAsync(links, 0xff, (size_t)nt * 4, st);
     if (e != cudaSuccess) return e;
     if (nt > 1)
         k_radix_tree<<<blocks_for(nt - 1), kThreads, 0, st>>>(A.keys_b, (int)nt, A.children, A.range,
@@ -470,7 +477,7 @@ cudaError_t gpu_build_binary(const float4 *vpos, uint32_t nv, const uint4 *tris,
                                          info);
     k_records<<<nb, kThreads, 0, st>>>(vpos, tris, A.vals_b, nt, nv, records);
     if (nt > 1) {
-        k_wide_flags<<<nb, kThreads, 0, st>>>((int)nt, A.collapsed, A.parent_inner, A.flag, info);
+        k_wide_flags<<<nb, kThreads, 0, st>>>((int)nt, A.collapsed, A.parent_inner, nodes, A.flag, links, info);
         cb = A.cub_bytes;
         e = cub::DeviceScan::ExclusiveSum(A.cub, cb, A.flag, A.excl, (int)nt, st);
         if (e != cudaSuccess) return e;

@@ -451,6 +451,17 @@ grt_status grt_build_device(grt_ctx *ctx, const float *vpos4_dev, uint32_t nv, c
 grt_status grt_build_scenes_device(grt_ctx *ctx, const grt_mesh *meshes, uint32_t count, uint32_t max_tris_per_node,
                                    grt_stream_t stream);
 
+/* Refits the context's scene (built by grt_build or grt_build_device) to new vertex positions:
+ * DEVICE float4 array of the built scene's nv vertices, copied. The tree keeps its topology;
+ * the triangle records and every node box (binary and 4-wide) are recomputed on the GPU from
+ * the new positions, which is far cheaper than a build when the mesh changes a little between
+ * uses (the steps of a gradient descent on the vertices). No counterpart in the reference,
+ * which rebuilds on every change (batch_rt::build, rt/cuda/base.cpp:88-117). The refitted tree
+ * is no longer the reference builder's: closest hits equal the reference's on the new vertices
+ * except near-ties, and grt_export_bvh fails until the next build. Ordered after earlier work on
+ * `stream`; returns when the refit is done. */
+grt_status grt_refit(grt_ctx *ctx, const float *vpos4_dev, uint32_t nv, grt_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif
