@@ -52,9 +52,11 @@ def parse_args():
     ap.add_argument("--profile-case", action="store_true",
                     help="run one tuned and one plain step (no graphs) and exit (for ncu captures)")
     ap.add_argument("--profile-paths", type=int, default=1 << 20, help="paths of the --profile-case step")
-    ap.add_argument("--workload", default="spheres", choices=["spheres", "soups64", "direct"],
+    ap.add_argument("--workload", default="spheres", choices=["spheres", "soups64", "direct", "adjoint"],
                     help="soups64: 64 uneven triangle soups traced in one launch, host vs GPU BVH builds; "
-                         "direct: light-source sampling, fused persistent kernel vs wavefront steps")
+                         "direct: light-source sampling, fused persistent kernel vs wavefront steps; "
+                         "adjoint: differentiable hits on the displaced icosphere, one optimisation step "
+                         "(tree update, closest hits, adjoint) with a host build, a GPU build or a refit")
     return ap.parse_args()
 
 
@@ -675,6 +677,79 @@ def run_direct(args, samples: int = 8):
     rt.close()
 
 
+def run_adjoint(args):
+    """Differentiable closest hits on the displaced icosphere (81,920 triangles, 512x512 camera
+    rays): one step of a gradient descent on the vertices = moving the vertices, updating the
+    tree, the closest hits and the adjoint (dL/dvertices, dL/drays) of a loss on (t, beta,
+    gamma). The tree update is a host build (the reference's way), a GPU build or a refit; the
+    vertices move every step, so every form does its update every step. Value: rays per second
+    of the refit form."""
+    import torch
+    import __graft_entry__ as ge
+    ge.load_package()
+    from illum_rt_gb300 import api, workloads as wl
+    sc, rays_np = wl.icosphere_primary(res=512)
+    n = rays_np.shape[0]
+    rays = torch.from_numpy(rays_np).cuda()
+    tris = torch.from_numpy(sc.tris.view(np.int32)).cuda()
+    v0 = torch.from_numpy(sc.vpos).cuda()
+    step_dir = torch.from_numpy(np.random.default_rng(6).normal(size=sc.vpos.shape).astype(np.float32)).cuda()
+    step_dir[:, 3] = 0.0
+    hits = torch.zeros((n, 4), device="cuda")
+    g3 = torch.from_numpy(np.random.default_rng(7).normal(size=(n, 3)).astype(np.float32)).cuda()
+    gv = torch.zeros((sc.vpos.shape[0], 3), device="cuda")
+    gr = torch.zeros((n, 8), device="cuda")
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    tuning = load_tuning(torch.cuda.get_device_name(0))
+    tracer = tuning.get("tracer", "persistent-speculative-while-while")
+
+    def run(form):
+        rt = api.BatchRayTracer(0)
+        rt.select(tracer)
+        rt.build_device(v0, tris, stream=sp)
+        vhost = sc.vpos.copy()
+
+        def one(i):
+            v = v0 + (1e-4 * (i % 7)) * step_dir
+            if form == "host":
+                vhost[:, :3] = v[:, :3].cpu().numpy()
+                rt.build(vhost, sc.tris)
+            elif form == "gpu":
+                rt.build_device(v, tris, stream=sp)
+            else:
+                rt.refit(v, stream=sp)
+            rt.trace(rays, hits, False, sp)
+            gv.zero_()
+            rt.adjoint(rays, hits, g3, gv, gr, vpos=v, stream=sp)
+
+        with torch.cuda.stream(stream):
+            for i in range(max(3, args.warmup)):
+                one(i)
+            rt.check(sp)
+            torch.cuda.synchronize()
+            steps = args.steps if form != "host" else max(3, min(args.steps, 10))
+            t0 = time.perf_counter()
+            for i in range(steps):
+                one(i)
+            rt.check(sp)
+            torch.cuda.synchronize()
+            ms = (time.perf_counter() - t0) * 1e3 / steps
+        rt.close()
+        return ms
+
+    res = {form: run(form) for form in ("refit", "gpu", "host")}
+    line = {"metric": "Mrays/s differentiable closest hits (tree update + trace + adjoint per step)",
+            "unit": "Mrays/s", "value": round(n / res["refit"] / 1e3, 1), "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": "icosphere-81920 (6 subdivisions, radial displacement 0.05), 512x512 rays",
+                       "tracer": tracer, "timing": "host wall clock per step, synchronised"},
+            "ms_per_step": {k: round(v, 4) for k, v in res.items()},
+            "speedup_refit_vs_host_build": round(res["host"] / res["refit"], 1),
+            "speedup_refit_vs_gpu_build": round(res["gpu"] / res["refit"], 2)}
+    print(json.dumps(line), flush=True)
+
+
 def run_profile_case(paths: int):
     """One tuned step, then one plain step (no graphs; 1,048,576 paths unless asked otherwise):
     a case whose launches ncu can capture one by one."""
@@ -704,6 +779,8 @@ def main():
         run_soups64(args)
     elif args.workload == "direct":
         run_direct(args)
+    elif args.workload == "adjoint":
+        run_adjoint(args)
     else:
         run_gb300(args)
 
