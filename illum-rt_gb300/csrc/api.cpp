@@ -241,7 +241,7 @@ grt_status grt_bvh_info(grt_ctx *c, grt_bvh_stats *out) {
 grt_status grt_export_bvh(grt_ctx *c, uint32_t *nodes14, uint32_t *index, uint32_t *root) {
     if (!c) return GRT_ERR_INVALID_ARG;
     if (!c->built) return fail(c, GRT_ERR_NOT_BUILT, "no scene has been built");
-    if (c->gpu_tree) return fail(c, GRT_ERR_INVALID_ARG, "a BVH built on the GPU has no reference tree to export");
+    if (c->gpu_tree) return fail(c, GRT_ERR_INVALID_ARG, "a BVH built on the GPU or refitted has no reference tree to export");
     export_tree(c->tree, nodes14, index, root);
     return GRT_OK;
 }

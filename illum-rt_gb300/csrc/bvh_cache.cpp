@@ -278,14 +278,14 @@ grt_status grt_bvh_cache_stats(const grt_ctx *c, uint64_t *hits, uint64_t *misse
 grt_status grt_export_bvh_obj(grt_ctx *c, int max_depth, const char *path) {
     if (!c || !path) return GRT_ERR_INVALID_ARG;
     if (!c->built) return fail(c, GRT_ERR_NOT_BUILT, "no scene has been built");
-    if (c->gpu_tree) return fail(c, GRT_ERR_INVALID_ARG, "a BVH built on the GPU has no reference tree to export");
+    if (c->gpu_tree) return fail(c, GRT_ERR_INVALID_ARG, "a BVH built on the GPU or refitted has no reference tree to export");
     return write_obj(c->tree, max_depth, path) ? GRT_OK : fail(c, GRT_ERR_INVALID_ARG, std::string("cannot write ") + path);
 }
 
 grt_status grt_bvh_leaf_stats(grt_ctx *c, grt_leaf_stats *s) {
     if (!c || !s) return GRT_ERR_INVALID_ARG;
     if (!c->built) return fail(c, GRT_ERR_NOT_BUILT, "no scene has been built");
-    if (c->gpu_tree) return fail(c, GRT_ERR_INVALID_ARG, "a BVH built on the GPU has no reference tree");
+    if (c->gpu_tree) return fail(c, GRT_ERR_INVALID_ARG, "a BVH built on the GPU or refitted has no reference tree");
     const char *e = leaf_stats(c->tree, s);
     return e ? fail(c, GRT_ERR_INVALID_ARG, e) : GRT_OK;
 }

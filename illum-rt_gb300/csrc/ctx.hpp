@@ -18,7 +18,7 @@ struct grt_ctx {
     int num_sms = 0;
     std::string err;
     bool built = false;
-    bool gpu_tree = false;  // built by grt_build_device: no reference tree to export
+    bool gpu_tree = false;  // built by grt_build_device or refitted: no reference tree to export
     grt::ref_tree tree;
     grt::dev_scene sc{};
     void *d_nodes = nullptr, *d_recs = nullptr, *d_vpos = nullptr, *d_tris = nullptr, *d_nodes4 = nullptr;
