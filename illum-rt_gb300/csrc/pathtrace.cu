@@ -463,7 +463,7 @@ __global__ void __launch_bounds__(256) k_pt_fused(dev_scene sc, pt_scene ps, pt_
         // traversal phase
         for (int it = 1;; ++it) {
             if (SPEC)
-                trav_spec_iter<STACK, false, false, WIDE, ALPHA, kPendPaths, kExitPaths>(s, tracing, plain, sc, r, stk, stride, err);
+                trav_spec_iter<STACK, false, false, WIDE, ALPHA, kPendPaths, kExitPaths, kVisitsPaths>(s, tracing, plain, sc, r, stk, stride, err);
             else if (tracing && plain)
                 trav_advance<ORDER, STACK, false, false, true, ALPHA>(s, sc, r, stk, stride, err);
             else if (tracing)

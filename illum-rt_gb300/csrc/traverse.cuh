@@ -571,7 +571,8 @@ __device__ __forceinline__ void spec_node4(trav_t &s, const dev_scene &sc, const
 // postponed leaf use the closest hit from before that leaf, so the ray may visit nodes the
 // reference would have culled. A triangle found there can replace the reference's answer only
 // if its t lies within rounding of the culled box's entry distance: a near-tie.
-template <int STACK, bool ANY, bool COUNT, bool WIDE = false, bool ALPHA = false, int PEND = 1, int EXIT = 0>
+template <int STACK, bool ANY, bool COUNT, bool WIDE = false, bool ALPHA = false, int PEND = 1, int EXIT = 0,
+          int VISITS = 3>
 __device__ __forceinline__ void trav_spec_iter(trav_t &s, bool active, bool plain, const dev_scene &sc,
                                                const ray_t &r, int *stk, int stride, unsigned *err) {
     const bool mine = active && !s.done;
@@ -608,18 +609,17 @@ __device__ __forceinline__ void trav_spec_iter(trav_t &s, bool active, bool plai
             }
         }
     };
-    // Three visits per warp vote (measured on GB300: 4.4 % faster than one visit per vote, and
-    // 1.2 % faster than two); a lane that has stopped searching may make up to two more
-    // speculative node visits before the leaf phase, which leaves its hit within the near-tie
-    // class. The warp's visit slots of this call are added to every live lane's step count (an
+    // VISITS node visits per warp vote (three measured on GB300 4.4 % faster than one visit per
+    // vote, and 1.2 % faster than two); a lane that has stopped searching may make up to
+    // VISITS - 1 more speculative node visits before the leaf phase, which leaves its hit within
+    // the near-tie class. The warp's visit slots of this call are added to every live lane's step count (an
     // upper bound of its own visits), so the work of a ray on a malformed tree stays bounded
     // across calls, without a per-visit count.
     uint32_t slots = 0;
     for (;;) {
-        visit();
-        visit();
-        visit();
-        slots += 3;
+#pragma unroll
+        for (int v = 0; v < VISITS; ++v) visit();
+        slots += VISITS;
         const bool searching = mine && !s.done && s.more && s.pend == 0;
         if (__popc(__ballot_sync(0xffffffffu, searching)) <= EXIT || slots >= kStepLimit) break;
     }
