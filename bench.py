@@ -769,9 +769,53 @@ def run_profile_case(paths: int):
     print(json.dumps({"profile_case": "ok", "paths": N_PATHS, "rays": rays_in_results(step)}))
 
 
+def run_profile_case_other(workload: str):
+    """One launch of the dominant kernel of the direct or soups64 workload at full size, for ncu:
+    direct: the fused direct-lighting kernel (speculative order, 8 light samples, 1024x1024);
+    soups64: the scene-set trace of all 64 soups (GPU-built trees)."""
+    import torch
+    import __graft_entry__ as ge
+    ge.load_package()
+    from illum_rt_gb300 import api, workloads as wl
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    tuning = load_tuning(torch.cuda.get_device_name(0))
+    rt = api.BatchRayTracer(0)
+    if workload == "direct":
+        sc, mats, rays_np = wl.lit_spheres(count=256, res=RES)
+        rays = torch.from_numpy(rays_np).cuda()
+        fb = torch.zeros((rays.shape[0], 4), device="cuda")
+        rt.build(sc.vpos, sc.tris)
+        rt.set_material_table(mats)
+        rt.select("speculative-while-while")
+        rt.direct(rays, fb, 8, mode=api.DL_FUSED, seed=3, stream=sp)
+        n = rays.shape[0] * 8
+    else:
+        tris_n, rays_n = wl.multi_scene_sizes()
+        scenes, rays = [], []
+        for i, (nt, nr) in enumerate(zip(tris_n, rays_n)):
+            sc = wl.soup(1000 + i, nt, sigma=0.5)
+            lo, hi = sc.bounds()
+            scenes.append((torch.from_numpy(sc.vpos).cuda(), torch.from_numpy(sc.tris.view(np.int32)).cuda()))
+            rays.append(torch.from_numpy(wl.shell_rays(2000 + i, lo, hi, nr)).cuda())
+        hits = [torch.zeros((r.shape[0], 4), device="cuda") for r in rays]
+        rt.select(tuning.get("tracer", "persistent-speculative-while-while"))
+        kw = {k: v for k, v in tuning.items() if k in ("block_threads", "refill_threshold", "refill_period")}
+        if kw:
+            rt.set_tuning(**kw)
+        rt.build_scenes_device(scenes, max_tris=tuning.get("max_tris", 4), stream=sp)
+        rt.trace_multi([(i, rays[i], hits[i]) for i in range(len(rays))], stream=sp)
+        n = sum(r.shape[0] for r in rays)
+    rt.check(sp)
+    rt.close()
+    print(json.dumps({"profile_case": "ok", "workload": workload, "units": int(n)}))
+
+
 def main():
     args = parse_args()
-    if args.profile_case:
+    if args.profile_case and args.workload in ("direct", "soups64"):
+        run_profile_case_other(args.workload)
+    elif args.profile_case:
         run_profile_case(args.profile_paths)
     elif args.impl == "reference":
         run_reference(args)
