@@ -172,11 +172,12 @@ __global__ void __launch_bounds__(256) k_add_albedo(dl_scene ds, const grt_hit *
 }
 
 // Fused form, warp-synchronous: a warp takes 32 consecutive pixels from the global counter,
-// traverses their camera rays together (closest hit), then for each sample prepares the light
-// samples, traverses the shadow rays together (any hit) and integrates into registers, in the
-// order the wavefront steps add to the frame buffer. All lanes of a warp are always in the same
-// phase, so every loop order works, the speculative ones included, and the shadow rays of one
-// sample stay as coherent as in the wavefront form.
+// traverses their camera rays together (closest hit), then for each sample prepares the
+// samples, traverses their rays together (any hit for shadow rays to a light, closest hit for
+// sampled directions) and integrates into registers, in the order the wavefront steps add to
+// the frame buffer. All lanes of a warp are always in the same phase, so every loop order works,
+// the speculative ones included, and the rays of one sample stay as coherent as in the
+// wavefront form.
 template <int ORDER, int STACK, bool ANY>
 __device__ __forceinline__ void trace_all(trav_t &s, bool active, bool plain, const dev_scene &sc, const ray_t &r,
                                           int *stk, int stride, unsigned *err) {
