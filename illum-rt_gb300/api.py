@@ -140,6 +140,7 @@ _PROTOS = {
     "grt_build_device": (I, [VP, VP, U32, VP, U32, U32, VP]),
     "grt_build_scenes_device": (I, [VP, VP, U32, U32, VP]),
     "grt_refit": (I, [VP, VP, U32, VP]),
+    "grt_incoherent_rays": (I, [VP, ctypes.c_float, ctypes.c_float, ctypes.c_uint64, VP, U32, VP]),
 }
 
 
@@ -245,6 +246,8 @@ class BatchRayTracer:
         self.bvh_type = "sah"         # `bvh type`
         self.bvh_max_tris_per_node = 4  # `bvh max_tris`
         self.bvh_planes = 16            # `bvh sah <planes>` of the CPU tracer
+        self.use_incoherence = False    # `incoherence r1 r2`
+        self.incoherence_r1 = self.incoherence_r2 = 0.0
         self.rd: RayData | None = None
         self.tracer = TRACERS[0]
 
@@ -267,11 +270,20 @@ class BatchRayTracer:
 
     # -- wf::batch_ray_tracer surface -----------------------------------------------------
     def interprete(self, command: str) -> bool:
-        """Script commands of the CUDA tracer and platform (`bvh type`, `bvh max_tris`,
-        rt/cuda/base.cpp:134-153; `raytracer`, rt/cuda/platform.cpp:102-131) and of the CPU
-        tracer (`bvh om|sm|sah <planes>|triangles single|multiple <n>|statistics|export
-        <depth> <file>`, rt/cpu/bvh2.cpp:192-241); returns False for unknown ones."""
+        """Script commands of the CUDA tracer and platform (`incoherence r1 r2`, `bvh type`,
+        `bvh max_tris`, rt/cuda/base.cpp:119-153; `raytracer`, rt/cuda/platform.cpp:102-131)
+        and of the CPU tracer (`bvh om|sm|sah <planes>|triangles single|multiple <n>|statistics|
+        export <depth> <file>`, rt/cpu/bvh2.cpp:192-241); returns False for unknown ones."""
         words = command.split()
+        if words and words[0] == "incoherence":
+            if len(words) != 3:
+                raise ValueError('"incoherence" requires exactly two positive float values')
+            r1, r2 = float(words[1]), float(words[2])
+            if r1 < 0 or r2 < 0:
+                raise ValueError('"incoherence" requires exactly two positive float values')
+            if r1 != 0 or r2 != 0:  # as the reference: 0 0 leaves the setting unchanged
+                self.use_incoherence, self.incoherence_r1, self.incoherence_r2 = True, r1, r2
+            return True
         if len(words) == 3 and words[:2] == ["bvh", "type"]:
             if words[2] not in SPLIT:
                 raise ValueError('"bvh type" must be one of "sm", "om", "sah"')
@@ -351,6 +363,17 @@ class BatchRayTracer:
         self._check(lib().grt_build_device(self.ctx, _ptr(vpos), int(vpos.shape[0]), _ptr(tris), int(tris.shape[0]),
                                            int(max_tris or self.bvh_max_tris_per_node), VP(stream or 0)))
         return self.info()
+
+    def incoherent_rays(self, n: int, seed: int = 1234, stream=None, r1=None, r2=None):
+        """grt_incoherent_rays: a CUDA tensor [n, 8] of the `incoherence r1 r2` test rays of the
+        built scene (the radii of the last `incoherence` command unless given)."""
+        import torch
+        rays = torch.empty((int(n), 8), dtype=torch.float32, device=f"cuda:{self.device}")
+        a = self.incoherence_r1 if r1 is None else r1
+        b = self.incoherence_r2 if r2 is None else r2
+        self._check(lib().grt_incoherent_rays(self.ctx, float(a), float(b), int(seed), _ptr(rays), int(n),
+                                              VP(stream or 0)))
+        return rays
 
     def refit(self, vpos, stream=None):
         """grt_refit: the built tree refitted to new vertex positions, a CUDA tensor float32

@@ -85,6 +85,7 @@ grt_status grt_destroy(grt_ctx *c) {
         if (c->d_scratch) cudaFree(c->d_scratch);
         if (c->d_albedo) cudaFree(c->d_albedo);
         if (c->d_dl_scratch) cudaFree(c->d_dl_scratch);
+        if (c->d_extent) cudaFree(c->d_extent);
         if (c->pt_graph.exec) cudaGraphExecDestroy(c->pt_graph.exec);
         if (c->d_err) cudaFree(c->d_err);
         if (c->h_flag) cudaFreeHost(c->h_flag);

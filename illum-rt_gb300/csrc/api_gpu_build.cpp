@@ -10,6 +10,7 @@
 
 #include "ctx.hpp"
 #include "gpu_build.hpp"
+#include "raygen.hpp"
 #include "refit.hpp"
 
 using namespace grt;
@@ -165,6 +166,24 @@ grt_status grt_refit(grt_ctx *c, const float *vpos4_dev, uint32_t nv, grt_stream
     c->gpu_tree = true;
     if (flags & kRefitBadTree) return fail(c, GRT_ERR_TRAVERSAL, "refit found a malformed tree");
     return GRT_OK;
+}
+
+grt_status grt_incoherent_rays(grt_ctx *c, float r1, float r2, uint64_t seed, float *rays_dev, uint32_t n,
+                               grt_stream_t stream) {
+    if (!c) return GRT_ERR_INVALID_ARG;
+    if (!c->built) return fail(c, GRT_ERR_NOT_BUILT, "grt_incoherent_rays before a successful build");
+    if (c->nv == 0) return fail(c, GRT_ERR_INVALID_ARG, "the scene has no vertices to place the spheres in");
+    if (!(r1 >= 0.f) || !(r2 >= 0.f))  // the reference's check (rt/cuda/base.cpp:125-126)
+        return fail(c, GRT_ERR_INVALID_ARG, "incoherence radii must be non-negative");
+    if (n == 0) return GRT_OK;
+    if (!rays_dev || !aligned16(rays_dev)) return fail(c, GRT_ERR_INVALID_ARG, "null or misaligned ray buffer");
+    device_guard g(c->device);
+    cudaError_t e = cudaSuccess;
+    if (!c->d_extent) e = cudaMalloc(&c->d_extent, 32);
+    if (e == cudaSuccess)
+        e = launch_incoherent_rays((const float4 *)c->d_vpos, c->nv, r1, r2, seed, (float4 *)rays_dev, n,
+                                   (uint32_t *)c->d_extent, (cudaStream_t)stream);
+    return e == cudaSuccess ? GRT_OK : cuda_fail(c, e, "generating the incoherent rays");
 }
 
 grt_status grt_build_scenes_device(grt_ctx *c, const grt_mesh *meshes, uint32_t count, uint32_t max_tris,

@@ -26,6 +26,7 @@ struct grt_ctx {
     // 4-wide node each binary node heads (-1: none); n_links entries each
     void *d_parent = nullptr, *d_wide_index = nullptr;
     void *d_refit = nullptr;  // refit scratch: flags, then one arrival counter per node
+    void *d_extent = nullptr;  // six words of scratch for the incoherent-ray generator
     uint32_t n_links = 0, n_records = 0;
     uint32_t nv = 0, nt = 0, depth = 0, stack_bound4 = 0;
     grt_bvh_stats stats{};

@@ -462,6 +462,19 @@ grt_status grt_build_scenes_device(grt_ctx *ctx, const grt_mesh *meshes, uint32_
  * `stream`; returns when the refit is done. */
 grt_status grt_refit(grt_ctx *ctx, const float *vpos4_dev, uint32_t nv, grt_stream_t stream);
 
+/* ---- ray generation ------------------------------------------------------------------- */
+
+/* The incoherent test rays of the reference CUDA tracer's `incoherence r1 r2` setting
+ * (rt/cuda/base.cpp:120-133; batch_cam_ray_setup, rt/cuda/rni.cpp:36-84; setup_ray_incoherent,
+ * rt/cuda/kernels.cu:75-156), written to DEVICE rays_dev (n rays, the grt_trace layout): two
+ * balls at the quarter points of the largest dimension of the built scene's vertex extent,
+ * radius r_max = a quarter of that dimension; each ray starts at a uniform point in the ball of
+ * radius r1 * r_max around the first centre and aims at a uniform point in the ball of radius
+ * r2 * r_max around the second (a radius of 0: the centre), t_min 0, t_max FLT_MAX. The random
+ * numbers come from a PCG32 stream per ray (seed + ray index) instead of cuRAND's MTGP32. */
+grt_status grt_incoherent_rays(grt_ctx *ctx, float r1, float r2, uint64_t seed, float *rays_dev, uint32_t n,
+                               grt_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif
