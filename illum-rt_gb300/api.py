@@ -80,6 +80,13 @@ DL_WAVEFRONT, DL_FUSED = 0, 1
 DL_SAMPLING = {"light": 0, "uniform": 1, "cosine": 2}  # GRT_DL_SAMPLE_*
 
 
+TIMING_KINDS = ("trace", "trace_multi", "pathtrace", "direct", "adjoint", "tree", "rays")  # GRT_TIME_*
+
+
+class Timing(ctypes.Structure):
+    _fields_ = [("calls", ctypes.c_uint64 * len(TIMING_KINDS)), ("ms", ctypes.c_double * len(TIMING_KINDS))]
+
+
 class Mesh(ctypes.Structure):
     _fields_ = [("vpos4", ctypes.c_void_p), ("nv", ctypes.c_uint32), ("tris4", ctypes.c_void_p), ("nt", ctypes.c_uint32)]
 
@@ -140,6 +147,8 @@ _PROTOS = {
     "grt_build_device": (I, [VP, VP, U32, VP, U32, U32, VP]),
     "grt_build_scenes_device": (I, [VP, VP, U32, U32, VP]),
     "grt_refit": (I, [VP, VP, U32, VP]),
+    "grt_set_timing": (I, [VP, I]),
+    "grt_timing_stats": (I, [VP, P(Timing), I]),
     "grt_incoherent_rays": (I, [VP, ctypes.c_float, ctypes.c_float, ctypes.c_uint64, VP, U32, VP]),
 }
 
@@ -363,6 +372,16 @@ class BatchRayTracer:
         self._check(lib().grt_build_device(self.ctx, _ptr(vpos), int(vpos.shape[0]), _ptr(tris), int(tris.shape[0]),
                                            int(max_tris or self.bvh_max_tris_per_node), VP(stream or 0)))
         return self.info()
+
+    def set_timing(self, enabled: bool = True):
+        """grt_set_timing: per-call device timers (the reference's wavefront step timers)."""
+        self._check(lib().grt_set_timing(self.ctx, int(bool(enabled))))
+
+    def timing_stats(self, reset: bool = False) -> dict:
+        """grt_timing_stats: {kind: (calls, device ms)} since the last reset."""
+        t = Timing()
+        self._check(lib().grt_timing_stats(self.ctx, ctypes.byref(t), int(bool(reset))))
+        return {k: (int(t.calls[i]), float(t.ms[i])) for i, k in enumerate(TIMING_KINDS)}
 
     def incoherent_rays(self, n: int, seed: int = 1234, stream=None, r1=None, r2=None):
         """grt_incoherent_rays: a CUDA tensor [n, 8] of the `incoherence r1 r2` test rays of the

@@ -86,6 +86,11 @@ grt_status grt_destroy(grt_ctx *c) {
         if (c->d_albedo) cudaFree(c->d_albedo);
         if (c->d_dl_scratch) cudaFree(c->d_dl_scratch);
         if (c->d_extent) cudaFree(c->d_extent);
+        for (const auto &q : c->timing.pending) {
+            cudaEventDestroy(q.a);
+            cudaEventDestroy(q.b);
+        }
+        for (cudaEvent_t e : c->timing.pool) cudaEventDestroy(e);
         if (c->pt_graph.exec) cudaGraphExecDestroy(c->pt_graph.exec);
         if (c->d_err) cudaFree(c->d_err);
         if (c->h_flag) cudaFreeHost(c->h_flag);
@@ -330,6 +335,66 @@ grt_status grt_get_tuning(grt_ctx *c, grt_tuning *t) {
     return GRT_OK;
 }
 
+timed_call::timed_call(grt_ctx *ctx, int k, cudaStream_t s) : c(ctx), kind(k), st(s) {
+    if (!c->timing.enabled) return;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return;
+    a = c->timing.take();
+    if (a && cudaEventRecord(a, st) != cudaSuccess) {
+        c->timing.pool.push_back(a);
+        a = nullptr;
+    }
+}
+
+timed_call::~timed_call() {
+    if (!a) return;
+    cudaEvent_t b = c->timing.take();
+    if (b && cudaEventRecord(b, st) == cudaSuccess) {
+        c->timing.pending.push_back({kind, a, b});
+        return;
+    }
+    c->timing.pool.push_back(a);
+    if (b) c->timing.pool.push_back(b);
+}
+
+grt_status grt_set_timing(grt_ctx *c, int enabled) {
+    if (!c) return GRT_ERR_INVALID_ARG;
+    c->timing.enabled = enabled != 0;
+    return GRT_OK;
+}
+
+grt_status grt_timing_stats(grt_ctx *c, grt_timing *out, int reset) {
+    if (!c) return GRT_ERR_INVALID_ARG;
+    device_guard g(c->device);
+    timing_state &t = c->timing;
+    cudaError_t err = cudaSuccess;
+    for (const auto &q : t.pending) {
+        float ms = 0.f;
+        cudaError_t e = cudaEventSynchronize(q.b);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, q.a, q.b);
+        if (e == cudaSuccess) {
+            t.calls[q.kind] += 1;
+            t.ms[q.kind] += ms;
+        } else if (err == cudaSuccess) {
+            err = e;
+        }
+        t.pool.push_back(q.a);
+        t.pool.push_back(q.b);
+    }
+    t.pending.clear();
+    if (out)
+        for (int k = 0; k < GRT_TIME_KINDS; ++k) {
+            out->calls[k] = t.calls[k];
+            out->ms[k] = t.ms[k];
+        }
+    if (reset)
+        for (int k = 0; k < GRT_TIME_KINDS; ++k) {
+            t.calls[k] = 0;
+            t.ms[k] = 0.0;
+        }
+    return err == cudaSuccess ? GRT_OK : cuda_fail(c, err, "reading the call timers");
+}
+
 grt_status grt_trace(grt_ctx *c, const float *rays_dev, grt_hit *hits_dev, uint32_t n, int any_hit,
                      grt_stream_t stream) {
     if (!c) return GRT_ERR_INVALID_ARG;
@@ -341,6 +406,7 @@ grt_status grt_trace(grt_ctx *c, const float *rays_dev, grt_hit *hits_dev, uint3
     if (needed_stack(c) > grt::kStackLarge)
         return fail(c, GRT_ERR_BVH_TOO_DEEP, "the selected tracer needs a deeper stack than the kernels have");
     device_guard g(c->device);
+    timed_call timer(c, GRT_TIME_TRACE, (cudaStream_t)stream);
     grt::launch_params lp = params_for(c, any_hit != 0);
     cudaError_t e;
     if (kTracers[c->tracer].persistent)

@@ -118,6 +118,7 @@ grt_status grt_direct(grt_ctx *c, const grt_direct_params *p, const float *rays_
     if (kTracers[c->tracer].alpha) return fail(c, GRT_ERR_INVALID_ARG, "direct lighting has no alpha-aware form");
     if (needed_stack(c) > kStackLarge) return fail(c, GRT_ERR_BVH_TOO_DEEP, "the BVH needs a deeper stack");
     device_guard g(c->device);
+    timed_call timer(c, GRT_TIME_DIRECT, (cudaStream_t)stream);
     const cudaStream_t st = (cudaStream_t)stream;
     const dl_scene ds = dl_scene_of(c);
     const float4 *rays = (const float4 *)rays_dev;
@@ -175,6 +176,7 @@ grt_status grt_hit_albedo(grt_ctx *c, uint32_t mode, const float *rays_dev, uint
     if (kTracers[c->tracer].alpha) return fail(c, GRT_ERR_INVALID_ARG, "albedo shading has no alpha-aware form");
     if (needed_stack(c) > kStackLarge) return fail(c, GRT_ERR_BVH_TOO_DEEP, "the BVH needs a deeper stack");
     device_guard g(c->device);
+    timed_call timer(c, GRT_TIME_DIRECT, (cudaStream_t)stream);
     const cudaStream_t st = (cudaStream_t)stream;
     const dl_scene ds = dl_scene_of(c);
     const float4 *rays = (const float4 *)rays_dev;

@@ -55,6 +55,7 @@ grt_status grt_build_device(grt_ctx *c, const float *vpos4_dev, uint32_t nv, con
     if (bad_mesh(m)) return fail(c, GRT_ERR_INVALID_ARG, "null, misaligned or oversized vertex / triangle array");
     if (max_tris < 1 || max_tris > 16) return fail(c, GRT_ERR_INVALID_ARG, "max_tris_per_node must be 1..16");
     device_guard g(c->device);
+    timed_call timer(c, GRT_TIME_TREE, (cudaStream_t)stream);
     free_scene(c);
     ++c->scene_generation;
     c->stats = grt_bvh_stats{};
@@ -132,6 +133,7 @@ grt_status grt_refit(grt_ctx *c, const float *vpos4_dev, uint32_t nv, grt_stream
         return fail(c, GRT_ERR_INVALID_ARG, "null or misaligned vertex array");
     if (c->n_links && !c->d_parent) return fail(c, GRT_ERR_INVALID_ARG, "this scene has no refit links");
     device_guard g(c->device);
+    timed_call timer(c, GRT_TIME_TREE, (cudaStream_t)stream);
     const cudaStream_t st = (cudaStream_t)stream;
     cudaError_t e = cudaSuccess;
     if (!c->d_refit) e = cudaMalloc(&c->d_refit, 256 + (size_t)std::max(c->n_links, 1u) * 4);
@@ -178,6 +180,7 @@ grt_status grt_incoherent_rays(grt_ctx *c, float r1, float r2, uint64_t seed, fl
     if (n == 0) return GRT_OK;
     if (!rays_dev || !aligned16(rays_dev)) return fail(c, GRT_ERR_INVALID_ARG, "null or misaligned ray buffer");
     device_guard g(c->device);
+    timed_call timer(c, GRT_TIME_RAYS, (cudaStream_t)stream);
     cudaError_t e = cudaSuccess;
     if (!c->d_extent) e = cudaMalloc(&c->d_extent, 32);
     if (e == cudaSuccess)
@@ -198,6 +201,7 @@ grt_status grt_build_scenes_device(grt_ctx *c, const grt_mesh *meshes, uint32_t 
         most = std::max(most, meshes[i].nt);
     }
     device_guard g(c->device);
+    timed_call timer(c, GRT_TIME_TREE, (cudaStream_t)stream);
     grt_free_multi(c);
     ++c->scene_generation;
     const cudaStream_t st = (cudaStream_t)stream;

@@ -166,6 +166,7 @@ grt_status grt_trace_multi(grt_ctx *c, const grt_ray_batch *batches, uint32_t co
     if (needed > kStackLarge)
         return fail(c, GRT_ERR_BVH_TOO_DEEP, "a scene needs a deeper stack than the kernels have");
     device_guard g(c->device);
+    timed_call timer(c, GRT_TIME_TRACE_MULTI, (cudaStream_t)stream);
     if (c->ms.batch_cap < count) {
         if (c->ms.d_batches) cudaFree(c->ms.d_batches);
         c->ms.d_batches = nullptr;

@@ -138,6 +138,7 @@ grt_status grt_compact_hits(grt_ctx *c, const grt_hit *hits_dev, uint32_t n, uin
     if (!count_dev || (n && (!hits_dev || !indices_dev)))
         return fail(c, GRT_ERR_INVALID_ARG, "null buffer for grt_compact_hits");
     device_guard g(c->device);
+    timed_call timer(c, GRT_TIME_RAYS, (cudaStream_t)stream);
     grt_status s = ensure_scratch(c, compact_scratch_bytes(n));
     if (s != GRT_OK) return s;
     cudaError_t e = launch_compact_hits(hits_dev, n, indices_dev, count_dev, (uint32_t *)c->d_scratch,
@@ -154,6 +155,7 @@ grt_status grt_shadow_rays(grt_ctx *c, const float *rays_dev, const grt_hit *hit
         !aligned16(shadow_rays_dev) || !aligned16(hits_dev))
         return fail(c, GRT_ERR_INVALID_ARG, "null or misaligned buffer for grt_shadow_rays");
     device_guard g(c->device);
+    timed_call timer(c, GRT_TIME_RAYS, (cudaStream_t)stream);
     grt_status s = ensure_scratch(c, compact_scratch_bytes(n));
     if (s != GRT_OK) return s;
     cudaError_t e = launch_shadow_rays(scene_for_shading(c), (const float4 *)rays_dev, hits_dev, n, light, eps,
@@ -182,6 +184,7 @@ grt_status grt_pathtrace(grt_ctx *c, const grt_pt_params *params, const float *p
     if (needed_stack(c) > grt::kStackLarge)
         return fail(c, GRT_ERR_BVH_TOO_DEEP, "the selected tracer needs a deeper stack than the kernels have");
     device_guard g(c->device);
+    timed_call timer(c, GRT_TIME_PATHTRACE, (cudaStream_t)stream);
     const bool wavefront = p.mode == GRT_PT_WAVEFRONT;
     const pt_layout L = layout_for(n_primary, n_paths, wavefront);
     grt_status s = ensure_scratch(c, L.total);
@@ -241,6 +244,7 @@ grt_status grt_adjoint(grt_ctx *c, const float *rays_dev, const grt_hit *hits_de
         !aligned16(grad_rays_dev) || (vpos_dev && vstride != 3 && vstride != 4))
         return fail(c, GRT_ERR_INVALID_ARG, "invalid buffer or vertex stride for grt_adjoint");
     device_guard g(c->device);
+    timed_call timer(c, GRT_TIME_ADJOINT, (cudaStream_t)stream);
     const float4 *vp = vpos_dev ? (const float4 *)vpos_dev : (const float4 *)c->d_vpos;
     const uint32_t stride = vpos_dev ? vstride : 4;
     cudaError_t e = launch_adjoint((const float4 *)rays_dev, hits_dev, grad_hits_dev, n, vp, stride,

@@ -13,6 +13,29 @@
 #include "bvh_builder.hpp"
 #include "grt_internal.hpp"
 
+// Per-call device timing (grt_set_timing): event pairs of the calls since the last read-out,
+// and the totals per kind.
+struct timing_state {
+    bool enabled = false;
+    struct pair {
+        int kind;
+        cudaEvent_t a, b;
+    };
+    std::vector<pair> pending;
+    std::vector<cudaEvent_t> pool;
+    uint64_t calls[GRT_TIME_KINDS] = {};
+    double ms[GRT_TIME_KINDS] = {};
+    cudaEvent_t take() {
+        if (!pool.empty()) {
+            cudaEvent_t e = pool.back();
+            pool.pop_back();
+            return e;
+        }
+        cudaEvent_t e = nullptr;
+        return cudaEventCreate(&e) == cudaSuccess ? e : nullptr;
+    }
+};
+
 struct grt_ctx {
     int device = 0;
     int num_sms = 0;
@@ -32,6 +55,7 @@ struct grt_ctx {
     grt_bvh_stats stats{};
     int tracer = 0;  // index into kTracers
     grt_tuning tuning{};
+    timing_state timing;
     unsigned *d_err = nullptr;      // status block (grt_internal.hpp): error bits, counter, abort request
     unsigned *d_counter = nullptr;  // work counter of the persistent kernels (d_err + 1)
     unsigned *h_flag = nullptr;     // pinned {1, 0, kAbortCounter}: the words grt_abort / grt_check write
@@ -97,6 +121,17 @@ struct device_guard {
     ~device_guard() {
         if (prev >= 0) cudaSetDevice(prev);
     }
+};
+
+// Records an event pair around a call's launches when timing is on (after the context's device
+// is current; the stream must not be capturing).
+struct timed_call {
+    grt_ctx *c;
+    int kind;
+    cudaStream_t st;
+    cudaEvent_t a = nullptr;
+    timed_call(grt_ctx *ctx, int k, cudaStream_t s);
+    ~timed_call();
 };
 
 inline grt_status fail(grt_ctx *c, grt_status s, const std::string &msg) {

@@ -462,6 +462,33 @@ grt_status grt_build_scenes_device(grt_ctx *ctx, const grt_mesh *meshes, uint32_
  * `stream`; returns when the refit is done. */
 grt_status grt_refit(grt_ctx *ctx, const float *vpos4_dev, uint32_t nv, grt_stream_t stream);
 
+/* ---- timing ----------------------------------------------------------------------------- */
+
+/* Per-call device times, the counterpart of the reference's wavefront step timers
+ * (time_this_wf_step, libgi/wavefront-rt.h:29: a CUDA event pair per step, folded into its
+ * stats timer, rt/cuda/base.cpp:17-45). While enabled, every call below of the given kind
+ * records an event pair on its stream around its launches (not while the stream is being
+ * captured into a graph); grt_timing_stats waits for the recorded pairs and returns, per kind,
+ * the number of calls and their summed device time since the last reset. Off by default: the
+ * traversal calls then record nothing. */
+enum {
+    GRT_TIME_TRACE = 0,        /* grt_trace */
+    GRT_TIME_TRACE_MULTI = 1,  /* grt_trace_multi */
+    GRT_TIME_PATHTRACE = 2,    /* grt_pathtrace */
+    GRT_TIME_DIRECT = 3,       /* grt_direct, grt_hit_albedo */
+    GRT_TIME_ADJOINT = 4,      /* grt_adjoint */
+    GRT_TIME_TREE = 5,         /* grt_build_device, grt_build_scenes_device, grt_refit */
+    GRT_TIME_RAYS = 6,         /* grt_incoherent_rays, grt_compact_hits, grt_shadow_rays */
+    GRT_TIME_KINDS = 7
+};
+typedef struct grt_timing {
+    uint64_t calls[GRT_TIME_KINDS];
+    double ms[GRT_TIME_KINDS];
+} grt_timing;
+grt_status grt_set_timing(grt_ctx *ctx, int enabled);
+/* Synchronises with the recorded calls; `reset` != 0 starts the totals again afterwards. */
+grt_status grt_timing_stats(grt_ctx *ctx, grt_timing *out, int reset);
+
 /* ---- ray generation ------------------------------------------------------------------- */
 
 /* The incoherent test rays of the reference CUDA tracer's `incoherence r1 r2` setting
