@@ -65,7 +65,7 @@ static const int kStackLarge = 64;
 // measured on GB300: how many leaves a lane may postpone before the warp's leaf phase, with how
 // many lanes still searching for their first leaf the warp stops visiting nodes, and (path
 // tracer) how many node visits each lane makes between two warp votes (3 elsewhere).
-static const int kPendPaths = 2, kExitPaths = 6, kVisitsPaths = 5;  // fused path tracer
+static const int kPendPaths = 2, kExitPaths = 8, kVisitsPaths = 5;  // fused path tracer
 static const int kPendDirect = 3, kExitDirect = 2;              // fused direct lighting
 static const int kPendTrace = 3, kExitTrace = 1;                // one-thread-per-ray batch traces
 static const int kPendPersistent = 3, kExitPersistent = 4;      // persistent batch traces, scene sets

@@ -564,7 +564,8 @@ __device__ __forceinline__ void spec_node4(trav_t &s, const dev_scene &sc, const
 // took 9 % off the fused path step and three 14 % off fused direct lighting). The warp leaves
 // the node phase once at most EXIT lanes are still searching for their first leaf; those lanes
 // resume where they stopped in the next call, so this changes when leaves are tested, not which
-// (leaving with up to 6 of 32 lanes still searching took another 5 % off the fused path step).
+// (leaving with up to 6 to 8 of 32 lanes still searching took another 5 % off the fused path
+// step).
 // Every lane of the warp must call this together (it ballots over the full warp); `active`
 // marks lanes with a ray.
 // Each ray's leaves are still tested in the reference's order, but node tests after a
