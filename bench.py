@@ -122,14 +122,15 @@ def measured_hbm_peak():
         return 6800.0, "fallback"
 
 
-def load_tuning(gpu_name: str) -> dict:
+def load_tuning(gpu_name: str, scene: str = "spheres") -> dict:
+    """The autotuner's entry for this GPU and scene class (the spheres one where there is none)."""
     path = os.path.join(ROOT, "illum-rt_gb300", "tuning.json")
     try:
         with open(path) as f:
             table = json.load(f)
     except Exception:
         return {}
-    for key in (f"{gpu_name}|spheres", "default|spheres"):
+    for key in (f"{gpu_name}|{scene}", f"{gpu_name}|spheres", "default|spheres"):
         if key in table:
             return table[key]
     return {}
@@ -570,11 +571,12 @@ def run_soups64(args):
     n_rays = sum(r.shape[0] for r in rays)
     stream = torch.cuda.Stream()
     sp = stream.cuda_stream
-    tuning = load_tuning(torch.cuda.get_device_name(0))
+    tuning = load_tuning(torch.cuda.get_device_name(0), "soups64")
     out = {"metric": "Mrays/s closest-hit, 64 uneven soups in one launch", "unit": "Mrays/s", "n_gpus": 1,
            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "dtype": "f32",
            "data": "synthetic (seeded)",
            "config": {"workload": "soups64", "scenes": 64, "triangles": int(sum(tris_n)), "rays": int(n_rays),
+                      "tuning": tuning or "defaults",
                       "l2": "inputs (344 MB of rays) larger than L2"}}
 
     def timed_trace(rt):
@@ -779,7 +781,7 @@ def run_profile_case_other(workload: str):
     from illum_rt_gb300 import api, workloads as wl
     stream = torch.cuda.Stream()
     sp = stream.cuda_stream
-    tuning = load_tuning(torch.cuda.get_device_name(0))
+    tuning = load_tuning(torch.cuda.get_device_name(0), workload)
     rt = api.BatchRayTracer(0)
     if workload == "direct":
         sc, mats, rays_np = wl.lit_spheres(count=256, res=RES)

@@ -8,7 +8,11 @@ fastest configuration is written to tuning.json under "<GPU name>|<scene class>"
 bench.py picks it up. Results do not depend on the launch parameters; a different leaf size
 gives a different (equally reference-built) BVH.
 
-Usage: python illum-rt_gb300/autotune.py [--quick] [--paths N]
+With --workload soups64 it tunes the scene-set trace instead: the 64 uneven soups of the
+benchmark, GPU-built trees of each leaf size, one persistent launch over all their rays, timed
+per candidate, written under "<GPU name>|soups64".
+
+Usage: python illum-rt_gb300/autotune.py [--quick] [--paths N] [--workload spheres|soups64]
 """
 from __future__ import annotations
 
@@ -83,6 +87,57 @@ def tune(quick: bool = False, n_paths: int = 4 << 20, res: int = 1024, log=print
     return best
 
 
+def tune_soups(quick: bool = False, log=print) -> dict:
+    """Launch parameters and leaf size of the scene-set trace over the 64-soup workload."""
+    import numpy as np
+    import torch
+    api, wl = _load_pkg()
+    tris_n, rays_n = wl.multi_scene_sizes()
+    scenes, rays = [], []
+    for i, (nt, nr) in enumerate(zip(tris_n, rays_n)):
+        sc = wl.soup(1000 + i, nt, sigma=0.5)
+        lo, hi = sc.bounds()
+        scenes.append((torch.from_numpy(sc.vpos).cuda(), torch.from_numpy(sc.tris.view(np.int32)).cuda()))
+        rays.append(torch.from_numpy(wl.shell_rays(2000 + i, lo, hi, nr)).cuda())
+    hits = [torch.zeros((r.shape[0], 4), device="cuda") for r in rays]
+    batches = [(i, rays[i], hits[i]) for i in range(len(rays))]
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    rt = api.BatchRayTracer(0)
+    orders = ["persistent-speculative-while-while"] if quick else ["persistent-while-while",
+                                                                  "persistent-speculative-while-while"]
+    leaf_sizes = [2] if quick else [2, 3, 4]
+    blocks = [64] if quick else [64, 128, 256]
+    thresholds = [20] if quick else [8, 12, 16, 20, 24, 28, 32]
+    periods = [2] if quick else [1, 2, 4]
+    best = None
+    t0 = time.time()
+    for leaf in leaf_sizes:
+        rt.build_scenes_device(scenes, max_tris=leaf, stream=sp)
+        for tracer, bt, th, per in itertools.product(orders, blocks, thresholds, periods):
+            rt.select(tracer)
+            rt.set_tuning(block_threads=bt, refill_threshold=th, refill_period=per, blocks_per_sm=0)
+            ms = float("inf")
+            for i in range(4):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                rt.trace_multi(batches, stream=sp)
+                e1.record(stream)
+                e1.synchronize()
+                if i:  # the first launch is a warm-up
+                    ms = min(ms, e0.elapsed_time(e1))
+            rt.check(sp)
+            cfg = {"tracer": tracer, "max_tris": leaf, "block_threads": bt, "refill_threshold": th,
+                   "refill_period": per, "ms": ms}
+            log(json.dumps(cfg))
+            if best is None or ms < best["ms"]:
+                best = cfg
+    rt.close()
+    best["searched"] = len(orders) * len(leaf_sizes) * len(blocks) * len(thresholds) * len(periods)
+    best["seconds"] = round(time.time() - t0, 1)
+    return best
+
+
 def save(best: dict, gpu_name: str, scene: str = "spheres"):
     table = {}
     if os.path.exists(TABLE):
@@ -98,6 +153,7 @@ if __name__ == "__main__":
     ap.add_argument("--quick", action="store_true")
     ap.add_argument("--paths", type=int, default=4 << 20)
     ap.add_argument("--out", default=None, help="also write the log of every candidate here")
+    ap.add_argument("--workload", default="spheres", choices=["spheres", "soups64"])
     a = ap.parse_args()
     import torch
     logf = open(a.out, "w") if a.out else None
@@ -107,6 +163,9 @@ if __name__ == "__main__":
         if logf:
             logf.write(line + "\n")
 
-    best = tune(quick=a.quick, n_paths=a.paths, log=log)
-    save(best, torch.cuda.get_device_name(0))
+    if a.workload == "soups64":
+        best = tune_soups(quick=a.quick, log=log)
+    else:
+        best = tune(quick=a.quick, n_paths=a.paths, log=log)
+    save(best, torch.cuda.get_device_name(0), a.workload)
     log("best " + json.dumps(best))
