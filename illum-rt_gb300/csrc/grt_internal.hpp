@@ -68,7 +68,7 @@ static const int kStackLarge = 64;
 static const int kPendPaths = 2, kExitPaths = 8, kVisitsPaths = 5;  // fused path tracer
 static const int kPendDirect = 3, kExitDirect = 2;              // fused direct lighting
 static const int kPendTrace = 3, kExitTrace = 1;                // one-thread-per-ray batch traces
-static const int kPendPersistent = 3, kExitPersistent = 4;      // persistent batch traces, scene sets
+static const int kPendPersistent = 2, kExitPersistent = 8;      // persistent batch traces, scene sets
 
 // Upper bound on traversal steps (inner nodes + leaves) of one ray. A DFS over a tree visits
 // each node at most once per ray, so a correct BVH never reaches it; it bounds the work of a
