@@ -122,6 +122,17 @@ def measured_hbm_peak():
         return 6800.0, "fallback"
 
 
+def tree_options(tuning: dict) -> dict:
+    """The reference builder's options of the tuned tree (leaf size, SAH planes, clipping)."""
+    return {"max_tris": tuning.get("max_tris", 4), "planes": tuning.get("planes", 16),
+            "esc": bool(tuning.get("esc", 1))}
+
+
+def tree_label(tuning: dict) -> str:
+    t = tree_options(tuning)
+    return "SAH %d planes, %s, leaf<=%d" % (t["planes"], "ESC" if t["esc"] else "no ESC", t["max_tris"])
+
+
 def load_tuning(gpu_name: str, scene: str = "spheres") -> dict:
     """The autotuner's entry for this GPU and scene class (the spheres one where there is none)."""
     path = os.path.join(ROOT, "illum-rt_gb300", "tuning.json")
@@ -177,7 +188,8 @@ class Step:
         sc, rays = wl.spheres_primary(res=RES)
         self.n_primary = rays.shape[0]
         self.rt = api.BatchRayTracer(device)
-        self.build_info = self.rt.build(sc.vpos, sc.tris, max_tris=tuning.get("max_tris", 4))
+        tree = tree_options(tuning)
+        self.build_info = self.rt.build(sc.vpos, sc.tris, **tree)
         self.rt_plain = api.BatchRayTracer(device)  # the reference's CUDA build defaults, untuned
         self.rt_plain.build(sc.vpos, sc.tris)
         self.rt_plain.select("while-while")
@@ -185,7 +197,7 @@ class Step:
         # the plain kernels on the tuned step's tree (its leaf size): the counting pass of the
         # roofline figure and the plain form on the same tree
         self.rt_tt = api.BatchRayTracer(device)
-        self.rt_tt.build(sc.vpos, sc.tris, max_tris=tuning.get("max_tris", 4))
+        self.rt_tt.build(sc.vpos, sc.tris, **tree)
         self.rt.select(tuning.get("tracer", "persistent-while-while"))
         kw = {k: v for k, v in tuning.items() if k in ("block_threads", "blocks_per_sm", "refill_threshold",
                                                          "refill_period", "stack_entries")}
@@ -477,7 +489,7 @@ def run_gb300(args):
         "warmup": args.warmup, "ms_per_step": round(statistics.mean(tuned_ms), 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": WORKLOAD, "triangles": 262144, "primary_rays": step.n_primary, "paths": N_PATHS,
-                   "rays_per_step": rays_tuned, "bvh": "SAH 16 planes, ESC, leaf<=%d" % tuning.get("max_tris", 4),
+                   "rays_per_step": rays_tuned, "bvh": tree_label(tuning),
                    "l2": "flushed between timed steps (512 MB write); the pipelined e2e loop adds no flush, each "
                          "of its steps moves about 256 MB of copies and results through L2",
                    "parallelism": f"replicas x{world}",
@@ -486,7 +498,7 @@ def run_gb300(args):
                             "rays_per_step": rays_plain, "loop_order": plain_order,
                             "order_ms": {k: round(v, 4) for k, v in plain_times.items()},
                             "bvh4_speculative_ms": round(plain_bvh4_ms, 4),
-                            "tuned_tree": {"bvh": "SAH 16 planes, ESC, leaf<=%d" % tuning.get("max_tris", 4),
+                            "tuned_tree": {"bvh": tree_label(tuning),
                                            "loop_order": tt_order,
                                            "order_ms": {k: round(v, 4) for k, v in tt_times.items()}}},
         "speedup_vs_plain": round(value / plain_value, 3),

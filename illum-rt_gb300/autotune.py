@@ -1,12 +1,15 @@
 """Autotuner for the persistent kernels: loop order, warps per block, refill threshold and
-period, leaf size.
+period, and the tree (leaf size, SAH candidate planes, early split clipping).
 
-For every candidate it builds the scene's BVH with that leaf size (the reference builder's
-`max_triangles_per_node`), sets the launch parameters through grt_set_tuning and times the
-fused path-tracing step (persistent primary trace + fused bounce loop) with CUDA events; the
-fastest configuration is written to tuning.json under "<GPU name>|<scene class>", where
-bench.py picks it up. Results do not depend on the launch parameters; a different leaf size
-gives a different (equally reference-built) BVH.
+For every candidate it builds the scene's BVH with the reference builder's options
+(`max_triangles_per_node`, `number_of_planes`, `esc`), sets the launch parameters through
+grt_set_tuning and times the fused path-tracing step (persistent primary trace + fused bounce
+loop) with CUDA events. Three stages: launch parameters and leaf size on trees of the
+reference's 16 planes with clipping; then, with the best launch, every leaf size, plane count
+and clipping choice; then the launch parameters again on the best tree. The fastest
+configuration is written to tuning.json under "<GPU name>|<scene class>", where bench.py picks
+it up. Results do not depend on the launch parameters; other tree options give a different
+(equally reference-built) BVH.
 
 With --workload soups64 it tunes the scene-set trace instead: the 64 uneven soups of the
 benchmark, GPU-built trees of each leaf size, one persistent launch over all their rays, timed
@@ -68,21 +71,56 @@ def tune(quick: bool = False, n_paths: int = 4 << 20, res: int = 1024, log=print
     blocks = [128] if quick else [64, 128, 256]
     thresholds = [12, 20, 28] if quick else [8, 12, 16, 20, 24, 28, 32]
     periods = [1, 4] if quick else [1, 2, 4, 8]
+    plane_counts = [16] if quick else [16, 32, 64, 128, 256]
+    clipping = [True] if quick else [True, False]
     best = None
+    searched = 0
     t0 = time.time()
-    for leaf in leaf_sizes:
-        rt.build(sc.vpos, sc.tris, max_tris=leaf)
-        for tracer, bt, th, per in itertools.product(orders, blocks, thresholds, periods):
+
+    def launch_sweep(tracers, tree):
+        nonlocal best, searched
+        for tracer, bt, th, per in itertools.product(tracers, blocks, thresholds, periods):
             rt.select(tracer)
             rt.set_tuning(block_threads=bt, refill_threshold=th, refill_period=per, blocks_per_sm=0)
             ms = time_config(rt, api, rays, hits, results, n_paths, stream)
-            cfg = {"tracer": tracer, "max_tris": leaf, "block_threads": bt, "refill_threshold": th,
-                   "refill_period": per, "ms": ms}
+            cfg = {"tracer": tracer, **tree, "block_threads": bt, "refill_threshold": th, "refill_period": per,
+                   "ms": ms}
             log(json.dumps(cfg))
+            searched += 1
             if best is None or ms < best["ms"]:
                 best = cfg
+
+    def build(tree):
+        rt.build(sc.vpos, sc.tris, max_tris=tree["max_tris"], planes=tree["planes"], esc=bool(tree["esc"]))
+
+    # stage 1: launch parameters and leaf size on the reference's tree options
+    for leaf in leaf_sizes:
+        tree = {"max_tris": leaf, "planes": 16, "esc": 1}
+        build(tree)
+        launch_sweep(orders, tree)
+    # stage 2: the tree options with the best launch
+    launch = {k: best[k] for k in ("tracer", "block_threads", "refill_threshold", "refill_period")}
+    rt.select(launch["tracer"])
+    rt.set_tuning(block_threads=launch["block_threads"], refill_threshold=launch["refill_threshold"],
+                  refill_period=launch["refill_period"], blocks_per_sm=0)
+    for leaf, planes, esc in itertools.product(leaf_sizes, plane_counts, clipping):
+        tree = {"max_tris": leaf, "planes": planes, "esc": int(esc)}
+        if planes == 16 and esc:
+            continue  # timed in stage 1
+        build(tree)
+        ms = time_config(rt, api, rays, hits, results, n_paths, stream)
+        cfg = {**launch, **tree, "ms": ms}
+        log(json.dumps(cfg))
+        searched += 1
+        if ms < best["ms"]:
+            best = cfg
+    # stage 3: the launch parameters again on the best tree
+    tree = {k: best[k] for k in ("max_tris", "planes", "esc")}
+    if tree != {"max_tris": best["max_tris"], "planes": 16, "esc": 1}:
+        build(tree)
+        launch_sweep([best["tracer"]], tree)
     rt.close()
-    best["searched"] = len(orders) * len(leaf_sizes) * len(blocks) * len(thresholds) * len(periods)
+    best["searched"] = searched
     best["seconds"] = round(time.time() - t0, 1)
     return best
 
