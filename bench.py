@@ -494,6 +494,11 @@ def run_gb300(args):
                          "of its steps moves about 256 MB of copies and results through L2",
                    "parallelism": f"replicas x{world}",
                    "tuning": tuning or "defaults"},
+        "step_ms_spread": {"tuned": [round(min(tuned_ms), 4), round(statistics.median(tuned_ms), 4),
+                                     round(max(tuned_ms), 4)],
+                           "plain": [round(min(plain_ms), 4), round(statistics.median(plain_ms), 4),
+                                     round(max(plain_ms), 4)],
+                           "form": "min, median, max of the timed steps"},
         "plain_wavefront": {"value": round(plain_value, 1), "ms_per_step": round(statistics.mean(plain_ms), 4),
                             "rays_per_step": rays_plain, "loop_order": plain_order,
                             "order_ms": {k: round(v, 4) for k, v in plain_times.items()},

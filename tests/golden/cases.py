@@ -125,6 +125,7 @@ BUILDERS = [
     ("sah8_1_esc", dict(split="sah", max_tris=1, planes=8, esc=True)),
     ("sm_4_esc", dict(split="sm", max_tris=4, planes=1, esc=True)),
     ("om_2", dict(split="om", max_tris=2, planes=1, esc=False)),
+    ("sah64_2", dict(split="sah", max_tris=2, planes=64, esc=False)),  # the benchmark's tuned tree
 ]
 
 

@@ -80,6 +80,21 @@ def test_other_builders_match_oracle(gpu_tracer, orc, wl, builder):
         assert (occluded(_trace(gpu_tracer, r2, True)) == o.any(r2)[0]).all()
 
 
+@pytest.mark.parametrize("tracer", TRACERS)
+def test_tuned_tree_spheres_matches_oracle(gpu_tracer, orc, wl, tracer):
+    """The benchmark's tuned tree (leaves of at most 2, 64 SAH planes, no clipping) on the
+    1024x1024 sphere frame, closest and any hit."""
+    sc, rays = wl.spheres_primary()
+    opts = dict(split="sah", max_tris=2, planes=64, esc=False)
+    o = orc.OracleBVH(sc.vpos, sc.tris, **opts)
+    gpu_tracer.build(sc.vpos, sc.tris, **opts)
+    gpu_tracer.select(tracer)
+    assert_hits_match(_trace(gpu_tracer, rays, False), o.closest(rays)[0], exact(tracer))
+    r2 = rays[::16].copy()
+    r2[:, 7] = 5.0
+    assert (occluded(_trace(gpu_tracer, r2, True)) == o.any(r2)[0]).all()
+
+
 def test_trace_host_path_matches(gpu_tracer, wl, orc):
     sc, rays = wl.heightfield_primary()
     gpu_tracer.build(sc.vpos, sc.tris)
