@@ -20,6 +20,7 @@ GPUs); value = all ranks' rays / the slowest rank's time.
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -450,12 +451,19 @@ def run_gb300(args):
     clocks = ClockSampler(local)
     barrier()
     clocks.start()
-    tuned_ms, pt_ms = time_steps(step, step.tuned, args.steps, split=True)
-    barrier()
-    plain_ms, _ = time_steps(step, step.plain, args.steps)
-    e2e_ms, _ = time_steps(step, step.e2e, args.steps)
-    step.e2e_pipelined(3)  # warm-up of the staging buffers and streams
-    e2e_pipe_ms = step.e2e_pipelined(args.steps)
+    # the host must not pause between a step's start event and its launches (the device would
+    # idle inside the timed interval): no garbage collection during the timed loops
+    gc.collect()
+    gc.disable()
+    try:
+        tuned_ms, pt_ms = time_steps(step, step.tuned, args.steps, split=True)
+        barrier()
+        plain_ms, _ = time_steps(step, step.plain, args.steps)
+        e2e_ms, _ = time_steps(step, step.e2e, args.steps)
+        step.e2e_pipelined(3)  # warm-up of the staging buffers and streams
+        e2e_pipe_ms = step.e2e_pipelined(args.steps)
+    finally:
+        gc.enable()
     barrier()
     clk = clocks.stop()
     step.rt.check(step.sp)
@@ -650,8 +658,12 @@ def run_direct(args, samples: int = 8):
     stream = torch.cuda.Stream()
     sp = stream.cuda_stream
     rt = api.BatchRayTracer(0)
+    # the reference default tree: on this scene (a floor of two large triangles under the
+    # spheres) the builder's split clipping pays; without it the fused frame took 2.78 ms
+    # instead of 2.38 ms
     rt.build(sc.vpos, sc.tris)
     rt.set_material_table(mats)
+    flush_buf = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB of L2
 
     def timed(mode, tracer, sampling="light"):
         rt.select(tracer)
@@ -660,6 +672,8 @@ def run_direct(args, samples: int = 8):
         rt.check(sp)
         times = []
         for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush_buf.fill_(1)  # L2 flushed between timed frames, outside the events
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
             rt.direct(rays, fb, samples, mode=mode, seed=3, stream=sp, sampling=sampling)
@@ -688,7 +702,8 @@ def run_direct(args, samples: int = 8):
             "value": round(n * samples / best_f[0] / 1e3, 1), "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded)",
             "config": {"workload": "lit_spheres-262150: 256 spheres, floor, 2 area lights, 1024x1024 camera rays",
-                       "samples_per_pixel": samples},
+                       "samples_per_pixel": samples,
+                       "l2": "flushed between timed frames (512 MB write)"},
             "fused_ms": round(best_f[0], 4), "fused_form": best_f[1], "wavefront_ms": round(best_w[0], 4),
             "wavefront_form": best_w[1], "speedup_fused_vs_wavefront": round(best_w[0] / best_f[0], 3),
             "all_ms": {k: round(v, 4) for k, v in res.items()}, "direction_sampling": directions}
