@@ -148,14 +148,15 @@ def load_tuning(gpu_name: str, scene: str = "spheres") -> dict:
     return {}
 
 
-def profile_traffic():
-    """DRAM bytes (read + write) per full-size launch of the fused kernel, from the line
-    `dram_bytes_per_launch: N` of the committed ncu summary, or None."""
+def profile_figure(key: str):
+    """A figure of the committed ncu summary of the fused kernel (a line `key: N`), or None:
+    `dram_bytes_per_launch` (DRAM read + write of one full-size launch) and
+    `l2_bytes_per_bounce_ray` (L2 sectors x 32 B per bounce ray)."""
     try:
         with open(os.path.join(ROOT, "profiles", "k_pt_fused_spheres.md")) as f:
             for line in f:
-                if line.strip().startswith("dram_bytes_per_launch:"):
-                    return int(line.split(":", 1)[1].strip().replace(",", ""))
+                if line.strip().startswith(key + ":"):
+                    return float(line.split(":", 1)[1].strip().replace(",", ""))
     except Exception:
         pass
     return None
@@ -482,13 +483,17 @@ def run_gb300(args):
     peak, peak_kind = measured_hbm_peak()
     pt_s = statistics.mean(pt_ms) / 1e3
     achieved = pt_bytes / pt_s / 1e9
-    traffic = profile_traffic()
+    traffic = profile_figure("dram_bytes_per_launch")
+    l2_per_ray = profile_figure("l2_bytes_per_bounce_ray")
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": traffic,
+                "frac": round(achieved / peak, 4), "traffic": int(traffic) if traffic is not None else None,
                 "kernel": "k_pt_fused", "peak_source": peak_kind,
                 "bytes_per_launch": pt_bytes, "bounce_rays": bounce_cnt[0],
                 "inner_nodes_per_ray": round(bounce_cnt[1] / max(1, bounce_cnt[0]), 2),
                 "tri_tests_per_ray": round(bounce_cnt[2] / max(1, bounce_cnt[0]), 2),
+                "l2_gbs": round(l2_per_ray * bounce_cnt[0] / pt_s / 1e9, 1) if l2_per_ray else None,
+                "l2_note": "L2 bytes per bounce ray from the ncu capture of the 1,048,576-path case x this "
+                           "launch's bounce rays / its measured time",
                 "note": "B_ray = 32 + 16 + 64 n_node + 48 n_tri, counted in the exact while-while order on the "
                         "tuned step's tree; the BVH (%.0f MB) stays L2-resident, so these bytes are mostly served "
                         "from L2" % (step.build_info["device_bytes"] / 1e6)}
