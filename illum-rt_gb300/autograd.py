@@ -17,6 +17,24 @@ import numpy as np
 import torch
 
 
+def _topology_key(tris, nv: int):
+    """Identity of a mesh's topology for the refit cache: the vertex and triangle counts and a
+    64-bit digest of the triangle array's contents (index and value of every word mixed, summed
+    modulo 2^64), so that a different triangle array, or an array edited in place, never reuses
+    a tree built for other triangles. Tensors are digested on their own device."""
+    if isinstance(tris, torch.Tensor):
+        t = tris.detach().reshape(-1).to(torch.int64) & 0xFFFFFFFF
+        i = torch.arange(1, t.numel() + 1, dtype=torch.int64, device=t.device)
+    else:
+        a = np.ascontiguousarray(tris, np.uint32).reshape(-1)
+        t = torch.from_numpy(a.astype(np.int64))
+        i = torch.arange(1, a.size + 1, dtype=torch.int64)
+    w = i * -7046029254386353131  # odd 64-bit multiplier; products wrap modulo 2^64
+    h1 = int(((t + 0x632BE5AB) * w).sum())
+    h2 = int(((t ^ (w >> 29)) * (w | 1) * 0x2545F491).sum())
+    return (int(nv), int(t.numel()), h1, h2)
+
+
 class _ClosestHits(torch.autograd.Function):
     @staticmethod
     def forward(ctx, vpos, rays, tracer, tris, builder):
@@ -27,7 +45,7 @@ class _ClosestHits(torch.autograd.Function):
                 v4[:, :3] = vpos.detach()
                 t4 = tris if isinstance(tris, torch.Tensor) else torch.from_numpy(
                     np.ascontiguousarray(tris, np.uint32).view(np.int32))
-                key = (int(vpos.shape[0]), id(tris))
+                key = _topology_key(tris, vpos.shape[0]) if builder == "refit" else None
                 if builder == "refit" and getattr(tracer, "_refit_key", None) == key:
                     tracer.refit(v4, stream=stream)
                 else:
@@ -67,6 +85,7 @@ class _ClosestHits(torch.autograd.Function):
 def closest_hits(tracer, vpos: torch.Tensor, tris, rays: torch.Tensor, builder: str = "reference"):
     """(t, beta, gamma, ref) of each ray, differentiable in vpos [nv, 3] and rays [n, 8].
     builder: "reference" (host build, hits bit-identical to the reference tracer with an exact
-    tracer), "gpu" (GPU build; hits equal except near-ties) or "refit" (the tracer's tree for
-    the same `tris` object refitted to the current vertices; hits equal except near-ties)."""
+    tracer), "gpu" (GPU build; hits equal except near-ties) or "refit" (the tracer's tree
+    refitted to the current vertices when it was built for triangles of the same contents, else
+    a GPU build; hits equal except near-ties)."""
     return _ClosestHits.apply(vpos, rays, tracer, tris, builder)

@@ -605,10 +605,13 @@ int fused_blocks_per_sm(int block_threads, int stack_entries, int order, bool al
 // ---- allocation-free compaction ------------------------------------------------------------
 //
 // grt_compact_hits_static is grt_compact_hits for callers that must not allocate device
-// memory: code running while a CUDA graph is being captured (cudaMalloc is not allowed there),
-// or code embedded in a host application whose device memory is owned by its own pool. Its only
-// temporary storage, one count per 2048-hit tile, lives in the fixed array below, which every
-// GPU that loads this library holds until the process exits.
+// memory: a renderer that reserves its whole device-memory budget up front and hands out
+// memory only from its own pool, or a frame loop that cannot afford cudaMalloc's implicit
+// device synchronisation in the middle of a frame. Its only temporary storage, one count per
+// 2048-hit tile, lives in the fixed array below, which every GPU that loads this library holds
+// until the process exits. The array's device address is looked up once per device and kept
+// for the life of the process, so a process that resets a device (cudaDeviceReset) must not
+// call this entry point on that device afterwards.
 
 namespace grt {
 namespace {

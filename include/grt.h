@@ -6,7 +6,7 @@
  * whose CUDA specialisation `wf::cuda::batch_rt` (rt/cuda/base.h:403-429) builds a BVH on the
  * host (rt/cuda/base.cpp:88-117) and launches traversal kernels over device ray buffers
  * (rt/cuda/tracers.cu:57-294). This header exposes the same operations over plain pointers and
- * sizes so that a thin adapter class can drop in for that path (INTEGRATION.md shows it).
+ * sizes so that a thin adapter class deriving from wf::cuda::batch_rt can drop in for that path.
  *
  * Data layouts are the reference's device layouts:
  *   vertex positions : float4 per vertex (x, y, z, 1)              rt/cuda/base.cpp:57-66
@@ -236,16 +236,19 @@ grt_status grt_compact_hits(grt_ctx *ctx, const grt_hit *hits_dev, uint32_t n, u
                             uint32_t *count_dev, grt_stream_t stream);
 
 /* Allocation-free variant of grt_compact_hits. It has no counterpart in the reference; it is
- * for callers that cannot call cudaMalloc: code that runs while a CUDA graph is being captured,
- * or a host application whose device memory belongs to its own pool. It needs no context, and
- * its only temporary storage (one count per 2048-hit tile) is a fixed 64 KiB array in device
- * memory that every GPU loading this library holds until the process exits. Limits:
+ * for callers that cannot call cudaMalloc: a renderer that reserves its whole device-memory
+ * budget up front and hands out memory only from its own pool, or a frame loop that cannot
+ * afford cudaMalloc's implicit device synchronisation in the middle of a frame. It needs no
+ * context, and its only temporary storage (one count per 2048-hit tile) is a fixed 64 KiB
+ * array in device memory that every GPU loading this library holds until the process exits.
+ * Limits:
  *   - n at most GRT_COMPACT_STATIC_MAX_HITS; larger n returns GRT_ERR_TOO_LARGE, nothing runs;
  *   - all calls share that one array, so calls whose kernels overlap on a GPU (for example on
  *     two streams at once) race and give wrong results: order them on one stream;
  *   - the first call on each device looks up the array's device address
- *     (cudaGetSymbolAddress) with that device current; make that first call before any stream
- *     capture begins.
+ *     (cudaGetSymbolAddress) with that device current and keeps it for the life of the
+ *     process; make that first call before any stream capture begins, and make no call on a
+ *     device after resetting it (cudaDeviceReset).
  * The array keeps the last call's tile counts; every call overwrites the counts it reads. */
 #define GRT_COMPACT_STATIC_MAX_HITS 33554432u
 grt_status grt_compact_hits_static(const grt_hit *hits_dev, uint32_t n, uint32_t *indices_dev, uint32_t *count_dev,

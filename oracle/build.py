@@ -11,6 +11,8 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+# where this recipe looks for the reference checkout unless GRT_REFERENCE_DIR names another
+REFERENCE_CHECKOUT = "/root/reference"
 
 
 def build(with_reference: bool = True) -> None:
@@ -22,7 +24,9 @@ def build(with_reference: bool = True) -> None:
         subprocess.run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
                         "-o", so, src], check=True)
     if with_reference:
-        subprocess.run(["sh", os.path.join(HERE, "build_ref.sh")], check=True, stdout=subprocess.DEVNULL)
+        env = dict(os.environ)
+        env.setdefault("GRT_REFERENCE_DIR", REFERENCE_CHECKOUT)
+        subprocess.run(["sh", os.path.join(HERE, "build_ref.sh")], check=True, stdout=subprocess.DEVNULL, env=env)
 
 
 if __name__ == "__main__":

@@ -1,14 +1,14 @@
 #!/bin/sh
 # Builds oracle/_ref/libref_bbvh.so from the reference's own CPU ray tracer sources, unmodified,
-# where they lie under the reference checkout (default /root/reference, or $GRT_REFERENCE_DIR).
-# Used only to pin the oracle restatement and to generate golden fixtures; prints a notice and
-# exits 0 when the reference checkout is absent (for example on the GPU machine).
+# where they lie under the reference checkout named by $GRT_REFERENCE_DIR (oracle/build.py sets
+# it). Used only to pin the oracle restatement and to generate golden fixtures; prints a notice
+# and exits 0 when the variable is unset or the checkout is absent (for example on the GPU machine).
 # -ffp-contract=off keeps every product unfused so the results do not depend on the host ISA.
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
-REF=${GRT_REFERENCE_DIR:-/root/reference}
+REF=${GRT_REFERENCE_DIR:-}
 OUT="$HERE/_ref"
-if [ ! -f "$REF/rt/cpu/bvh2.cpp" ]; then
+if [ -z "$REF" ] || [ ! -f "$REF/rt/cpu/bvh2.cpp" ]; then
     echo "build_ref: reference sources not found at $REF; skipping oracle/_ref"
     exit 0
 fi

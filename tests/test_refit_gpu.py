@@ -148,3 +148,33 @@ def test_autograd_refit_matches_gpu_builds(api, wl):
         opt.step()
     a.close()
     b.close()
+
+
+def test_autograd_refit_rebuilds_for_new_topology(api, wl):
+    """A triangle array with the same vertex count but other contents, whether a new array or
+    the old one edited in place, gets a tree of its own: the refit builder never refits a tree
+    built for other triangles."""
+    import torch
+    from illum_rt_gb300 import autograd
+    sc = wl.icosphere(levels=4)
+    rays = _dev(wl.camera_rays((0.0, 0.0, 3.0), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 50.0, 128, 128), np.float32)
+    a, b = api.BatchRayTracer(0), api.BatchRayTracer(0)
+    a.select("while-while")
+    b.select("while-while")
+    v = torch.from_numpy(sc.vpos[:, :3].copy()).cuda()
+    perm = np.random.default_rng(11).permutation(sc.tris.shape[0])
+    tris = sc.tris.copy()
+    autograd.closest_hits(a, v, tris, rays, builder="refit")
+    for kind in ("new array", "edited in place"):
+        if kind == "new array":
+            tris = np.ascontiguousarray(tris[perm])
+        else:
+            tris[:] = tris[np.roll(np.arange(tris.shape[0]), 7)]
+            tris[:, :3] = tris[:, [0, 2, 1]]  # the same triangles wound the other way
+        t1, b1, g1, r1 = autograd.closest_hits(a, v, tris, rays, builder="refit")
+        t2, b2, g2, r2 = autograd.closest_hits(b, v, tris, rays, builder="gpu")
+        h1 = torch.stack([t1, b1, g1, r1.view(torch.float32)], 1).cpu().numpy()
+        h2 = torch.stack([t2, b2, g2, r2.view(torch.float32)], 1).cpu().numpy()
+        assert same_bits(h1, h2).all(), kind
+    a.close()
+    b.close()

@@ -1,11 +1,13 @@
 """The allocation-free compaction entry point (grt_compact_hits_static) against the regular
 one (grt_compact_hits).
 
-grt_compact_hits_static serves callers that cannot call cudaMalloc — code running during CUDA
-graph capture, or applications that own all device memory through their own pool. It keeps its
-tile counts in a fixed device array shared by all calls, so this test makes two calls in a row
-(the second smaller, over different hits) and checks each against the regular entry point,
-which takes its scratch from a context. The file is named so that pytest collects it last."""
+grt_compact_hits_static serves callers that cannot call cudaMalloc: renderers whose device
+memory all comes from their own up-front pool, and frame loops that cannot take cudaMalloc's
+implicit device synchronisation. It keeps its tile counts in a fixed device array shared by all
+calls, so this test makes two calls in a row (the second smaller, over different hits) and
+checks each against the regular entry point, which takes its scratch from a context; then an
+empty call, which must still set the count to zero. The file is named so that pytest collects
+it last."""
 import ctypes
 
 import numpy as np
@@ -55,6 +57,11 @@ def test_static_compaction_matches_context_compaction(api):
             assert c == int(cnt_ctx.item()) == want.size
             assert torch.equal(idx_static[:c], idx_ctx[:c])
             assert (idx_static[:c].cpu().numpy() == want).all()
+        # no hits at all: the count is written (zero) and no kernel reads the array
+        cnt_static.fill_(-1)
+        assert fn(hits.data_ptr(), 0, idx_static.data_ptr(), cnt_static.data_ptr(), stream) == GRT_OK
+        torch.cuda.synchronize()
+        assert int(cnt_static.item()) == 0
         # beyond the fixed capacity the call is refused before anything runs
         assert fn(hits.data_ptr(), MAX_HITS + 1, idx_static.data_ptr(), cnt_static.data_ptr(), stream) == \
             GRT_ERR_TOO_LARGE
