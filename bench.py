@@ -50,6 +50,8 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the full-size oracle check of the timed configuration")
     ap.add_argument("--profile-case", action="store_true",
                     help="run one tuned and one plain step (no graphs) and exit (for ncu captures)")
     ap.add_argument("--profile-paths", type=int, default=1 << 20, help="paths of the --profile-case step")
@@ -148,6 +150,17 @@ def load_tuning(gpu_name: str, scene: str = "spheres") -> dict:
     return {}
 
 
+def gpu_name_from_smi() -> str:
+    """The GPU's name from nvidia-smi (no CUDA context), for the tuning table's key."""
+    try:
+        out = subprocess.run(["nvidia-smi", "-i", "0", "--query-gpu=name", "--format=csv,noheader"],
+                             capture_output=True, text=True, timeout=30)
+        name = out.stdout.strip().splitlines()[0].strip() if out.returncode == 0 and out.stdout.strip() else ""
+    except Exception:
+        name = ""
+    return name or "NVIDIA GB300"
+
+
 def profile_figure(key: str):
     """A figure of the committed ncu summary of the fused kernel (a line `key: N`), or None:
     `dram_bytes_per_launch` (DRAM read + write of one full-size launch) and
@@ -228,12 +241,16 @@ class Step:
             ev.record(self.stream)
         self.rt.pathtrace(self.p_fused, self.rays, self.hits, N_PATHS, self.results, None, self.sp)
 
-    def plain(self):
+    def plain(self, ev=None):
         self.rt_plain.trace(self.rays, self.hits, False, self.sp)
+        if ev is not None:
+            ev.record(self.stream)
         self.rt_plain.pathtrace(self.p_plain, self.rays, self.hits, N_PATHS, self.results, None, self.sp)
 
-    def plain_tuned_tree(self):
+    def plain_tuned_tree(self, ev=None):
         self.rt_tt.trace(self.rays, self.hits, False, self.sp)
+        if ev is not None:
+            ev.record(self.stream)
         self.rt_tt.pathtrace(self.p_plain, self.rays, self.hits, N_PATHS, self.results, None, self.sp)
 
     def e2e(self):
@@ -344,15 +361,17 @@ def time_steps(step: Step, fn, k: int, flush=True, split=False):
 class CpuStep:
     """One step of the workload on the host cores through the oracle port of the reference CPU
     tracer (OpenMP over rays, rt/cpu/wavefront.cpp:53-70, all host threads): closest hits of the
-    1024x1024 primary rays, then the diffuse paths started at those hits."""
+    1024x1024 primary rays, then the diffuse paths started at those hits. The scene and rays
+    come from the oracle's own generators (bit-identical to the library's), and the tree from
+    the reference builder with the given options (those of the GPU step's tree), so this loads
+    nothing but the oracle."""
 
-    def __init__(self, rays_np, n_paths: int, threads: int = 0):
+    def __init__(self, n_paths: int, tree: dict | None = None, threads: int = 0):
         import __graft_entry__ as ge
-        from illum_rt_gb300 import workloads as wl
         self.orc = ge.load_oracle()
-        sc = wl.spheres()
-        self.o = self.orc.OracleBVH(sc.vpos, sc.tris)
-        self.rays = rays_np
+        vpos, tris, self.rays = self.orc.spheres_primary(res=RES)
+        self.tree = tree_options(tree or {})
+        self.o = self.orc.OracleBVH(vpos, tris, **self.tree)
         self.n_paths = n_paths
         self.threads = threads
 
@@ -368,10 +387,9 @@ class CpuStep:
         return self.rays.shape[0] + int(res[:, 1].sum()), dt
 
 
-def cpu_baseline(rays_np, min_seconds: float = 10.0, min_reps: int = 3):
+def cpu_baseline(cs: CpuStep, min_seconds: float = 10.0, min_reps: int = 3):
     """The full step on the host cores, one warm-up step, then repeated until at least
     `min_seconds` of work; the median rate of the repetitions (Mrays/s)."""
-    cs = CpuStep(rays_np, N_PATHS)
     cs.run()
     rates, n_tot, t_tot = [], 0, 0.0
     while t_tot < min_seconds or len(rates) < min_reps:
@@ -380,6 +398,73 @@ def cpu_baseline(rays_np, min_seconds: float = 10.0, min_reps: int = 3):
         n_tot += n
         t_tot += dt
     return statistics.median(rates), len(rates), n_tot, t_tot, cs.cores()
+
+
+NEAR_TIE = 1e-6  # |t1 - t2| <= NEAR_TIE * t: two closest hits equal within float rounding
+
+
+def classify_hits(got: np.ndarray, want: np.ndarray) -> dict:
+    """Hit records float32 [n, 4] (t, beta, gamma, ref bits) against the oracle's: rows whose
+    bits differ, and whether each of them is a near-tie (both hit, other triangle, |t1 - t2|
+    <= 1e-6 t); a row naming the same triangle with other bits is never a near-tie."""
+    g = np.ascontiguousarray(got, np.float32)
+    w = np.ascontiguousarray(want, np.float32)
+    gu, wu = g.view(np.uint32), w.view(np.uint32)
+    rows = np.nonzero((gu != wu).any(axis=1))[0]
+    tg, tw = g[rows, 0].astype(np.float64), w[rows, 0].astype(np.float64)
+    near = (gu[rows, 3] != wu[rows, 3]) & (tg < 3e38) & (tw < 3e38) & (np.abs(tg - tw) <= NEAR_TIE * np.abs(tw))
+    return {"differing": int(rows.size), "all_near_ties": bool(near.all()), "not_near_ties": int((~near).sum())}
+
+
+def classify_paths(res_g: np.ndarray, bh_g: np.ndarray, res_o: np.ndarray, bh_o: np.ndarray) -> dict:
+    """Path results uint32 [n, 4] and bounce-hit records float32 [n, bounces, 4] against the
+    oracle's. A path may differ only through a near-tie at its first differing bounce hit
+    (from there on it legitimately follows another ray); a path whose results differ while
+    all its bounce hits agree, or whose first differing hit is not a near-tie, is a mismatch."""
+    ru, ro = np.ascontiguousarray(res_g).view(np.uint32), np.ascontiguousarray(res_o).view(np.uint32)
+    bg, bo = np.ascontiguousarray(bh_g, np.float32), np.ascontiguousarray(bh_o, np.float32)
+    hit_diff = (bg.view(np.uint32) != bo.view(np.uint32)).any(axis=2)  # [n, bounces]
+    paths = np.nonzero((ru != ro).any(axis=1) | hit_diff.any(axis=1))[0]
+    d = hit_diff[paths]
+    has = d.any(axis=1)
+    k = np.argmax(d, axis=1)
+    tg = bg[paths, k, 0].astype(np.float64)
+    tw = bo[paths, k, 0].astype(np.float64)
+    ref_g, ref_o = bg[paths, k, 3].view(np.uint32), bo[paths, k, 3].view(np.uint32)
+    near = has & (ref_g != ref_o) & (tg < 3e38) & (tw < 3e38) & (np.abs(tg - tw) <= NEAR_TIE * np.abs(tw))
+    return {"differing": int(paths.size), "all_near_ties": bool(near.all()), "not_near_ties": int((~near).sum())}
+
+
+def oracle_parity(step: Step, cs: CpuStep) -> dict:
+    """The timed configuration against the oracle at full size: the tuned step (same tree, tracer,
+    launch and graph as the timed loop) once more with its bounce hits recorded, its 1,048,576
+    primary hits against the oracle's closest hits, then all 4,194,304 paths against the
+    oracle's paths started from the same primary hits. Recording the bounce hits must leave the
+    path results of the timed form unchanged."""
+    torch = step.torch
+    results_timed = step.results.cpu().numpy()
+    bh = torch.zeros((N_PATHS, 5, 4), dtype=torch.float32, device=step.dev)
+    res = torch.zeros_like(step.results)
+    step.rt.trace(step.rays, step.hits, False, step.sp)
+    step.rt.pathtrace(step.p_fused, step.rays, step.hits, N_PATHS, res, bh, step.sp)
+    step.rt.check(step.sp)
+    prim_g = step.hits.cpu().numpy()
+    res_g, bh_g = res.cpu().numpy(), bh.cpu().numpy()
+    del bh, res
+    rays = step.h_rays.numpy()
+    same_rays = bool((rays.view(np.uint32) == cs.rays.view(np.uint32)).all())
+    prim_o, _ = cs.o.closest(rays)
+    prim = classify_hits(prim_g, prim_o)
+    res_o, bh_o = cs.o.pathtrace(rays, prim_g, N_PATHS, bounce_hits=True)
+    paths = classify_paths(res_g, bh_g, res_o, bh_o)
+    timed_equal = bool((results_timed.view(np.uint32) == res_g.view(np.uint32)).all())
+    ok = same_rays and timed_equal and prim["all_near_ties"] and paths["all_near_ties"]
+    return {"ok": ok, "against": "oracle port of rt/cpu/bvh2.cpp on the same tree (%s)" % tree_label(cs.tree),
+            "primary_rays": int(rays.shape[0]), "primary_differing": prim["differing"],
+            "primary_exact_or_near_tie": prim["all_near_ties"], "paths": N_PATHS,
+            "paths_differing": paths["differing"], "all_near_ties": paths["all_near_ties"],
+            "timed_results_equal_recorded": timed_equal, "same_rays": same_rays,
+            "near_tie": "other triangle with |t1 - t2| <= 1e-6 t at the first differing hit"}
 
 
 def rays_in_results(step: Step) -> int:
@@ -443,6 +528,7 @@ def run_gb300(args):
     for _ in range(max(3, args.warmup)):
         step.tuned()
         step.plain()
+        step.plain_tuned_tree()
         step.e2e()
     step.rt.check(step.sp)
     step.rt_plain.check(step.sp)
@@ -459,7 +545,8 @@ def run_gb300(args):
     try:
         tuned_ms, pt_ms = time_steps(step, step.tuned, args.steps, split=True)
         barrier()
-        plain_ms, _ = time_steps(step, step.plain, args.steps)
+        plain_ms, plain_pt_ms = time_steps(step, step.plain, args.steps, split=True)
+        tt_ms, tt_pt_ms = time_steps(step, step.plain_tuned_tree, args.steps, split=True)
         e2e_ms, _ = time_steps(step, step.e2e, args.steps)
         step.e2e_pipelined(3)  # warm-up of the staging buffers and streams
         e2e_pipe_ms = step.e2e_pipelined(args.steps)
@@ -511,17 +598,31 @@ def run_gb300(args):
                                      round(max(tuned_ms), 4)],
                            "plain": [round(min(plain_ms), 4), round(statistics.median(plain_ms), 4),
                                      round(max(plain_ms), 4)],
+                           "plain_same_tree": [round(min(tt_ms), 4), round(statistics.median(tt_ms), 4),
+                                               round(max(tt_ms), 4)],
                            "form": "min, median, max of the timed steps"},
         "plain_wavefront": {"value": round(plain_value, 1), "ms_per_step": round(statistics.mean(plain_ms), 4),
                             "rays_per_step": rays_plain, "loop_order": plain_order,
                             "order_ms": {k: round(v, 4) for k, v in plain_times.items()},
                             "bvh4_speculative_ms": round(plain_bvh4_ms, 4),
                             "tuned_tree": {"bvh": tree_label(tuning),
-                                           "loop_order": tt_order,
+                                           "loop_order": tt_order, "ms_per_step": round(statistics.mean(tt_ms), 4),
                                            "order_ms": {k: round(v, 4) for k, v in tt_times.items()}}},
         "speedup_vs_plain": round(value / plain_value, 3),
-        "speedup_vs_plain_same_tree": round(tt_times[tt_order] / statistics.mean(tuned_ms), 3),
+        "speedup_vs_plain_same_tree": round(statistics.mean(tt_ms) / statistics.mean(tuned_ms), 3),
         "speedup_vs_plain_while_while": round(plain_times["while-while"] / statistics.mean(tuned_ms), 3),
+        "diffuse_only": {
+            "rays_per_step": rays_tuned - step.n_primary,
+            "tuned_ms": round(statistics.mean(pt_ms), 4),
+            "plain_ms": round(statistics.mean(plain_pt_ms), 4),
+            "plain_same_tree_ms": round(statistics.mean(tt_pt_ms), 4),
+            "Mrays_s": round((rays_tuned - step.n_primary) / statistics.mean(pt_ms) / 1e3, 1),
+            "speedup_vs_plain": round(statistics.mean(plain_pt_ms) / statistics.mean(pt_ms), 3),
+            "speedup_vs_plain_same_tree": round(statistics.mean(tt_pt_ms) / statistics.mean(pt_ms), 3),
+            "spread_ms": {"tuned": [round(min(pt_ms), 4), round(max(pt_ms), 4)],
+                          "plain_same_tree": [round(min(tt_pt_ms), 4), round(max(tt_pt_ms), 4)]},
+            "form": "the diffuse bounce part of each timed step alone (after the primary trace), L2 flushed "
+                    "before each step"},
         "e2e": {"value": round(job_value(rays_tuned, args.steps, t_e2e_pipe, world), 1), "unit": "Mrays/s",
                 "ms_per_step": round(e2e_pipe_ms / args.steps, 4), "h2d_bytes_per_step": int(step.n_primary * 32),
                 "d2h_bytes_per_step": int(N_PATHS * 16),
@@ -533,12 +634,17 @@ def run_gb300(args):
         "clocks": clk,
         "build_ms": round(step.build_info["build_ms"], 1),
     }
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        rays_np = step.h_rays.numpy()
-        v, reps, n, dt, cores = cpu_baseline(rays_np)
+    cs = None
+    if rank == 0 and (not args.no_parity or (world == 1 and not args.no_cpu_baseline)):
+        cs = CpuStep(N_PATHS, tuning)
+    if cs is not None and not args.no_parity:
+        line["parity"] = oracle_parity(step, cs)
+    if cs is not None and world == 1 and not args.no_cpu_baseline:
+        v, reps, n, dt, cores = cpu_baseline(cs)
         line["cpu_baseline"] = {"value": round(v, 2), "unit": "Mrays/s", "cores": cores, "kind": "port",
-                                "sample": f"the full step (1024x1024 primary rays + 4,194,304 diffuse paths) "
-                                          f"x {reps} after 1 warm-up: {n} rays in {dt:.1f} s, median rate"}
+                                "sample": f"the full step (1024x1024 primary rays + 4,194,304 diffuse paths, "
+                                          f"{tree_label(tuning)}) x {reps} after 1 warm-up: {n} rays in {dt:.1f} s, "
+                                          f"median rate"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -554,11 +660,9 @@ def run_reference(args):
     rank, world, _ = dist_info()
     if rank != 0:
         return
-    import __graft_entry__ as ge
-    ge.load_package()
-    from illum_rt_gb300 import workloads as wl
-    _, rays = wl.spheres_primary(res=RES)
-    cs = CpuStep(rays, N_PATHS)
+    tuning = load_tuning(gpu_name_from_smi())
+    cs = CpuStep(N_PATHS, tuning)
+    rays = cs.rays
     for _ in range(args.warmup):
         cs.run()
     n_tot, t_tot = 0, 0.0
@@ -572,9 +676,12 @@ def run_reference(args):
             "warmup": args.warmup, "ms_per_step": round(1e3 * t_tot / args.steps, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "impl": "reference",
             "config": {"workload": WORKLOAD, "triangles": 262144, "primary_rays": rays.shape[0], "paths": N_PATHS,
-                       "rays_per_step": n_tot // max(1, args.steps)},
+                       "rays_per_step": n_tot // max(1, args.steps), "bvh": tree_label(tuning)},
             "cpu_baseline": {"value": round(value, 2), "unit": "Mrays/s", "cores": cores, "kind": "port",
                              "sample": f"the full step x {args.steps} after {args.warmup} warm-up, OpenMP over rays"},
+            "ref_source": "oracle port of rt/cpu/bvh2.cpp and rt/cpu/wavefront.cpp:53-70 (its trees and hits pinned "
+                          "to the reference compiled from its sources, tests/golden), scene and rays from the "
+                          "oracle's own generators; the reference's CPU build needs its sources, absent on this host",
             "e2e": {"value": round(value, 2), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 

@@ -1,4 +1,4 @@
-"""Builds the oracle (oracle.cpp -> _build/liboracle.so) and, where the reference sources are
+"""Builds the oracle (oracle.cpp, scenes.cpp -> _build/liboracle.so) and, where the reference sources are
 present, the reference harness (build_ref.sh -> _ref/libref_bbvh.so).
 
 Test infrastructure: called by __graft_entry__.build() and by the tests; nothing in the
@@ -19,10 +19,10 @@ def build(with_reference: bool = True) -> None:
     out = os.path.join(HERE, "_build")
     os.makedirs(out, exist_ok=True)
     so = os.path.join(out, "liboracle.so")
-    src = os.path.join(HERE, "oracle.cpp")
-    if not os.path.exists(so) or os.path.getmtime(so) < os.path.getmtime(src):
+    srcs = [os.path.join(HERE, f) for f in ("oracle.cpp", "scenes.cpp")]
+    if not os.path.exists(so) or os.path.getmtime(so) < max(os.path.getmtime(s) for s in srcs):
         subprocess.run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
-                        "-o", so, src], check=True)
+                        "-o", so] + srcs, check=True)
     if with_reference:
         env = dict(os.environ)
         env.setdefault("GRT_REFERENCE_DIR", REFERENCE_CHECKOUT)

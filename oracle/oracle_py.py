@@ -299,3 +299,38 @@ def adjoint64(vpos3, tris4, rays6, refs, grad3):
     f.argtypes = [ctypes.c_void_p] * 5 + [ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p]
     f(_p(vpos3), _p(tris4), _p(rays6), _p(refs), _p(grad3), refs.shape[0], _p(gv), _p(gr))
     return gv, gr
+
+
+# ---- the oracle's own copy of the benchmark workload (scenes.cpp) --------------------------
+
+def spheres_scene(seed=2, count=256, slices=32, stacks=16, cext=10.0, rmin=0.2, rmax=1.5):
+    """(vpos float32 [nv, 4], tris uint32 [nt, 4]) of the UV-sphere scene."""
+    v = np.zeros((count * (stacks + 1) * slices, 4), np.float32)
+    t = np.zeros((count * 2 * slices * stacks, 4), np.uint32)
+    f = _orc().orc_scene_spheres
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, ctypes.c_float,
+                  ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p]
+    if f(seed, count, slices, stacks, cext, rmin, rmax, _p(v), _p(t)) != 0:
+        raise ValueError("slices and stacks must divide 32 and 16")
+    return v, t
+
+
+def camera_rays(pos, look, up, fovy_deg, w, h, tmin=1e-4):
+    """float32 [w h, 8] pixel-centre pinhole rays, (o, t_min, d, t_max)."""
+    r = np.zeros((w * h, 8), np.float32)
+    p, lk, u = (np.asarray(x, np.float32) for x in (pos, look, up))
+    f = _orc().orc_camera_rays
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_float, ctypes.c_uint32,
+                  ctypes.c_uint32, ctypes.c_float, ctypes.c_void_p]
+    if f(_p(p), _p(lk), _p(u), fovy_deg, w, h, tmin, _p(r)) != 0:
+        raise ValueError("field of view outside (0, 180) degrees")
+    return r
+
+
+def spheres_primary(res=1024):
+    """The benchmark workload: the 262,144-triangle sphere scene and its res x res primary rays
+    from (0, 0, 35) towards the origin, 65 degrees vertical field of view."""
+    v, t = spheres_scene()
+    return v, t, camera_rays((0.0, 0.0, 35.0), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 65.0, res, res)

@@ -38,3 +38,62 @@ def test_profile_figures_are_present_and_plausible():
     # deepest plausible traversal
     assert l2 is not None and 48 < l2 < 10000
     assert bench.profile_figure("no_such_key") is None
+
+
+def _hits(n, seed):
+    import numpy as np
+    g = np.random.default_rng(seed)
+    h = np.zeros((n, 4), np.float32)
+    h[:, 0] = g.uniform(1, 50, n).astype(np.float32)
+    h[:, 1:3] = g.uniform(0, 0.5, (n, 2)).astype(np.float32)
+    h[:, 3] = g.integers(0, 1 << 20, n).astype(np.uint32).view(np.float32)
+    return h
+
+
+def test_classify_hits_near_ties_and_mismatches():
+    import numpy as np
+    want = _hits(1000, 1)
+    got = want.copy()
+    assert bench.classify_hits(got, want) == {"differing": 0, "all_near_ties": True, "not_near_ties": 0}
+    # another triangle at a t within 1e-6 t: a near-tie
+    got[5, 3] = np.uint32(7).view(np.float32)
+    got[5, 0] = np.nextafter(want[5, 0], np.float32(1e9))
+    r = bench.classify_hits(got, want)
+    assert r["differing"] == 1 and r["all_near_ties"]
+    # the same triangle with another beta: never a near-tie
+    got[9, 1] += np.float32(0.01)
+    r = bench.classify_hits(got, want)
+    assert r["differing"] == 2 and not r["all_near_ties"] and r["not_near_ties"] == 1
+    # another triangle far away, and a miss against a hit
+    got = want.copy()
+    got[3, 3] = np.uint32(8).view(np.float32)
+    got[3, 0] = want[3, 0] * np.float32(1.01)
+    got[4, 0] = np.float32(3.4028234663852886e38)
+    got[4, 3] = np.uint32(9).view(np.float32)
+    assert bench.classify_hits(got, want)["not_near_ties"] == 2
+
+
+def test_classify_paths_first_differing_bounce():
+    import numpy as np
+    n, b = 200, 5
+    bh_o = _hits(n * b, 2).reshape(n, b, 4)
+    res_o = np.random.default_rng(3).integers(0, 1 << 30, (n, 4)).astype(np.uint32)
+    res_g, bh_g = res_o.copy(), bh_o.copy()
+    assert bench.classify_paths(res_g, bh_g, res_o, bh_o)["differing"] == 0
+    # path 10 leaves through a near-tie at bounce 2 and then differs in everything after it
+    bh_g[10, 2, 3] = np.uint32(12345).view(np.float32)
+    bh_g[10, 2, 0] = np.nextafter(bh_o[10, 2, 0], np.float32(0))
+    bh_g[10, 3:] = _hits(2, 9)
+    res_g[10] += 1
+    r = bench.classify_paths(res_g, bh_g, res_o, bh_o)
+    assert r == {"differing": 1, "all_near_ties": True, "not_near_ties": 0}
+    # path 20: results differ but every bounce hit agrees (a shading mismatch)
+    res_g[20, 0] ^= 1
+    r = bench.classify_paths(res_g, bh_g, res_o, bh_o)
+    assert r["differing"] == 2 and r["not_near_ties"] == 1
+    # path 30: first differing hit is far from the oracle's
+    res_g[20] = res_o[20]
+    bh_g[30, 0, 0] = bh_o[30, 0, 0] * np.float32(2)
+    bh_g[30, 0, 3] = np.uint32(1).view(np.float32)
+    r = bench.classify_paths(res_g, bh_g, res_o, bh_o)
+    assert r["differing"] == 2 and r["not_near_ties"] == 1
