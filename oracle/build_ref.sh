@@ -1,5 +1,6 @@
 #!/bin/sh
 # Builds oracle/_ref/libref_bbvh.so from the reference's own CPU ray tracer sources, unmodified,
+# and oracle/_ref/libref_sampling.so from its camera source and sampling / shading headers,
 # where they lie under the reference checkout named by $GRT_REFERENCE_DIR (oracle/build.py sets
 # it). Used only to pin the oracle restatement and to generate golden fixtures; prints a notice
 # and exits 0 when the variable is unset or the checkout is absent (for example on the GPU machine).
@@ -17,4 +18,5 @@ CXX=${CXX:-g++}
 FLAGS="-std=c++17 -O2 -fPIC -fopenmp -ffp-contract=off -DNDEBUG -w -I$HERE/shim -I$REF -I$REF/libgi"
 $CXX $FLAGS -shared -o "$OUT/libref_bbvh.so" \
     "$HERE/ref_harness.cpp" "$REF/rt/cpu/bvh2.cpp" "$REF/libgi/timer.cpp" "$REF/libgi/rt.cpp"
-echo "build_ref: built $OUT/libref_bbvh.so"
+$CXX $FLAGS -shared -o "$OUT/libref_sampling.so" "$HERE/ref_sampling.cpp" "$REF/libgi/camera.cpp"
+echo "build_ref: built $OUT/libref_bbvh.so and $OUT/libref_sampling.so"

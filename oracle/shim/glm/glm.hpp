@@ -16,6 +16,7 @@
 #include <cmath>
 #include <cstdint>
 #include <string>
+#include <type_traits>
 
 namespace glm {
 
@@ -82,6 +83,18 @@ struct mat4 {
     }
 };
 
+// Right-hand operand of a compound assignment: a scalar of any arithmetic type is first
+// converted to the vector's component type (as glm does, e.g. `normal *= -1`); a vector
+// passes through unchanged.
+template <typename T, typename V, typename std::enable_if<std::is_arithmetic<V>::value, int>::type = 0>
+T shim_operand(const V &b) {
+    return T(b);
+}
+template <typename T, typename V, typename std::enable_if<!std::is_arithmetic<V>::value, int>::type = 0>
+const V &shim_operand(const V &b) {
+    return b;
+}
+
 #define GRT_SHIM_BINOP(OP)                                                                          \
     template <typename T> vec<2, T> operator OP(const vec<2, T> &a, const vec<2, T> &b) {            \
         return vec<2, T>(a.x OP b.x, a.y OP b.y);                                                   \
@@ -111,7 +124,7 @@ struct mat4 {
         return vec<4, T>(s OP a.x, s OP a.y, s OP a.z, s OP a.w);                                   \
     }                                                                                               \
     template <int L, typename T, typename V> vec<L, T> &operator OP##=(vec<L, T> &a, const V &b) {  \
-        a = a OP b;                                                                                 \
+        a = a OP shim_operand<T>(b);                                                                \
         return a;                                                                                   \
     }
 
@@ -167,6 +180,9 @@ inline vec2 normalize(const vec2 &a) { return a * (1.0f / std::sqrt(dot(a, a)));
 inline vec3 abs(const vec3 &a) { return vec3(std::fabs(a.x), std::fabs(a.y), std::fabs(a.z)); }
 inline vec2 floor(const vec2 &a) { return vec2(std::floor(a.x), std::floor(a.y)); }
 inline float radians(float d) { return d * float(M_PI / 180.0); }
+inline vec3 fract(const vec3 &a) { return vec3(a.x - std::floor(a.x), a.y - std::floor(a.y), a.z - std::floor(a.z)); }
+// mix(x, y, a) = x * (1 - a) + y * a
+inline vec3 mix(const vec3 &x, const vec3 &y, float a) { return x * (1.0f - a) + y * a; }
 
 template <int L, typename T> std::string to_string(const vec<L, T> &v) {
     std::string s = "vec(";
