@@ -96,6 +96,12 @@ class RayBatch(ctypes.Structure):
                 ("hits_dev", ctypes.c_void_p)]
 
 
+class Camera(ctypes.Structure):
+    """grt_camera: the fields of the reference's struct camera (libgi/camera.h:7-24)."""
+    _fields_ = [("pos", ctypes.c_float * 3), ("dir", ctypes.c_float * 3), ("up", ctypes.c_float * 3),
+                ("near_w", ctypes.c_float), ("near_h", ctypes.c_float)]
+
+
 class Config(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("reserved", ctypes.c_uint32)]
 
@@ -150,6 +156,7 @@ _PROTOS = {
     "grt_set_timing": (I, [VP, I]),
     "grt_timing_stats": (I, [VP, P(Timing), I]),
     "grt_incoherent_rays": (I, [VP, ctypes.c_float, ctypes.c_float, ctypes.c_uint64, VP, U32, VP]),
+    "grt_camera_rays": (I, [VP, P(Camera), U32, U32, VP, I, ctypes.c_uint64, VP, VP]),
 }
 
 
@@ -392,6 +399,30 @@ class BatchRayTracer:
         b = self.incoherence_r2 if r2 is None else r2
         self._check(lib().grt_incoherent_rays(self.ctx, float(a), float(b), int(seed), _ptr(rays), int(n),
                                               VP(stream or 0)))
+        return rays
+
+    def camera_rays(self, pos, dir, up, near_w, near_h, w: int, h: int, rays=None, offsets=None, jitter=False,
+                    seed: int = 0, stream=None):
+        """grt_camera_rays: the w x h camera rays of the primary-ray step as cam_ray computes them
+        (libgi/camera.cpp:11-28), into `rays` (a CUDA tensor [w h, 8], allocated if None).
+        offsets: a CUDA tensor [w h, 2] of sub-pixel offsets in [-0.5, 0.5), or None (then PCG
+        jitter from `seed` when `jitter`, else pixel centres)."""
+        import torch
+        n = int(w) * int(h)
+        if rays is None:
+            rays = torch.empty((n, 8), dtype=torch.float32, device=f"cuda:{self.device}")
+        _check_cuda_tensor(rays, "rays", 8)
+        if rays.shape[0] < n:
+            raise ValueError("rays holds fewer than w * h rays")
+        if offsets is not None:
+            _check_cuda_tensor(offsets, "offsets", 2)
+            if offsets.shape[0] < n:
+                raise ValueError("offsets holds fewer than w * h pairs")
+        cam = Camera((ctypes.c_float * 3)(*pos), (ctypes.c_float * 3)(*dir), (ctypes.c_float * 3)(*up),
+                     float(near_w), float(near_h))
+        self._check(lib().grt_camera_rays(self.ctx, ctypes.byref(cam), int(w), int(h),
+                                          _ptr(offsets) if offsets is not None else None, int(bool(jitter)),
+                                          int(seed), _ptr(rays), VP(stream or 0)))
         return rays
 
     def refit(self, vpos, stream=None):

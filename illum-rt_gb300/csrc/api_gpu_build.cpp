@@ -189,6 +189,25 @@ grt_status grt_incoherent_rays(grt_ctx *c, float r1, float r2, uint64_t seed, fl
     return e == cudaSuccess ? GRT_OK : cuda_fail(c, e, "generating the incoherent rays");
 }
 
+grt_status grt_camera_rays(grt_ctx *c, const grt_camera *cam, uint32_t w, uint32_t h, const float *offsets_dev,
+                           int jitter, uint64_t seed, float *rays_dev, grt_stream_t stream) {
+    if (!c) return GRT_ERR_INVALID_ARG;
+    if (!cam) return fail(c, GRT_ERR_INVALID_ARG, "no camera");
+    const uint64_t n = (uint64_t)w * h;
+    if (n > 0xFFFFFFFFull) return fail(c, GRT_ERR_INVALID_ARG, "more than 2^32 - 1 rays");
+    if (n == 0) return GRT_OK;
+    if (!rays_dev || !aligned16(rays_dev)) return fail(c, GRT_ERR_INVALID_ARG, "null or misaligned ray buffer");
+    if (offsets_dev && ((uintptr_t)offsets_dev & 7u))
+        return fail(c, GRT_ERR_INVALID_ARG, "misaligned offset buffer (needs 8-byte alignment)");
+    const float v[11] = {cam->pos[0], cam->pos[1], cam->pos[2], cam->dir[0], cam->dir[1], cam->dir[2],
+                         cam->up[0],  cam->up[1],  cam->up[2],  cam->near_w, cam->near_h};
+    device_guard g(c->device);
+    timed_call timer(c, GRT_TIME_RAYS, (cudaStream_t)stream);
+    const cudaError_t e = launch_camera_rays(v, w, h, (const float2 *)offsets_dev, jitter != 0, seed,
+                                             (float4 *)rays_dev, (cudaStream_t)stream);
+    return e == cudaSuccess ? GRT_OK : cuda_fail(c, e, "generating the camera rays");
+}
+
 grt_status grt_build_scenes_device(grt_ctx *c, const grt_mesh *meshes, uint32_t count, uint32_t max_tris,
                                    grt_stream_t stream) {
     if (!c) return GRT_ERR_INVALID_ARG;

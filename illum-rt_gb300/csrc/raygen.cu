@@ -1,4 +1,6 @@
-// Incoherent test rays: the reference CUDA tracer's `incoherence r1 r2` setting
+// Camera rays of the primary-ray step (grt_camera_rays; cam_ray, libgi/camera.cpp:11-28, in its
+// own float arithmetic), and incoherent test rays: the reference CUDA tracer's
+// `incoherence r1 r2` setting
 // (rt/cuda/base.cpp:120-133), which replaces the camera rays by rays between two spheres placed
 // in the scene (batch_cam_ray_setup::run, rt/cuda/rni.cpp:36-84; setup_ray_incoherent,
 // rt/cuda/kernels.cu:75-156):
@@ -109,7 +111,59 @@ __global__ void __launch_bounds__(kThreads) k_incoherent(const uint32_t *__restr
     rays[2 * (size_t)i + 1] = make_float4(d.x, d.y, d.z, FLT_MAX);
 }
 
+// The camera of the primary-ray step, by value.
+struct cam_t {
+    pm::f3 pos, dir, up;
+    float near_w, near_h;
+};
+
+// cam_ray (libgi/camera.cpp:11-28) for pixel i = y w + x, every operation rounded as the float
+// code rounds it (glm's normalize is a * (1 / sqrt(dot(a, a))), its dot ((x x' + y y') + z z'),
+// its cross (a.y b.z - b.y a.z, a.z b.x - b.z a.x, a.x b.y - b.x a.y)). One thread per ray;
+// the 32-byte ray is written with two 16-byte stores.
+__global__ void __launch_bounds__(kThreads) k_camera_rays(cam_t cam, uint32_t w, uint32_t h,
+                                                          const float2 *__restrict__ offsets, int jitter,
+                                                          uint64_t seed, float4 *rays) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (uint64_t)w * h) return;
+    const uint32_t y = (uint32_t)(i / w), x = (uint32_t)(i - (uint64_t)y * w);
+    auto cross = [](pm::f3 a, pm::f3 b) -> pm::f3 {
+        return {pm::sub(pm::mul(a.y, b.z), pm::mul(b.y, a.z)), pm::sub(pm::mul(a.z, b.x), pm::mul(b.z, a.x)),
+                pm::sub(pm::mul(a.x, b.y), pm::mul(b.x, a.y))};
+    };
+    const pm::f3 U = pm::normalize3(cross(cam.dir, cam.up));
+    const pm::f3 V = pm::normalize3(cross(U, cam.dir));
+    float ox = 0.f, oy = 0.f;
+    if (offsets) {
+        const float2 o = offsets[i];
+        ox = o.x;
+        oy = o.y;
+    } else if (jitter) {
+        pm::pcg32 rng;
+        rng.set_sequence(seed + i);
+        ox = pm::sub(rng.uniform(), 0.5f);
+        oy = pm::sub(rng.uniform(), 0.5f);
+    }
+    const float u = pm::mul(cam.near_w, pm::sub(pm::mul(pm::div(pm::add(pm::add((float)x, 0.5f), ox), (float)w), 2.0f), 1.0f));
+    const float v = pm::mul(cam.near_h, pm::sub(pm::mul(pm::div(pm::add(pm::add((float)y, 0.5f), oy), (float)h), 2.0f), 1.0f));
+    const pm::f3 d = pm::normalize3({pm::add(pm::add(cam.dir.x, pm::mul(U.x, u)), pm::mul(V.x, v)),
+                                     pm::add(pm::add(cam.dir.y, pm::mul(U.y, u)), pm::mul(V.y, v)),
+                                     pm::add(pm::add(cam.dir.z, pm::mul(U.z, u)), pm::mul(V.z, v))});
+    rays[2 * i] = make_float4(cam.pos.x, cam.pos.y, cam.pos.z, 1e-4f);
+    rays[2 * i + 1] = make_float4(d.x, d.y, d.z, FLT_MAX);
+}
+
 }  // namespace
+
+cudaError_t launch_camera_rays(const float c[11], uint32_t w, uint32_t h, const float2 *offsets, bool jitter,
+                               uint64_t seed, float4 *rays, cudaStream_t st) {
+    const uint64_t n = (uint64_t)w * h;
+    if (n == 0) return cudaSuccess;
+    cam_t cam = {{c[0], c[1], c[2]}, {c[3], c[4], c[5]}, {c[6], c[7], c[8]}, c[9], c[10]};
+    k_camera_rays<<<(unsigned)((n + kThreads - 1) / kThreads), kThreads, 0, st>>>(cam, w, h, offsets, jitter ? 1 : 0,
+                                                                                 seed, rays);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_incoherent_rays(const float4 *vpos, uint32_t nv, float r1, float r2, uint64_t seed, float4 *rays,
                                    uint32_t n, uint32_t *bounds, cudaStream_t st) {

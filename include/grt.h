@@ -481,7 +481,7 @@ enum {
     GRT_TIME_DIRECT = 3,       /* grt_direct, grt_hit_albedo */
     GRT_TIME_ADJOINT = 4,      /* grt_adjoint */
     GRT_TIME_TREE = 5,         /* grt_build_device, grt_build_scenes_device, grt_refit */
-    GRT_TIME_RAYS = 6,         /* grt_incoherent_rays, grt_compact_hits, grt_shadow_rays */
+    GRT_TIME_RAYS = 6,         /* grt_incoherent_rays, grt_camera_rays, grt_compact_hits, grt_shadow_rays */
     GRT_TIME_KINDS = 7
 };
 typedef struct grt_timing {
@@ -504,6 +504,29 @@ grt_status grt_timing_stats(grt_ctx *ctx, grt_timing *out, int reset);
  * numbers come from a PCG32 stream per ray (seed + ray index) instead of cuRAND's MTGP32. */
 grt_status grt_incoherent_rays(grt_ctx *ctx, float r1, float r2, uint64_t seed, float *rays_dev, uint32_t n,
                                grt_stream_t stream);
+
+/* A pinhole camera as the reference's struct camera holds it (libgi/camera.h:7-24): position,
+ * view direction (normalised), up vector, and the half extents of the near plane at distance 1
+ * (camera::update_frustum: near_h = tan(fovy / 2), near_w = aspect * near_h). */
+typedef struct grt_camera {
+    float pos[3], dir[3], up[3];
+    float near_w, near_h;
+} grt_camera;
+
+/* The camera rays of a w x h image on the device: the primary-ray step of the wavefront
+ * algorithms (batch_cam_ray_setup -> setup_rays, rt/cuda/rni.cpp:86-99, rt/cuda/kernels.cu:26-61)
+ * computed as the reference's cam_ray computes them on the CPU (libgi/camera.cpp:11-28), bit for
+ * bit: U = normalize(cross(dir, up)), V = normalize(cross(U, dir)),
+ * u = near_w ((x + 0.5 + offset.x) / w * 2 - 1), v likewise with y and near_h,
+ * d = normalize(dir + U u + V v); origin pos, t_min = 1e-4 (ray::eps), t_max = FLT_MAX. Ray (x, y)
+ * goes to index y w + x of DEVICE rays_dev (the grt_trace layout, 2 w h float4).
+ * Sub-pixel offsets (cam_ray's `offset`, in [-0.5, 0.5)): offsets_dev, two floats per pixel in
+ * device memory, when given; otherwise with jitter != 0 two uniform_float draws minus 0.5 from a
+ * PCG32 stream per pixel (rng_pcg::set_sequence(seed + pixel index)); otherwise the pixel
+ * centres. (The reference's CUDA setup_rays builds rays with unnormalised U and V and t_min 0;
+ * this step follows cam_ray, the rays of the CPU tracer the hits are defined against.) */
+grt_status grt_camera_rays(grt_ctx *ctx, const grt_camera *camera, uint32_t w, uint32_t h, const float *offsets_dev,
+                           int jitter, uint64_t seed, float *rays_dev, grt_stream_t stream);
 
 #ifdef __cplusplus
 }

@@ -334,3 +334,34 @@ def spheres_primary(res=1024):
     from (0, 0, 35) towards the origin, 65 degrees vertical field of view."""
     v, t = spheres_scene()
     return v, t, camera_rays((0.0, 0.0, 35.0), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 65.0, res, res)
+
+
+def cam_rays(pos, dir, up, near_w, near_h, w, h, offsets=None, jitter=False, seed=0):
+    """float32 [w h, 8] camera rays in cam_ray's float arithmetic (scenes.cpp orc_cam_rays)."""
+    r = np.zeros((w * h, 8), np.float32)
+    p, d, u = (np.asarray(x, np.float32) for x in (pos, dir, up))
+    off = np.ascontiguousarray(offsets, np.float32) if offsets is not None else None
+    f = _orc().orc_cam_rays
+    f.restype = None
+    f.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_float, ctypes.c_float, ctypes.c_uint32, ctypes.c_uint32,
+                                          ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_void_p]
+    f(_p(p), _p(d), _p(u), near_w, near_h, w, h, _p(off) if off is not None else None, int(bool(jitter)), seed, _p(r))
+    return r
+
+
+def ref_cam_rays(pos, dir, up, near_w, near_h, w, h, offsets=None, jitter=False, seed=0):
+    """The same rays from the reference's own cam_ray (oracle/_ref/libref_sampling.so), or None
+    where the reference build is absent."""
+    path = os.path.join(HERE, "_ref", "libref_sampling.so")
+    if not os.path.exists(path):
+        return None
+    lib = ctypes.CDLL(path)
+    r = np.zeros((w * h, 8), np.float32)
+    p, d, u = (np.asarray(x, np.float32) for x in (pos, dir, up))
+    off = np.ascontiguousarray(offsets, np.float32) if offsets is not None else None
+    f = lib.refs_cam_rays_offsets
+    f.restype = None
+    f.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_float, ctypes.c_float, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_void_p]
+    f(_p(p), _p(d), _p(u), near_w, near_h, w, h, _p(off) if off is not None else None, int(bool(jitter)), seed, _p(r))
+    return r

@@ -112,4 +112,33 @@ void refs_cam_rays(const float *pos3, const float *dir3, const float *up3, float
         }
 }
 
+// cam_ray at every pixel of a camera given as the struct's fields (near_w and near_h set
+// directly rather than from a field of view), with sub-pixel offsets: offsets2 (two floats per
+// pixel) when given; otherwise, with jitter != 0, (uniform_float() - 0.5, uniform_float() - 0.5)
+// from rng_pcg(seed + pixel index); otherwise the pixel centres.
+void refs_cam_rays_offsets(const float *pos3, const float *dir3, const float *up3, float near_w, float near_h, int w,
+                           int h, const float *offsets2, int jitter, uint64_t seed, float *rays8) {
+    camera cam(vec3(dir3[0], dir3[1], dir3[2]), vec3(pos3[0], pos3[1], pos3[2]), vec3(up3[0], up3[1], up3[2]), 60.0f,
+               w, h);
+    cam.near_w = near_w;
+    cam.near_h = near_h;
+    for (int y = 0; y < h; ++y)
+        for (int x = 0; x < w; ++x) {
+            const size_t i = (size_t)y * w + x;
+            vec2 off(0.0f, 0.0f);
+            if (offsets2) {
+                off = vec2(offsets2[2 * i], offsets2[2 * i + 1]);
+            } else if (jitter) {
+                rng_pcg rng(seed + i);
+                const float ox = rng.uniform_float() - 0.5f;
+                const float oy = rng.uniform_float() - 0.5f;
+                off = vec2(ox, oy);
+            }
+            const ray r = cam_ray(cam, x, y, off);
+            float *o = rays8 + 8 * i;
+            o[0] = r.o.x, o[1] = r.o.y, o[2] = r.o.z, o[3] = r.t_min;
+            o[4] = r.d.x, o[5] = r.d.y, o[6] = r.d.z, o[7] = r.t_max;
+        }
+}
+
 }  // extern "C"

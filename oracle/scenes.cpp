@@ -171,4 +171,49 @@ int orc_camera_rays(const float *pos3, const float *look3, const float *up3, flo
     return 0;
 }
 
+// Camera rays as the reference's cam_ray (libgi/camera.cpp:11-28) computes them, in float:
+// U = normalize(cross(dir, up)), V = normalize(cross(U, dir)), u = ((x + 0.5 + off.x) / w * 2 - 1)
+// near_w, v likewise, d = normalize((dir + U u) + V v) with normalize(a) = a * (1 / sqrt(a . a)),
+// origin pos, t_min = 1e-4 (ray::eps, libgi/rt.h:25), t_max = FLT_MAX. Offsets: offsets2 (two
+// floats per pixel), or with jitter != 0 two PCG32 uniform floats minus 0.5 from the stream of
+// sequence seed + pixel index, or zero. The file is compiled with -ffp-contract=off, so every
+// float operation rounds as written.
+void orc_cam_rays(const float *pos3, const float *dir3, const float *up3, float near_w, float near_h, uint32_t w,
+                  uint32_t h, const float *offsets2, int jitter, uint64_t seed, float *rays8) {
+    struct f3 {
+        float x, y, z;
+    };
+    auto cross = [](f3 a, f3 b) -> f3 {
+        return {a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y};
+    };
+    auto norm = [](f3 a) -> f3 {
+        const float k = 1.0f / std::sqrt((a.x * a.x + a.y * a.y) + a.z * a.z);
+        return {a.x * k, a.y * k, a.z * k};
+    };
+    const f3 dir = {dir3[0], dir3[1], dir3[2]}, up = {up3[0], up3[1], up3[2]};
+    const f3 U = norm(cross(dir, up));
+    const f3 V = norm(cross(U, dir));
+    for (uint32_t y = 0; y < h; ++y)
+        for (uint32_t x = 0; x < w; ++x) {
+            const uint64_t i = (uint64_t)y * w + x;
+            float ox = 0.0f, oy = 0.0f;
+            if (offsets2) {
+                ox = offsets2[2 * i];
+                oy = offsets2[2 * i + 1];
+            } else if (jitter) {
+                pcg rng(seed + i);
+                const uint32_t a = rng.step(), b = rng.step();
+                const float fa = (float)a * 0x1p-32f, fb = (float)b * 0x1p-32f;
+                ox = (fa < 0x1.fffffep-1f ? fa : 0x1.fffffep-1f) - 0.5f;
+                oy = (fb < 0x1.fffffep-1f ? fb : 0x1.fffffep-1f) - 0.5f;
+            }
+            const float u = near_w * ((((float)x + 0.5f) + ox) / (float)w * 2.0f - 1.0f);
+            const float v = near_h * ((((float)y + 0.5f) + oy) / (float)h * 2.0f - 1.0f);
+            const f3 d = norm({(dir.x + U.x * u) + V.x * v, (dir.y + U.y * u) + V.y * v, (dir.z + U.z * u) + V.z * v});
+            float *r = rays8 + 8 * i;
+            r[0] = pos3[0], r[1] = pos3[1], r[2] = pos3[2], r[3] = 1e-4f;
+            r[4] = d.x, r[5] = d.y, r[6] = d.z, r[7] = FLT_MAX;
+        }
+}
+
 }  // extern "C"

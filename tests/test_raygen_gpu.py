@@ -98,3 +98,47 @@ def test_incoherence_command_and_tracing(api, orc, scene_rt):
     assert (want[:, 0] < 3e38).mean() > 0.1  # the rays cross the sphere field
     with pytest.raises(api.GRTError):
         rt.incoherent_rays(10, r1=-1.0, r2=0.0)
+
+
+def _golden_camera():
+    import os
+    return dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "golden_camera.npz")))
+
+
+def test_camera_rays_equal_reference_cam_ray(api, orc):
+    """grt_camera_rays against the reference's own cam_ray (golden cases: pixel centres, PCG
+    jitter, explicit offsets) and against the oracle's restatement at 1024x1024 and 1920x1080,
+    bit for bit."""
+    import torch
+    from make_golden_camera import camera_cases
+    g = _golden_camera()
+    rt = api.BatchRayTracer(0)
+    for name, pos, d, up, nw, nh, w, h, mode, seed, _ in camera_cases():
+        off = g.get(name + "/offsets")
+        d_off = torch.from_numpy(off).cuda() if off is not None else None
+        rays = rt.camera_rays(pos, d, up, nw, nh, w, h, offsets=d_off, jitter=mode == "jitter", seed=seed)
+        torch.cuda.synchronize()
+        assert (rays.cpu().numpy().view(np.uint32) == g[name + "/rays"].view(np.uint32)).all(), name
+    d = np.array((0.0, 0.0, -1.0), np.float32)
+    for w, h, jitter in ((1024, 1024, True), (1920, 1080, False)):
+        rays = rt.camera_rays((0.0, 0.0, 35.0), d, (0.0, 1.0, 0.0), 0.6370703 * w / h, 0.6370703, w, h,
+                              jitter=jitter, seed=5)
+        torch.cuda.synchronize()
+        want = orc.cam_rays((0.0, 0.0, 35.0), d, (0.0, 1.0, 0.0), 0.6370703 * w / h, 0.6370703, w, h, None, jitter, 5)
+        assert (rays.cpu().numpy().view(np.uint32) == want.view(np.uint32)).all(), (w, h)
+    rt.close()
+
+
+def test_camera_rays_arguments(api):
+    import torch
+    rt = api.BatchRayTracer(0)
+    ok = torch.zeros((16, 8), device="cuda")
+    cam = ((0.0, 0.0, 5.0), (0.0, 0.0, -1.0), (0.0, 1.0, 0.0), 0.5, 0.5)
+    rt.camera_rays(*cam, 4, 4, rays=ok)
+    with pytest.raises(ValueError):
+        rt.camera_rays(*cam, 5, 4, rays=ok)  # too small
+    raw = torch.zeros(16 * 8 + 1, device="cuda")
+    with pytest.raises(api.GRTError):
+        rt.camera_rays(*cam, 4, 4, rays=raw[1:].view(16, 8))  # misaligned
+    rt.camera_rays(*cam, 0, 4, rays=ok)  # no pixels: nothing to do
+    rt.close()
