@@ -214,8 +214,7 @@ class Step:
         self.rt_tt = api.BatchRayTracer(device)
         self.rt_tt.build(sc.vpos, sc.tris, **tree)
         self.rt.select(tuning.get("tracer", "persistent-while-while"))
-        kw = {k: v for k, v in tuning.items() if k in ("block_threads", "blocks_per_sm", "refill_threshold",
-                                                         "refill_period", "stack_entries")}
+        kw = {k: v for k, v in tuning.items() if k in api.TUNING_KEYS}
         self.tracer = tuning.get("tracer", "persistent-while-while")
         if kw:
             self.rt.set_tuning(**kw)
@@ -733,7 +732,7 @@ def run_soups64(args):
     for kind in ("host", "gpu"):
         rt = api.BatchRayTracer(0)
         rt.select(tuning.get("tracer", "persistent-speculative-while-while"))
-        kw = {k: v for k, v in tuning.items() if k in ("block_threads", "refill_threshold", "refill_period")}
+        kw = {k: v for k, v in tuning.items() if k in api.TUNING_KEYS}
         if kw:
             rt.set_tuning(**kw)
         torch.cuda.synchronize()
@@ -946,7 +945,7 @@ def run_profile_case_other(workload: str):
             rays.append(torch.from_numpy(wl.shell_rays(2000 + i, lo, hi, nr)).cuda())
         hits = [torch.zeros((r.shape[0], 4), device="cuda") for r in rays]
         rt.select(tuning.get("tracer", "persistent-speculative-while-while"))
-        kw = {k: v for k, v in tuning.items() if k in ("block_threads", "refill_threshold", "refill_period")}
+        kw = {k: v for k, v in tuning.items() if k in api.TUNING_KEYS}
         if kw:
             rt.set_tuning(**kw)
         rt.build_scenes_device(scenes, max_tris=tuning.get("max_tris", 4), stream=sp)

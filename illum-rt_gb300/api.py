@@ -60,7 +60,12 @@ class AlphaTexture(ctypes.Structure):
 
 class Tuning(ctypes.Structure):
     _fields_ = [("block_threads", ctypes.c_int), ("blocks_per_sm", ctypes.c_int), ("refill_threshold", ctypes.c_int),
-                ("refill_period", ctypes.c_int), ("stack_entries", ctypes.c_int)]
+                ("refill_period", ctypes.c_int), ("stack_entries", ctypes.c_int), ("spec_pend", ctypes.c_int),
+                ("spec_exit", ctypes.c_int), ("spec_visits", ctypes.c_int)]
+
+
+# grt_tuning fields a tuning-table entry may set (the rest of an entry names the tracer and tree)
+TUNING_KEYS = tuple(k for k, _ in Tuning._fields_)
 
 
 class PtParams(ctypes.Structure):

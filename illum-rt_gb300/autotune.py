@@ -1,12 +1,15 @@
 """Autotuner for the persistent kernels: loop order, warps per block, refill threshold and
-period, and the tree (leaf size, SAH candidate planes, early split clipping).
+period, the tree (leaf size, SAH candidate planes, early split clipping), and for the
+speculative order its warp-level parameters (leaves postponed per lane, lanes still searching
+when the warp leaves its node phase, node visits per warp vote) and the traversal stack size.
 
 For every candidate it builds the scene's BVH with the reference builder's options
 (`max_triangles_per_node`, `number_of_planes`, `esc`), sets the launch parameters through
 grt_set_tuning and times the fused path-tracing step (persistent primary trace + fused bounce
 loop) with CUDA events. Three stages: launch parameters and leaf size on trees of the
 reference's 16 planes with clipping; then, with the best launch, every leaf size, plane count
-and clipping choice; then the launch parameters again on the best tree. The fastest
+and clipping choice; then the launch parameters again on the best tree; then, for a speculative
+tracer, the grid of its warp-level parameters and stack sizes on that tree. The fastest
 configuration is written to tuning.json under "<GPU name>|<scene class>", where bench.py picks
 it up. Results do not depend on the launch parameters; other tree options give a different
 (equally reference-built) BVH.
@@ -116,13 +119,44 @@ def tune(quick: bool = False, n_paths: int = 4 << 20, res: int = 1024, log=print
             best = cfg
     # stage 3: the launch parameters again on the best tree
     tree = {k: best[k] for k in ("max_tris", "planes", "esc")}
+    build(tree)
     if tree != {"max_tris": best["max_tris"], "planes": 16, "esc": 1}:
-        build(tree)
         launch_sweep([best["tracer"]], tree)
+    # stage 4: the speculative order's warp-level parameters and the stack size
+    if "speculative" in best["tracer"]:
+        best = spec_sweep(rt, best, quick, log,
+                          lambda: time_config(rt, api, rays, hits, results, n_paths, stream))
+        searched += best.pop("_searched")
     rt.close()
     best["searched"] = searched
     best["seconds"] = round(time.time() - t0, 1)
     return best
+
+
+SPEC_GRID = {"spec_pend": [1, 2, 3], "spec_exit": [4, 6, 8, 12], "spec_visits": [3, 5], "stack_entries": [0, 32]}
+SPEC_GRID_QUICK = {"spec_pend": [2], "spec_exit": [8], "spec_visits": [3, 5], "stack_entries": [0]}
+
+
+def spec_sweep(rt, best: dict, quick: bool, log, timer) -> dict:
+    """Times every point of the speculative grid (leaves postponed, exit lanes, visits per vote,
+    stack entries; 0 = the tree's depth) with the best tracer, tree and launch; returns the
+    best configuration with its grid values (and the number of points under `_searched`)."""
+    launch = {k: best[k] for k in ("block_threads", "refill_threshold", "refill_period")}
+    grid = SPEC_GRID_QUICK if quick else SPEC_GRID
+    keys = list(grid)
+    out, n = dict(best), 0
+    for vals in itertools.product(*(grid[k] for k in keys)):
+        spec = dict(zip(keys, vals))
+        rt.set_tuning(**launch, blocks_per_sm=0, **spec)
+        ms = timer()
+        cfg = {**best, **spec, "ms": ms}
+        log(json.dumps(cfg))
+        n += 1
+        if ms < out["ms"]:
+            out = cfg
+    rt.set_tuning(**launch, blocks_per_sm=0, **{k: out.get(k, 0) for k in keys})
+    out["_searched"] = n
+    return out
 
 
 def tune_soups(quick: bool = False, log=print) -> dict:
@@ -170,8 +204,28 @@ def tune_soups(quick: bool = False, log=print) -> dict:
             log(json.dumps(cfg))
             if best is None or ms < best["ms"]:
                 best = cfg
+    searched = len(orders) * len(leaf_sizes) * len(blocks) * len(thresholds) * len(periods)
+    if "speculative" in best["tracer"]:
+        rt.build_scenes_device(scenes, max_tris=best["max_tris"], stream=sp)
+        rt.select(best["tracer"])
+
+        def timer():
+            ms = float("inf")
+            for i in range(4):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                rt.trace_multi(batches, stream=sp)
+                e1.record(stream)
+                e1.synchronize()
+                if i:
+                    ms = min(ms, e0.elapsed_time(e1))
+            rt.check(sp)
+            return ms
+
+        best = spec_sweep(rt, best, quick, log, timer)
+        searched += best.pop("_searched")
     rt.close()
-    best["searched"] = len(orders) * len(leaf_sizes) * len(blocks) * len(thresholds) * len(periods)
+    best["searched"] = searched
     best["seconds"] = round(time.time() - t0, 1)
     return best
 

@@ -323,7 +323,8 @@ grt_status grt_set_tuning(grt_ctx *c, const grt_tuning *t) {
     if (!c || !t) return GRT_ERR_INVALID_ARG;
     if (t->block_threads < 0 || t->block_threads % 32 || t->block_threads > 256 || t->blocks_per_sm < 0 ||
         t->refill_threshold < 0 || t->refill_threshold > 32 || t->refill_period < 0 || t->stack_entries < 0 ||
-        t->stack_entries > grt::kStackLarge)
+        t->stack_entries > grt::kStackLarge || t->spec_pend < 0 || t->spec_pend > 3 || t->spec_exit < 0 ||
+        t->spec_exit > 32 || t->spec_visits < 0 || t->spec_visits > 16)
         return fail(c, GRT_ERR_INVALID_ARG, "tuning value out of range");
     c->tuning = *t;
     return GRT_OK;

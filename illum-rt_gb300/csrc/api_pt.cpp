@@ -192,6 +192,7 @@ grt_status grt_pathtrace(grt_ctx *c, const grt_pt_params *params, const float *p
     const pt_params_dev pp = {p.max_bounces, p.rr_start, p.rr_continue, p.eps, p.seed};
     launch_params lp_trace = params_for(c, false);  // one-thread-per-ray kernel of the wavefront form
     launch_params lp = lp_trace;
+    lp.spec = tuned_spec(c->tuning, kSpecPaths);
     lp.grid_blocks = (c->tuning.blocks_per_sm > 0 ? c->tuning.blocks_per_sm
                                                   : fused_blocks_per_sm(lp.block_threads, lp.stack_entries, lp.order, scene_for(c).alpha != nullptr)) *
                      c->num_sms;
@@ -207,7 +208,8 @@ grt_status grt_pathtrace(grt_ctx *c, const grt_pt_params *params, const float *p
         fbits(p.rr_continue), fbits(p.eps), p.seed, (uint64_t)(uintptr_t)c->d_scratch, c->scene_generation,
         (uint64_t)(uintptr_t)c->d_albedo, c->n_albedo, (uint64_t)(uintptr_t)st, (uint64_t)lp.block_threads,
         (uint64_t)lp.grid_blocks, (uint64_t)lp.refill_threshold, (uint64_t)lp.refill_period,
-        (uint64_t)lp.stack_entries, (uint64_t)lp.order, (uint64_t)lp_trace.block_threads,
+        (uint64_t)lp.stack_entries, (uint64_t)lp.order, (uint64_t)lp_trace.block_threads, (uint64_t)lp.spec.pend,
+        (uint64_t)lp.spec.exit, (uint64_t)lp.spec.visits,
         (uint64_t)(uintptr_t)lp_trace.counters, (uint64_t)(uintptr_t)scene_for(c).alpha};
     if (!c->pt_graph.exec || c->pt_graph.key != key) {
         if (c->pt_graph.exec) cudaGraphExecDestroy(c->pt_graph.exec);

@@ -202,6 +202,15 @@ inline int needed_stack(const grt_ctx *c) {
     return kTracers[c->tracer].order == WIDE_SPECULATIVE ? (int)c->stack_bound4 : (int)c->depth;
 }
 
+// The speculative parameters of a persistent kernel family: its default with the tuned values
+// of grt_tuning in place of the defaults where set.
+inline spec_cfg tuned_spec(const grt_tuning &t, spec_cfg d) {
+    if (t.spec_pend > 0) d.pend = t.spec_pend;
+    if (t.spec_exit > 0) d.exit = t.spec_exit;
+    if (t.spec_visits > 0) d.visits = t.spec_visits;
+    return d;
+}
+
 inline launch_params params_for(grt_ctx *c, bool any_hit) {
     grt::launch_params lp{};
     const grt_tuning &t = c->tuning;
@@ -213,6 +222,7 @@ inline launch_params params_for(grt_ctx *c, bool any_hit) {
     lp.refill_period = t.refill_period > 0 ? t.refill_period : 4;
     lp.counters = c->d_trav_counters;
     lp.order = kTracers[c->tracer].order;
+    lp.spec = kTracers[c->tracer].persistent ? tuned_spec(t, kSpecPersistent) : kSpecTrace;
     if (kTracers[c->tracer].persistent) {
         int per_sm = t.blocks_per_sm > 0 ? t.blocks_per_sm
                                          : grt::persistent_blocks_per_sm(lp.block_threads, lp.stack_entries, any_hit,

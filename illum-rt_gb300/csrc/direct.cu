@@ -178,27 +178,30 @@ __global__ void __launch_bounds__(256) k_add_albedo(dl_scene ds, const grt_hit *
 // the frame buffer. All lanes of a warp are always in the same phase, so every loop order works,
 // the speculative ones included, and the rays of one sample stay as coherent as in the
 // wavefront form.
-template <int ORDER, int STACK, bool ANY>
+template <int ORDER, bool ANY>
 __device__ __forceinline__ void trace_all(trav_t &s, bool active, bool plain, const dev_scene &sc, const ray_t &r,
-                                          int *stk, int stride, unsigned *err) {
+                                          int *stk, int stride, int cap, unsigned *err) {
     constexpr bool SPEC = ORDER == SPECULATIVE || ORDER == WIDE_SPECULATIVE;
     constexpr bool WIDE = ORDER == WIDE_SPECULATIVE;
     while (__any_sync(kFull, active && !s.done)) {
         if (SPEC)
-            trav_spec_iter<STACK, ANY, false, WIDE, false, kPendDirect, kExitDirect>(s, active, plain, sc, r, stk, stride, err);
+            trav_spec_iter<ANY, false, WIDE, false>(s, active, plain, sc, r, stk, stride, cap,
+                                                   spec_cfg{kSpecDirect.pend, kSpecDirect.exit, kSpecDirect.visits},
+                                                   err);
         else if (active && !s.done && plain)
-            trav_advance<ORDER, STACK, ANY, false, true>(s, sc, r, stk, stride, err);
+            trav_advance<ORDER, ANY, false, true>(s, sc, r, stk, stride, cap, err);
         else if (active && !s.done)
-            trav_advance<ORDER, STACK, ANY, false, false>(s, sc, r, stk, stride, err);
+            trav_advance<ORDER, ANY, false, false>(s, sc, r, stk, stride, cap, err);
     }
 }
 
 // DIR: a direction strategy (closest-hit rays, k::integrate_dir) instead of light sampling
 // (any-hit shadow rays, k::integrate_light).
-template <int ORDER, int STACK, bool DIR>
+template <int ORDER, bool DIR>
 __global__ void __launch_bounds__(256) k_dl_fused(dev_scene sc, dl_scene ds, const float4 *__restrict__ rays,
                                                   uint32_t n, uint32_t samples, uint64_t seed, uint32_t sampling,
-                                                  uint32_t albedo, float4 *fb, unsigned *err, unsigned *counter) {
+                                                  uint32_t albedo, float4 *fb, unsigned *err, unsigned *counter,
+                                                  int cap) {
     extern __shared__ int s_stack[];
     if (stop_requested_at_entry(err)) return;  // the host asked the context to stop
     constexpr bool WIDE = ORDER == WIDE_SPECULATIVE;
@@ -219,7 +222,7 @@ __global__ void __launch_bounds__(256) k_dl_fused(dev_scene sc, dl_scene ds, con
         float4 acc = active ? fb[pix] : make_float4(0.f, 0.f, 0.f, 0.f);
         trav_init(s, sc, r, WIDE);
         bool plain = active && sc.finite && ray_is_plain(r);
-        trace_all<ORDER, STACK, false>(s, active, plain, sc, r, stk, stride, err);
+        trace_all<ORDER, false>(s, active, plain, sc, r, stk, stride, cap, err);
         const float ht = active ? s.hit.t : FLT_MAX;
         const uint32_t href = s.hit.ref;
         if (albedo && active) acc = plus4(acc, albedo_of(ds, ht, href));  // primary-wf's shading
@@ -233,7 +236,7 @@ __global__ void __launch_bounds__(256) k_dl_fused(dev_scene sc, dl_scene ds, con
             if (shoot) r = shadow_ray(p.org, p.dir, p.tmax);
             trav_init(s, sc, r, WIDE);
             plain = shoot && sc.finite && ray_is_plain(r);
-            trace_all<ORDER, STACK, !DIR>(s, shoot, plain, sc, r, stk, stride, err);
+            trace_all<ORDER, !DIR>(s, shoot, plain, sc, r, stk, stride, cap, err);
             if (active) {
                 f3 rad = {0.f, 0.f, 0.f};
                 if (shoot)
@@ -246,33 +249,22 @@ __global__ void __launch_bounds__(256) k_dl_fused(dev_scene sc, dl_scene ds, con
     }
 }
 
-template <int ORDER, int STACK, bool DIR> const void *fused_ptr() { return (const void *)k_dl_fused<ORDER, STACK, DIR>; }
-
-template <int ORDER, int STACK, bool DIR>
-cudaError_t fused_run(const dev_scene &sc, const dl_scene &ds, const float4 *rays, uint32_t n, uint32_t samples,
-                      uint64_t seed, uint32_t sampling, uint32_t albedo, float4 *fb, int bt, int num_sms,
-                      unsigned *err, unsigned *counter, cudaStream_t st) {
-    const size_t smem = (size_t)STACK * bt * sizeof(int);
-    int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dl_fused<ORDER, STACK, DIR>, bt, smem);
-    if (e != cudaSuccess) return e;
-    if (per_sm < 1) per_sm = 1;
-    e = cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
-    if (e != cudaSuccess) return e;
-    k_dl_fused<ORDER, STACK, DIR><<<per_sm * num_sms, bt, smem, st>>>(sc, ds, rays, n, samples, seed, sampling,
-                                                                       albedo, fb, err, counter);
-    return cudaGetLastError();
-}
+template <int ORDER, bool DIR> const void *fused_ptr() { return (const void *)k_dl_fused<ORDER, DIR>; }
 
 template <int ORDER, bool DIR>
 cudaError_t fused_run(const dev_scene &sc, const dl_scene &ds, const float4 *rays, uint32_t n, uint32_t samples,
                       uint64_t seed, uint32_t sampling, uint32_t albedo, float4 *fb, int stack_entries, int bt,
                       int num_sms, unsigned *err, unsigned *counter, cudaStream_t st) {
-    return stack_entries <= kStackSmall
-               ? fused_run<ORDER, kStackSmall, DIR>(sc, ds, rays, n, samples, seed, sampling, albedo, fb, bt, num_sms,
-                                                    err, counter, st)
-               : fused_run<ORDER, kStackLarge, DIR>(sc, ds, rays, n, samples, seed, sampling, albedo, fb, bt, num_sms,
-                                                    err, counter, st);
+    const size_t smem = (size_t)stack_entries * bt * sizeof(int);
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dl_fused<ORDER, DIR>, bt, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    e = cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
+    if (e != cudaSuccess) return e;
+    k_dl_fused<ORDER, DIR><<<per_sm * num_sms, bt, smem, st>>>(sc, ds, rays, n, samples, seed, sampling, albedo, fb,
+                                                                err, counter, stack_entries);
+    return cudaGetLastError();
 }
 
 }  // namespace
@@ -322,15 +314,9 @@ cudaError_t launch_dl_fused(const dev_scene &sc, const dl_scene &ds, const float
 
 cudaError_t prepare_dl_kernels() {
     const int bytes = kStackLarge * 256 * (int)sizeof(int);
-    for (const void *f :
-         {fused_ptr<IF_IF, kStackSmall, false>(), fused_ptr<IF_IF, kStackLarge, false>(),
-          fused_ptr<WHILE_WHILE, kStackSmall, false>(), fused_ptr<WHILE_WHILE, kStackLarge, false>(),
-          fused_ptr<SPECULATIVE, kStackSmall, false>(), fused_ptr<SPECULATIVE, kStackLarge, false>(),
-          fused_ptr<WIDE_SPECULATIVE, kStackSmall, false>(), fused_ptr<WIDE_SPECULATIVE, kStackLarge, false>(),
-          fused_ptr<IF_IF, kStackSmall, true>(), fused_ptr<IF_IF, kStackLarge, true>(),
-          fused_ptr<WHILE_WHILE, kStackSmall, true>(), fused_ptr<WHILE_WHILE, kStackLarge, true>(),
-          fused_ptr<SPECULATIVE, kStackSmall, true>(), fused_ptr<SPECULATIVE, kStackLarge, true>(),
-          fused_ptr<WIDE_SPECULATIVE, kStackSmall, true>(), fused_ptr<WIDE_SPECULATIVE, kStackLarge, true>()}) {
+    for (const void *f : {fused_ptr<IF_IF, false>(), fused_ptr<WHILE_WHILE, false>(), fused_ptr<SPECULATIVE, false>(),
+                          fused_ptr<WIDE_SPECULATIVE, false>(), fused_ptr<IF_IF, true>(), fused_ptr<WHILE_WHILE, true>(),
+                          fused_ptr<SPECULATIVE, true>(), fused_ptr<WIDE_SPECULATIVE, true>()}) {
         cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
         if (e != cudaSuccess) return e;
     }

@@ -57,18 +57,23 @@ __device__ __forceinline__ bool stop_requested_at_entry(unsigned *err) {
 }
 #endif
 
-// Stack variants compiled into the library (entries per thread, shared memory).
-static const int kStackSmall = 32;
+// Largest traversal stack (entries per thread, in shared memory) a launch may ask for; a
+// launch allocates exactly the entries it asks for (the tree's depth unless tuned deeper).
 static const int kStackLarge = 64;
 
-// The speculative loop order's warp-level parameters (traverse.cuh), per kernel family, as
-// measured on GB300: how many leaves a lane may postpone before the warp's leaf phase, with how
-// many lanes still searching for their first leaf the warp stops visiting nodes, and (path
-// tracer) how many node visits each lane makes between two warp votes (3 elsewhere).
-static const int kPendPaths = 2, kExitPaths = 8, kVisitsPaths = 5;  // fused path tracer
-static const int kPendDirect = 3, kExitDirect = 2;              // fused direct lighting
-static const int kPendTrace = 3, kExitTrace = 1;                // one-thread-per-ray batch traces
-static const int kPendPersistent = 2, kExitPersistent = 8;      // persistent batch traces, scene sets
+// The speculative loop order's warp-level parameters (traverse.cuh): how many leaves a lane may
+// postpone before the warp's leaf phase (1 to 3), with how many lanes still searching for their
+// first leaf the warp stops visiting nodes, and how many node visits each lane makes between two
+// warp votes. Launch arguments; the defaults per kernel family are the ones measured best on
+// GB300, and the persistent families (fused path tracer, persistent traces, scene sets) take
+// the tuned values of grt_tuning when set.
+struct spec_cfg {
+    int pend, exit, visits;
+};
+constexpr spec_cfg kSpecPaths = {2, 8, 5};       // fused path tracer
+constexpr spec_cfg kSpecDirect = {3, 2, 3};      // fused direct lighting
+constexpr spec_cfg kSpecTrace = {3, 1, 3};       // one-thread-per-ray batch traces
+constexpr spec_cfg kSpecPersistent = {2, 8, 3};  // persistent batch traces, scene sets
 
 // Upper bound on traversal steps (inner nodes + leaves) of one ray. A DFS over a tree visits
 // each node at most once per ray, so a correct BVH never reaches it; it bounds the work of a
@@ -87,7 +92,8 @@ struct launch_params {
     int grid_blocks;        // persistent kernels: total resident blocks
     int refill_threshold;
     int refill_period;
-    int stack_entries;
+    int stack_entries;             // traversal stack entries per thread (the launch's shared memory)
+    spec_cfg spec;                 // speculative order: the family default or the tuned values
     int order;                     // loop_order
     unsigned long long *counters;  // one-thread-per-ray kernel: rays, inner nodes, triangle tests (or null)
 };
@@ -105,7 +111,7 @@ cudaError_t launch_trace_persistent(const dev_scene &sc, const float4 *rays, grt
 // before any launch, so that launches need no attribute calls and can be captured).
 cudaError_t prepare_trace_kernels();
 
-// Occupancy of the persistent kernel for a block size and stack variant (blocks per SM).
+// Occupancy of the persistent kernel for a block size and stack size (blocks per SM).
 int persistent_blocks_per_sm(int block_threads, int stack_entries, bool any_hit, int order, bool alpha);
 
 }  // namespace grt

@@ -28,11 +28,12 @@ __device__ __forceinline__ uint32_t find_batch(const multi_batch *__restrict__ b
     return lo;
 }
 
-template <int ORDER, int STACK, bool ANY>
+template <int ORDER, bool ANY>
 __global__ void __launch_bounds__(256) k_trace_multi(const dev_scene *__restrict__ scenes,
                                                      const multi_batch *__restrict__ batches, uint32_t nbatch,
                                                      uint32_t total, unsigned *err, unsigned *counter,
-                                                     int refill_threshold, int refill_period) {
+                                                     int refill_threshold, int refill_period, int cap,
+                                                     spec_cfg spec) {
     extern __shared__ int s_stack[];
     if (stop_requested_at_entry(err)) return;  // the host asked the context to stop
     constexpr bool SPEC = ORDER == SPECULATIVE || ORDER == WIDE_SPECULATIVE;
@@ -82,11 +83,11 @@ __global__ void __launch_bounds__(256) k_trace_multi(const dev_scene *__restrict
         }
         for (int it = 1;; ++it) {
             if (SPEC)
-                trav_spec_iter<STACK, ANY, false, WIDE, false, kPendPersistent, kExitPersistent>(s, have, plain, sc, r, stk, stride, err);
+                trav_spec_iter<ANY, false, WIDE, false>(s, have, plain, sc, r, stk, stride, cap, spec, err);
             else if (have && plain)
-                trav_advance<ORDER, STACK, ANY, false, true>(s, sc, r, stk, stride, err);
+                trav_advance<ORDER, ANY, false, true>(s, sc, r, stk, stride, cap, err);
             else if (have)
-                trav_advance<ORDER, STACK, ANY, false, false>(s, sc, r, stk, stride, err);
+                trav_advance<ORDER, ANY, false, false>(s, sc, r, stk, stride, cap, err);
             if (have && s.done) {
                 store_hit<ANY>(hits, idx, s);
                 have = false;
@@ -99,38 +100,28 @@ __global__ void __launch_bounds__(256) k_trace_multi(const dev_scene *__restrict
     }
 }
 
-template <int ORDER, int STACK, bool ANY>
+template <int ORDER, bool ANY>
 cudaError_t multi_launch(const dev_scene *scenes, const multi_batch *batches, uint32_t nbatch, uint32_t total,
                          const launch_params &lp, unsigned *err, unsigned *counter, cudaStream_t st) {
-    const size_t smem = (size_t)STACK * lp.block_threads * sizeof(int);
+    const size_t smem = (size_t)lp.stack_entries * lp.block_threads * sizeof(int);
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
-    k_trace_multi<ORDER, STACK, ANY><<<lp.grid_blocks, lp.block_threads, smem, st>>>(
-        scenes, batches, nbatch, total, err, counter, lp.refill_threshold, lp.refill_period);
+    k_trace_multi<ORDER, ANY><<<lp.grid_blocks, lp.block_threads, smem, st>>>(
+        scenes, batches, nbatch, total, err, counter, lp.refill_threshold, lp.refill_period, lp.stack_entries, lp.spec);
     return cudaGetLastError();
 }
 
-template <int ORDER, int STACK>
+template <int ORDER>
 cudaError_t multi_any(bool any_hit, const dev_scene *scenes, const multi_batch *batches, uint32_t nbatch,
                       uint32_t total, const launch_params &lp, unsigned *err, unsigned *counter, cudaStream_t st) {
-    return any_hit ? multi_launch<ORDER, STACK, true>(scenes, batches, nbatch, total, lp, err, counter, st)
-                   : multi_launch<ORDER, STACK, false>(scenes, batches, nbatch, total, lp, err, counter, st);
-}
-
-template <int ORDER>
-cudaError_t multi_stack(bool any_hit, const dev_scene *scenes, const multi_batch *batches, uint32_t nbatch,
-                        uint32_t total, const launch_params &lp, unsigned *err, unsigned *counter, cudaStream_t st) {
-    return lp.stack_entries <= kStackSmall
-               ? multi_any<ORDER, kStackSmall>(any_hit, scenes, batches, nbatch, total, lp, err, counter, st)
-               : multi_any<ORDER, kStackLarge>(any_hit, scenes, batches, nbatch, total, lp, err, counter, st);
+    return any_hit ? multi_launch<ORDER, true>(scenes, batches, nbatch, total, lp, err, counter, st)
+                   : multi_launch<ORDER, false>(scenes, batches, nbatch, total, lp, err, counter, st);
 }
 
 template <int ORDER> cudaError_t attrs(int bytes) {
     const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
-    cudaError_t e = cudaFuncSetAttribute(k_trace_multi<ORDER, kStackSmall, false>, a, bytes);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_multi<ORDER, kStackSmall, true>, a, bytes);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_multi<ORDER, kStackLarge, false>, a, bytes);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_multi<ORDER, kStackLarge, true>, a, bytes);
+    cudaError_t e = cudaFuncSetAttribute(k_trace_multi<ORDER, false>, a, bytes);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_multi<ORDER, true>, a, bytes);
     return e;
 }
 
@@ -141,11 +132,11 @@ cudaError_t launch_trace_multi(const dev_scene *scenes, const multi_batch *batch
                                cudaStream_t st) {
     if (total == 0) return cudaSuccess;
     switch (lp.order) {
-        case WHILE_WHILE: return multi_stack<WHILE_WHILE>(any_hit, scenes, batches, nbatch, total, lp, err, counter, st);
-        case SPECULATIVE: return multi_stack<SPECULATIVE>(any_hit, scenes, batches, nbatch, total, lp, err, counter, st);
+        case WHILE_WHILE: return multi_any<WHILE_WHILE>(any_hit, scenes, batches, nbatch, total, lp, err, counter, st);
+        case SPECULATIVE: return multi_any<SPECULATIVE>(any_hit, scenes, batches, nbatch, total, lp, err, counter, st);
         case WIDE_SPECULATIVE:
-            return multi_stack<WIDE_SPECULATIVE>(any_hit, scenes, batches, nbatch, total, lp, err, counter, st);
-        default: return multi_stack<IF_IF>(any_hit, scenes, batches, nbatch, total, lp, err, counter, st);
+            return multi_any<WIDE_SPECULATIVE>(any_hit, scenes, batches, nbatch, total, lp, err, counter, st);
+        default: return multi_any<IF_IF>(any_hit, scenes, batches, nbatch, total, lp, err, counter, st);
     }
 }
 
@@ -160,26 +151,11 @@ cudaError_t prepare_multi_kernels() {
 
 int multi_blocks_per_sm(int block_threads, int stack_entries, int order) {
     int blocks = 0;
-    const bool small = stack_entries <= kStackSmall;
-    const size_t smem = (size_t)(small ? kStackSmall : kStackLarge) * block_threads * sizeof(int);
-    const void *fn = nullptr;
-    switch (order) {
-        case WHILE_WHILE:
-            fn = small ? (const void *)k_trace_multi<WHILE_WHILE, kStackSmall, false>
-                       : (const void *)k_trace_multi<WHILE_WHILE, kStackLarge, false>;
-            break;
-        case SPECULATIVE:
-            fn = small ? (const void *)k_trace_multi<SPECULATIVE, kStackSmall, false>
-                       : (const void *)k_trace_multi<SPECULATIVE, kStackLarge, false>;
-            break;
-        case WIDE_SPECULATIVE:
-            fn = small ? (const void *)k_trace_multi<WIDE_SPECULATIVE, kStackSmall, false>
-                       : (const void *)k_trace_multi<WIDE_SPECULATIVE, kStackLarge, false>;
-            break;
-        default:
-            fn = small ? (const void *)k_trace_multi<IF_IF, kStackSmall, false>
-                       : (const void *)k_trace_multi<IF_IF, kStackLarge, false>;
-    }
+    const size_t smem = (size_t)stack_entries * block_threads * sizeof(int);
+    const void *fn = order == WHILE_WHILE        ? (const void *)k_trace_multi<WHILE_WHILE, false>
+                     : order == SPECULATIVE      ? (const void *)k_trace_multi<SPECULATIVE, false>
+                     : order == WIDE_SPECULATIVE ? (const void *)k_trace_multi<WIDE_SPECULATIVE, false>
+                                                 : (const void *)k_trace_multi<IF_IF, false>;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, block_threads, smem) != cudaSuccess) return 1;
     return blocks > 0 ? blocks : 1;
 }

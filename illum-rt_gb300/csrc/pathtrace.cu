@@ -383,21 +383,22 @@ __global__ void k_wf_shade(pt_scene ps, pt_params_dev pp, const uint32_t *__rest
 // lanes shade their hit together (Russian roulette, next bounce direction) and go back to
 // traversal, or finish their path and take a new one from the global path counter. Shading and
 // path set-up therefore run warp-coherently instead of one lane at a time.
-template <int ORDER, int STACK, bool ALPHA>
+template <int ORDER, bool ALPHA>
 __global__ void __launch_bounds__(256) k_pt_fused(dev_scene sc, pt_scene ps, pt_params_dev pp,
                                                   const float4 *__restrict__ prim_rays,
                                                   const grt_hit *__restrict__ prim_hits,
                                                   const uint32_t *__restrict__ hit_list,
                                                   const uint32_t *__restrict__ n_list, uint32_t n_paths,
                                                   grt_path_result *results, grt_hit *bounce_hits, unsigned *err,
-                                                  unsigned *counter, int refill_threshold, int refill_period) {
+                                                  unsigned *counter, int refill_threshold, int refill_period, int cap,
+                                                  spec_cfg spec) {
     extern __shared__ int s_stack[];
     if (stop_requested_at_entry(err)) return;  // the host asked the context to stop
     const unsigned lane = threadIdx.x & 31u;
     const unsigned lanes_below = (1u << lane) - 1u;
     int *stk = s_stack + threadIdx.x;
     const int stride = blockDim.x;
-    const path_slots slots = path_slots_at(s_stack, STACK);
+    const path_slots slots = path_slots_at(s_stack, cap);
     constexpr bool SPEC = ORDER == SPECULATIVE || ORDER == WIDE_SPECULATIVE;
     constexpr bool WIDE = ORDER == WIDE_SPECULATIVE;
     const int me = threadIdx.x;
@@ -463,11 +464,11 @@ __global__ void __launch_bounds__(256) k_pt_fused(dev_scene sc, pt_scene ps, pt_
         // traversal phase
         for (int it = 1;; ++it) {
             if (SPEC)
-                trav_spec_iter<STACK, false, false, WIDE, ALPHA, kPendPaths, kExitPaths, kVisitsPaths>(s, tracing, plain, sc, r, stk, stride, err);
+                trav_spec_iter<false, false, WIDE, ALPHA>(s, tracing, plain, sc, r, stk, stride, cap, spec, err);
             else if (tracing && plain)
-                trav_advance<ORDER, STACK, false, false, true, ALPHA>(s, sc, r, stk, stride, err);
+                trav_advance<ORDER, false, false, true, ALPHA>(s, sc, r, stk, stride, cap, err);
             else if (tracing)
-                trav_advance<ORDER, STACK, false, false, false, ALPHA>(s, sc, r, stk, stride, err);
+                trav_advance<ORDER, false, false, false, ALPHA>(s, sc, r, stk, stride, cap, err);
             if (tracing && s.done) {
                 tracing = false;
                 waiting = true;
@@ -480,18 +481,18 @@ __global__ void __launch_bounds__(256) k_pt_fused(dev_scene sc, pt_scene ps, pt_
     }
 }
 
-template <int ORDER, int STACK>
+template <int ORDER>
 cudaError_t fused_launch(const dev_scene &sc, const pt_scene &ps, const pt_params_dev &pp, const float4 *prim_rays,
                          const grt_hit *prim_hits, const uint32_t *hit_list, const uint32_t *n_list, uint32_t n_paths,
                          grt_path_result *results, grt_hit *bounce_hits, const launch_params &lp, unsigned *err,
                          unsigned *counter, cudaStream_t st) {
-    const size_t smem = (size_t)(STACK * sizeof(int) + kPathSlotBytes) * lp.block_threads;
-    auto kern = sc.alpha ? k_pt_fused<ORDER, STACK, true> : k_pt_fused<ORDER, STACK, false>;
+    const size_t smem = (size_t)(lp.stack_entries * sizeof(int) + kPathSlotBytes) * lp.block_threads;
+    auto kern = sc.alpha ? k_pt_fused<ORDER, true> : k_pt_fused<ORDER, false>;
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
     kern<<<lp.grid_blocks, lp.block_threads, smem, st>>>(sc, ps, pp, prim_rays, prim_hits, hit_list, n_list, n_paths,
                                                          results, bounce_hits, err, counter, lp.refill_threshold,
-                                                         lp.refill_period);
+                                                         lp.refill_period, lp.stack_entries, lp.spec);
     return cudaGetLastError();
 }
 
@@ -547,55 +548,34 @@ cudaError_t launch_fused(const dev_scene &sc, const pt_scene &ps, const pt_param
                          grt_path_result *results, grt_hit *bounce_hits, const launch_params &lp, unsigned *err,
                          unsigned *counter, cudaStream_t st) {
     if (n_paths == 0) return cudaSuccess;
-    const bool small = lp.stack_entries <= kStackSmall;
-    auto f = lp.order == WHILE_WHILE
-                 ? (small ? fused_launch<WHILE_WHILE, kStackSmall> : fused_launch<WHILE_WHILE, kStackLarge>)
-             : lp.order == SPECULATIVE
-                 ? (small ? fused_launch<SPECULATIVE, kStackSmall> : fused_launch<SPECULATIVE, kStackLarge>)
-             : lp.order == WIDE_SPECULATIVE
-                 ? (small ? fused_launch<WIDE_SPECULATIVE, kStackSmall> : fused_launch<WIDE_SPECULATIVE, kStackLarge>)
-                 : (small ? fused_launch<IF_IF, kStackSmall> : fused_launch<IF_IF, kStackLarge>);
+    auto f = lp.order == WHILE_WHILE        ? fused_launch<WHILE_WHILE>
+             : lp.order == SPECULATIVE      ? fused_launch<SPECULATIVE>
+             : lp.order == WIDE_SPECULATIVE ? fused_launch<WIDE_SPECULATIVE>
+                                            : fused_launch<IF_IF>;
     return f(sc, ps, pp, prim_rays, prim_hits, hit_list, n_list, n_paths, results, bounce_hits, lp, err, counter, st);
+}
+
+template <bool ALPHA> const void *fused_fn(int order) {
+    return order == WHILE_WHILE        ? (const void *)k_pt_fused<WHILE_WHILE, ALPHA>
+           : order == SPECULATIVE      ? (const void *)k_pt_fused<SPECULATIVE, ALPHA>
+           : order == WIDE_SPECULATIVE ? (const void *)k_pt_fused<WIDE_SPECULATIVE, ALPHA>
+                                       : (const void *)k_pt_fused<IF_IF, ALPHA>;
 }
 
 cudaError_t prepare_pt_kernels() {
     const int bytes = (kStackLarge * (int)sizeof(int) + kPathSlotBytes) * 256;
-    for (const void *f : {(const void *)k_pt_fused<IF_IF, kStackSmall, false>, (const void *)k_pt_fused<IF_IF, kStackLarge, false>,
-                          (const void *)k_pt_fused<WHILE_WHILE, kStackSmall, false>,
-                          (const void *)k_pt_fused<WHILE_WHILE, kStackLarge, false>,
-                          (const void *)k_pt_fused<SPECULATIVE, kStackSmall, false>,
-                          (const void *)k_pt_fused<SPECULATIVE, kStackLarge, false>,
-                          (const void *)k_pt_fused<WIDE_SPECULATIVE, kStackSmall, false>,
-                          (const void *)k_pt_fused<WIDE_SPECULATIVE, kStackLarge, false>,
-                          (const void *)k_pt_fused<IF_IF, kStackSmall, true>, (const void *)k_pt_fused<IF_IF, kStackLarge, true>,
-                          (const void *)k_pt_fused<WHILE_WHILE, kStackSmall, true>,
-                          (const void *)k_pt_fused<WHILE_WHILE, kStackLarge, true>,
-                          (const void *)k_pt_fused<SPECULATIVE, kStackSmall, true>,
-                          (const void *)k_pt_fused<SPECULATIVE, kStackLarge, true>,
-                          (const void *)k_pt_fused<WIDE_SPECULATIVE, kStackSmall, true>,
-                          (const void *)k_pt_fused<WIDE_SPECULATIVE, kStackLarge, true>}) {
-        cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-        if (e != cudaSuccess) return e;
-    }
+    for (int order : {(int)IF_IF, (int)WHILE_WHILE, (int)SPECULATIVE, (int)WIDE_SPECULATIVE})
+        for (const void *f : {fused_fn<false>(order), fused_fn<true>(order)}) {
+            cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+            if (e != cudaSuccess) return e;
+        }
     return cudaSuccess;
-}
-
-template <bool ALPHA> const void *fused_fn(int order, bool small) {
-    return order == WHILE_WHILE      ? (small ? (const void *)k_pt_fused<WHILE_WHILE, kStackSmall, ALPHA>
-                                              : (const void *)k_pt_fused<WHILE_WHILE, kStackLarge, ALPHA>)
-           : order == SPECULATIVE      ? (small ? (const void *)k_pt_fused<SPECULATIVE, kStackSmall, ALPHA>
-                                                : (const void *)k_pt_fused<SPECULATIVE, kStackLarge, ALPHA>)
-           : order == WIDE_SPECULATIVE ? (small ? (const void *)k_pt_fused<WIDE_SPECULATIVE, kStackSmall, ALPHA>
-                                                : (const void *)k_pt_fused<WIDE_SPECULATIVE, kStackLarge, ALPHA>)
-                                       : (small ? (const void *)k_pt_fused<IF_IF, kStackSmall, ALPHA>
-                                                : (const void *)k_pt_fused<IF_IF, kStackLarge, ALPHA>);
 }
 
 int fused_blocks_per_sm(int block_threads, int stack_entries, int order, bool alpha) {
     int blocks = 0;
-    const bool small = stack_entries <= kStackSmall;
-    const size_t smem = (size_t)((small ? kStackSmall : kStackLarge) * sizeof(int) + kPathSlotBytes) * block_threads;
-    const void *fn = alpha ? fused_fn<true>(order, small) : fused_fn<false>(order, small);
+    const size_t smem = (size_t)(stack_entries * sizeof(int) + kPathSlotBytes) * block_threads;
+    const void *fn = alpha ? fused_fn<true>(order) : fused_fn<false>(order);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, block_threads, smem) != cudaSuccess) return 1;
     return blocks > 0 ? blocks : 1;
 }

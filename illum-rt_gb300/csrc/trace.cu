@@ -30,10 +30,11 @@ constexpr int plain_min_blocks() {
     return ORDER == IF_IF ? 5 : ORDER == WIDE_SPECULATIVE ? 1 : 4;
 }
 
-template <int ORDER, int STACK, bool ANY, bool COUNT, bool ALPHA>
+template <int ORDER, bool ANY, bool COUNT, bool ALPHA>
 __global__ void __launch_bounds__(256, plain_min_blocks<ORDER>()) k_trace_plain(const float4 *__restrict__ rays, grt_hit *__restrict__ hits,
                                                      uint32_t n, const uint32_t *__restrict__ n_dev, dev_scene sc,
-                                                     unsigned *err, unsigned long long *counters) {
+                                                     unsigned *err, unsigned long long *counters, int cap,
+                                                     spec_cfg spec) {
     extern __shared__ int s_stack[];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (n_dev) n = *n_dev;  // ray count produced on the device (wavefront queues)
@@ -50,12 +51,12 @@ __global__ void __launch_bounds__(256, plain_min_blocks<ORDER>()) k_trace_plain(
     const bool plain = active && sc.finite && ray_is_plain(r);
     if (SPEC) {  // the whole warp stays in the loop until its last ray ends
         while (__any_sync(kFull, active && !s.done))
-            trav_spec_iter<STACK, ANY, COUNT, WIDE, ALPHA, kPendTrace, kExitTrace>(s, active, plain, sc, r, stk, stride, err);
+            trav_spec_iter<ANY, COUNT, WIDE, ALPHA>(s, active, plain, sc, r, stk, stride, cap, spec, err);
         if (!active) return;
     } else if (plain) {  // one loop per slab variant: the choice is made once per ray
-        while (!s.done) trav_advance<ORDER, STACK, ANY, COUNT, true, ALPHA>(s, sc, r, stk, stride, err);
+        while (!s.done) trav_advance<ORDER, ANY, COUNT, true, ALPHA>(s, sc, r, stk, stride, cap, err);
     } else {
-        while (!s.done) trav_advance<ORDER, STACK, ANY, COUNT, false, ALPHA>(s, sc, r, stk, stride, err);
+        while (!s.done) trav_advance<ORDER, ANY, COUNT, false, ALPHA>(s, sc, r, stk, stride, cap, err);
     }
     store_hit<ANY>(hits, i, s);
     if (COUNT) {
@@ -65,10 +66,11 @@ __global__ void __launch_bounds__(256, plain_min_blocks<ORDER>()) k_trace_plain(
     }
 }
 
-template <int ORDER, int STACK, bool ANY, bool ALPHA>
+template <int ORDER, bool ANY, bool ALPHA>
 __global__ void __launch_bounds__(256) k_trace_persistent(const float4 *__restrict__ rays, grt_hit *__restrict__ hits,
                                                           uint32_t n, dev_scene sc, unsigned *err,
-                                                          unsigned *counter, int refill_threshold, int refill_period) {
+                                                          unsigned *counter, int refill_threshold, int refill_period,
+                                                          int cap, spec_cfg spec) {
     extern __shared__ int s_stack[];
     if (stop_requested_at_entry(err)) return;  // the host asked the context to stop
     constexpr bool SPEC = ORDER == SPECULATIVE || ORDER == WIDE_SPECULATIVE;
@@ -114,11 +116,11 @@ __global__ void __launch_bounds__(256) k_trace_persistent(const float4 *__restri
         // traverse; every `refill_period` iterations the warp counts its busy lanes
         for (int it = 1;; ++it) {
             if (SPEC)
-                trav_spec_iter<STACK, ANY, false, WIDE, ALPHA, kPendPersistent, kExitPersistent>(s, have, plain, sc, r, stk, stride, err);
+                trav_spec_iter<ANY, false, WIDE, ALPHA>(s, have, plain, sc, r, stk, stride, cap, spec, err);
             else if (have && plain)
-                trav_advance<ORDER, STACK, ANY, false, true, ALPHA>(s, sc, r, stk, stride, err);
+                trav_advance<ORDER, ANY, false, true, ALPHA>(s, sc, r, stk, stride, cap, err);
             else if (have)
-                trav_advance<ORDER, STACK, ANY, false, false, ALPHA>(s, sc, r, stk, stride, err);
+                trav_advance<ORDER, ANY, false, false, ALPHA>(s, sc, r, stk, stride, cap, err);
             if (have && s.done) {
                 store_hit<ANY>(hits, idx, s);
                 have = false;
@@ -131,90 +133,78 @@ __global__ void __launch_bounds__(256) k_trace_persistent(const float4 *__restri
     }
 }
 
-template <int ORDER, int STACK, bool ANY>
+template <int ORDER, bool ANY>
 cudaError_t plain_launch(const dev_scene &sc, const float4 *rays, grt_hit *hits, uint32_t n, const uint32_t *n_dev,
                          const launch_params &lp, unsigned *err, cudaStream_t st) {
     const int bt = lp.block_threads;
-    const size_t smem = (size_t)STACK * bt * sizeof(int);
-    const uint32_t blocks = (n + bt - 1) / bt;
-    // the alpha-aware instances only when the scene carries texture data (the test costs
-    // registers even when it never runs)
+    const unsigned blocks = (n + bt - 1) / bt;
+    const size_t smem = (size_t)lp.stack_entries * bt * sizeof(int);
+    const int cap = lp.stack_entries;
     if (lp.counters && sc.alpha)
-        k_trace_plain<ORDER, STACK, ANY, true, true><<<blocks, bt, smem, st>>>(rays, hits, n, n_dev, sc, err, lp.counters);
+        k_trace_plain<ORDER, ANY, true, true><<<blocks, bt, smem, st>>>(rays, hits, n, n_dev, sc, err, lp.counters, cap,
+                                                                        lp.spec);
     else if (lp.counters)
-        k_trace_plain<ORDER, STACK, ANY, true, false><<<blocks, bt, smem, st>>>(rays, hits, n, n_dev, sc, err, lp.counters);
+        k_trace_plain<ORDER, ANY, true, false><<<blocks, bt, smem, st>>>(rays, hits, n, n_dev, sc, err, lp.counters, cap,
+                                                                         lp.spec);
     else if (sc.alpha)
-        k_trace_plain<ORDER, STACK, ANY, false, true><<<blocks, bt, smem, st>>>(rays, hits, n, n_dev, sc, err, nullptr);
+        k_trace_plain<ORDER, ANY, false, true><<<blocks, bt, smem, st>>>(rays, hits, n, n_dev, sc, err, nullptr, cap,
+                                                                         lp.spec);
     else
-        k_trace_plain<ORDER, STACK, ANY, false, false><<<blocks, bt, smem, st>>>(rays, hits, n, n_dev, sc, err, nullptr);
+        k_trace_plain<ORDER, ANY, false, false><<<blocks, bt, smem, st>>>(rays, hits, n, n_dev, sc, err, nullptr, cap,
+                                                                          lp.spec);
     return cudaGetLastError();
 }
 
-template <int ORDER, int STACK, bool ANY>
+template <int ORDER, bool ANY>
 cudaError_t persistent_launch(const dev_scene &sc, const float4 *rays, grt_hit *hits, uint32_t n,
                               const launch_params &lp, unsigned *err, unsigned *counter, cudaStream_t st) {
     const int bt = lp.block_threads;
-    const size_t smem = (size_t)STACK * bt * sizeof(int);
+    const size_t smem = (size_t)lp.stack_entries * bt * sizeof(int);
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
     if (sc.alpha)
-        k_trace_persistent<ORDER, STACK, ANY, true><<<lp.grid_blocks, bt, smem, st>>>(
-            rays, hits, n, sc, err, counter, lp.refill_threshold, lp.refill_period);
+        k_trace_persistent<ORDER, ANY, true><<<lp.grid_blocks, bt, smem, st>>>(
+            rays, hits, n, sc, err, counter, lp.refill_threshold, lp.refill_period, lp.stack_entries, lp.spec);
     else
-        k_trace_persistent<ORDER, STACK, ANY, false><<<lp.grid_blocks, bt, smem, st>>>(
-            rays, hits, n, sc, err, counter, lp.refill_threshold, lp.refill_period);
+        k_trace_persistent<ORDER, ANY, false><<<lp.grid_blocks, bt, smem, st>>>(
+            rays, hits, n, sc, err, counter, lp.refill_threshold, lp.refill_period, lp.stack_entries, lp.spec);
     return cudaGetLastError();
 }
 
-// Dispatch of the runtime choices (loop order, stack variant, any-hit) to template instances.
-template <template <int, int, bool> class F, typename... A>
-cudaError_t dispatch(int order, int stack_entries, bool any_hit, A &&...a) {
-    const bool small = stack_entries <= kStackSmall;
-    if (order == WIDE_SPECULATIVE) {
-        if (small)
-            return any_hit ? F<WIDE_SPECULATIVE, kStackSmall, true>::run(a...)
-                           : F<WIDE_SPECULATIVE, kStackSmall, false>::run(a...);
-        return any_hit ? F<WIDE_SPECULATIVE, kStackLarge, true>::run(a...)
-                       : F<WIDE_SPECULATIVE, kStackLarge, false>::run(a...);
-    }
-    if (order == SPECULATIVE) {
-        if (small)
-            return any_hit ? F<SPECULATIVE, kStackSmall, true>::run(a...) : F<SPECULATIVE, kStackSmall, false>::run(a...);
-        return any_hit ? F<SPECULATIVE, kStackLarge, true>::run(a...) : F<SPECULATIVE, kStackLarge, false>::run(a...);
-    }
-    if (order == WHILE_WHILE) {
-        if (small)
-            return any_hit ? F<WHILE_WHILE, kStackSmall, true>::run(a...) : F<WHILE_WHILE, kStackSmall, false>::run(a...);
-        return any_hit ? F<WHILE_WHILE, kStackLarge, true>::run(a...) : F<WHILE_WHILE, kStackLarge, false>::run(a...);
-    }
-    if (small) return any_hit ? F<IF_IF, kStackSmall, true>::run(a...) : F<IF_IF, kStackSmall, false>::run(a...);
-    return any_hit ? F<IF_IF, kStackLarge, true>::run(a...) : F<IF_IF, kStackLarge, false>::run(a...);
+// Dispatch of the runtime choices (loop order, any-hit) to template instances.
+template <template <int, bool> class F, typename... A>
+cudaError_t dispatch(int order, bool any_hit, A &&...a) {
+    if (order == WIDE_SPECULATIVE)
+        return any_hit ? F<WIDE_SPECULATIVE, true>::run(a...) : F<WIDE_SPECULATIVE, false>::run(a...);
+    if (order == SPECULATIVE) return any_hit ? F<SPECULATIVE, true>::run(a...) : F<SPECULATIVE, false>::run(a...);
+    if (order == WHILE_WHILE) return any_hit ? F<WHILE_WHILE, true>::run(a...) : F<WHILE_WHILE, false>::run(a...);
+    return any_hit ? F<IF_IF, true>::run(a...) : F<IF_IF, false>::run(a...);
 }
 
-template <int O, int S, bool A> struct plain_f {
-    template <typename... X> static cudaError_t run(X &&...x) { return plain_launch<O, S, A>(x...); }
+template <int O, bool A> struct plain_f {
+    template <typename... X> static cudaError_t run(X &&...x) { return plain_launch<O, A>(x...); }
 };
-template <int O, int S, bool A> struct persistent_f {
-    template <typename... X> static cudaError_t run(X &&...x) { return persistent_launch<O, S, A>(x...); }
+template <int O, bool A> struct persistent_f {
+    template <typename... X> static cudaError_t run(X &&...x) { return persistent_launch<O, A>(x...); }
 };
-template <int O, int S, bool A> struct attr_f {
+template <int O, bool A> struct attr_f {
     static cudaError_t run(int bytes) {
         const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
-        cudaError_t e = cudaFuncSetAttribute(k_trace_plain<O, S, A, false, false>, a, bytes);
-        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_plain<O, S, A, true, false>, a, bytes);
-        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_plain<O, S, A, false, true>, a, bytes);
-        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_plain<O, S, A, true, true>, a, bytes);
-        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_persistent<O, S, A, false>, a, bytes);
-        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_persistent<O, S, A, true>, a, bytes);
+        cudaError_t e = cudaFuncSetAttribute(k_trace_plain<O, A, false, false>, a, bytes);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_plain<O, A, true, false>, a, bytes);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_plain<O, A, false, true>, a, bytes);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_plain<O, A, true, true>, a, bytes);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_persistent<O, A, false>, a, bytes);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_persistent<O, A, true>, a, bytes);
         return e;
     }
 };
-template <int O, int S, bool A> struct occupancy_f {
-    static cudaError_t run(int block_threads, bool alpha, int *blocks) {
-        const size_t smem = (size_t)S * block_threads * sizeof(int);
-        return alpha ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_trace_persistent<O, S, A, true>,
+template <int O, bool A> struct occupancy_f {
+    static cudaError_t run(int block_threads, int stack_entries, bool alpha, int *blocks) {
+        const size_t smem = (size_t)stack_entries * block_threads * sizeof(int);
+        return alpha ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_trace_persistent<O, A, true>,
                                                                      block_threads, smem)
-                     : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_trace_persistent<O, S, A, false>,
+                     : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_trace_persistent<O, A, false>,
                                                                      block_threads, smem);
     }
 };
@@ -224,29 +214,28 @@ template <int O, int S, bool A> struct occupancy_f {
 cudaError_t launch_trace_plain(const dev_scene &sc, const float4 *rays, grt_hit *hits, uint32_t n, bool any_hit,
                                const launch_params &lp, unsigned *err, cudaStream_t stream, const uint32_t *n_dev) {
     if (n == 0) return cudaSuccess;
-    return dispatch<plain_f>(lp.order, lp.stack_entries, any_hit, sc, rays, hits, n, n_dev, lp, err, stream);
+    return dispatch<plain_f>(lp.order, any_hit, sc, rays, hits, n, n_dev, lp, err, stream);
 }
 
 cudaError_t launch_trace_persistent(const dev_scene &sc, const float4 *rays, grt_hit *hits, uint32_t n, bool any_hit,
                                     const launch_params &lp, unsigned *err, unsigned *counter, cudaStream_t stream) {
     if (n == 0) return cudaSuccess;
-    return dispatch<persistent_f>(lp.order, lp.stack_entries, any_hit, sc, rays, hits, n, lp, err, counter, stream);
+    return dispatch<persistent_f>(lp.order, any_hit, sc, rays, hits, n, lp, err, counter, stream);
 }
 
 cudaError_t prepare_trace_kernels() {
-    const int bytes = kStackLarge * 256 * (int)sizeof(int);  // largest stack variant at 256 threads
+    const int bytes = kStackLarge * 256 * (int)sizeof(int);  // largest stack at 256 threads
     for (int order : {(int)IF_IF, (int)WHILE_WHILE, (int)SPECULATIVE, (int)WIDE_SPECULATIVE})
-        for (int stack : {kStackSmall, kStackLarge})
-            for (bool any : {false, true}) {
-                cudaError_t e = dispatch<attr_f>(order, stack, any, bytes);
-                if (e != cudaSuccess) return e;
-            }
+        for (bool any : {false, true}) {
+            cudaError_t e = dispatch<attr_f>(order, any, bytes);
+            if (e != cudaSuccess) return e;
+        }
     return cudaSuccess;
 }
 
 int persistent_blocks_per_sm(int block_threads, int stack_entries, bool any_hit, int order, bool alpha) {
     int blocks = 0;
-    if (dispatch<occupancy_f>(order, stack_entries, any_hit, block_threads, alpha, &blocks) != cudaSuccess) return 1;
+    if (dispatch<occupancy_f>(order, any_hit, block_threads, stack_entries, alpha, &blocks) != cudaSuccess) return 1;
     return blocks > 0 ? blocks : 1;
 }
 

@@ -326,8 +326,8 @@ __device__ __forceinline__ void node_test(const float4 *np, const trav_t &s, con
 // `cur` instead of being pushed and popped straight back, and a leaf is tested when it would
 // be popped. Grouping a warp's node visits in one loop and its leaf tests after it keeps the
 // lanes on the same code path far more often than one node-or-leaf per iteration would.
-template <int STACK, bool ANY, bool PLAIN, bool COUNT = false, bool ALPHA = false>
-__device__ __forceinline__ void trav_iter(trav_t &s, const dev_scene &sc, const ray_t &r, int *stk, int stride,
+template <bool ANY, bool PLAIN, bool COUNT = false, bool ALPHA = false>
+__device__ __forceinline__ void trav_iter(trav_t &s, const dev_scene &sc, const ray_t &r, int *stk, int stride, int cap,
                                           unsigned *err) {
     while (s.cur >= 0) {
         if (++s.steps > kStepLimit) {
@@ -342,7 +342,7 @@ __device__ __forceinline__ void trav_iter(trav_t &s, const dev_scene &sc, const 
         node_test<ANY, PLAIN>(sc.nodes + 4 * (size_t)s.cur, s, r, hl, hr, dl, dr, cl, cr);
         if (hl && hr) {
             const bool left_first = dl < dr;
-            if (s.sp >= STACK) {
+            if (s.sp >= cap) {
                 atomicOr(err, ERR_STACK_OVERFLOW);
                 s.done = true;
                 return;
@@ -399,8 +399,8 @@ __device__ __forceinline__ void trav_iter(trav_t &s, const dev_scene &sc, const 
 // The if-if order: one inner node or one leaf per call (the reference's if-if tracer,
 // rt/cuda/trace-kernels.cu:1058-1149, visits in the same per-ray order as while-while). Lanes of
 // a warp at nodes and lanes at leaves take different branches in the same call.
-template <int STACK, bool ANY, bool PLAIN, bool COUNT = false, bool ALPHA = false>
-__device__ __forceinline__ void trav_step(trav_t &s, const dev_scene &sc, const ray_t &r, int *stk, int stride,
+template <bool ANY, bool PLAIN, bool COUNT = false, bool ALPHA = false>
+__device__ __forceinline__ void trav_step(trav_t &s, const dev_scene &sc, const ray_t &r, int *stk, int stride, int cap,
                                           unsigned *err) {
     if (++s.steps > kStepLimit) {
         atomicOr(err, ERR_STEP_LIMIT);
@@ -415,7 +415,7 @@ __device__ __forceinline__ void trav_step(trav_t &s, const dev_scene &sc, const 
         node_test<ANY, PLAIN>(sc.nodes + 4 * (size_t)s.cur, s, r, hl, hr, dl, dr, cl, cr);
         if (hl && hr) {
             const bool left_first = dl < dr;
-            if (s.sp >= STACK) {
+            if (s.sp >= cap) {
                 atomicOr(err, ERR_STACK_OVERFLOW);
                 s.done = true;
                 return;
@@ -463,8 +463,8 @@ __device__ __forceinline__ void trav_step(trav_t &s, const dev_scene &sc, const 
 
 // Inner-node visit shared by the speculative order: box tests of `cur`, then near child,
 // push of the far child, or pop. Clears `more` when the stack runs empty.
-template <int STACK, bool ANY, bool PLAIN>
-__device__ __forceinline__ void spec_node(trav_t &s, const dev_scene &sc, const ray_t &r, int *stk, int stride,
+template <bool ANY, bool PLAIN>
+__device__ __forceinline__ void spec_node(trav_t &s, const dev_scene &sc, const ray_t &r, int *stk, int stride, int cap,
                                           unsigned *err) {
     float dl, dr;
     bool hl, hr;
@@ -472,7 +472,7 @@ __device__ __forceinline__ void spec_node(trav_t &s, const dev_scene &sc, const 
     node_test<ANY, PLAIN>(sc.nodes + 4 * (size_t)s.cur, s, r, hl, hr, dl, dr, cl, cr);
     if (hl && hr) {
         const bool left_first = dl < dr;
-        if (s.sp >= STACK) {
+        if (s.sp >= cap) {
             atomicOr(err, ERR_STACK_OVERFLOW);
             s.done = true;
             return;
@@ -494,8 +494,8 @@ __device__ __forceinline__ void spec_node(trav_t &s, const dev_scene &sc, const 
 // five-comparator sorting network), the nearest kept in `cur` and the others pushed farthest
 // first. Every child box is a subset of the binary box the collapse skipped, and rounding is
 // monotone, so a child the reference would reach is never culled here.
-template <int STACK, bool ANY, bool PLAIN>
-__device__ __forceinline__ void spec_node4(trav_t &s, const dev_scene &sc, const ray_t &r, int *stk, int stride,
+template <bool ANY, bool PLAIN>
+__device__ __forceinline__ void spec_node4(trav_t &s, const dev_scene &sc, const ray_t &r, int *stk, int stride, int cap,
                                            unsigned *err) {
     const float4 *np = sc.nodes4 + 8 * (size_t)s.cur;
     float k[4];
@@ -535,7 +535,7 @@ __device__ __forceinline__ void spec_node4(trav_t &s, const dev_scene &sc, const
     for (int i = 3; i >= 0; --i) {
         if (c[i] == kEmptyWideChild) continue;
         if (next != kEmptyWideChild) {
-            if (s.sp >= STACK) {
+            if (s.sp >= cap) {
                 atomicOr(err, ERR_STACK_OVERFLOW);
                 s.done = true;
                 return;
@@ -559,23 +559,24 @@ __device__ __forceinline__ void spec_node4(trav_t &s, const dev_scene &sc, const
 // rt/cuda/trace-kernels.cu:1433-1540, after Aila and Laine): a lane that reaches a leaf
 // postpones it and keeps visiting inner nodes while other lanes of the warp are still looking
 // for their first leaf; then all postponed leaves are tested together. The reference postpones
-// one leaf; here a lane may postpone up to PEND (1 to 3) before the leaf phase, so that lanes
+// one leaf; here a lane may postpone up to cfg.pend (1 to 3) before the leaf phase, so that lanes
 // already holding a leaf do useful work instead of idling while the warp searches (on GB300 two
 // took 9 % off the fused path step and three 14 % off fused direct lighting). The warp leaves
-// the node phase once at most EXIT lanes are still searching for their first leaf; those lanes
+// the node phase once at most cfg.exit lanes are still searching for their first leaf; those lanes
 // resume where they stopped in the next call, so this changes when leaves are tested, not which
 // (leaving with up to 6 to 8 of 32 lanes still searching took another 5 % off the fused path
-// step).
+// step). The three parameters (cfg: postponed leaves, exit count, node visits per vote) and the
+// stack capacity `cap` are launch arguments, chosen per kernel family and by the autotuner.
 // Every lane of the warp must call this together (it ballots over the full warp); `active`
 // marks lanes with a ray.
 // Each ray's leaves are still tested in the reference's order, but node tests after a
 // postponed leaf use the closest hit from before that leaf, so the ray may visit nodes the
 // reference would have culled. A triangle found there can replace the reference's answer only
 // if its t lies within rounding of the culled box's entry distance: a near-tie.
-template <int STACK, bool ANY, bool COUNT, bool WIDE = false, bool ALPHA = false, int PEND = 1, int EXIT = 0,
-          int VISITS = 3>
+template <bool ANY, bool COUNT, bool WIDE = false, bool ALPHA = false>
 __device__ __forceinline__ void trav_spec_iter(trav_t &s, bool active, bool plain, const dev_scene &sc,
-                                               const ray_t &r, int *stk, int stride, unsigned *err) {
+                                               const ray_t &r, int *stk, int stride, int cap, const spec_cfg &cfg,
+                                               unsigned *err) {
     const bool mine = active && !s.done;
     // One node visit (or postponement of a reached leaf) of this lane, if it has one to make.
     auto visit = [&]() {
@@ -583,22 +584,22 @@ __device__ __forceinline__ void trav_spec_iter(trav_t &s, bool active, bool plai
             if (COUNT) ++s.n_inner;
             if (WIDE) {
                 if (plain)
-                    spec_node4<STACK, ANY, true>(s, sc, r, stk, stride, err);
+                    spec_node4<ANY, true>(s, sc, r, stk, stride, cap, err);
                 else
-                    spec_node4<STACK, ANY, false>(s, sc, r, stk, stride, err);
+                    spec_node4<ANY, false>(s, sc, r, stk, stride, cap, err);
             } else {
                 if (plain)
-                    spec_node<STACK, ANY, true>(s, sc, r, stk, stride, err);
+                    spec_node<ANY, true>(s, sc, r, stk, stride, cap, err);
                 else
-                    spec_node<STACK, ANY, false>(s, sc, r, stk, stride, err);
+                    spec_node<ANY, false>(s, sc, r, stk, stride, cap, err);
             }
         }
-        const bool slot = PEND == 1 ? s.pend == 0 : PEND == 2 ? s.pend2 == 0 : s.pend3 == 0;
+        const bool slot = cfg.pend <= 1 ? s.pend == 0 : cfg.pend == 2 ? s.pend2 == 0 : s.pend3 == 0;
         if (mine && !s.done && s.more && s.cur < 0 && slot) {
-            // postpone the leaf and go on with the next node
+            // postpone the leaf into the first free slot and go on with the next node
             if (s.pend == 0)
                 s.pend = s.cur;
-            else if (PEND == 2 || s.pend2 == 0)
+            else if (s.pend2 == 0)
                 s.pend2 = s.cur;
             else
                 s.pend3 = s.cur;
@@ -610,19 +611,18 @@ __device__ __forceinline__ void trav_spec_iter(trav_t &s, bool active, bool plai
             }
         }
     };
-    // VISITS node visits per warp vote (three measured on GB300 4.4 % faster than one visit per
-    // vote, and 1.2 % faster than two); a lane that has stopped searching may make up to
-    // VISITS - 1 more speculative node visits before the leaf phase, which leaves its hit within
+    // cfg.visits node visits per warp vote (three measured on GB300 4.4 % faster than one visit
+    // per vote, and 1.2 % faster than two); a lane that has stopped searching may make up to
+    // cfg.visits - 1 more speculative node visits before the leaf phase, which leaves its hit within
     // the near-tie class. The warp's visit slots of this call are added to every live lane's step count (an
     // upper bound of its own visits), so the work of a ray on a malformed tree stays bounded
     // across calls, without a per-visit count.
     uint32_t slots = 0;
     for (;;) {
-#pragma unroll
-        for (int v = 0; v < VISITS; ++v) visit();
-        slots += VISITS;
+        for (int v = 0; v < cfg.visits; ++v) visit();
+        slots += (uint32_t)cfg.visits;
         const bool searching = mine && !s.done && s.more && s.pend == 0;
-        if (__popc(__ballot_sync(0xffffffffu, searching)) <= EXIT || slots >= kStepLimit) break;
+        if (__popc(__ballot_sync(0xffffffffu, searching)) <= cfg.exit || slots >= kStepLimit) break;
     }
     if (mine && !s.done) {
         s.steps += slots;
@@ -635,8 +635,8 @@ __device__ __forceinline__ void trav_spec_iter(trav_t &s, bool active, bool plai
         while (s.pend != 0 && !s.done) {
             uint32_t first, count;
             leaf_range(s.pend, first, count);
-            s.pend = PEND > 1 ? s.pend2 : 0;
-            s.pend2 = PEND > 2 ? s.pend3 : 0;
+            s.pend = s.pend2;  // slots beyond the postponing limit stay 0
+            s.pend2 = s.pend3;
             s.pend3 = 0;
             ++s.steps;
             const float4 *rp = sc.records + 3 * (size_t)first;
@@ -666,13 +666,13 @@ __device__ __forceinline__ void trav_spec_iter(trav_t &s, bool active, bool plai
 
 // One iteration of a non-speculative loop order for this lane's ray (PLAIN: min/max slab test,
 // see ray_is_plain). The speculative order is trav_spec_iter, which the whole warp calls together.
-template <int ORDER, int STACK, bool ANY, bool COUNT, bool PLAIN, bool ALPHA = false>
+template <int ORDER, bool ANY, bool COUNT, bool PLAIN, bool ALPHA = false>
 __device__ __forceinline__ void trav_advance(trav_t &s, const dev_scene &sc, const ray_t &r, int *stk, int stride,
-                                             unsigned *err) {
+                                             int cap, unsigned *err) {
     if (ORDER == WHILE_WHILE)
-        trav_iter<STACK, ANY, PLAIN, COUNT, ALPHA>(s, sc, r, stk, stride, err);
+        trav_iter<ANY, PLAIN, COUNT, ALPHA>(s, sc, r, stk, stride, cap, err);
     else
-        trav_step<STACK, ANY, PLAIN, COUNT, ALPHA>(s, sc, r, stk, stride, err);
+        trav_step<ANY, PLAIN, COUNT, ALPHA>(s, sc, r, stk, stride, cap, err);
 }
 
 // Writes one result in the reference's encodings (see include/grt.h).

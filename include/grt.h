@@ -39,7 +39,7 @@ extern "C" {
 #endif
 
 #define GRT_VERSION_MAJOR 1
-#define GRT_VERSION_MINOR 0
+#define GRT_VERSION_MINOR 1
 
 /* A cudaStream_t. NULL means the legacy default stream. */
 typedef struct CUstream_st *grt_stream_t;
@@ -94,13 +94,22 @@ typedef struct grt_bvh_stats {
     double upload_ms;       /* host-to-device copies */
 } grt_bvh_stats;
 
-/* Launch parameters picked by the autotuner (or by hand). Zero fields mean "default". */
+/* Launch parameters picked by the autotuner (or by hand). Zero fields mean "default". The
+ * reference's counterparts are compile-time constants of its CUDA tracers (BATCH_SIZE,
+ * DYNAMIC_FETCH_THRESHOLD, STACK_SIZE; rt/cuda/trace-kernels.cu:6-8). */
 typedef struct grt_tuning {
     int block_threads;     /* threads per block (multiple of 32) */
     int blocks_per_sm;     /* persistent kernels: resident blocks per SM */
     int refill_threshold;  /* persistent kernels: refill a warp when fewer lanes are active */
     int refill_period;     /* persistent kernels: traversal steps between refill checks */
-    int stack_entries;     /* 0 = smallest variant that fits the BVH depth */
+    int stack_entries;     /* traversal stack entries per thread (shared memory); 0 = the BVH's
+                              depth, larger values up to 64 allowed, smaller ones raised to it */
+    /* Speculative loop order of the persistent kernels (fused path tracer, persistent traces,
+     * scene sets); 0 = the measured default of each kernel family: */
+    int spec_pend;         /* leaves a lane may postpone before the warp's leaf phase, 1..3 */
+    int spec_exit;         /* the warp leaves its node phase once at most this many lanes still
+                              search for their first leaf, 1..32 */
+    int spec_visits;       /* node visits per lane between two warp votes, 1..16 */
 } grt_tuning;
 
 /* ---- context ------------------------------------------------------------------------ */

@@ -85,8 +85,7 @@ def test_timed_configuration_full_size_matches_oracle(api, orc, spheres_full):
     import bench
     tuning = bench.load_tuning(torch.cuda.get_device_name(0))
     tree = bench.tree_options(tuning)
-    launch = {k: v for k, v in tuning.items() if k in ("block_threads", "blocks_per_sm", "refill_threshold",
-                                                       "refill_period", "stack_entries")}
+    launch = {k: v for k, v in tuning.items() if k in api.TUNING_KEYS}
     sc, rays_np, rays = spheres_full
     prim, res, bh = _paths(api, sc, rays, tuning.get("tracer", "persistent-speculative-while-while"), api.PT_FUSED,
                            tree=tree, tuning=launch, bounce_hits=True)
