@@ -182,6 +182,7 @@ grt_status grt_trace_multi(grt_ctx *c, const grt_ray_batch *batches, uint32_t co
     launch_params lp{};
     const grt_tuning &t = c->tuning;
     lp.order = order;
+    lp.spec = tuned_spec(t, kSpecPersistent);
     lp.stack_entries = std::max(t.stack_entries, needed);
     lp.block_threads = t.block_threads > 0 ? t.block_threads : 128;
     lp.refill_threshold = t.refill_threshold > 0 ? t.refill_threshold : 20;

@@ -70,6 +70,10 @@ static const int kStackLarge = 64;
 struct spec_cfg {
     int pend, exit, visits;
 };
+// The launch functions refuse (cudaErrorInvalidValue) parameters outside these ranges.
+inline bool spec_ok(const spec_cfg &c) {
+    return c.pend >= 1 && c.pend <= 3 && c.exit >= 0 && c.exit <= 32 && c.visits >= 1 && c.visits <= 16;
+}
 constexpr spec_cfg kSpecPaths = {2, 8, 5};       // fused path tracer
 constexpr spec_cfg kSpecDirect = {3, 2, 3};      // fused direct lighting
 constexpr spec_cfg kSpecTrace = {3, 1, 3};       // one-thread-per-ray batch traces

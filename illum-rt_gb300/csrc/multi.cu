@@ -131,6 +131,7 @@ cudaError_t launch_trace_multi(const dev_scene *scenes, const multi_batch *batch
                                bool any_hit, const launch_params &lp, unsigned *err, unsigned *counter,
                                cudaStream_t st) {
     if (total == 0) return cudaSuccess;
+    if (!spec_ok(lp.spec)) return cudaErrorInvalidValue;
     switch (lp.order) {
         case WHILE_WHILE: return multi_any<WHILE_WHILE>(any_hit, scenes, batches, nbatch, total, lp, err, counter, st);
         case SPECULATIVE: return multi_any<SPECULATIVE>(any_hit, scenes, batches, nbatch, total, lp, err, counter, st);

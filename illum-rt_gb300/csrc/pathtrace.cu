@@ -548,6 +548,7 @@ cudaError_t launch_fused(const dev_scene &sc, const pt_scene &ps, const pt_param
                          grt_path_result *results, grt_hit *bounce_hits, const launch_params &lp, unsigned *err,
                          unsigned *counter, cudaStream_t st) {
     if (n_paths == 0) return cudaSuccess;
+    if (!spec_ok(lp.spec)) return cudaErrorInvalidValue;
     auto f = lp.order == WHILE_WHILE        ? fused_launch<WHILE_WHILE>
              : lp.order == SPECULATIVE      ? fused_launch<SPECULATIVE>
              : lp.order == WIDE_SPECULATIVE ? fused_launch<WIDE_SPECULATIVE>

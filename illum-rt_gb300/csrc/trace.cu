@@ -214,12 +214,14 @@ template <int O, bool A> struct occupancy_f {
 cudaError_t launch_trace_plain(const dev_scene &sc, const float4 *rays, grt_hit *hits, uint32_t n, bool any_hit,
                                const launch_params &lp, unsigned *err, cudaStream_t stream, const uint32_t *n_dev) {
     if (n == 0) return cudaSuccess;
+    if (!spec_ok(lp.spec)) return cudaErrorInvalidValue;
     return dispatch<plain_f>(lp.order, any_hit, sc, rays, hits, n, n_dev, lp, err, stream);
 }
 
 cudaError_t launch_trace_persistent(const dev_scene &sc, const float4 *rays, grt_hit *hits, uint32_t n, bool any_hit,
                                     const launch_params &lp, unsigned *err, unsigned *counter, cudaStream_t stream) {
     if (n == 0) return cudaSuccess;
+    if (!spec_ok(lp.spec)) return cudaErrorInvalidValue;
     return dispatch<persistent_f>(lp.order, any_hit, sc, rays, hits, n, lp, err, counter, stream);
 }
 

@@ -617,10 +617,13 @@ __device__ __forceinline__ void trav_spec_iter(trav_t &s, bool active, bool plai
     // the near-tie class. The warp's visit slots of this call are added to every live lane's step count (an
     // upper bound of its own visits), so the work of a ray on a malformed tree stays bounded
     // across calls, without a per-visit count.
+    // At least one visit per vote: every pass then moves each searching lane on by a node or a
+    // postponed leaf, so the loop ends (and `slots` reaches the step limit on a malformed tree).
+    const int visits = cfg.visits > 0 ? cfg.visits : 1;
     uint32_t slots = 0;
     for (;;) {
-        for (int v = 0; v < cfg.visits; ++v) visit();
-        slots += (uint32_t)cfg.visits;
+        for (int v = 0; v < visits; ++v) visit();
+        slots += (uint32_t)visits;
         const bool searching = mine && !s.done && s.more && s.pend == 0;
         if (__popc(__ballot_sync(0xffffffffu, searching)) <= cfg.exit || slots >= kStepLimit) break;
     }
