@@ -689,7 +689,8 @@ def run_soups64(args):
     """64 triangle soups of log-uniform size in [1,024, 1,048,576] triangles with log-uniform ray
     batches in [4,096, 1,048,576] (7,738,242 triangles, 10,745,442 rays), all batches in one
     persistent launch. Reports the wall time of the host build (the reference builder, scenes in
-    parallel) and of the GPU build, and the trace rate on each tree."""
+    parallel) and of the GPU builds (radix tree, and PLOC clustering), and the trace rate on
+    each tree."""
     import torch
     import __graft_entry__ as ge
     ge.load_package()
@@ -729,8 +730,10 @@ def run_soups64(args):
         rt.check(sp)
         return e0.elapsed_time(e1) / args.steps
 
-    for kind in ("host", "gpu"):
+    for kind in ("host", "gpu", "gpu_ploc"):
         rt = api.BatchRayTracer(0)
+        if kind == "gpu_ploc":
+            rt.set_device_builder("ploc")
         rt.select(tuning.get("tracer", "persistent-speculative-while-while"))
         kw = {k: v for k, v in tuning.items() if k in api.TUNING_KEYS}
         if kw:
@@ -739,7 +742,7 @@ def run_soups64(args):
         t0 = time.perf_counter()
         if kind == "host":
             rt.build_scenes(scenes, max_tris=tuning.get("max_tris", 4))
-        else:
+        else:  # the radix-tree builder (the scene-set default) or PLOC clustering
             rt.build_scenes_device(d_scenes, max_tris=tuning.get("max_tris", 4), stream=sp)
         build_s = time.perf_counter() - t0
         ms = timed_trace(rt)

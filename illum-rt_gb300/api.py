@@ -162,6 +162,7 @@ _PROTOS = {
     "grt_timing_stats": (I, [VP, P(Timing), I]),
     "grt_incoherent_rays": (I, [VP, ctypes.c_float, ctypes.c_float, ctypes.c_uint64, VP, U32, VP]),
     "grt_camera_rays": (I, [VP, P(Camera), U32, U32, VP, I, ctypes.c_uint64, VP, VP]),
+    "grt_set_device_builder": (I, [VP, I]),
 }
 
 
@@ -374,6 +375,13 @@ class BatchRayTracer:
         o = make_opts(split or self.bvh_type, max_tris or self.bvh_max_tris_per_node, planes or self.bvh_planes, esc)
         self._check(lib().grt_build(self.ctx, _ptr(v), v.shape[0], _ptr(t), t.shape[0], ctypes.byref(o)))
         return self.info()
+
+    DEVICE_BUILDERS = {"default": 0, "lbvh": 1, "ploc": 2}
+
+    def set_device_builder(self, method: str):
+        """grt_set_device_builder: "ploc", "lbvh" or "default" (PLOC for single scenes, LBVH for
+        scene sets)."""
+        self._check(lib().grt_set_device_builder(self.ctx, self.DEVICE_BUILDERS[method]))
 
     def build_device(self, vpos, tris, max_tris=None, stream=None) -> dict:
         """The GPU builder (grt_build_device) on CUDA tensors: vpos float32 [nv, 4], tris

@@ -48,6 +48,14 @@ bool bad_mesh(const grt_mesh &m) {
 
 extern "C" {
 
+grt_status grt_set_device_builder(grt_ctx *c, int method) {
+    if (!c) return GRT_ERR_INVALID_ARG;
+    if (method != GRT_DEVICE_BUILD_DEFAULT && method != GRT_DEVICE_BUILD_LBVH && method != GRT_DEVICE_BUILD_PLOC)
+        return fail(c, GRT_ERR_INVALID_ARG, "unknown device builder");
+    c->device_builder = method;
+    return GRT_OK;
+}
+
 grt_status grt_build_device(grt_ctx *c, const float *vpos4_dev, uint32_t nv, const uint32_t *tris4_dev, uint32_t nt,
                             uint32_t max_tris, grt_stream_t stream) {
     if (!c) return GRT_ERR_INVALID_ARG;
@@ -65,7 +73,8 @@ grt_status grt_build_device(grt_ctx *c, const float *vpos4_dev, uint32_t nv, con
 
     build_temps tmp;
     const size_t nb = (size_t)std::max(nt, 2u) * 64, rb = (size_t)std::max(nt, 1u) * 48;
-    const size_t scratch = gpu_build_scratch_bytes(nt);
+    const int method = c->device_builder == GRT_DEVICE_BUILD_LBVH ? GB_METHOD_LBVH : GB_METHOD_PLOC;
+    const size_t scratch = gpu_build_scratch_bytes(nt, method);
     cudaError_t e = cudaMalloc(&c->d_nodes, nb);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_recs, rb);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_vpos, std::max<size_t>((size_t)nv * 16, 16));
@@ -79,7 +88,7 @@ grt_status grt_build_device(grt_ctx *c, const float *vpos4_dev, uint32_t nv, con
     if (e == cudaSuccess)
         e = gpu_build_binary((const float4 *)c->d_vpos, nv, (const uint4 *)c->d_tris, nt, (int)max_tris, tmp.scratch,
                              scratch, (float4 *)c->d_nodes, (float4 *)c->d_recs, tmp.wide_index,
-                             (int32_t *)c->d_parent, tmp.info, st);
+                             (int32_t *)c->d_parent, tmp.info, method, st);
     int32_t info[8] = {0};
     if (e == cudaSuccess) e = cudaMemcpyAsync(info, tmp.info, sizeof(info), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -240,7 +249,8 @@ grt_status grt_build_scenes_device(grt_ctx *c, const grt_mesh *meshes, uint32_t 
     }
     build_temps tmp;
     int32_t *wide_pool = nullptr;
-    const size_t scratch = gpu_build_scratch_bytes(most);
+    const int method = c->device_builder == GRT_DEVICE_BUILD_PLOC ? GB_METHOD_PLOC : GB_METHOD_LBVH;
+    const size_t scratch = gpu_build_scratch_bytes(most, method);
     cudaError_t e = cudaMalloc(&c->ms.d_nodes, tot[0]);
     if (e == cudaSuccess) e = cudaMalloc(&c->ms.d_recs, tot[1]);
     if (e == cudaSuccess) e = cudaMalloc((void **)&wide_pool, tot[2]);
@@ -252,7 +262,7 @@ grt_status grt_build_scenes_device(grt_ctx *c, const grt_mesh *meshes, uint32_t 
         e = gpu_build_binary((const float4 *)m.vpos4, m.nv, (const uint4 *)m.tris4, m.nt, (int)max_tris, tmp.scratch,
                              scratch, (float4 *)((char *)c->ms.d_nodes + off[i][0]),
                              (float4 *)((char *)c->ms.d_recs + off[i][1]), (int32_t *)((char *)wide_pool + off[i][2]),
-                             nullptr, tmp.info + 8 * (size_t)i, st);
+                             nullptr, tmp.info + 8 * (size_t)i, method, st);
     }
     std::vector<int32_t> info((size_t)count * 8, 0);
     if (e == cudaSuccess) e = cudaMemcpyAsync(info.data(), tmp.info, info.size() * 4, cudaMemcpyDeviceToHost, st);

@@ -55,6 +55,7 @@ struct grt_ctx {
     grt_bvh_stats stats{};
     int tracer = 0;  // index into kTracers
     grt_tuning tuning{};
+    int device_builder = GRT_DEVICE_BUILD_DEFAULT;  // grt_set_device_builder
     timing_state timing;
     unsigned *d_err = nullptr;      // status block (grt_internal.hpp): error bits, counter, abort request
     unsigned *d_counter = nullptr;  // work counter of the persistent kernels (d_err + 1)

@@ -22,6 +22,7 @@
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
 
+#include <algorithm>
 #include <cfloat>
 
 #include "gpu_build.hpp"
@@ -166,6 +167,225 @@ __global__ void __launch_bounds__(kThreads) k_radix_tree(const uint32_t *__restr
     else
         parent_leaf[~right] = i;
     if (i == 0) parent_inner[0] = -1;
+}
+
+// ---- 3'. PLOC: parallel locally-ordered clustering over the Morton order --------------------
+//
+// After Meister and Bittner, "Parallel Locally-Ordered Clustering for Bounding Volume Hierarchy
+// Construction" (IEEE TVCG 2018): the sorted triangles start as clusters; in every iteration
+// each cluster finds, among the kPlocRadius clusters on either side of it in the current list,
+// the one whose union box has the smallest surface area; mutual nearest neighbours merge into a
+// new inner node, and the list is compacted in order. Ties are broken by the nearer list
+// position, then by parity (an even position prefers its right neighbour, an odd one its left),
+// so that coincident triangles pair up and halve each iteration. After a budget of iterations
+// any remaining clusters are paired by position ((0, 1), (2, 3), ...), which bounds the number of
+// iterations and the tree's depth. Every index comes from a prefix sum, so the tree is the same
+// on every run. Cluster ids: sorted position k for a triangle, n + q for the q-th inner node made.
+// The finished tree is renumbered into the radix tree's form (children, ranges and parents, the
+// root as inner node 0, leaves as positions of a depth-first order), so the rest of the build
+// (bottom-up fit, SAH collapse, records, 4-wide collapse) is shared.
+
+constexpr int kPlocRadius = 16;
+
+struct ploc_state {
+    int32_t m;      // clusters in the current list
+    int32_t made;   // inner nodes made so far
+    int32_t err;    // an index outside its array was met (never for a well-formed run)
+    int32_t pad;
+};
+
+__global__ void __launch_bounds__(kThreads) k_ploc_init(const float4 *__restrict__ lo, const float4 *__restrict__ hi,
+                                                        const uint32_t *__restrict__ order, int n, int32_t *cl,
+                                                        float4 *box_lo, float4 *box_hi, int32_t *parent,
+                                                        ploc_state *ps) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k == 0) *ps = {n, 0, 0, 0};
+    if (k >= n) return;
+    const uint32_t prim = order[k];
+    cl[k] = k;
+    box_lo[k] = lo[prim];
+    box_hi[k] = hi[prim];
+    parent[k] = -1;
+    if (k < n - 1) parent[n + k] = -1;
+}
+
+// Nearest neighbour of every cluster (or, when `forced`, its pairing partner). The block's
+// clusters and kPlocRadius on either side are staged in shared memory.
+__global__ void __launch_bounds__(kThreads) k_ploc_nn(const int32_t *__restrict__ cl,
+                                                      const float4 *__restrict__ box_lo,
+                                                      const float4 *__restrict__ box_hi,
+                                                      const ploc_state *__restrict__ ps, int forced, int32_t *nn) {
+    __shared__ float4 s_lo[kThreads + 2 * kPlocRadius], s_hi[kThreads + 2 * kPlocRadius];
+    const int m = ps->m;
+    const int b0 = blockIdx.x * kThreads;
+    if (m <= 1 || b0 >= m) return;
+    const int i = b0 + threadIdx.x;
+    if (forced) {
+        if (i < m) nn[i] = (i ^ 1) < m ? (i ^ 1) : -1;
+        return;
+    }
+    for (int t = threadIdx.x; t < kThreads + 2 * kPlocRadius; t += kThreads) {
+        const int g = b0 - kPlocRadius + t;
+        if (g >= 0 && g < m) {
+            const int id = cl[g];
+            s_lo[t] = box_lo[id];
+            s_hi[t] = box_hi[id];
+        }
+    }
+    __syncthreads();
+    if (i >= m) return;
+    const int me = threadIdx.x + kPlocRadius;
+    const float4 a_lo = s_lo[me], a_hi = s_hi[me];
+    float best = __int_as_float(0x7f800000);
+    int bj = -1, bd = 1 << 30;
+    const bool even = (i & 1) == 0;
+    for (int d = -kPlocRadius; d <= kPlocRadius; ++d) {
+        const int j = i + d;
+        if (d == 0 || j < 0 || j >= m) continue;
+        const float4 b_lo = s_lo[me + d], b_hi = s_hi[me + d];
+        const float4 ulo = make_float4(fminf(a_lo.x, b_lo.x), fminf(a_lo.y, b_lo.y), fminf(a_lo.z, b_lo.z), 0.f);
+        const float4 uhi = make_float4(fmaxf(a_hi.x, b_hi.x), fmaxf(a_hi.y, b_hi.y), fmaxf(a_hi.z, b_hi.z), 0.f);
+        const float area = half_area(ulo, uhi);
+        const int ad = d < 0 ? -d : d;
+        const bool pref = even ? d > 0 : d < 0;
+        if (area < best || (area == best && (ad < bd || (ad == bd && pref)))) {
+            best = area;
+            bj = j;
+            bd = ad;
+        }
+    }
+    nn[i] = bj;
+}
+
+// Merge flags: high word 1 for the lower position of a mutual pair (it makes the new node),
+// low word 1 for every position that stays in the list (all but the higher one of a pair).
+__global__ void __launch_bounds__(kThreads) k_ploc_flags(const int32_t *__restrict__ nn,
+                                                         const ploc_state *__restrict__ ps, int n,
+                                                         unsigned long long *flags) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int m = ps->m;
+    unsigned long long f = 0;
+    if (i < m && m > 1) {
+        const int j = nn[i];
+        const bool mutual = j >= 0 && j < m && nn[j] == i;
+        const bool merge = mutual && i < j, drop = mutual && i > j;
+        f = ((unsigned long long)(merge ? 1u : 0u) << 32) | (drop ? 0u : 1u);
+    } else if (i < m) {
+        f = 1;
+    }
+    flags[i] = f;
+}
+
+__global__ void __launch_bounds__(kThreads) k_ploc_apply(const int32_t *__restrict__ cl, const int32_t *__restrict__ nn,
+                                                         const unsigned long long *__restrict__ flags,
+                                                         const unsigned long long *__restrict__ excl, int n,
+                                                         ploc_state *ps, int2 *kid, float4 *box_lo,
+                                                         float4 *box_hi, int32_t *parent, int32_t *cl_next) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int m = ps->m;
+    if (i >= m || m <= 1) return;
+    const unsigned long long f = flags[i], e = excl[i];
+    const int keep_pos = (int)(uint32_t)e;
+    if (f >> 32) {
+        const int j = nn[i];
+        const int q = ps->made + (int)(e >> 32);
+        if (q < 0 || q >= n - 1 || j < 0 || j >= m) {
+            atomicOr(&ps->err, 1);
+            return;
+        }
+        const int a = cl[i], b = cl[j];
+        const int id = n + q;
+        kid[q] = make_int2(a, b);
+        const float4 al = box_lo[a], ah = box_hi[a], bl = box_lo[b], bh = box_hi[b];
+        box_lo[id] = make_float4(fminf(al.x, bl.x), fminf(al.y, bl.y), fminf(al.z, bl.z), 0.f);
+        box_hi[id] = make_float4(fmaxf(ah.x, bh.x), fmaxf(ah.y, bh.y), fmaxf(ah.z, bh.z), 0.f);
+        parent[a] = q;
+        parent[b] = q;
+        cl_next[keep_pos] = id;
+    } else if (f & 1u) {
+        cl_next[keep_pos] = cl[i];
+    }
+}
+
+// The list's new length and the inner nodes made so far, from the last position's flags.
+__global__ void k_ploc_state(const unsigned long long *__restrict__ flags,
+                             const unsigned long long *__restrict__ excl, ploc_state *ps) {
+    const int m = ps->m;
+    if (m <= 1) return;
+    const unsigned long long t = excl[m - 1] + flags[m - 1];
+    ps->m = (int)(uint32_t)t;
+    ps->made += (int)(t >> 32);
+}
+
+// Triangle counts of the inner nodes: creation order puts children before parents, so one
+// pass per node in order would do; in parallel, each inner node climbs from its first-finished
+// child with the second-arrival rule (an atomic per node; no thread waits for another).
+__global__ void __launch_bounds__(kThreads) k_ploc_counts(const int2 *__restrict__ kid, const int32_t *__restrict__ parent,
+                                                          int n, uint32_t *visits, int32_t *cnt, ploc_state *ps) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int q = parent[k];
+    for (int climb = 0; climb < kMaxClimb && q >= 0; ++climb) {
+        if (q >= n - 1) {
+            atomicOr(&ps->err, 2);
+            return;
+        }
+        __threadfence();
+        if (atomicAdd(visits + q, 1u) == 0u) return;  // the sibling's thread continues
+        __threadfence();
+        const int2 c = kid[q];
+        const int ca = c.x < n ? 1 : __ldcg(cnt + (c.x - n)), cb = c.y < n ? 1 : __ldcg(cnt + (c.y - n));
+        cnt[q] = ca + cb;
+        q = parent[n + q];
+    }
+    if (q >= 0) atomicOr(&ps->err, 4);
+}
+
+__device__ __forceinline__ int ploc_size(const int32_t *cnt, int n, int id) { return id < n ? 1 : cnt[id - n]; }
+
+// Depth-first start position of every cluster id (its subtree's first triangle): the sizes of
+// the left siblings of all its right-hand ancestors. Then the radix-tree form: inner node q
+// becomes n - 2 - q (the root, made last, becomes 0), a triangle at sorted position k becomes
+// leaf position pos(k), and `order2` lists the primitives in depth-first order.
+__global__ void __launch_bounds__(kThreads) k_ploc_emit(const int2 *__restrict__ kid, const int32_t *__restrict__ parent,
+                                                        const int32_t *__restrict__ cnt,
+                                                        const uint32_t *__restrict__ order, int n, int2 *children,
+                                                        int2 *range, int32_t *parent_inner, int32_t *parent_leaf,
+                                                        uint32_t *order2, ploc_state *ps) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;  // cluster id: 0..n-1 triangles, n..2n-2 inner
+    if (x >= 2 * n - 1) return;
+    int start = 0, v = x, climb = 0;
+    for (; climb < kMaxClimb && parent[v] >= 0; ++climb) {
+        const int q = parent[v];
+        if (q >= n - 1) {
+            atomicOr(&ps->err, 8);
+            return;
+        }
+        const int2 c = kid[q];
+        if (c.y == v) start += ploc_size(cnt, n, c.x);
+        v = n + q;
+    }
+    if (climb >= kMaxClimb || v != 2 * n - 2 || start < 0 || start >= n) {
+        atomicOr(&ps->err, 16);
+        return;
+    }
+    if (x < n) {
+        order2[start] = order[x];
+        const int p = parent[x];
+        parent_leaf[start] = p >= 0 ? n - 2 - p : -1;
+    } else {
+        const int q = x - n, me = n - 2 - q;
+        const int2 c = kid[q];
+        range[me] = make_int2(start, start + cnt[q] - 1);
+        const int p = parent[x];
+        parent_inner[me] = p >= 0 ? n - 2 - p : -1;
+        // children: inner nodes by their new numbers, triangles by their depth-first positions
+        // (a triangle's position is its parent's start, plus the left sibling's size if right)
+        const int l = c.x < n ? ~start : n - 2 - (c.x - n);
+        const int r = c.y < n ? ~(start + ploc_size(cnt, n, c.x)) : n - 2 - (c.y - n);
+        children[me] = make_int2(l, r);
+    }
 }
 
 // What a child hands to its parent in the bottom-up pass (two per inner node).
@@ -390,7 +610,7 @@ __global__ void k_init_info(int32_t *info, uint32_t *cbounds) {
 
 inline size_t up256(size_t b) { return (b + 255) & ~(size_t)255; }
 
-// scratch layout for up to n triangles
+// scratch layout for up to n triangles (the PLOC arrays only when `ploc`)
 struct arena {
     float4 *lo, *hi;
     uint32_t *keys_a, *keys_b, *vals_a, *vals_b, *cbounds, *visits;
@@ -398,19 +618,30 @@ struct arena {
     int32_t *parent_inner, *parent_leaf, *flag, *excl;
     slot *slots;
     uint8_t *collapsed;
+    // PLOC: cluster lists, boxes and parents of all 2n - 1 cluster ids, children of the inner
+    // nodes made, nearest neighbours, merge flags and their prefix sums, subtree sizes, the
+    // depth-first primitive order, the climbing counters and the iteration state
+    int32_t *cl_a, *cl_b, *pparent, *nn, *cnt;
+    float4 *box_lo, *box_hi;
+    int2 *kid;
+    unsigned long long *pflags, *pexcl;
+    uint32_t *order2, *pvisits;
+    ploc_state *ps;
     void *cub;
     size_t cub_bytes, total;
 };
 
 size_t cub_bytes_for(uint32_t n) {
-    size_t a = 0, b = 0;
+    size_t a = 0, b = 0, c = 0;
     cub::DeviceRadixSort::SortPairs(nullptr, a, (const uint32_t *)nullptr, (uint32_t *)nullptr,
                                     (const uint32_t *)nullptr, (uint32_t *)nullptr, (int)n, 0, 30);
     cub::DeviceScan::ExclusiveSum(nullptr, b, (const int32_t *)nullptr, (int32_t *)nullptr, (int)n);
-    return a > b ? a : b;
+    cub::DeviceScan::ExclusiveSum(nullptr, c, (const unsigned long long *)nullptr, (unsigned long long *)nullptr,
+                                  (int)n);
+    return std::max(a, std::max(b, c));
 }
 
-arena carve(void *base, uint32_t n) {
+arena carve(void *base, uint32_t n, bool ploc) {
     arena A{};
     char *p = (char *)base;
     size_t off = 0;
@@ -436,6 +667,21 @@ arena carve(void *base, uint32_t n) {
     A.excl = (int32_t *)take(m * 4);
     A.slots = (slot *)take(m * 2 * sizeof(slot));
     A.collapsed = (uint8_t *)take(m);
+    if (ploc) {
+        A.cl_a = (int32_t *)take(m * 4);
+        A.cl_b = (int32_t *)take(m * 4);
+        A.pparent = (int32_t *)take(2 * m * 4);
+        A.nn = (int32_t *)take(m * 4);
+        A.cnt = (int32_t *)take(m * 4);
+        A.box_lo = (float4 *)take(2 * m * 16);
+        A.box_hi = (float4 *)take(2 * m * 16);
+        A.kid = (int2 *)take(m * 8);
+        A.pflags = (unsigned long long *)take(m * 8);
+        A.pexcl = (unsigned long long *)take(m * 8);
+        A.order2 = (uint32_t *)take(m * 4);
+        A.pvisits = (uint32_t *)take(m * 4);
+        A.ps = (ploc_state *)take(sizeof(ploc_state));
+    }
     A.cub_bytes = cub_bytes_for((uint32_t)m);
     A.cub = take(A.cub_bytes);
     A.total = off;
@@ -446,12 +692,73 @@ inline unsigned blocks_for(uint32_t n) { return (n + kThreads - 1) / kThreads; }
 
 }  // namespace
 
-size_t gpu_build_scratch_bytes(uint32_t max_tris) { return carve(nullptr, max_tris).total; }
+size_t gpu_build_scratch_bytes(uint32_t max_tris, int method) {
+    return carve(nullptr, max_tris, method == GB_METHOD_PLOC).total;
+}
+
+namespace {
+
+__global__ void k_ploc_report(const ploc_state *ps, int32_t *info) {
+    if (ps->err || ps->m != 1) atomicOr(info + GB_ERR, GB_ERR_TREE);
+}
+
+// Iterations of nearest-neighbour merging before the remaining clusters are paired by position,
+// and the number of pairing iterations that always finishes the tree.
+int ploc_budget(uint32_t n) {
+    int lg = 0;
+    while ((1u << lg) < n) ++lg;
+    return 48 + 2 * lg;
+}
+int ploc_pairing_rounds(uint32_t n) {
+    int lg = 0;
+    while ((1u << lg) < n) ++lg;
+    return lg + 1;
+}
+
+// The PLOC tree of the n >= 2 sorted triangles in the radix tree's form (children, range,
+// parent_inner, parent_leaf) with its depth-first primitive order in A.order2. The list length
+// is read back every 8 iterations, so that no launch is made once the tree is finished.
+cudaError_t ploc_tree(const arena &A, int n, cudaStream_t st) {
+    const unsigned nb = (n + kThreads - 1) / kThreads;
+    k_ploc_init<<<nb, kThreads, 0, st>>>(A.lo, A.hi, A.vals_b, n, A.cl_a, A.box_lo, A.box_hi, A.pparent, A.ps);
+    int32_t *cur = A.cl_a, *next = A.cl_b;
+    const int budget = ploc_budget((uint32_t)n), total = budget + ploc_pairing_rounds((uint32_t)n);
+    cudaError_t e = cudaGetLastError();
+    for (int it = 0; it < total && e == cudaSuccess; ++it) {
+        if (it % 8 == 7) {  // stop once one cluster is left
+            int32_t m = 0;
+            e = cudaMemcpyAsync(&m, &A.ps->m, sizeof(m), cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess || m <= 1) break;
+        }
+        k_ploc_nn<<<nb, kThreads, 0, st>>>(cur, A.box_lo, A.box_hi, A.ps, it >= budget ? 1 : 0, A.nn);
+        k_ploc_flags<<<nb, kThreads, 0, st>>>(A.nn, A.ps, n, A.pflags);
+        size_t cb = A.cub_bytes;
+        e = cub::DeviceScan::ExclusiveSum(A.cub, cb, A.pflags, A.pexcl, n, st);
+        if (e != cudaSuccess) break;
+        k_ploc_apply<<<nb, kThreads, 0, st>>>(cur, A.nn, A.pflags, A.pexcl, n, A.ps, A.kid, A.box_lo, A.box_hi,
+                                              A.pparent, next);
+        k_ploc_state<<<1, 1, 0, st>>>(A.pflags, A.pexcl, A.ps);
+        std::swap(cur, next);
+        e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(A.pvisits, 0, (size_t)n * 4, st);
+    if (e != cudaSuccess) return e;
+    k_ploc_counts<<<nb, kThreads, 0, st>>>(A.kid, A.pparent, n, A.pvisits, A.cnt, A.ps);
+    k_ploc_emit<<<(2 * n - 1 + kThreads - 1) / kThreads, kThreads, 0, st>>>(A.kid, A.pparent, A.cnt, A.vals_b, n,
+                                                                         A.children, A.range, A.parent_inner,
+                                                                         A.parent_leaf, A.order2, A.ps);
+    return cudaGetLastError();
+}
+
+}  // namespace
 
 cudaError_t gpu_build_binary(const float4 *vpos, uint32_t nv, const uint4 *tris, uint32_t nt, int max_leaf,
                              void *scratch, size_t scratch_bytes, float4 *nodes, float4 *records,
-                             int32_t *wide_index, int32_t *links, int32_t *info, cudaStream_t st) {
-    arena A = carve(scratch, nt);
+                             int32_t *wide_index, int32_t *links, int32_t *info, int method, cudaStream_t st) {
+    const bool ploc = method == GB_METHOD_PLOC && nt > 1;
+    arena A = carve(scratch, nt, method == GB_METHOD_PLOC);
     if (A.total > scratch_bytes) return cudaErrorInvalidValue;
     k_init_info<<<1, 32, 0, st>>>(info, A.cbounds);
     if (nt == 0) return cudaGetLastError();
@@ -469,13 +776,20 @@ cudaError_t gpu_build_binary(const float4 *vpos, uint32_t nv, const uint4 *tris,
     if (e == cudaSuccess) e = cudaMemsetAsync(A.parent_leaf, 0xff, (size_t)nt * 4, st);
     if (e == cudaSuccess && links) e = cudaMemsetAsync(links, 0xff, (size_t)nt * 4, st);
     if (e != cudaSuccess) return e;
-    if (nt > 1)
+    const uint32_t *order = A.vals_b;  // primitives in leaf order
+    if (ploc) {
+        e = ploc_tree(A, (int)nt, st);
+        if (e != cudaSuccess) return e;
+        k_ploc_report<<<1, 1, 0, st>>>(A.ps, info);
+        order = A.order2;
+    } else if (nt > 1) {
         k_radix_tree<<<blocks_for(nt - 1), kThreads, 0, st>>>(A.keys_b, (int)nt, A.children, A.range,
                                                               A.parent_inner, A.parent_leaf);
-    k_bottom_up<<<nb, kThreads, 0, st>>>(A.lo, A.hi, A.vals_b, (int)nt, max_leaf, A.children, A.range,
+    }
+    k_bottom_up<<<nb, kThreads, 0, st>>>(A.lo, A.hi, order, (int)nt, max_leaf, A.children, A.range,
                                          A.parent_inner, A.parent_leaf, A.slots, A.visits, A.collapsed, nodes,
                                          info);
-    k_records<<<nb, kThreads, 0, st>>>(vpos, tris, A.vals_b, nt, nv, records);
+    k_records<<<nb, kThreads, 0, st>>>(vpos, tris, order, nt, nv, records);
     if (nt > 1) {
         k_wide_flags<<<nb, kThreads, 0, st>>>((int)nt, A.collapsed, A.parent_inner, nodes, A.flag, links, info);
         cb = A.cub_bytes;

@@ -21,17 +21,22 @@ enum gpu_build_info : int {
 };
 enum : int { GB_ERR_INDEX = 1, GB_ERR_DEPTH = 2, GB_ERR_TREE = 4 };
 
-// Scratch bytes for scenes of up to `max_tris` triangles.
-size_t gpu_build_scratch_bytes(uint32_t max_tris);
+// How the binary tree over the Morton-sorted triangles is formed: the radix tree of the codes
+// (linear BVH), or agglomerative clustering in Morton order (PLOC).
+enum : int { GB_METHOD_LBVH = 0, GB_METHOD_PLOC = 1 };
+
+// Scratch bytes for scenes of up to `max_tris` triangles built with `method`.
+size_t gpu_build_scratch_bytes(uint32_t max_tris, int method);
 
 // Phase 1 of one scene: binary nodes (max(nt - 1, 1) x 64 B), records (nt x 48 B), for every
 // binary node its 4-wide node index (wide_index, nt ints, -1 for none) and, if `links` is not
 // null, its refit link (nt ints: (parent << 1) | side for the inner nodes in the tree, -1
-// elsewhere). `info` (int32[8], device) receives the fields above. Stream-ordered; nothing is
-// read back.
+// elsewhere). `info` (int32[8], device) receives the fields above. Stream-ordered; the LBVH
+// method reads nothing back, PLOC reads its cluster count back every 8 iterations (so that it
+// stops launching once the tree is finished).
 cudaError_t gpu_build_binary(const float4 *vpos, uint32_t nv, const uint4 *tris, uint32_t nt, int max_leaf,
                              void *scratch, size_t scratch_bytes, float4 *nodes, float4 *records,
-                             int32_t *wide_index, int32_t *links, int32_t *info, cudaStream_t st);
+                             int32_t *wide_index, int32_t *links, int32_t *info, int method, cudaStream_t st);
 
 // Phase 2: the 4-wide nodes (info[GB_WIDE_NODES] x 128 B) from the binary nodes of phase 1.
 cudaError_t gpu_build_wide(const float4 *nodes, const int32_t *wide_index, uint32_t nt, float4 *nodes4,

@@ -1,5 +1,6 @@
 """GPU BVH construction (grt_build_device, grt_build_scenes_device): trees built on the GPU
-from device arrays, traced by every tracer, against the oracle on the reference's tree.
+from device arrays, with both tree builders (PLOC clustering and the Morton radix tree), traced
+by every tracer, against the oracle on the reference's tree.
 Closest hits may differ from the reference only as near-ties (another tree visits triangles in
 another order); any-hit answers are equal. Also: degenerate inputs, errors, and the statistics
 of the trees."""
@@ -49,9 +50,16 @@ def oracles(orc, golden_scenes):
     return {name: orc.OracleBVH(v, t) for name, (v, t, _, _) in golden_scenes.items()}
 
 
+@pytest.fixture(params=["ploc", "lbvh"])
+def builder(request, gpu_tracer):
+    gpu_tracer.set_device_builder(request.param)
+    yield request.param
+    gpu_tracer.set_device_builder("default")
+
+
 @pytest.mark.parametrize("max_tris", [1, 4, 16])
 @pytest.mark.parametrize("name", GOLDEN_CASES)
-def test_gpu_tree_hits_match_oracle(gpu_tracer, golden_scenes, oracles, name, max_tris):
+def test_gpu_tree_hits_match_oracle(gpu_tracer, golden_scenes, oracles, name, max_tris, builder):
     v, t, rays, any_rays = golden_scenes[name]
     info = gpu_tracer.build_device(_dev(v, np.float32), _dev(t, np.uint32), max_tris=max_tris)
     assert info["tri_records"] == t.shape[0] and info["depth"] <= 64
@@ -65,7 +73,7 @@ def test_gpu_tree_hits_match_oracle(gpu_tracer, golden_scenes, oracles, name, ma
     gpu_tracer.select("while-while")
 
 
-def test_gpu_tree_spheres_full_frame(gpu_tracer, wl, orc):
+def test_gpu_tree_spheres_full_frame(gpu_tracer, wl, orc, builder):
     sc, rays = wl.spheres_primary(res=1024)
     info = gpu_tracer.build_device(_dev(sc.vpos, np.float32), _dev(sc.tris, np.uint32), max_tris=4)
     assert info["inner_nodes"] > 0
@@ -76,7 +84,7 @@ def test_gpu_tree_spheres_full_frame(gpu_tracer, wl, orc):
     gpu_tracer.select("while-while")
 
 
-def test_gpu_tree_degenerate_inputs(gpu_tracer, api):
+def test_gpu_tree_degenerate_inputs(gpu_tracer, api, builder):
     import torch
     ray = np.array([[0.2, 0.2, 1.0, 1e-4, 0.0, 0.0, -1.0, 3e38]], np.float32)
     tri = np.array([[0, 1, 2, 7]], np.uint32)
@@ -117,13 +125,18 @@ def test_gpu_tree_errors(gpu_tracer, api):
         gpu_tracer.export_bvh()
     with pytest.raises(ValueError):
         gpu_tracer.build_device(torch.zeros((3, 3), device="cuda"), _dev(np.array([[0, 1, 2, 0]]), np.uint32))
+    with pytest.raises(KeyError):
+        gpu_tracer.set_device_builder("octree")
+    assert api.lib().grt_set_device_builder(gpu_tracer.ctx, 7) == 1  # invalid argument
 
 
+@pytest.mark.parametrize("set_builder", ["default", "ploc"])
 @pytest.mark.parametrize("tracer", ["persistent-while-while", "persistent-speculative-while-while",
                                     "persistent-bvh4-speculative-while-while"])
-def test_gpu_scene_set_matches_oracle(api, orc, wl, tracer):
+def test_gpu_scene_set_matches_oracle(api, orc, wl, tracer, set_builder):
     import torch
     rt = api.BatchRayTracer(0)
+    rt.set_device_builder(set_builder)
     scenes, rays, oracles = [], [], []
     for i in range(10):
         ntri = wl.log_uniform(93, 2 * i, 1024, 1 << 16)
