@@ -178,6 +178,7 @@ inline float length(const vec2 &a) { return std::sqrt(dot(a, a)); }
 inline vec3 normalize(const vec3 &a) { return a * (1.0f / std::sqrt(dot(a, a))); }
 inline vec2 normalize(const vec2 &a) { return a * (1.0f / std::sqrt(dot(a, a))); }
 inline vec3 abs(const vec3 &a) { return vec3(std::fabs(a.x), std::fabs(a.y), std::fabs(a.z)); }
+inline float abs(float x) { return std::fabs(x); }
 inline vec2 floor(const vec2 &a) { return vec2(std::floor(a.x), std::floor(a.y)); }
 inline float radians(float d) { return d * float(M_PI / 180.0); }
 inline vec3 fract(const vec3 &a) { return vec3(a.x - std::floor(a.x), a.y - std::floor(a.y), a.z - std::floor(a.z)); }

@@ -66,6 +66,14 @@ void ptm_tan2_theta(const float *cos_t, uint32_t n, float *out) {
     for (uint32_t i = 0; i < n; ++i) out[i] = dl::tan2_theta(cos_t[i]);
 }
 
+void ptm_ggx_d(const float *cos_t, const float *roughness, uint32_t n, float *out) {
+    for (uint32_t i = 0; i < n; ++i) out[i] = dl::ggx_d(cos_t[i], roughness[i]);
+}
+
+void ptm_ggx_g1(const float *cos_t, const float *roughness, uint32_t n, float *out) {
+    for (uint32_t i = 0; i < n; ++i) out[i] = dl::ggx_g1(cos_t[i], roughness[i]);
+}
+
 void ptm_luma(const float *rgb3, uint32_t n, float *out) {
     for (uint32_t i = 0; i < n; ++i) out[i] = dl::luma({rgb3[3 * i], rgb3[3 * i + 1], rgb3[3 * i + 2]});
 }

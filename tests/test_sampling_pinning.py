@@ -8,7 +8,8 @@ reference's functions compiled from its sources (oracle/_ref/libref_sampling.so)
 
 * bit for bit: the PCG32 stream (rng_pcg, libgi/random.h:59-96), align and
   flip_normals_to_ray (libgi/util.h:212-225), fresnel_dielectric and tan2_theta
-  (libgi/util.h:91-106, 141-160), luma (libgi/color.h:4-6);
+  (libgi/util.h:91-106, 141-160), luma (libgi/color.h:4-6), the GGX terms ggx_d and ggx_g1
+  (libgi/material.cpp:237-260, the same code as rt/cuda/bounce.cu:298-313);
 * within a stated bound: sin and cos of 2 pi u, which the library evaluates with its own
   polynomial (sincos_turns) where the reference calls sinf / cosf of a float angle, and through it
   the cosine- and uniform-hemisphere samples (libgi/sampling.h:13-36); the pinhole camera rays,
@@ -124,6 +125,17 @@ def test_fresnel_tan2_luma_bit_exact(ptm, ref):
     ptm.ptm_luma(_p(rgb), U32(10000), _p(a))
     ref.refs_luma(_p(rgb), U32(10000), _p(b))
     assert (_bits(a) == _bits(b)).all()
+
+
+def test_ggx_terms_bit_exact(ptm, ref):
+    g = np.random.default_rng(4)
+    cos = np.concatenate([g.uniform(-0.2, 1.0, 200_000), [0.0, -0.0, 1.0, 1e-30, 1e-20, 0.5]]).astype(np.float32)
+    rough = np.concatenate([g.uniform(0.0, 1.0, 200_000), [0.1, 0.0, 1.0, 0.5, 0.05, 0.0]]).astype(np.float32)
+    for name in ("ggx_d", "ggx_g1"):
+        a, b = np.zeros_like(cos), np.zeros_like(cos)
+        getattr(ptm, "ptm_" + name)(_p(cos), _p(rough), U32(cos.size), _p(a))
+        getattr(ref, "refs_" + name)(_p(cos), _p(rough), U32(cos.size), _p(b))
+        assert (_bits(a) == _bits(b)).all(), name
 
 
 def test_hemisphere_samples_within_bound_of_reference(ptm, ref):
