@@ -628,7 +628,7 @@ def run_gb300(args):
                 "form": "host copies double-buffered across steps on two copy streams",
                 "serial": {"value": round(e2e_value, 1), "ms_per_step": round(statistics.mean(e2e_ms), 4),
                            "form": "copy in, step, copy out on one stream"}},
-        "gpu_launches": 5 * args.steps,
+        "gpu_launches": 6 * args.steps,
         "roofline": roofline,
         "clocks": clk,
         "build_ms": round(step.build_info["build_ms"], 1),

@@ -33,7 +33,7 @@ pt_scene scene_for_shading(grt_ctx *c) {
 
 // Carves the arena: [hit list | compaction counts | counters (64 words) | wavefront buffers].
 struct pt_layout {
-    size_t hit_list, compact, counters, states, queue0, queue1, rays0, rays1, hits, total;
+    size_t hit_list, compact, counters, states, queue0, queue1, rays0, rays1, hits, starts, total;
 };
 
 pt_layout layout_for(uint32_t n_primary, uint32_t n_paths, bool wavefront) {
@@ -58,6 +58,9 @@ pt_layout layout_for(uint32_t n_primary, uint32_t n_paths, bool wavefront) {
         off = align256(off + (size_t)n_paths * 32);
         L.hits = off;
         off = align256(off + (size_t)n_paths * 16);
+    } else {
+        L.starts = off;
+        off = align256(off + (size_t)n_paths * 32);
     }
     L.total = off;
     return L;
@@ -80,7 +83,7 @@ cudaError_t enqueue_pathtrace(grt_ctx *c, const grt_pt_params &p, const pt_param
     if (e != cudaSuccess) return e;
     if (p.mode == GRT_PT_FUSED)
         return launch_fused(scene_for(c), ps, pp, (const float4 *)prim_rays, prim_hits, hit_list, n_list, n_paths, results,
-                            bounce_hits, lp, c->d_err, c->d_counter, st);
+                            bounce_hits, lp, c->d_err, c->d_counter, at<float4>(c, L.starts), st);
     uint32_t *queue[2] = {at<uint32_t>(c, L.queue0), at<uint32_t>(c, L.queue1)};
     float4 *rays[2] = {at<float4>(c, L.rays0), at<float4>(c, L.rays1)};
     grt_hit *hits = at<grt_hit>(c, L.hits);

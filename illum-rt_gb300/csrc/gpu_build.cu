@@ -487,6 +487,130 @@ __global__ void __launch_bounds__(kThreads) k_bottom_up(const float4 *__restrict
     atomicOr(info + GB_ERR, GB_ERR_DEPTH);
 }
 
+// ---- 4b. depth-first layout of the inner nodes ----------------------------------------------
+//
+// The radix tree numbers inner nodes by split position and PLOC by creation; neither keeps a
+// node near the child a ray visits next. The host flattener keeps the reference's preorder (a
+// parent followed by its left subtree, so the left child shares the parent's 128-byte line
+// pair), and these passes give GPU-built trees the same layout: which inner nodes are in the
+// final tree (no collapsed ancestor), the inner-node count of every subtree (bottom-up, second
+// arrival continues), every node's preorder position (the sum, over its ancestors, of one plus
+// the left sibling subtree's count where the path turns right), and the scatter of the nodes
+// to their positions with their child references renumbered.
+
+__device__ __forceinline__ int child_ref_of(const float4 *nodes, int i, int side) {
+    return __float_as_int(nodes[4 * (size_t)i + 2 * side + 1].z);
+}
+
+__global__ void __launch_bounds__(kThreads) k_reach(int n, const uint8_t *__restrict__ collapsed,
+                                                    const int32_t *__restrict__ parent_inner, int32_t *reach,
+                                                    int32_t *info) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int r = 0;
+    if (i < n - 1 && !collapsed[i]) {
+        r = 1;
+        int q = i, climb = 0;
+        for (; q != 0 && climb < kMaxClimb; ++climb) {
+            q = parent_inner[q];
+            if (q < 0 || q >= n - 1) {
+                atomicOr(info + GB_ERR, GB_ERR_TREE);
+                r = 0;
+                break;
+            }
+            if (collapsed[q]) {
+                r = 0;
+                break;
+            }
+        }
+        if (climb >= kMaxClimb) {
+            atomicOr(info + GB_ERR, GB_ERR_DEPTH);
+            r = 0;
+        }
+    }
+    reach[i] = r;
+}
+
+// Inner-node count of every final subtree; threads start at the final tree's bottom inner nodes.
+__global__ void __launch_bounds__(kThreads) k_icount(int n, const float4 *__restrict__ nodes,
+                                                     const int32_t *__restrict__ parent_inner,
+                                                     const int32_t *__restrict__ reach, uint32_t *arrive,
+                                                     int32_t *icount, int32_t *info) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1 || !reach[i]) return;
+    if (child_ref_of(nodes, i, 0) >= 0 || child_ref_of(nodes, i, 1) >= 0) return;
+    icount[i] = 1;
+    int v = i;
+    for (int climb = 0; climb < kMaxClimb; ++climb) {
+        if (v == 0) return;
+        const int p = parent_inner[v];
+        if (p < 0 || p >= n - 1) {
+            atomicOr(info + GB_ERR, GB_ERR_TREE);
+            return;
+        }
+        const int l = child_ref_of(nodes, p, 0), r = child_ref_of(nodes, p, 1);
+        if (l >= n - 1 || r >= n - 1) {
+            atomicOr(info + GB_ERR, GB_ERR_TREE);
+            return;
+        }
+        __threadfence();
+        if (l >= 0 && r >= 0 && atomicAdd(arrive + p, 1u) == 0u) return;  // the sibling's thread continues
+        __threadfence();
+        icount[p] = 1 + (l >= 0 ? __ldcg(icount + l) : 0) + (r >= 0 ? __ldcg(icount + r) : 0);
+        v = p;
+    }
+    atomicOr(info + GB_ERR, GB_ERR_DEPTH);
+}
+
+__global__ void __launch_bounds__(kThreads) k_dfs_pos(int n, const float4 *__restrict__ nodes,
+                                                      const int32_t *__restrict__ parent_inner,
+                                                      const int32_t *__restrict__ reach,
+                                                      const int32_t *__restrict__ icount, int32_t *pos,
+                                                      int32_t *info) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1 || !reach[i]) return;
+    int s = 0, v = i, climb = 0;
+    for (; v != 0 && climb < kMaxClimb; ++climb) {
+        const int p = parent_inner[v];
+        if (p < 0 || p >= n - 1) {
+            atomicOr(info + GB_ERR, GB_ERR_TREE);
+            return;
+        }
+        const int l = child_ref_of(nodes, p, 0);
+        s += 1 + ((l >= 0 && l != v) ? icount[l] : 0);
+        v = p;
+    }
+    if (v != 0 || s >= n - 1) {
+        atomicOr(info + GB_ERR, GB_ERR_TREE);
+        return;
+    }
+    pos[i] = s;
+}
+
+// The final tree's inner nodes at their preorder positions, inner child references renumbered;
+// parents and collapse flags in the new numbering (positions beyond the tree stay collapsed).
+__global__ void __launch_bounds__(kThreads) k_relayout(int n, const float4 *__restrict__ nodes,
+                                                       const int32_t *__restrict__ parent_inner,
+                                                       const int32_t *__restrict__ reach,
+                                                       const int32_t *__restrict__ pos, float4 *out_nodes,
+                                                       int32_t *out_parent, uint8_t *out_collapsed) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1 || !reach[i]) return;
+    const int j = pos[i];
+    if (j < 0 || j >= n - 1) return;
+    const float4 *src = nodes + 4 * (size_t)i;
+    float4 *dst = out_nodes + 4 * (size_t)j;
+    for (int side = 0; side < 2; ++side) {
+        float4 xy = src[2 * side], z = src[2 * side + 1];
+        const int c = __float_as_int(z.z);
+        if (c >= 0 && c < n - 1) z.z = __int_as_float(pos[c]);
+        dst[2 * side] = xy;
+        dst[2 * side + 1] = z;
+    }
+    out_parent[j] = i == 0 ? -1 : pos[parent_inner[i]];
+    out_collapsed[j] = 0;
+}
+
 // records in sorted order: v0 + original id, v0 - v1 + material, v0 - v2
 __global__ void __launch_bounds__(kThreads) k_records(const float4 *__restrict__ vpos, const uint4 *__restrict__ tris,
                                                       const uint32_t *__restrict__ order, uint32_t n, uint32_t nv,
@@ -789,6 +913,27 @@ cudaError_t gpu_build_binary(const float4 *vpos, uint32_t nv, const uint4 *tris,
     k_bottom_up<<<nb, kThreads, 0, st>>>(A.lo, A.hi, order, (int)nt, max_leaf, A.children, A.range,
                                          A.parent_inner, A.parent_leaf, A.slots, A.visits, A.collapsed, nodes,
                                          info);
+    if (nt > 1) {
+        // depth-first layout; the bottom-up pass's slots and the sort's key and value arrays are
+        // free now and hold the new nodes, positions, parents and flags
+        float4 *tmp_nodes = (float4 *)A.slots;
+        int32_t *reach = A.flag, *icount = A.excl, *pos = (int32_t *)A.keys_a, *new_parent = (int32_t *)A.vals_a;
+        uint8_t *new_collapsed = (uint8_t *)A.keys_b;
+        e = cudaMemsetAsync(A.visits, 0, (size_t)nt * 4, st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(new_collapsed, 1, (size_t)nt, st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(new_parent, 0xff, (size_t)nt * 4, st);
+        if (e != cudaSuccess) return e;
+        k_reach<<<nb, kThreads, 0, st>>>((int)nt, A.collapsed, A.parent_inner, reach, info);
+        k_icount<<<nb, kThreads, 0, st>>>((int)nt, nodes, A.parent_inner, reach, A.visits, icount, info);
+        k_dfs_pos<<<nb, kThreads, 0, st>>>((int)nt, nodes, A.parent_inner, reach, icount, pos, info);
+        k_relayout<<<nb, kThreads, 0, st>>>((int)nt, nodes, A.parent_inner, reach, pos, tmp_nodes, new_parent,
+                                            new_collapsed);
+        e = cudaMemcpyAsync(nodes, tmp_nodes, (size_t)(nt - 1) * 64, cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(A.parent_inner, new_parent, (size_t)nt * 4, cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(A.collapsed, new_collapsed, (size_t)nt, cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) return e;
+    }
     k_records<<<nb, kThreads, 0, st>>>(vpos, tris, order, nt, nv, records);
     if (nt > 1) {
         k_wide_flags<<<nb, kThreads, 0, st>>>((int)nt, A.collapsed, A.parent_inner, nodes, A.flag, links, info);

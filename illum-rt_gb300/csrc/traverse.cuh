@@ -573,11 +573,14 @@ __device__ __forceinline__ void spec_node4(trav_t &s, const dev_scene &sc, const
 // postponed leaf use the closest hit from before that leaf, so the ray may visit nodes the
 // reference would have culled. A triangle found there can replace the reference's answer only
 // if its t lies within rounding of the culled box's entry distance: a near-tie.
-template <bool ANY, bool COUNT, bool WIDE = false, bool ALPHA = false>
+template <bool ANY, bool COUNT, bool WIDE = false, bool ALPHA = false, int VISITS = 0, int PEND = 0>
 __device__ __forceinline__ void trav_spec_iter(trav_t &s, bool active, bool plain, const dev_scene &sc,
                                                const ray_t &r, int *stk, int stride, int cap, const spec_cfg &cfg,
                                                unsigned *err) {
     const bool mine = active && !s.done;
+    // VISITS / PEND > 0: instances for the common values, whose loop the compiler unrolls and
+    // whose unused postponement slots it drops; 0: the values of `cfg`.
+    const int pend = PEND > 0 ? PEND : cfg.pend;
     // One node visit (or postponement of a reached leaf) of this lane, if it has one to make.
     auto visit = [&]() {
         if (mine && !s.done && s.more && s.cur >= 0) {
@@ -594,12 +597,12 @@ __device__ __forceinline__ void trav_spec_iter(trav_t &s, bool active, bool plai
                     spec_node<ANY, false>(s, sc, r, stk, stride, cap, err);
             }
         }
-        const bool slot = cfg.pend <= 1 ? s.pend == 0 : cfg.pend == 2 ? s.pend2 == 0 : s.pend3 == 0;
+        const bool slot = pend <= 1 ? s.pend == 0 : pend == 2 ? s.pend2 == 0 : s.pend3 == 0;
         if (mine && !s.done && s.more && s.cur < 0 && slot) {
             // postpone the leaf into the first free slot and go on with the next node
             if (s.pend == 0)
                 s.pend = s.cur;
-            else if (s.pend2 == 0)
+            else if (pend == 2 || s.pend2 == 0)
                 s.pend2 = s.cur;
             else
                 s.pend3 = s.cur;
@@ -619,10 +622,11 @@ __device__ __forceinline__ void trav_spec_iter(trav_t &s, bool active, bool plai
     // across calls, without a per-visit count.
     // At least one visit per vote: every pass then moves each searching lane on by a node or a
     // postponed leaf, so the loop ends (and `slots` reaches the step limit on a malformed tree).
-    const int visits = cfg.visits > 0 ? cfg.visits : 1;
+    const int visits = VISITS > 0 ? VISITS : (cfg.visits > 0 ? cfg.visits : 1);
     uint32_t slots = 0;
     for (;;) {
-        for (int v = 0; v < visits; ++v) visit();
+#pragma unroll
+        for (int v = 0; v < (VISITS > 0 ? VISITS : visits); ++v) visit();
         slots += (uint32_t)visits;
         const bool searching = mine && !s.done && s.more && s.pend == 0;
         if (__popc(__ballot_sync(0xffffffffu, searching)) <= cfg.exit || slots >= kStepLimit) break;
