@@ -188,7 +188,7 @@ grt_status grt_trace_multi(grt_ctx *c, const grt_ray_batch *batches, uint32_t co
     lp.refill_threshold = t.refill_threshold > 0 ? t.refill_threshold : 20;
     lp.refill_period = t.refill_period > 0 ? t.refill_period : 4;
     lp.grid_blocks =
-        (t.blocks_per_sm > 0 ? t.blocks_per_sm : multi_blocks_per_sm(lp.block_threads, lp.stack_entries, order)) *
+        (t.blocks_per_sm > 0 ? t.blocks_per_sm : multi_blocks_per_sm(lp.block_threads, lp.stack_entries, order, lp.spec)) *
         c->num_sms;
     e = launch_trace_multi((const dev_scene *)c->ms.d_table, (const multi_batch *)c->ms.d_batches, count,
                            (uint32_t)total, any_hit != 0, lp, c->d_err, c->d_counter, (cudaStream_t)stream);

@@ -197,7 +197,8 @@ grt_status grt_pathtrace(grt_ctx *c, const grt_pt_params *params, const float *p
     launch_params lp = lp_trace;
     lp.spec = tuned_spec(c->tuning, kSpecPaths);
     lp.grid_blocks = (c->tuning.blocks_per_sm > 0 ? c->tuning.blocks_per_sm
-                                                  : fused_blocks_per_sm(lp.block_threads, lp.stack_entries, lp.order, scene_for(c).alpha != nullptr)) *
+                                                  : fused_blocks_per_sm(lp.block_threads, lp.stack_entries, lp.order, scene_for(c).alpha != nullptr,
+                                                                      lp.spec)) *
                      c->num_sms;
     cudaStream_t st = (cudaStream_t)stream;
     if (!p.use_graph) {

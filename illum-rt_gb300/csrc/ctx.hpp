@@ -227,7 +227,8 @@ inline launch_params params_for(grt_ctx *c, bool any_hit) {
     if (kTracers[c->tracer].persistent) {
         int per_sm = t.blocks_per_sm > 0 ? t.blocks_per_sm
                                          : grt::persistent_blocks_per_sm(lp.block_threads, lp.stack_entries, any_hit,
-                                                                         lp.order, scene_for(c).alpha != nullptr);
+                                                                         lp.order, scene_for(c).alpha != nullptr,
+                                                                         lp.spec);
         lp.grid_blocks = per_sm * c->num_sms;
     }
     return lp;

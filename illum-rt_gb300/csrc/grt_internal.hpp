@@ -74,6 +74,19 @@ struct spec_cfg {
 inline bool spec_ok(const spec_cfg &c) {
     return c.pend >= 1 && c.pend <= 3 && c.exit >= 0 && c.exit <= 32 && c.visits >= 1 && c.visits <= 16;
 }
+// Kernel instances of the speculative order compiled for common (visits per vote, postponed
+// leaves) pairs, whose node loop the compiler unrolls and whose unused postponement slots it
+// drops (2 % off the fused path step on GB300 against the run-time form); instance 0 takes the
+// values at run time. fast_path_of picks the instance of a configuration.
+constexpr int kFastPaths = 5;
+constexpr int kFastVisits[kFastPaths] = {0, 5, 3, 3, 5};
+constexpr int kFastPend[kFastPaths] = {0, 2, 2, 3, 3};
+inline int fast_path_of(const spec_cfg &c) {
+    for (int f = 1; f < kFastPaths; ++f)
+        if (c.visits == kFastVisits[f] && c.pend == kFastPend[f]) return f;
+    return 0;
+}
+
 constexpr spec_cfg kSpecPaths = {2, 8, 5};       // fused path tracer
 constexpr spec_cfg kSpecDirect = {3, 2, 3};      // fused direct lighting
 constexpr spec_cfg kSpecTrace = {3, 1, 3};       // one-thread-per-ray batch traces
@@ -115,7 +128,9 @@ cudaError_t launch_trace_persistent(const dev_scene &sc, const float4 *rays, grt
 // before any launch, so that launches need no attribute calls and can be captured).
 cudaError_t prepare_trace_kernels();
 
-// Occupancy of the persistent kernel for a block size and stack size (blocks per SM).
-int persistent_blocks_per_sm(int block_threads, int stack_entries, bool any_hit, int order, bool alpha);
+// Occupancy of the persistent kernel for a block size and stack size (blocks per SM), of the
+// instance that a launch with speculative parameters `spec` runs.
+int persistent_blocks_per_sm(int block_threads, int stack_entries, bool any_hit, int order, bool alpha,
+                             const spec_cfg &spec);
 
 }  // namespace grt

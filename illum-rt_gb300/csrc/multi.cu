@@ -28,7 +28,7 @@ __device__ __forceinline__ uint32_t find_batch(const multi_batch *__restrict__ b
     return lo;
 }
 
-template <int ORDER, bool ANY>
+template <int ORDER, bool ANY, int FP = 0>
 __global__ void __launch_bounds__(256) k_trace_multi(const dev_scene *__restrict__ scenes,
                                                      const multi_batch *__restrict__ batches, uint32_t nbatch,
                                                      uint32_t total, unsigned *err, unsigned *counter,
@@ -83,7 +83,8 @@ __global__ void __launch_bounds__(256) k_trace_multi(const dev_scene *__restrict
         }
         for (int it = 1;; ++it) {
             if (SPEC)
-                trav_spec_iter<ANY, false, WIDE, false>(s, have, plain, sc, r, stk, stride, cap, spec, err);
+                trav_spec_iter<ANY, false, WIDE, false, kFastVisits[FP], kFastPend[FP]>(s, have, plain, sc, r, stk,
+                                                                                        stride, cap, spec, err);
             else if (have && plain)
                 trav_advance<ORDER, ANY, false, true>(s, sc, r, stk, stride, cap, err);
             else if (have)
@@ -100,13 +101,30 @@ __global__ void __launch_bounds__(256) k_trace_multi(const dev_scene *__restrict
     }
 }
 
+using multi_fn = void (*)(const dev_scene *, const multi_batch *, uint32_t, uint32_t, unsigned *, unsigned *, int, int,
+                          int, spec_cfg);
+
+// The scene-set kernel instance for fast-path instance `fp` (speculative order only).
+template <int ORDER, bool ANY> multi_fn multi_kernel_of(int fp) {
+    if (ORDER == SPECULATIVE) {
+        switch (fp) {
+            case 1: return k_trace_multi<ORDER, ANY, ORDER == SPECULATIVE ? 1 : 0>;
+            case 2: return k_trace_multi<ORDER, ANY, ORDER == SPECULATIVE ? 2 : 0>;
+            case 3: return k_trace_multi<ORDER, ANY, ORDER == SPECULATIVE ? 3 : 0>;
+            case 4: return k_trace_multi<ORDER, ANY, ORDER == SPECULATIVE ? 4 : 0>;
+            default: break;
+        }
+    }
+    return k_trace_multi<ORDER, ANY>;
+}
+
 template <int ORDER, bool ANY>
 cudaError_t multi_launch(const dev_scene *scenes, const multi_batch *batches, uint32_t nbatch, uint32_t total,
                          const launch_params &lp, unsigned *err, unsigned *counter, cudaStream_t st) {
     const size_t smem = (size_t)lp.stack_entries * lp.block_threads * sizeof(int);
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
-    k_trace_multi<ORDER, ANY><<<lp.grid_blocks, lp.block_threads, smem, st>>>(
+    multi_kernel_of<ORDER, ANY>(fast_path_of(lp.spec))<<<lp.grid_blocks, lp.block_threads, smem, st>>>(
         scenes, batches, nbatch, total, err, counter, lp.refill_threshold, lp.refill_period, lp.stack_entries, lp.spec);
     return cudaGetLastError();
 }
@@ -120,8 +138,11 @@ cudaError_t multi_any(bool any_hit, const dev_scene *scenes, const multi_batch *
 
 template <int ORDER> cudaError_t attrs(int bytes) {
     const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
-    cudaError_t e = cudaFuncSetAttribute(k_trace_multi<ORDER, false>, a, bytes);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_multi<ORDER, true>, a, bytes);
+    cudaError_t e = cudaSuccess;
+    for (int fp = 0; fp < kFastPaths && e == cudaSuccess; ++fp) {
+        e = cudaFuncSetAttribute(multi_kernel_of<ORDER, false>(fp), a, bytes);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(multi_kernel_of<ORDER, true>(fp), a, bytes);
+    }
     return e;
 }
 
@@ -150,13 +171,14 @@ cudaError_t prepare_multi_kernels() {
     return e;
 }
 
-int multi_blocks_per_sm(int block_threads, int stack_entries, int order) {
+int multi_blocks_per_sm(int block_threads, int stack_entries, int order, const spec_cfg &spec) {
     int blocks = 0;
     const size_t smem = (size_t)stack_entries * block_threads * sizeof(int);
-    const void *fn = order == WHILE_WHILE        ? (const void *)k_trace_multi<WHILE_WHILE, false>
-                     : order == SPECULATIVE      ? (const void *)k_trace_multi<SPECULATIVE, false>
-                     : order == WIDE_SPECULATIVE ? (const void *)k_trace_multi<WIDE_SPECULATIVE, false>
-                                                 : (const void *)k_trace_multi<IF_IF, false>;
+    const int fp = fast_path_of(spec);
+    const void *fn = order == WHILE_WHILE        ? (const void *)multi_kernel_of<WHILE_WHILE, false>(fp)
+                     : order == SPECULATIVE      ? (const void *)multi_kernel_of<SPECULATIVE, false>(fp)
+                     : order == WIDE_SPECULATIVE ? (const void *)multi_kernel_of<WIDE_SPECULATIVE, false>(fp)
+                                                 : (const void *)multi_kernel_of<IF_IF, false>(fp);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, block_threads, smem) != cudaSuccess) return 1;
     return blocks > 0 ? blocks : 1;
 }

@@ -18,6 +18,6 @@ cudaError_t launch_trace_multi(const dev_scene *scenes, const multi_batch *batch
                                bool any_hit, const launch_params &lp, unsigned *err, unsigned *counter,
                                cudaStream_t st);
 cudaError_t prepare_multi_kernels();
-int multi_blocks_per_sm(int block_threads, int stack_entries, int order);
+int multi_blocks_per_sm(int block_threads, int stack_entries, int order, const spec_cfg &spec);
 
 }  // namespace grt

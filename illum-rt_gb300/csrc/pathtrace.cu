@@ -403,7 +403,7 @@ __global__ void k_pt_starts(pt_scene ps, pt_params_dev pp, const float4 *__restr
 // lanes shade their hit together (Russian roulette, next bounce direction) and go back to
 // traversal, or finish their path and take a new one from the global path counter. Shading and
 // path set-up therefore run warp-coherently instead of one lane at a time.
-template <int ORDER, bool ALPHA>
+template <int ORDER, bool ALPHA, int FP = 0>
 __global__ void __launch_bounds__(256) k_pt_fused(dev_scene sc, pt_scene ps, pt_params_dev pp,
                                                   const float4 *__restrict__ prim_rays,
                                                   const grt_hit *__restrict__ prim_hits,
@@ -489,7 +489,8 @@ __global__ void __launch_bounds__(256) k_pt_fused(dev_scene sc, pt_scene ps, pt_
         // traversal phase
         for (int it = 1;; ++it) {
             if (SPEC)
-                trav_spec_iter<false, false, WIDE, ALPHA>(s, tracing, plain, sc, r, stk, stride, cap, spec, err);
+                trav_spec_iter<false, false, WIDE, ALPHA, kFastVisits[FP], kFastPend[FP]>(s, tracing, plain, sc, r, stk,
+                                                                                          stride, cap, spec, err);
             else if (tracing && plain)
                 trav_advance<ORDER, false, false, true, ALPHA>(s, sc, r, stk, stride, cap, err);
             else if (tracing)
@@ -506,13 +507,40 @@ __global__ void __launch_bounds__(256) k_pt_fused(dev_scene sc, pt_scene ps, pt_
     }
 }
 
+using fused_fn_t = void (*)(dev_scene, pt_scene, pt_params_dev, const float4 *, const grt_hit *, const uint32_t *,
+                           const uint32_t *, uint32_t, grt_path_result *, grt_hit *, unsigned *, unsigned *, int, int,
+                           int, spec_cfg, const float4 *);
+
+// The fused kernel instance for the loop order, alpha-aware tracing and fast-path instance `fp`
+// (the speculative order without alpha has the instances of kFastVisits / kFastPend).
+template <int ORDER> fused_fn_t fused_kernel_of(bool alpha, int fp) {
+    if (alpha) return k_pt_fused<ORDER, true>;
+    if (ORDER == SPECULATIVE) {
+        switch (fp) {
+            case 1: return k_pt_fused<ORDER, false, ORDER == SPECULATIVE ? 1 : 0>;
+            case 2: return k_pt_fused<ORDER, false, ORDER == SPECULATIVE ? 2 : 0>;
+            case 3: return k_pt_fused<ORDER, false, ORDER == SPECULATIVE ? 3 : 0>;
+            case 4: return k_pt_fused<ORDER, false, ORDER == SPECULATIVE ? 4 : 0>;
+            default: break;
+        }
+    }
+    return k_pt_fused<ORDER, false>;
+}
+
+fused_fn_t fused_kernel(int order, bool alpha, int fp) {
+    return order == WHILE_WHILE        ? fused_kernel_of<WHILE_WHILE>(alpha, fp)
+           : order == SPECULATIVE      ? fused_kernel_of<SPECULATIVE>(alpha, fp)
+           : order == WIDE_SPECULATIVE ? fused_kernel_of<WIDE_SPECULATIVE>(alpha, fp)
+                                       : fused_kernel_of<IF_IF>(alpha, fp);
+}
+
 template <int ORDER>
 cudaError_t fused_launch(const dev_scene &sc, const pt_scene &ps, const pt_params_dev &pp, const float4 *prim_rays,
                          const grt_hit *prim_hits, const uint32_t *hit_list, const uint32_t *n_list, uint32_t n_paths,
                          grt_path_result *results, grt_hit *bounce_hits, const launch_params &lp, unsigned *err,
                          unsigned *counter, float4 *starts, cudaStream_t st) {
     const size_t smem = (size_t)(lp.stack_entries * sizeof(int) + kPathSlotBytes) * lp.block_threads;
-    auto kern = sc.alpha ? k_pt_fused<ORDER, true> : k_pt_fused<ORDER, false>;
+    const fused_fn_t kern = fused_kernel_of<ORDER>(sc.alpha != nullptr, fast_path_of(lp.spec));
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
     k_pt_starts<<<(n_paths + 255) / 256, 256, 0, st>>>(ps, pp, prim_rays, prim_hits, hit_list, n_list, n_paths, starts);
@@ -583,27 +611,21 @@ cudaError_t launch_fused(const dev_scene &sc, const pt_scene &ps, const pt_param
              st);
 }
 
-template <bool ALPHA> const void *fused_fn(int order) {
-    return order == WHILE_WHILE        ? (const void *)k_pt_fused<WHILE_WHILE, ALPHA>
-           : order == SPECULATIVE      ? (const void *)k_pt_fused<SPECULATIVE, ALPHA>
-           : order == WIDE_SPECULATIVE ? (const void *)k_pt_fused<WIDE_SPECULATIVE, ALPHA>
-                                       : (const void *)k_pt_fused<IF_IF, ALPHA>;
-}
-
 cudaError_t prepare_pt_kernels() {
     const int bytes = (kStackLarge * (int)sizeof(int) + kPathSlotBytes) * 256;
     for (int order : {(int)IF_IF, (int)WHILE_WHILE, (int)SPECULATIVE, (int)WIDE_SPECULATIVE})
-        for (const void *f : {fused_fn<false>(order), fused_fn<true>(order)}) {
+        for (int fp = 0; fp <= kFastPaths; ++fp) {  // fp == kFastPaths: the alpha-aware instance
+            const void *f = (const void *)fused_kernel(order, fp == kFastPaths, fp == kFastPaths ? 0 : fp);
             cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
             if (e != cudaSuccess) return e;
         }
     return cudaSuccess;
 }
 
-int fused_blocks_per_sm(int block_threads, int stack_entries, int order, bool alpha) {
+int fused_blocks_per_sm(int block_threads, int stack_entries, int order, bool alpha, const spec_cfg &spec) {
     int blocks = 0;
     const size_t smem = (size_t)(stack_entries * sizeof(int) + kPathSlotBytes) * block_threads;
-    const void *fn = alpha ? fused_fn<true>(order) : fused_fn<false>(order);
+    const void *fn = (const void *)fused_kernel(order, alpha, alpha ? 0 : fast_path_of(spec));
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, block_threads, smem) != cudaSuccess) return 1;
     return blocks > 0 ? blocks : 1;
 }

@@ -42,7 +42,7 @@ cudaError_t launch_fused(const dev_scene &sc, const pt_scene &ps, const pt_param
                          const grt_hit *prim_hits, const uint32_t *hit_list, const uint32_t *n_list, uint32_t n_paths,
                          grt_path_result *results, grt_hit *bounce_hits, const launch_params &lp, unsigned *err,
                          unsigned *counter, float4 *starts, cudaStream_t st);
-int fused_blocks_per_sm(int block_threads, int stack_entries, int order, bool alpha);
+int fused_blocks_per_sm(int block_threads, int stack_entries, int order, bool alpha, const spec_cfg &spec);
 // Raises the dynamic shared-memory limit of the path-tracing kernels (once per device).
 cudaError_t prepare_pt_kernels();
 

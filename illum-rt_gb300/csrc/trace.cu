@@ -30,7 +30,7 @@ constexpr int plain_min_blocks() {
     return ORDER == IF_IF ? 5 : ORDER == WIDE_SPECULATIVE ? 1 : 4;
 }
 
-template <int ORDER, bool ANY, bool COUNT, bool ALPHA>
+template <int ORDER, bool ANY, bool COUNT, bool ALPHA, int FP = 0>
 __global__ void __launch_bounds__(256, plain_min_blocks<ORDER>()) k_trace_plain(const float4 *__restrict__ rays, grt_hit *__restrict__ hits,
                                                      uint32_t n, const uint32_t *__restrict__ n_dev, dev_scene sc,
                                                      unsigned *err, unsigned long long *counters, int cap,
@@ -51,7 +51,8 @@ __global__ void __launch_bounds__(256, plain_min_blocks<ORDER>()) k_trace_plain(
     const bool plain = active && sc.finite && ray_is_plain(r);
     if (SPEC) {  // the whole warp stays in the loop until its last ray ends
         while (__any_sync(kFull, active && !s.done))
-            trav_spec_iter<ANY, COUNT, WIDE, ALPHA>(s, active, plain, sc, r, stk, stride, cap, spec, err);
+            trav_spec_iter<ANY, COUNT, WIDE, ALPHA, kFastVisits[FP], kFastPend[FP]>(s, active, plain, sc, r, stk,
+                                                                                      stride, cap, spec, err);
         if (!active) return;
     } else if (plain) {  // one loop per slab variant: the choice is made once per ray
         while (!s.done) trav_advance<ORDER, ANY, COUNT, true, ALPHA>(s, sc, r, stk, stride, cap, err);
@@ -66,7 +67,7 @@ __global__ void __launch_bounds__(256, plain_min_blocks<ORDER>()) k_trace_plain(
     }
 }
 
-template <int ORDER, bool ANY, bool ALPHA>
+template <int ORDER, bool ANY, bool ALPHA, int FP = 0>
 __global__ void __launch_bounds__(256) k_trace_persistent(const float4 *__restrict__ rays, grt_hit *__restrict__ hits,
                                                           uint32_t n, dev_scene sc, unsigned *err,
                                                           unsigned *counter, int refill_threshold, int refill_period,
@@ -116,7 +117,8 @@ __global__ void __launch_bounds__(256) k_trace_persistent(const float4 *__restri
         // traverse; every `refill_period` iterations the warp counts its busy lanes
         for (int it = 1;; ++it) {
             if (SPEC)
-                trav_spec_iter<ANY, false, WIDE, ALPHA>(s, have, plain, sc, r, stk, stride, cap, spec, err);
+                trav_spec_iter<ANY, false, WIDE, ALPHA, kFastVisits[FP], kFastPend[FP]>(s, have, plain, sc, r, stk,
+                                                                                        stride, cap, spec, err);
             else if (have && plain)
                 trav_advance<ORDER, ANY, false, true, ALPHA>(s, sc, r, stk, stride, cap, err);
             else if (have)
@@ -149,10 +151,31 @@ cudaError_t plain_launch(const dev_scene &sc, const float4 *rays, grt_hit *hits,
     else if (sc.alpha)
         k_trace_plain<ORDER, ANY, false, true><<<blocks, bt, smem, st>>>(rays, hits, n, n_dev, sc, err, nullptr, cap,
                                                                          lp.spec);
+    else if (ORDER == SPECULATIVE && fast_path_of(lp.spec) == 3)  // the one-thread-per-ray default
+        k_trace_plain<ORDER, ANY, false, false, ORDER == SPECULATIVE ? 3 : 0><<<blocks, bt, smem, st>>>(
+            rays, hits, n, n_dev, sc, err, nullptr, cap, lp.spec);
     else
         k_trace_plain<ORDER, ANY, false, false><<<blocks, bt, smem, st>>>(rays, hits, n, n_dev, sc, err, nullptr, cap,
                                                                           lp.spec);
     return cudaGetLastError();
+}
+
+// The persistent kernel instance for alpha-aware tracing or fast-path instance `fp` (the
+// speculative order only has instances beyond 0).
+using persistent_fn = void (*)(const float4 *, grt_hit *, uint32_t, dev_scene, unsigned *, unsigned *, int, int, int,
+                               spec_cfg);
+template <int ORDER, bool ANY> persistent_fn persistent_kernel_of(bool alpha, int fp) {
+    if (alpha) return k_trace_persistent<ORDER, ANY, true>;
+    if (ORDER == SPECULATIVE) {
+        switch (fp) {
+            case 1: return k_trace_persistent<ORDER, ANY, false, ORDER == SPECULATIVE ? 1 : 0>;
+            case 2: return k_trace_persistent<ORDER, ANY, false, ORDER == SPECULATIVE ? 2 : 0>;
+            case 3: return k_trace_persistent<ORDER, ANY, false, ORDER == SPECULATIVE ? 3 : 0>;
+            case 4: return k_trace_persistent<ORDER, ANY, false, ORDER == SPECULATIVE ? 4 : 0>;
+            default: break;
+        }
+    }
+    return k_trace_persistent<ORDER, ANY, false>;
 }
 
 template <int ORDER, bool ANY>
@@ -162,12 +185,9 @@ cudaError_t persistent_launch(const dev_scene &sc, const float4 *rays, grt_hit *
     const size_t smem = (size_t)lp.stack_entries * bt * sizeof(int);
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
-    if (sc.alpha)
-        k_trace_persistent<ORDER, ANY, true><<<lp.grid_blocks, bt, smem, st>>>(
-            rays, hits, n, sc, err, counter, lp.refill_threshold, lp.refill_period, lp.stack_entries, lp.spec);
-    else
-        k_trace_persistent<ORDER, ANY, false><<<lp.grid_blocks, bt, smem, st>>>(
-            rays, hits, n, sc, err, counter, lp.refill_threshold, lp.refill_period, lp.stack_entries, lp.spec);
+    const int fp = (ORDER == SPECULATIVE && !sc.alpha) ? fast_path_of(lp.spec) : 0;
+    persistent_kernel_of<ORDER, ANY>(sc.alpha != nullptr, fp)<<<lp.grid_blocks, bt, smem, st>>>(
+        rays, hits, n, sc, err, counter, lp.refill_threshold, lp.refill_period, lp.stack_entries, lp.spec);
     return cudaGetLastError();
 }
 
@@ -194,18 +214,19 @@ template <int O, bool A> struct attr_f {
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_plain<O, A, true, false>, a, bytes);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_plain<O, A, false, true>, a, bytes);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_plain<O, A, true, true>, a, bytes);
-        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_persistent<O, A, false>, a, bytes);
-        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_persistent<O, A, true>, a, bytes);
+        if (e == cudaSuccess && O == SPECULATIVE)
+            e = cudaFuncSetAttribute(k_trace_plain<O, A, false, false, O == SPECULATIVE ? 3 : 0>, a, bytes);
+        for (int fp = 0; fp < kFastPaths && e == cudaSuccess; ++fp)
+            e = cudaFuncSetAttribute(persistent_kernel_of<O, A>(false, fp), a, bytes);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(persistent_kernel_of<O, A>(true, 0), a, bytes);
         return e;
     }
 };
 template <int O, bool A> struct occupancy_f {
-    static cudaError_t run(int block_threads, int stack_entries, bool alpha, int *blocks) {
+    static cudaError_t run(int block_threads, int stack_entries, bool alpha, int fp, int *blocks) {
         const size_t smem = (size_t)stack_entries * block_threads * sizeof(int);
-        return alpha ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_trace_persistent<O, A, true>,
-                                                                     block_threads, smem)
-                     : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_trace_persistent<O, A, false>,
-                                                                     block_threads, smem);
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, persistent_kernel_of<O, A>(alpha, fp),
+                                                             block_threads, smem);
     }
 };
 
@@ -235,9 +256,11 @@ cudaError_t prepare_trace_kernels() {
     return cudaSuccess;
 }
 
-int persistent_blocks_per_sm(int block_threads, int stack_entries, bool any_hit, int order, bool alpha) {
+int persistent_blocks_per_sm(int block_threads, int stack_entries, bool any_hit, int order, bool alpha,
+                             const spec_cfg &spec) {
     int blocks = 0;
-    if (dispatch<occupancy_f>(order, any_hit, block_threads, stack_entries, alpha, &blocks) != cudaSuccess) return 1;
+    const int fp = (order == SPECULATIVE && !alpha) ? fast_path_of(spec) : 0;
+    if (dispatch<occupancy_f>(order, any_hit, block_threads, stack_entries, alpha, fp, &blocks) != cudaSuccess) return 1;
     return blocks > 0 ? blocks : 1;
 }
 
