@@ -55,11 +55,13 @@ def parse_args():
     ap.add_argument("--profile-case", action="store_true",
                     help="run one tuned and one plain step (no graphs) and exit (for ncu captures)")
     ap.add_argument("--profile-paths", type=int, default=1 << 20, help="paths of the --profile-case step")
-    ap.add_argument("--workload", default="spheres", choices=["spheres", "soups64", "direct", "adjoint"],
+    ap.add_argument("--workload", default="spheres", choices=["spheres", "soups64", "direct", "adjoint", "gputree"],
                     help="soups64: 64 uneven triangle soups traced in one launch, host vs GPU BVH builds; "
                          "direct: light-source sampling, fused persistent kernel vs wavefront steps; "
                          "adjoint: differentiable hits on the displaced icosphere, one optimisation step "
-                         "(tree update, closest hits, adjoint) with a host build, a GPU build or a refit")
+                         "(tree update, closest hits, adjoint) with a host build, a GPU build or a refit; "
+                         "gputree: the tuned spheres step on GPU-built trees (PLOC, radix tree) against the "
+                         "host-built tree, with build times")
     return ap.parse_args()
 
 
@@ -898,6 +900,57 @@ def run_adjoint(args):
     print(json.dumps(line), flush=True)
 
 
+def run_gputree(args):
+    """The tuned spheres step (persistent primary trace + fused loop, L2 flushed before each step) on
+    the host-built tuned tree and on trees built on the GPU from device arrays by PLOC and by the
+    radix tree, leaves of at most 1-4; build wall times, also for a 1,048,576-triangle soup."""
+    import torch
+    import __graft_entry__ as ge
+    ge.load_package()
+    from illum_rt_gb300 import api, workloads as wl
+    step = Step(api, wl, 0, load_tuning(torch.cuda.get_device_name(0)))
+    sc, _ = wl.spheres_primary(res=RES)
+    v = torch.from_numpy(sc.vpos).cuda()
+    t = torch.from_numpy(sc.tris.view(np.int32)).cuda()
+    out = {"metric": "ms per tuned spheres step on GPU-built trees", "unit": "ms", "higher_is_better": False,
+           "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "data": "synthetic (seeded)",
+           "config": {"workload": WORKLOAD, "l2": "flushed between timed steps"}, "trees": {}}
+
+    def timed():
+        for _ in range(max(3, args.warmup)):
+            step.tuned()
+        step.rt.check(step.sp)
+        gc.disable()
+        try:
+            tot, part = time_steps(step, step.tuned, args.steps, split=True)
+        finally:
+            gc.enable()
+        return {"step_ms": round(statistics.mean(tot), 4), "fused_ms": round(statistics.mean(part), 4)}
+
+    out["trees"]["host"] = dict(timed(), bvh=tree_label(load_tuning(torch.cuda.get_device_name(0))))
+    for builder in ("ploc", "lbvh"):
+        for leaf in (1, 2, 3, 4):
+            step.rt.set_device_builder(builder)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            info = step.rt.build_device(v, t, max_tris=leaf, stream=step.sp)
+            build_ms = (time.perf_counter() - t0) * 1e3
+            out["trees"][f"{builder}_leaf{leaf}"] = dict(timed(), build_ms=round(build_ms, 2), depth=info["depth"],
+                                                         inner_nodes=info["inner_nodes"])
+    s = wl.soup(1000, 1 << 20)
+    sv, st = torch.from_numpy(s.vpos).cuda(), torch.from_numpy(s.tris.view(np.int32)).cuda()
+    rt = api.BatchRayTracer(0)
+    for builder in ("ploc", "lbvh"):
+        rt.set_device_builder(builder)
+        rt.build_device(sv, st, max_tris=2)  # warm-up of the allocations
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rt.build_device(sv, st, max_tris=2)
+        out[f"soup_1048576_{builder}_build_ms"] = round((time.perf_counter() - t0) * 1e3, 2)
+    rt.close()
+    print(json.dumps(out), flush=True)
+
+
 def run_profile_case(paths: int):
     """One tuned step, then one plain step (no graphs; 1,048,576 paths unless asked otherwise):
     a case whose launches ncu can capture one by one."""
@@ -973,6 +1026,8 @@ def main():
         run_direct(args)
     elif args.workload == "adjoint":
         run_adjoint(args)
+    elif args.workload == "gputree":
+        run_gputree(args)
     else:
         run_gb300(args)
 
