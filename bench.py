@@ -177,6 +177,20 @@ def profile_figure(key: str):
     return None
 
 
+def limiter_figures():
+    """What bounds the fused kernel instead of HBM, from the committed ncu capture of the
+    1,048,576-path case: node-fetch latency and SIMT efficiency (lanes per instruction, issue
+    slots busy, L2 throughput)."""
+    lanes = profile_figure("lanes_per_instruction")
+    issue = profile_figure("issue_active_pct")
+    l2 = profile_figure("l2_throughput_pct")
+    if lanes is None:
+        return None
+    return {"kind": "node-fetch latency and SIMT efficiency", "lanes_per_instruction": lanes,
+            "issue_active_pct": issue, "l2_throughput_pct": l2,
+            "source": "ncu --set full of k_pt_fused, 1,048,576-path case"}
+
+
 def max_over_ranks(x: float, world: int, device: str = "cuda") -> float:
     """The largest `x` over all ranks (the slowest rank's time); `x` itself for one rank."""
     if world == 1:
@@ -584,7 +598,8 @@ def run_gb300(args):
                            "launch's bounce rays / its measured time",
                 "note": "B_ray = 32 + 16 + 64 n_node + 48 n_tri, counted in the exact while-while order on the "
                         "tuned step's tree; the BVH (%.0f MB) stays L2-resident, so these bytes are mostly served "
-                        "from L2" % (step.build_info["device_bytes"] / 1e6)}
+                        "from L2" % (step.build_info["device_bytes"] / 1e6),
+                "limiter": limiter_figures()}
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(statistics.mean(tuned_ms), 4), "higher_is_better": True,
@@ -732,10 +747,12 @@ def run_soups64(args):
         rt.check(sp)
         return e0.elapsed_time(e1) / args.steps
 
-    for kind in ("host", "gpu", "gpu_ploc"):
+    for kind in ("host", "gpu", "gpu_ploc", "gpu_sah"):
         rt = api.BatchRayTracer(0)
         if kind == "gpu_ploc":
             rt.set_device_builder("ploc")
+        elif kind == "gpu_sah":
+            rt.set_device_builder("sah", planes=min(256, tuning.get("planes", 16)))
         rt.select(tuning.get("tracer", "persistent-speculative-while-while"))
         kw = {k: v for k, v in tuning.items() if k in api.TUNING_KEYS}
         if kw:
@@ -744,7 +761,7 @@ def run_soups64(args):
         t0 = time.perf_counter()
         if kind == "host":
             rt.build_scenes(scenes, max_tris=tuning.get("max_tris", 4))
-        else:  # the radix-tree builder (the scene-set default) or PLOC clustering
+        else:  # the radix-tree builder (the scene-set default), PLOC clustering or SAH splits
             rt.build_scenes_device(d_scenes, max_tris=tuning.get("max_tris", 4), stream=sp)
         build_s = time.perf_counter() - t0
         ms = timed_trace(rt)
@@ -902,8 +919,9 @@ def run_adjoint(args):
 
 def run_gputree(args):
     """The tuned spheres step (persistent primary trace + fused loop, L2 flushed before each step) on
-    the host-built tuned tree and on trees built on the GPU from device arrays by PLOC and by the
-    radix tree, leaves of at most 1-4; build wall times, also for a 1,048,576-triangle soup."""
+    the host-built tuned tree and on trees built on the GPU from device arrays by the SAH builder
+    (the tuned tree's plane count), by PLOC and by the radix tree, leaves of at most 1-4; build
+    wall times, also for a 1,048,576-triangle soup."""
     import torch
     import __graft_entry__ as ge
     ge.load_package()
@@ -927,10 +945,12 @@ def run_gputree(args):
             gc.enable()
         return {"step_ms": round(statistics.mean(tot), 4), "fused_ms": round(statistics.mean(part), 4)}
 
-    out["trees"]["host"] = dict(timed(), bvh=tree_label(load_tuning(torch.cuda.get_device_name(0))))
-    for builder in ("ploc", "lbvh"):
+    tuning = load_tuning(torch.cuda.get_device_name(0))
+    out["trees"]["host"] = dict(timed(), bvh=tree_label(tuning))
+    planes = min(256, int(tree_options(tuning)["planes"]))
+    for builder in ("sah", "ploc", "lbvh"):
         for leaf in (1, 2, 3, 4):
-            step.rt.set_device_builder(builder)
+            step.rt.set_device_builder(builder, planes=planes)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             info = step.rt.build_device(v, t, max_tris=leaf, stream=step.sp)
@@ -940,8 +960,8 @@ def run_gputree(args):
     s = wl.soup(1000, 1 << 20)
     sv, st = torch.from_numpy(s.vpos).cuda(), torch.from_numpy(s.tris.view(np.int32)).cuda()
     rt = api.BatchRayTracer(0)
-    for builder in ("ploc", "lbvh"):
-        rt.set_device_builder(builder)
+    for builder in ("sah", "ploc", "lbvh"):
+        rt.set_device_builder(builder, planes=planes)
         rt.build_device(sv, st, max_tris=2)  # warm-up of the allocations
         torch.cuda.synchronize()
         t0 = time.perf_counter()

@@ -163,6 +163,7 @@ _PROTOS = {
     "grt_incoherent_rays": (I, [VP, ctypes.c_float, ctypes.c_float, ctypes.c_uint64, VP, U32, VP]),
     "grt_camera_rays": (I, [VP, P(Camera), U32, U32, VP, I, ctypes.c_uint64, VP, VP]),
     "grt_set_device_builder": (I, [VP, I]),
+    "grt_set_device_sah_planes": (I, [VP, U32]),
 }
 
 
@@ -376,12 +377,15 @@ class BatchRayTracer:
         self._check(lib().grt_build(self.ctx, _ptr(v), v.shape[0], _ptr(t), t.shape[0], ctypes.byref(o)))
         return self.info()
 
-    DEVICE_BUILDERS = {"default": 0, "lbvh": 1, "ploc": 2}
+    DEVICE_BUILDERS = {"default": 0, "lbvh": 1, "ploc": 2, "sah": 3}
 
-    def set_device_builder(self, method: str):
-        """grt_set_device_builder: "ploc", "lbvh" or "default" (PLOC for single scenes, LBVH for
-        scene sets)."""
+    def set_device_builder(self, method: str, planes: int | None = None):
+        """grt_set_device_builder: "sah", "ploc", "lbvh" or "default" (SAH for single scenes, LBVH
+        for scene sets); `planes`: grt_set_device_sah_planes (candidate planes of the SAH
+        builder, 1..256)."""
         self._check(lib().grt_set_device_builder(self.ctx, self.DEVICE_BUILDERS[method]))
+        if planes is not None:
+            self._check(lib().grt_set_device_sah_planes(self.ctx, int(planes)))
 
     def build_device(self, vpos, tris, max_tris=None, stream=None) -> dict:
         """The GPU builder (grt_build_device) on CUDA tensors: vpos float32 [nv, 4], tris

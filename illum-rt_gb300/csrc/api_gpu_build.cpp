@@ -39,6 +39,18 @@ grt_status check_info(grt_ctx *c, const int32_t *info, const std::string &what) 
     return GRT_OK;
 }
 
+// The builder of grt_set_device_builder; the default is the SAH method for one scene and the
+// radix tree for scene sets (whose many small scenes would pay the SAH method's rounds of
+// launches once each).
+int builder_method(int b, bool scene_set) {
+    switch (b) {
+    case GRT_DEVICE_BUILD_LBVH: return GB_METHOD_LBVH;
+    case GRT_DEVICE_BUILD_PLOC: return GB_METHOD_PLOC;
+    case GRT_DEVICE_BUILD_SAH: return GB_METHOD_SAH;
+    default: return scene_set ? GB_METHOD_LBVH : GB_METHOD_SAH;
+    }
+}
+
 bool bad_mesh(const grt_mesh &m) {
     return (m.nv && !m.vpos4) || (m.nt && !m.tris4) || !aligned16(m.vpos4) || !aligned16(m.tris4) ||
            m.nt > kMaxGpuTris;
@@ -50,9 +62,18 @@ extern "C" {
 
 grt_status grt_set_device_builder(grt_ctx *c, int method) {
     if (!c) return GRT_ERR_INVALID_ARG;
-    if (method != GRT_DEVICE_BUILD_DEFAULT && method != GRT_DEVICE_BUILD_LBVH && method != GRT_DEVICE_BUILD_PLOC)
+    if (method != GRT_DEVICE_BUILD_DEFAULT && method != GRT_DEVICE_BUILD_LBVH && method != GRT_DEVICE_BUILD_PLOC &&
+        method != GRT_DEVICE_BUILD_SAH)
         return fail(c, GRT_ERR_INVALID_ARG, "unknown device builder");
     c->device_builder = method;
+    return GRT_OK;
+}
+
+grt_status grt_set_device_sah_planes(grt_ctx *c, uint32_t planes) {
+    if (!c) return GRT_ERR_INVALID_ARG;
+    if (planes < 1 || planes > (uint32_t)kMaxSahPlanes)
+        return fail(c, GRT_ERR_INVALID_ARG, "SAH planes must be 1..256");
+    c->device_planes = (int)planes;
     return GRT_OK;
 }
 
@@ -73,7 +94,7 @@ grt_status grt_build_device(grt_ctx *c, const float *vpos4_dev, uint32_t nv, con
 
     build_temps tmp;
     const size_t nb = (size_t)std::max(nt, 2u) * 64, rb = (size_t)std::max(nt, 1u) * 48;
-    const int method = c->device_builder == GRT_DEVICE_BUILD_LBVH ? GB_METHOD_LBVH : GB_METHOD_PLOC;
+    const int method = builder_method(c->device_builder, false);
     const size_t scratch = gpu_build_scratch_bytes(nt, method);
     cudaError_t e = cudaMalloc(&c->d_nodes, nb);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_recs, rb);
@@ -88,7 +109,7 @@ grt_status grt_build_device(grt_ctx *c, const float *vpos4_dev, uint32_t nv, con
     if (e == cudaSuccess)
         e = gpu_build_binary((const float4 *)c->d_vpos, nv, (const uint4 *)c->d_tris, nt, (int)max_tris, tmp.scratch,
                              scratch, (float4 *)c->d_nodes, (float4 *)c->d_recs, tmp.wide_index,
-                             (int32_t *)c->d_parent, tmp.info, method, st);
+                             (int32_t *)c->d_parent, tmp.info, method, c->device_planes, st);
     int32_t info[8] = {0};
     if (e == cudaSuccess) e = cudaMemcpyAsync(info, tmp.info, sizeof(info), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -249,7 +270,7 @@ grt_status grt_build_scenes_device(grt_ctx *c, const grt_mesh *meshes, uint32_t 
     }
     build_temps tmp;
     int32_t *wide_pool = nullptr;
-    const int method = c->device_builder == GRT_DEVICE_BUILD_PLOC ? GB_METHOD_PLOC : GB_METHOD_LBVH;
+    const int method = builder_method(c->device_builder, true);
     const size_t scratch = gpu_build_scratch_bytes(most, method);
     cudaError_t e = cudaMalloc(&c->ms.d_nodes, tot[0]);
     if (e == cudaSuccess) e = cudaMalloc(&c->ms.d_recs, tot[1]);
@@ -262,7 +283,7 @@ grt_status grt_build_scenes_device(grt_ctx *c, const grt_mesh *meshes, uint32_t 
         e = gpu_build_binary((const float4 *)m.vpos4, m.nv, (const uint4 *)m.tris4, m.nt, (int)max_tris, tmp.scratch,
                              scratch, (float4 *)((char *)c->ms.d_nodes + off[i][0]),
                              (float4 *)((char *)c->ms.d_recs + off[i][1]), (int32_t *)((char *)wide_pool + off[i][2]),
-                             nullptr, tmp.info + 8 * (size_t)i, method, st);
+                             nullptr, tmp.info + 8 * (size_t)i, method, c->device_planes, st);
     }
     std::vector<int32_t> info((size_t)count * 8, 0);
     if (e == cudaSuccess) e = cudaMemcpyAsync(info.data(), tmp.info, info.size() * 4, cudaMemcpyDeviceToHost, st);

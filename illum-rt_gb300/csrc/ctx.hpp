@@ -56,6 +56,7 @@ struct grt_ctx {
     int tracer = 0;  // index into kTracers
     grt_tuning tuning{};
     int device_builder = GRT_DEVICE_BUILD_DEFAULT;  // grt_set_device_builder
+    int device_planes = 256;                         // grt_set_device_sah_planes
     timing_state timing;
     unsigned *d_err = nullptr;      // status block (grt_internal.hpp): error bits, counter, abort request
     unsigned *d_counter = nullptr;  // work counter of the persistent kernels (d_err + 1)

@@ -17,6 +17,8 @@
 //      contiguous ranges of the sorted order, so records are stored in that order;
 //   5. the 4-wide tree: the binary inner nodes at even depth, each taking its children's
 //      children (the same collapse as flatten_bvh4 on the host).
+// Instead of steps 2 and 3, the SAH method (gpu_build_sah.cu) splits top down with the
+// reference's SAH rule, and steps 4 and 5 follow as for the others.
 // The trees differ from the reference builder's, so closest hits equal the reference's except
 // near-ties, as for the speculative tracers.
 #include <cub/device/device_radix_sort.cuh>
@@ -63,6 +65,7 @@ __global__ void __launch_bounds__(kThreads) k_prims(const float4 *__restrict__ v
                                                     float4 *hi_out, uint32_t *cbounds, int32_t *info) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     float cmin[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, cmax[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    float bmin[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, bmax[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
     if (i < nt) {
         const uint4 t = tris[i];
         float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), hi = lo;
@@ -81,6 +84,12 @@ __global__ void __launch_bounds__(kThreads) k_prims(const float4 *__restrict__ v
                 cmin[0] = cmax[0] = cx;
                 cmin[1] = cmax[1] = cy;
                 cmin[2] = cmax[2] = cz;
+                bmin[0] = lo.x;
+                bmin[1] = lo.y;
+                bmin[2] = lo.z;
+                bmax[0] = hi.x;
+                bmax[1] = hi.y;
+                bmax[2] = hi.z;
             }
         }
         lo_out[i] = lo;
@@ -92,6 +101,8 @@ __global__ void __launch_bounds__(kThreads) k_prims(const float4 *__restrict__ v
         for (int o = 16; o > 0; o >>= 1) {
             cmin[a] = fminf(cmin[a], __shfl_xor_sync(0xffffffffu, cmin[a], o));
             cmax[a] = fmaxf(cmax[a], __shfl_xor_sync(0xffffffffu, cmax[a], o));
+            bmin[a] = fminf(bmin[a], __shfl_xor_sync(0xffffffffu, bmin[a], o));
+            bmax[a] = fmaxf(bmax[a], __shfl_xor_sync(0xffffffffu, bmax[a], o));
         }
     }
     if ((threadIdx.x & 31u) == 0 && cmin[0] <= cmax[0]) {
@@ -99,6 +110,8 @@ __global__ void __launch_bounds__(kThreads) k_prims(const float4 *__restrict__ v
         for (int a = 0; a < 3; ++a) {
             atomicMin(cbounds + a, ordered(cmin[a]));
             atomicMax(cbounds + 3 + a, ordered(cmax[a]));
+            atomicMin(cbounds + 6 + a, ordered(bmin[a]));
+            atomicMax(cbounds + 9 + a, ordered(bmax[a]));
         }
     }
 }
@@ -403,11 +416,14 @@ __device__ __forceinline__ slot load_slot(const slot *p) {
     return s;
 }
 
-// 4. bottom-up fit, SAH collapse and binary node output. For the 4-wide stack bound every inner
+// 4. bottom-up fit, SAH collapse and binary node output (`every_small_subtree`: every subtree of
+// at most max_leaf triangles becomes a leaf, the reference's rule, for the SAH method's trees,
+// which are split down to single triangles). For the 4-wide stack bound every inner
 // node also carries B (the bound of a 4-wide node placed there: its wide children less one plus
 // the largest B among its inner grandchildren) and M (the largest B among its inner children).
 __global__ void __launch_bounds__(kThreads) k_bottom_up(const float4 *__restrict__ plo, const float4 *__restrict__ phi,
                                                         const uint32_t *__restrict__ order, int n, int max_leaf,
+                                                        int every_small_subtree,
                                                         const int2 *__restrict__ children,
                                                         const int2 *__restrict__ range,
                                                         const int32_t *__restrict__ parent_inner,
@@ -449,7 +465,7 @@ __global__ void __launch_bounds__(kThreads) k_bottom_up(const float4 *__restrict
         const float cnt = a.hi.w + b.hi.w;
         const float keep = area + a.lo.w + b.lo.w;
         const float as_leaf = area * cnt;
-        const bool leaf = cnt <= (float)max_leaf && !(as_leaf > keep);
+        const bool leaf = cnt <= (float)max_leaf && (every_small_subtree || !(as_leaf > keep));
         collapsed[node] = leaf ? 1 : 0;
         if (leaf) {
             p.lo.w = as_leaf;
@@ -726,10 +742,11 @@ __global__ void __launch_bounds__(kThreads) k_wide_nodes(const float4 *__restric
     }
 }
 
+// bounds: centre min (3), centre max (3), box min (3), box max (3), ordered-encoded
 __global__ void k_init_info(int32_t *info, uint32_t *cbounds) {
     if (threadIdx.x < 8) info[threadIdx.x] = threadIdx.x == GB_FINITE ? 1 : 0;
-    if (threadIdx.x < 3) cbounds[threadIdx.x] = 0xffffffffu;
-    else if (threadIdx.x < 6) cbounds[threadIdx.x] = 0u;
+    const unsigned t = threadIdx.x;
+    if (t < 12) cbounds[t] = (t < 3 || (t >= 6 && t < 9)) ? 0xffffffffu : 0u;
 }
 
 inline size_t up256(size_t b) { return (b + 255) & ~(size_t)255; }
@@ -751,6 +768,7 @@ struct arena {
     unsigned long long *pflags, *pexcl;
     uint32_t *order2, *pvisits;
     ploc_state *ps;
+    void *sah;  // the SAH method's scratch (gpu_build_sah.cu)
     void *cub;
     size_t cub_bytes, total;
 };
@@ -765,7 +783,8 @@ size_t cub_bytes_for(uint32_t n) {
     return std::max(a, std::max(b, c));
 }
 
-arena carve(void *base, uint32_t n, bool ploc) {
+arena carve(void *base, uint32_t n, int method) {
+    const bool ploc = method == GB_METHOD_PLOC;
     arena A{};
     char *p = (char *)base;
     size_t off = 0;
@@ -781,7 +800,7 @@ arena carve(void *base, uint32_t n, bool ploc) {
     A.keys_b = (uint32_t *)take(m * 4);
     A.vals_a = (uint32_t *)take(m * 4);
     A.vals_b = (uint32_t *)take(m * 4);
-    A.cbounds = (uint32_t *)take(8 * 4);
+    A.cbounds = (uint32_t *)take(16 * 4);
     A.visits = (uint32_t *)take(m * 4);
     A.children = (int2 *)take(m * 8);
     A.range = (int2 *)take(m * 8);
@@ -806,6 +825,7 @@ arena carve(void *base, uint32_t n, bool ploc) {
         A.pvisits = (uint32_t *)take(m * 4);
         A.ps = (ploc_state *)take(sizeof(ploc_state));
     }
+    if (method == GB_METHOD_SAH) A.sah = take(sah_scratch_bytes((uint32_t)m));
     A.cub_bytes = cub_bytes_for((uint32_t)m);
     A.cub = take(A.cub_bytes);
     A.total = off;
@@ -817,7 +837,7 @@ inline unsigned blocks_for(uint32_t n) { return (n + kThreads - 1) / kThreads; }
 }  // namespace
 
 size_t gpu_build_scratch_bytes(uint32_t max_tris, int method) {
-    return carve(nullptr, max_tris, method == GB_METHOD_PLOC).total;
+    return carve(nullptr, max_tris, method).total;
 }
 
 namespace {
@@ -880,19 +900,23 @@ cudaError_t ploc_tree(const arena &A, int n, cudaStream_t st) {
 
 cudaError_t gpu_build_binary(const float4 *vpos, uint32_t nv, const uint4 *tris, uint32_t nt, int max_leaf,
                              void *scratch, size_t scratch_bytes, float4 *nodes, float4 *records,
-                             int32_t *wide_index, int32_t *links, int32_t *info, int method, cudaStream_t st) {
-    const bool ploc = method == GB_METHOD_PLOC && nt > 1;
-    arena A = carve(scratch, nt, method == GB_METHOD_PLOC);
+                             int32_t *wide_index, int32_t *links, int32_t *info, int method, int planes,
+                             cudaStream_t st) {
+    const bool ploc = method == GB_METHOD_PLOC && nt > 1, sah = method == GB_METHOD_SAH && nt > 1;
+    if (method == GB_METHOD_SAH && (planes < 1 || planes > kMaxSahPlanes)) return cudaErrorInvalidValue;
+    arena A = carve(scratch, nt, method);
     if (A.total > scratch_bytes) return cudaErrorInvalidValue;
     k_init_info<<<1, 32, 0, st>>>(info, A.cbounds);
     if (nt == 0) return cudaGetLastError();
     const unsigned nb = blocks_for(nt);
     k_prims<<<nb, kThreads, 0, st>>>(vpos, nv, tris, nt, A.lo, A.hi, A.cbounds, info);
-    k_morton<<<nb, kThreads, 0, st>>>(A.lo, A.hi, nt, A.cbounds, A.keys_a, A.vals_a);
     size_t cb = A.cub_bytes;
-    cudaError_t e = cub::DeviceRadixSort::SortPairs(A.cub, cb, A.keys_a, A.keys_b, A.vals_a, A.vals_b, (int)nt, 0,
-                                                    30, st);
-    if (e != cudaSuccess) return e;
+    cudaError_t e = cudaSuccess;
+    if (!sah) {
+        k_morton<<<nb, kThreads, 0, st>>>(A.lo, A.hi, nt, A.cbounds, A.keys_a, A.vals_a);
+        e = cub::DeviceRadixSort::SortPairs(A.cub, cb, A.keys_a, A.keys_b, A.vals_a, A.vals_b, (int)nt, 0, 30, st);
+        if (e != cudaSuccess) return e;
+    }
     // parents start at -1, so a position the tree misses is caught instead of read as an index
     e = cudaMemsetAsync(A.visits, 0, (size_t)nt * 4, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(A.collapsed, 1, (size_t)nt, st);
@@ -901,7 +925,11 @@ cudaError_t gpu_build_binary(const float4 *vpos, uint32_t nv, const uint4 *tris,
     if (e == cudaSuccess && links) e = cudaMemsetAsync(links, 0xff, (size_t)nt * 4, st);
     if (e != cudaSuccess) return e;
     const uint32_t *order = A.vals_b;  // primitives in leaf order
-    if (ploc) {
+    if (sah) {
+        e = sah_tree(A.sah, nt, planes, A.lo, A.hi, A.cbounds + 6, A.children, A.range, A.parent_inner,
+                     A.parent_leaf, A.flag, A.excl, A.cub, A.cub_bytes, &order, info, st);
+        if (e != cudaSuccess) return e;
+    } else if (ploc) {
         e = ploc_tree(A, (int)nt, st);
         if (e != cudaSuccess) return e;
         k_ploc_report<<<1, 1, 0, st>>>(A.ps, info);
@@ -910,7 +938,7 @@ cudaError_t gpu_build_binary(const float4 *vpos, uint32_t nv, const uint4 *tris,
         k_radix_tree<<<blocks_for(nt - 1), kThreads, 0, st>>>(A.keys_b, (int)nt, A.children, A.range,
                                                               A.parent_inner, A.parent_leaf);
     }
-    k_bottom_up<<<nb, kThreads, 0, st>>>(A.lo, A.hi, order, (int)nt, max_leaf, A.children, A.range,
+    k_bottom_up<<<nb, kThreads, 0, st>>>(A.lo, A.hi, order, (int)nt, max_leaf, sah ? 1 : 0, A.children, A.range,
                                          A.parent_inner, A.parent_leaf, A.slots, A.visits, A.collapsed, nodes,
                                          info);
     if (nt > 1) {

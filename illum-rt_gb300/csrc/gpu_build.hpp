@@ -21,9 +21,12 @@ enum gpu_build_info : int {
 };
 enum : int { GB_ERR_INDEX = 1, GB_ERR_DEPTH = 2, GB_ERR_TREE = 4 };
 
-// How the binary tree over the Morton-sorted triangles is formed: the radix tree of the codes
-// (linear BVH), or agglomerative clustering in Morton order (PLOC).
-enum : int { GB_METHOD_LBVH = 0, GB_METHOD_PLOC = 1 };
+// How the binary tree is formed: the radix tree of the Morton codes (linear BVH), agglomerative
+// clustering in Morton order (PLOC), or top-down binned SAH splits (gpu_build_sah.cu).
+enum : int { GB_METHOD_LBVH = 0, GB_METHOD_PLOC = 1, GB_METHOD_SAH = 2 };
+
+// Most candidate planes per node of the SAH method.
+constexpr int kMaxSahPlanes = 256;
 
 // Scratch bytes for scenes of up to `max_tris` triangles built with `method`.
 size_t gpu_build_scratch_bytes(uint32_t max_tris, int method);
@@ -34,9 +37,22 @@ size_t gpu_build_scratch_bytes(uint32_t max_tris, int method);
 // elsewhere). `info` (int32[8], device) receives the fields above. Stream-ordered; the LBVH
 // method reads nothing back, PLOC reads its cluster count back every 8 iterations (so that it
 // stops launching once the tree is finished).
+// `planes` (1 .. kMaxSahPlanes) is the SAH method's candidate count per node; the SAH method
+// reads a node count back every 4 levels of its top part.
 cudaError_t gpu_build_binary(const float4 *vpos, uint32_t nv, const uint4 *tris, uint32_t nt, int max_leaf,
                              void *scratch, size_t scratch_bytes, float4 *nodes, float4 *records,
-                             int32_t *wide_index, int32_t *links, int32_t *info, int method, cudaStream_t st);
+                             int32_t *wide_index, int32_t *links, int32_t *info, int method, int planes,
+                             cudaStream_t st);
+
+// The SAH method's full binary tree over the n >= 2 primitives with boxes plo / phi (`bounds`:
+// the ordered-encoded min corner then max corner of all of them): children, range and parent
+// links in the radix tree's form, and the primitive order (*order, inside `scratch`). `flag`,
+// `excl` (n ints) and the scan workspace are scratch of the caller.
+size_t sah_scratch_bytes(uint32_t n);
+cudaError_t sah_tree(void *scratch, uint32_t n, int planes, const float4 *plo, const float4 *phi,
+                     const uint32_t *bounds, int2 *children, int2 *range, int32_t *parent_inner,
+                     int32_t *parent_leaf, int32_t *flag, int32_t *excl, void *cub_tmp, size_t cub_bytes,
+                     const uint32_t **order, int32_t *info, cudaStream_t st);
 
 // Phase 2: the 4-wide nodes (info[GB_WIDE_NODES] x 128 B) from the binary nodes of phase 1.
 cudaError_t gpu_build_wide(const float4 *nodes, const int32_t *wide_index, uint32_t nt, float4 *nodes4,

@@ -39,7 +39,7 @@ extern "C" {
 #endif
 
 #define GRT_VERSION_MAJOR 1
-#define GRT_VERSION_MINOR 1
+#define GRT_VERSION_MINOR 2
 
 /* A cudaStream_t. NULL means the legacy default stream. */
 typedef struct CUstream_st *grt_stream_t;
@@ -447,10 +447,10 @@ grt_status grt_set_alpha(grt_ctx *ctx, const float *texcoords2, uint32_t nv, con
 
 /* Builds the scene of grt_build on the GPU from DEVICE arrays in the same layouts (vertices
  * float4, triangles uint4 with the material id in w). No counterpart in the reference, whose
- * builds all run on the host (batch_rt::build, rt/cuda/base.cpp:88-117): the triangles sorted by
- * the Morton codes of their box centres, a binary tree over that order (see
- * grt_set_device_builder), subtrees of at most max_tris_per_node (1..16) triangles turned into
- * leaves where the SAH cost says so, and its 4-wide collapse.
+ * builds all run on the host (batch_rt::build, rt/cuda/base.cpp:88-117): a binary tree over the
+ * triangles (see grt_set_device_builder), subtrees of at most max_tris_per_node (1..16)
+ * triangles turned into leaves (by the SAH builder always, as the reference's builder does; by
+ * the others where the SAH cost says so), and its 4-wide collapse.
  * The tree differs from the reference builder's, so closest hits equal the reference's except
  * near-ties (any-hit answers are equal). Every tracer can trace it; grt_export_bvh has no
  * reference tree to export and fails. The arrays are copied, so the caller may free them after
@@ -464,17 +464,24 @@ grt_status grt_build_device(grt_ctx *ctx, const float *vpos4_dev, uint32_t nv, c
 grt_status grt_build_scenes_device(grt_ctx *ctx, const grt_mesh *meshes, uint32_t count, uint32_t max_tris_per_node,
                                    grt_stream_t stream);
 
-/* How the GPU builder forms the binary tree over the Morton order:
- *   GRT_DEVICE_BUILD_PLOC: agglomerative clustering (PLOC, Meister and Bittner 2018): clusters
- *     merge with their mutual nearest neighbour (smallest union surface area) among the 16 on
- *     either side in the Morton-ordered list, iteration after iteration. Trees close to the
- *     host SAH builder's in quality; builds take tens of short launches;
+/* How the GPU builder forms the binary tree:
+ *   GRT_DEVICE_BUILD_SAH: top-down splits with the reference builder's SAH rule
+ *     (rt/cpu/bvh-ctor.h:386-488: the major axis of each node's box, evenly spaced candidate
+ *     planes, see grt_set_device_sah_planes, the least surface-area cost), the candidates binned
+ *     on the GPU instead of partitioned in place. Trees of the host SAH builder's quality; the
+ *     top part of the tree takes a few launches per level;
+ *   GRT_DEVICE_BUILD_PLOC: agglomerative clustering (PLOC, Meister and Bittner 2018) in Morton
+ *     order: clusters merge with their mutual nearest neighbour (smallest union surface area)
+ *     among the 16 on either side in the list, iteration after iteration;
  *   GRT_DEVICE_BUILD_LBVH: the radix tree of the Morton codes (Karras 2012), built in one pass:
  *     the fastest build, trees that trace slower.
- * GRT_DEVICE_BUILD_DEFAULT uses PLOC for grt_build_device and LBVH for grt_build_scenes_device
- * (whose many small scenes would pay the clustering's launches once each). */
-enum { GRT_DEVICE_BUILD_DEFAULT = 0, GRT_DEVICE_BUILD_LBVH = 1, GRT_DEVICE_BUILD_PLOC = 2 };
+ * GRT_DEVICE_BUILD_DEFAULT uses SAH for grt_build_device and LBVH for grt_build_scenes_device
+ * (whose many small scenes would pay the SAH builder's launches once each). */
+enum { GRT_DEVICE_BUILD_DEFAULT = 0, GRT_DEVICE_BUILD_LBVH = 1, GRT_DEVICE_BUILD_PLOC = 2, GRT_DEVICE_BUILD_SAH = 3 };
 grt_status grt_set_device_builder(grt_ctx *ctx, int method);
+/* Candidate planes per node of GRT_DEVICE_BUILD_SAH (1..256, default 256; as many as a node has
+ * triangles when that is fewer), the reference builder's `planes` option. */
+grt_status grt_set_device_sah_planes(grt_ctx *ctx, uint32_t planes);
 
 /* Refits the context's scene (built by grt_build or grt_build_device) to new vertex positions:
  * DEVICE float4 array of the built scene's nv vertices, copied. The tree keeps its topology;

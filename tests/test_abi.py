@@ -30,7 +30,7 @@ def test_every_declared_symbol_is_exported(api):
 
 def test_version_and_defaults(api):
     L = api.lib()
-    assert L.grt_version() == 1001
+    assert L.grt_version() == 1002
     o = api.BvhOpts()
     L.grt_bvh_opts_default(ctypes.byref(o))
     assert (o.split, o.max_tris_per_node, o.number_of_planes, o.esc) == (2, 4, 16, 1)

@@ -50,7 +50,7 @@ def oracles(orc, golden_scenes):
     return {name: orc.OracleBVH(v, t) for name, (v, t, _, _) in golden_scenes.items()}
 
 
-@pytest.fixture(params=["ploc", "lbvh"])
+@pytest.fixture(params=["sah", "ploc", "lbvh"])
 def builder(request, gpu_tracer):
     gpu_tracer.set_device_builder(request.param)
     yield request.param
@@ -128,9 +128,45 @@ def test_gpu_tree_errors(gpu_tracer, api):
     with pytest.raises(KeyError):
         gpu_tracer.set_device_builder("octree")
     assert api.lib().grt_set_device_builder(gpu_tracer.ctx, 7) == 1  # invalid argument
+    for planes in (0, 257):
+        assert api.lib().grt_set_device_sah_planes(gpu_tracer.ctx, planes) == 1
 
 
-@pytest.mark.parametrize("set_builder", ["default", "ploc"])
+def test_sah_builder_tree_quality_equals_host_tree(api, wl):
+    """The GPU SAH builder follows the reference builder's split rule, so its tree is visited like
+    the host tree built with the same options: inner nodes and triangle tests per bounce ray
+    (counted in the exact while-while order over 200,000 diffuse paths of the sphere scene)
+    within 3 % of the host tree's, and the same depth up to 2 levels."""
+    import torch
+    sc, rays = wl.spheres_primary(res=512)
+    d_rays = _dev(rays, np.float32)
+    counts = {}
+    for form in ("host", "sah"):
+        rt = api.BatchRayTracer(0)
+        if form == "host":
+            info = rt.build(sc.vpos, sc.tris, max_tris=2, planes=256, esc=False)
+        else:
+            rt.set_device_builder("sah", planes=256)
+            info = rt.build_device(_dev(sc.vpos, np.float32), _dev(sc.tris, np.uint32), max_tris=2)
+        rt.select("while-while")
+        hits = torch.zeros((rays.shape[0], 4), device="cuda")
+        stream = torch.cuda.current_stream().cuda_stream
+        rt.trace(d_rays, hits, False, stream)
+        cnt = torch.zeros(3, dtype=torch.int64, device="cuda")
+        res = torch.zeros((200_000, 4), dtype=torch.int32, device="cuda")
+        rt.set_traversal_counters(cnt)
+        rt.pathtrace(api.BatchRayTracer.pt_params(mode=0, seed=5), d_rays, hits, 200_000, res, None, stream)
+        rt.check(stream, timeout_ms=60000)
+        rt.set_traversal_counters(None)
+        c = [int(x) for x in cnt.cpu().numpy()]
+        counts[form] = (c[1] / c[0], c[2] / c[0], info["depth"])
+        rt.close()
+    (hn, ht, hd), (gn, gt, gd) = counts["host"], counts["sah"]
+    print(f"per bounce ray: host {hn:.2f} nodes {ht:.2f} tris depth {hd}; GPU SAH {gn:.2f} nodes {gt:.2f} tris depth {gd}")
+    assert abs(gn - hn) <= 0.03 * hn and abs(gt - ht) <= 0.03 * ht and abs(gd - hd) <= 2
+
+
+@pytest.mark.parametrize("set_builder", ["default", "ploc", "sah"])
 @pytest.mark.parametrize("tracer", ["persistent-while-while", "persistent-speculative-while-while",
                                     "persistent-bvh4-speculative-while-while"])
 def test_gpu_scene_set_matches_oracle(api, orc, wl, tracer, set_builder):
