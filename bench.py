@@ -55,6 +55,8 @@ def parse_args():
     ap.add_argument("--profile-case", action="store_true",
                     help="run one tuned and one plain step (no graphs) and exit (for ncu captures)")
     ap.add_argument("--profile-paths", type=int, default=1 << 20, help="paths of the --profile-case step")
+    ap.add_argument("--profile-tracer", default=None,
+                    help="tracer of the --profile-case step's tuned form instead of the tuning table's")
     ap.add_argument("--workload", default="spheres", choices=["spheres", "soups64", "direct", "adjoint", "gputree"],
                     help="soups64: 64 uneven triangle soups traced in one launch, host vs GPU BVH builds; "
                          "direct: light-source sampling, fused persistent kernel vs wavefront steps; "
@@ -971,16 +973,20 @@ def run_gputree(args):
     print(json.dumps(out), flush=True)
 
 
-def run_profile_case(paths: int):
+def run_profile_case(paths: int, tracer: str | None = None):
     """One tuned step, then one plain step (no graphs; 1,048,576 paths unless asked otherwise):
-    a case whose launches ncu can capture one by one."""
+    a case whose launches ncu can capture one by one. `tracer` replaces the tuned form's tracer
+    (the tuning table's launch parameters stay)."""
     import torch
     import __graft_entry__ as ge
     global N_PATHS
     N_PATHS = paths
     ge.load_package()
     from illum_rt_gb300 import api, workloads as wl
-    step = Step(api, wl, 0, load_tuning(torch.cuda.get_device_name(0)))
+    tuning = load_tuning(torch.cuda.get_device_name(0))
+    if tracer:
+        tuning = dict(tuning, tracer=tracer)
+    step = Step(api, wl, 0, tuning)
     step.p_fused.use_graph = 0
     step.p_plain.use_graph = 0
     step.tuned()
@@ -1037,7 +1043,7 @@ def main():
     if args.profile_case and args.workload in ("direct", "soups64"):
         run_profile_case_other(args.workload)
     elif args.profile_case:
-        run_profile_case(args.profile_paths)
+        run_profile_case(args.profile_paths, args.profile_tracer)
     elif args.impl == "reference":
         run_reference(args)
     elif args.workload == "soups64":
