@@ -4,7 +4,9 @@
 // builder makes (indices in range, depth within the traversal stacks).
 #include <algorithm>
 #include <array>
+#include <atomic>
 #include <chrono>
+#include <thread>
 #include <string>
 #include <vector>
 
@@ -38,6 +40,9 @@ grt_status check_info(grt_ctx *c, const int32_t *info, const std::string &what) 
                         " exceeds the largest traversal stack (" + std::to_string(kStackLarge) + ")");
     return GRT_OK;
 }
+
+// Host threads (each with a stream) that build the scenes of a scene set concurrently.
+constexpr uint32_t kBuildWorkers = 8;
 
 // The builder of grt_set_device_builder; the default is the SAH method for one scene and the
 // radix tree for scene sets (whose many small scenes would pay the SAH method's rounds of
@@ -275,19 +280,59 @@ grt_status grt_build_scenes_device(grt_ctx *c, const grt_mesh *meshes, uint32_t 
     cudaError_t e = cudaMalloc(&c->ms.d_nodes, tot[0]);
     if (e == cudaSuccess) e = cudaMalloc(&c->ms.d_recs, tot[1]);
     if (e == cudaSuccess) e = cudaMalloc((void **)&wide_pool, tot[2]);
-    if (e == cudaSuccess) e = cudaMalloc(&tmp.scratch, scratch);
     if (e == cudaSuccess) e = cudaMalloc(&tmp.info, (size_t)count * 8 * 4);
     tmp.wide_index = wide_pool;
-    for (uint32_t i = 0; i < count && e == cudaSuccess; ++i) {
-        const grt_mesh &m = meshes[i];
-        e = gpu_build_binary((const float4 *)m.vpos4, m.nv, (const uint4 *)m.tris4, m.nt, (int)max_tris, tmp.scratch,
-                             scratch, (float4 *)((char *)c->ms.d_nodes + off[i][0]),
-                             (float4 *)((char *)c->ms.d_recs + off[i][1]), (int32_t *)((char *)wide_pool + off[i][2]),
-                             nullptr, tmp.info + 8 * (size_t)i, method, c->device_planes, st);
+    // The scenes are built by up to kBuildWorkers host threads, each on a stream of its own with
+    // scratch of its own: a build is a chain of short launches (and, for the SAH and PLOC
+    // builders, read-backs), so one scene at a time leaves most of the GPU idle. The worker
+    // streams start after earlier work on `st`, and `st` waits for all of them.
+    const int workers = (int)std::min<uint32_t>(count, kBuildWorkers);
+    std::vector<cudaStream_t> wst(workers, nullptr);
+    std::vector<void *> wscratch(workers, nullptr);
+    std::vector<cudaEvent_t> wdone(workers, nullptr);
+    cudaEvent_t ready = nullptr;
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ready, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventRecord(ready, st);
+    for (int w = 0; w < workers && e == cudaSuccess; ++w) {
+        e = cudaStreamCreateWithFlags(&wst[w], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&wdone[w], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(wst[w], ready, 0);
+        if (e == cudaSuccess) e = cudaMalloc(&wscratch[w], scratch);
+    }
+    if (e == cudaSuccess) {
+        std::atomic<uint32_t> next{0};
+        std::vector<cudaError_t> werr(workers, cudaSuccess);
+        std::vector<std::thread> pool;
+        for (int w = 0; w < workers; ++w)
+            pool.emplace_back([&, w] {
+                werr[w] = cudaSetDevice(c->device);
+                for (uint32_t i; werr[w] == cudaSuccess && (i = next++) < count;) {
+                    const grt_mesh &m = meshes[i];
+                    werr[w] = gpu_build_binary((const float4 *)m.vpos4, m.nv, (const uint4 *)m.tris4, m.nt,
+                                               (int)max_tris, wscratch[w], scratch,
+                                               (float4 *)((char *)c->ms.d_nodes + off[i][0]),
+                                               (float4 *)((char *)c->ms.d_recs + off[i][1]),
+                                               (int32_t *)((char *)wide_pool + off[i][2]), nullptr,
+                                               tmp.info + 8 * (size_t)i, method, c->device_planes, wst[w]);
+                }
+                if (werr[w] == cudaSuccess) werr[w] = cudaEventRecord(wdone[w], wst[w]);
+            });
+        for (auto &t : pool) t.join();
+        for (int w = 0; w < workers; ++w) {
+            if (e == cudaSuccess) e = werr[w];
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(st, wdone[w], 0);
+        }
     }
     std::vector<int32_t> info((size_t)count * 8, 0);
     if (e == cudaSuccess) e = cudaMemcpyAsync(info.data(), tmp.info, info.size() * 4, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    for (int w = 0; w < workers; ++w) {  // every worker stream has finished, or the call fails anyway
+        if (wst[w]) cudaStreamSynchronize(wst[w]);
+        if (wscratch[w]) cudaFree(wscratch[w]);
+        if (wdone[w]) cudaEventDestroy(wdone[w]);
+        if (wst[w]) cudaStreamDestroy(wst[w]);
+    }
+    if (ready) cudaEventDestroy(ready);
     if (e != cudaSuccess) {
         grt_free_multi(c);
         return cuda_fail(c, e, "building the scene set on the GPU");

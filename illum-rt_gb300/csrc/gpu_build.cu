@@ -836,6 +836,27 @@ inline unsigned blocks_for(uint32_t n) { return (n + kThreads - 1) / kThreads; }
 
 }  // namespace
 
+namespace {
+struct pinned_word {
+    int32_t *p = nullptr;
+    int32_t fallback = 0;
+    pinned_word() {
+        if (cudaMallocHost((void **)&p, sizeof(int32_t)) != cudaSuccess) {
+            cudaGetLastError();
+            p = nullptr;
+        }
+    }
+    ~pinned_word() {
+        if (p) cudaFreeHost(p);
+    }
+};
+}  // namespace
+
+int32_t *readback_word() {
+    thread_local pinned_word w;
+    return w.p ? w.p : &w.fallback;
+}
+
 size_t gpu_build_scratch_bytes(uint32_t max_tris, int method) {
     return carve(nullptr, max_tris, method).total;
 }
@@ -870,10 +891,10 @@ cudaError_t ploc_tree(const arena &A, int n, cudaStream_t st) {
     cudaError_t e = cudaGetLastError();
     for (int it = 0; it < total && e == cudaSuccess; ++it) {
         if (it % 8 == 7) {  // stop once one cluster is left
-            int32_t m = 0;
-            e = cudaMemcpyAsync(&m, &A.ps->m, sizeof(m), cudaMemcpyDeviceToHost, st);
+            int32_t *m = readback_word();
+            e = cudaMemcpyAsync(m, &A.ps->m, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
             if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-            if (e != cudaSuccess || m <= 1) break;
+            if (e != cudaSuccess || *m <= 1) break;
         }
         k_ploc_nn<<<nb, kThreads, 0, st>>>(cur, A.box_lo, A.box_hi, A.ps, it >= budget ? 1 : 0, A.nn);
         k_ploc_flags<<<nb, kThreads, 0, st>>>(A.nn, A.ps, n, A.pflags);

@@ -54,6 +54,10 @@ cudaError_t sah_tree(void *scratch, uint32_t n, int planes, const float4 *plo, c
                      int32_t *parent_leaf, int32_t *flag, int32_t *excl, void *cub_tmp, size_t cub_bytes,
                      const uint32_t **order, int32_t *info, cudaStream_t st);
 
+// A pinned host word for the builders' read-backs, one per host thread (a copy into pageable
+// memory goes through a staging buffer that serialises the threads of a scene-set build).
+int32_t *readback_word();
+
 // Phase 2: the 4-wide nodes (info[GB_WIDE_NODES] x 128 B) from the binary nodes of phase 1.
 cudaError_t gpu_build_wide(const float4 *nodes, const int32_t *wide_index, uint32_t nt, float4 *nodes4,
                            cudaStream_t st);

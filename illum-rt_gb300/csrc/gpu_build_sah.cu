@@ -708,10 +708,10 @@ cudaError_t sah_tree(void *scratch, uint32_t n, int planes, const float4 *plo, c
     const int max_rounds = (int)n;
     for (int round = 0; e == cudaSuccess; ++round) {
         if (round % 4 == 3 || round >= max_rounds) {  // stop once no large node is left
-            int left = 0;
-            e = cudaMemcpyAsync(&left, n_large[cur], sizeof(int), cudaMemcpyDeviceToHost, st);
+            int32_t *left = readback_word();
+            e = cudaMemcpyAsync(left, n_large[cur], sizeof(int32_t), cudaMemcpyDeviceToHost, st);
             if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-            if (e != cudaSuccess || left == 0) break;
+            if (e != cudaSuccess || *left == 0) break;
             if (round >= max_rounds) return cudaErrorInvalidValue;
         }
         k_sah_bin<<<nb, kT, 0, st>>>(tasks[cur], n_large[cur], idx[cur], plo, phi, (int)n, planes, A.task_of,
