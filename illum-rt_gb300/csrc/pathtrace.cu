@@ -488,7 +488,11 @@ __global__ void __launch_bounds__(256) k_pt_fused(dev_scene sc, pt_scene ps, pt_
         }
         // traversal phase
         for (int it = 1;; ++it) {
-            if (SPEC)
+            if (SPEC && __all_sync(kFull, !tracing || plain))  // every ray of the warp plain (nearly always)
+                trav_spec_iter<false, false, WIDE, ALPHA, kFastVisits[FP], kFastPend[FP], true>(s, tracing, plain, sc, r,
+                                                                                                stk, stride, cap, spec,
+                                                                                                err);
+            else if (SPEC)
                 trav_spec_iter<false, false, WIDE, ALPHA, kFastVisits[FP], kFastPend[FP]>(s, tracing, plain, sc, r, stk,
                                                                                           stride, cap, spec, err);
             else if (tracing && plain)

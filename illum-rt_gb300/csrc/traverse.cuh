@@ -573,7 +573,10 @@ __device__ __forceinline__ void spec_node4(trav_t &s, const dev_scene &sc, const
 // postponed leaf use the closest hit from before that leaf, so the ray may visit nodes the
 // reference would have culled. A triangle found there can replace the reference's answer only
 // if its t lies within rounding of the culled box's entry distance: a near-tie.
-template <bool ANY, bool COUNT, bool WIDE = false, bool ALPHA = false, int VISITS = 0, int PEND = 0>
+// ALL_PLAIN: the caller has checked that every active lane's ray is plain, so the node visits
+// take the packed slab test without a per-lane choice (half the code of the unrolled visits).
+template <bool ANY, bool COUNT, bool WIDE = false, bool ALPHA = false, int VISITS = 0, int PEND = 0,
+          bool ALL_PLAIN = false>
 __device__ __forceinline__ void trav_spec_iter(trav_t &s, bool active, bool plain, const dev_scene &sc,
                                                const ray_t &r, int *stk, int stride, int cap, const spec_cfg &cfg,
                                                unsigned *err) {
@@ -586,12 +589,12 @@ __device__ __forceinline__ void trav_spec_iter(trav_t &s, bool active, bool plai
         if (mine && !s.done && s.more && s.cur >= 0) {
             if (COUNT) ++s.n_inner;
             if (WIDE) {
-                if (plain)
+                if (ALL_PLAIN || plain)
                     spec_node4<ANY, true>(s, sc, r, stk, stride, cap, err);
                 else
                     spec_node4<ANY, false>(s, sc, r, stk, stride, cap, err);
             } else {
-                if (plain)
+                if (ALL_PLAIN || plain)
                     spec_node<ANY, true>(s, sc, r, stk, stride, cap, err);
                 else
                     spec_node<ANY, false>(s, sc, r, stk, stride, cap, err);
