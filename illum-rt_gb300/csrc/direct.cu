@@ -184,7 +184,11 @@ __device__ __forceinline__ void trace_all(trav_t &s, bool active, bool plain, co
     constexpr bool SPEC = ORDER == SPECULATIVE || ORDER == WIDE_SPECULATIVE;
     constexpr bool WIDE = ORDER == WIDE_SPECULATIVE;
     while (__any_sync(kFull, active && !s.done)) {
-        if (SPEC)
+        if (SPEC && __all_sync(kFull, !active || plain))
+            trav_spec_iter<ANY, false, WIDE, false, kSpecDirect.visits, kSpecDirect.pend, true>(
+                s, active, plain, sc, r, stk, stride, cap,
+                spec_cfg{kSpecDirect.pend, kSpecDirect.exit, kSpecDirect.visits}, err);
+        else if (SPEC)
             trav_spec_iter<ANY, false, WIDE, false, kSpecDirect.visits, kSpecDirect.pend>(s, active, plain, sc, r, stk,
                                                                                            stride, cap,
                                                    spec_cfg{kSpecDirect.pend, kSpecDirect.exit, kSpecDirect.visits},
