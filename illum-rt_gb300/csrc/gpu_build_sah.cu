@@ -6,7 +6,9 @@
 // candidate in its place (once). Where the reference partitions and sorts primitives in place,
 // this builder bins them, so its trees differ from the reference's in detail (not in quality):
 // the reference's in-place partition never classifies the element where its two pointers meet,
-// this one classifies every primitive, and equal centres are ordered by position.
+// this one classifies every primitive, and equal centres are ordered by position; and for nodes
+// of more than kSmall primitives, whose planes are closely spaced, the median (taken there in
+// position order) is used only when no plane separates the node.
 //
 // The output is a full binary tree over single primitives in the form the bottom-up pass of
 // gpu_build.cu takes (children, range, parent links, the primitive order), whose leaf collapse
