@@ -40,6 +40,13 @@ def test_profile_figures_are_present_and_plausible():
     assert bench.profile_figure("no_such_key") is None
 
 
+def test_limiter_figures_come_from_the_committed_capture():
+    lim = bench.limiter_figures()
+    assert lim is not None and lim["kind"]
+    assert 1 <= lim["lanes_per_instruction"] <= 32
+    assert 0 < lim["issue_active_pct"] <= 100 and 0 < lim["l2_throughput_pct"] <= 100
+
+
 def _hits(n, seed):
     import numpy as np
     g = np.random.default_rng(seed)
