@@ -749,12 +749,12 @@ def run_soups64(args):
         rt.check(sp)
         return e0.elapsed_time(e1) / args.steps
 
-    for kind in ("host", "gpu", "gpu_ploc", "gpu_sah"):
+    for kind in ("host", "gpu", "gpu_ploc", "gpu_lbvh"):
         rt = api.BatchRayTracer(0)
         if kind == "gpu_ploc":
             rt.set_device_builder("ploc")
-        elif kind == "gpu_sah":
-            rt.set_device_builder("sah", planes=min(256, tuning.get("planes", 16)))
+        elif kind == "gpu_lbvh":
+            rt.set_device_builder("lbvh")
         rt.select(tuning.get("tracer", "persistent-speculative-while-while"))
         kw = {k: v for k, v in tuning.items() if k in api.TUNING_KEYS}
         if kw:
@@ -763,7 +763,7 @@ def run_soups64(args):
         t0 = time.perf_counter()
         if kind == "host":
             rt.build_scenes(scenes, max_tris=tuning.get("max_tris", 4))
-        else:  # the radix-tree builder (the scene-set default), PLOC clustering or SAH splits
+        else:  # the default device builder (SAH splits), PLOC clustering or the radix tree
             rt.build_scenes_device(d_scenes, max_tris=tuning.get("max_tris", 4), stream=sp)
         build_s = time.perf_counter() - t0
         ms = timed_trace(rt)

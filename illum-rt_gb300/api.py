@@ -380,9 +380,8 @@ class BatchRayTracer:
     DEVICE_BUILDERS = {"default": 0, "lbvh": 1, "ploc": 2, "sah": 3}
 
     def set_device_builder(self, method: str, planes: int | None = None):
-        """grt_set_device_builder: "sah", "ploc", "lbvh" or "default" (SAH for single scenes, LBVH
-        for scene sets); `planes`: grt_set_device_sah_planes (candidate planes of the SAH
-        builder, 1..256)."""
+        """grt_set_device_builder: "sah", "ploc", "lbvh" or "default" (SAH); `planes`:
+        grt_set_device_sah_planes (candidate planes of the SAH builder, 1..256)."""
         self._check(lib().grt_set_device_builder(self.ctx, self.DEVICE_BUILDERS[method]))
         if planes is not None:
             self._check(lib().grt_set_device_sah_planes(self.ctx, int(planes)))

@@ -44,15 +44,13 @@ grt_status check_info(grt_ctx *c, const int32_t *info, const std::string &what) 
 // Host threads (each with a stream) that build the scenes of a scene set concurrently.
 constexpr uint32_t kBuildWorkers = 8;
 
-// The builder of grt_set_device_builder; the default is the SAH method for one scene and the
-// radix tree for scene sets (whose many small scenes would pay the SAH method's rounds of
-// launches once each).
-int builder_method(int b, bool scene_set) {
+// The builder of grt_set_device_builder; the default is the SAH method (trees of the
+// reference builder's quality).
+int builder_method(int b) {
     switch (b) {
     case GRT_DEVICE_BUILD_LBVH: return GB_METHOD_LBVH;
     case GRT_DEVICE_BUILD_PLOC: return GB_METHOD_PLOC;
-    case GRT_DEVICE_BUILD_SAH: return GB_METHOD_SAH;
-    default: return scene_set ? GB_METHOD_LBVH : GB_METHOD_SAH;
+    default: return GB_METHOD_SAH;
     }
 }
 
@@ -99,7 +97,7 @@ grt_status grt_build_device(grt_ctx *c, const float *vpos4_dev, uint32_t nv, con
 
     build_temps tmp;
     const size_t nb = (size_t)std::max(nt, 2u) * 64, rb = (size_t)std::max(nt, 1u) * 48;
-    const int method = builder_method(c->device_builder, false);
+    const int method = builder_method(c->device_builder);
     const size_t scratch = gpu_build_scratch_bytes(nt, method);
     cudaError_t e = cudaMalloc(&c->d_nodes, nb);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_recs, rb);
@@ -275,7 +273,7 @@ grt_status grt_build_scenes_device(grt_ctx *c, const grt_mesh *meshes, uint32_t 
     }
     build_temps tmp;
     int32_t *wide_pool = nullptr;
-    const int method = builder_method(c->device_builder, true);
+    const int method = builder_method(c->device_builder);
     const size_t scratch = gpu_build_scratch_bytes(most, method);
     cudaError_t e = cudaMalloc(&c->ms.d_nodes, tot[0]);
     if (e == cudaSuccess) e = cudaMalloc(&c->ms.d_recs, tot[1]);

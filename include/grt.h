@@ -474,9 +474,9 @@ grt_status grt_build_scenes_device(grt_ctx *ctx, const grt_mesh *meshes, uint32_
  *     order: clusters merge with their mutual nearest neighbour (smallest union surface area)
  *     among the 16 on either side in the list, iteration after iteration;
  *   GRT_DEVICE_BUILD_LBVH: the radix tree of the Morton codes (Karras 2012), built in one pass:
- *     the fastest build, trees that trace slower.
- * GRT_DEVICE_BUILD_DEFAULT uses SAH for grt_build_device and LBVH for grt_build_scenes_device
- * (whose many small scenes would pay the SAH builder's launches once each). */
+ *     the fastest build (for scenes rebuilt every frame), trees that trace a few per cent slower.
+ * GRT_DEVICE_BUILD_DEFAULT is GRT_DEVICE_BUILD_SAH. grt_build_scenes_device builds the scenes of
+ * a set concurrently (up to 8 host threads, each with a stream of its own). */
 enum { GRT_DEVICE_BUILD_DEFAULT = 0, GRT_DEVICE_BUILD_LBVH = 1, GRT_DEVICE_BUILD_PLOC = 2, GRT_DEVICE_BUILD_SAH = 3 };
 grt_status grt_set_device_builder(grt_ctx *ctx, int method);
 /* Candidate planes per node of GRT_DEVICE_BUILD_SAH (1..256, default 256; as many as a node has

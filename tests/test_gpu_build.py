@@ -166,7 +166,7 @@ def test_sah_builder_tree_quality_equals_host_tree(api, wl):
     assert abs(gn - hn) <= 0.03 * hn and abs(gt - ht) <= 0.03 * ht and abs(gd - hd) <= 2
 
 
-@pytest.mark.parametrize("set_builder", ["default", "ploc", "sah"])
+@pytest.mark.parametrize("set_builder", ["default", "ploc", "lbvh"])
 @pytest.mark.parametrize("tracer", ["persistent-while-while", "persistent-speculative-while-while",
                                     "persistent-bvh4-speculative-while-while"])
 def test_gpu_scene_set_matches_oracle(api, orc, wl, tracer, set_builder):
