@@ -111,6 +111,35 @@ def test_gpu_tree_degenerate_inputs(gpu_tracer, api, builder):
     gpu_tracer.select("while-while")
 
 
+def test_gpu_tree_nan_vertices(gpu_tracer, wl, orc, builder):
+    """Triangles with NaN vertex coordinates (which the host builder refuses) go into the tree
+    without an error or an endless build, and are never hit; every other hit equals the
+    oracle's on the finite triangles alone, up to near-ties."""
+    sc = wl.soup(77, 3000, sigma=0.5)
+    lo, hi = sc.bounds()
+    rays = wl.shell_rays(78, lo, hi, 20000)
+    nv = sc.vpos.shape[0]
+    nan_v = np.array([[np.nan, 0, 0, 0], [0, np.nan, 0, 0], [np.nan, np.nan, np.nan, 0]], np.float32)
+    v = np.concatenate([sc.vpos, nan_v])
+    bad = []
+    for k in range(30):  # one, two or three NaN vertices
+        good = [int(x) for x in sc.tris[(7 * k) % sc.tris.shape[0], :3]]
+        cut = 1 + k % 3
+        bad.append([nv + (k + j) % 3 if j < cut else good[j] for j in range(3)] + [0])
+    t = np.concatenate([sc.tris, np.array(bad, np.uint32)])
+    info = gpu_tracer.build_device(_dev(v, np.float32), _dev(t, np.uint32), max_tris=2)
+    assert info["tri_records"] == t.shape[0]
+    want, _ = orc.OracleBVH(sc.vpos, sc.tris).closest(rays)
+    want_any, _ = orc.OracleBVH(sc.vpos, sc.tris).any(rays)
+    for tracer in ("while-while", "persistent-speculative-while-while"):
+        gpu_tracer.select(tracer)
+        got = _trace(gpu_tracer, rays, False)
+        assert (got.view(np.uint32)[:, 3] < sc.tris.shape[0]).all(), "a NaN triangle was hit"
+        assert_hits_match(got, want, False, f"NaN vertices, {tracer}")
+        assert (_occluded(_trace(gpu_tracer, rays, True)) == want_any).all(), tracer
+    gpu_tracer.select("while-while")
+
+
 def test_gpu_tree_errors(gpu_tracer, api):
     import torch
     v = _dev(np.zeros((3, 4)), np.float32)
