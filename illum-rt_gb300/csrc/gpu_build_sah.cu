@@ -148,35 +148,84 @@ __device__ __forceinline__ int task_of_pos(const sah_task *tasks, int cnt, int j
     return k;
 }
 
-// per position: its node, its interval, and the interval's count and box
+// Per position: its node, its interval, and the interval's count and box. A block whose
+// positions all lie in one node (most blocks of the top levels, where one node holds many
+// blocks' worth) accumulates in shared memory and adds each interval it touched to the global
+// bins once; other blocks add every position to the global bins. Counts, minima and maxima do
+// not depend on the order of the additions, so the bins are the same either way.
 __global__ void __launch_bounds__(kT) k_sah_bin(const sah_task *__restrict__ tasks, const int *__restrict__ n_tasks,
                                                 const uint32_t *__restrict__ idx, const float4 *__restrict__ plo,
                                                 const float4 *__restrict__ phi, int n, int planes, int32_t *task_of,
                                                 uint16_t *binpos, sah_bin *bins) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n) return;
+    __shared__ uint32_t s_cnt[kMaxSahPlanes + 1], s_lo[3][kMaxSahPlanes + 1], s_hi[3][kMaxSahPlanes + 1];
+    __shared__ int s_task;
+    const int j0 = blockIdx.x * blockDim.x;
+    const int j = j0 + threadIdx.x;
     const int cnt = *n_tasks;
-    const int k = task_of_pos(tasks, cnt, j);
-    task_of[j] = k;
-    if (k < 0) return;
-    const sah_task t = tasks[k];
-    const float surf = surface_rn(t.lo.x, t.lo.y, t.lo.z, t.hi.x, t.hi.y, t.hi.z);
-    if (!(surf > 0.f)) return;  // split at the median, no bins
-    const int m = t.m.z - t.m.y, P = min(planes, m);
-    const int ax = major_axis(t.lo.x, t.lo.y, t.lo.z, t.hi.x, t.hi.y, t.hi.z);
-    const float blo = comp(t.lo, ax), q = __fdiv_rn(__fsub_rn(comp(t.hi, ax), blo), (float)(P + 1));
-    const uint32_t p = idx[j];
-    const float4 l = plo[p], h = phi[p];
-    const int b = bin_of(centre(comp(l, ax), comp(h, ax)), blo, q, P);
-    binpos[j] = (uint16_t)b;
-    sah_bin *B = bins + (size_t)t.m.y + k + b;
-    atomicAdd(&B->cnt, 1u);
-    atomicMin(&B->lo[0], ordered(l.x));
-    atomicMin(&B->lo[1], ordered(l.y));
-    atomicMin(&B->lo[2], ordered(l.z));
-    atomicMax(&B->hi[0], ordered(h.x));
-    atomicMax(&B->hi[1], ordered(h.y));
-    atomicMax(&B->hi[2], ordered(h.z));
+    if (threadIdx.x == 0) {
+        const int jl = min(j0 + (int)blockDim.x, n) - 1;
+        const int k0 = task_of_pos(tasks, cnt, j0), k1 = task_of_pos(tasks, cnt, jl);
+        s_task = (k0 >= 0 && k0 == k1) ? k0 : -1;
+    }
+    for (int b = threadIdx.x; b <= kMaxSahPlanes; b += blockDim.x) {
+        s_cnt[b] = 0u;
+        s_lo[0][b] = s_lo[1][b] = s_lo[2][b] = kFull;
+        s_hi[0][b] = s_hi[1][b] = s_hi[2][b] = 0u;
+    }
+    __syncthreads();
+    const int local = s_task;
+    int k = -1;
+    if (j < n) {
+        k = local >= 0 ? local : task_of_pos(tasks, cnt, j);
+        task_of[j] = k;
+    }
+    if (k >= 0) {
+        const sah_task t = tasks[k];
+        const float surf = surface_rn(t.lo.x, t.lo.y, t.lo.z, t.hi.x, t.hi.y, t.hi.z);
+        if (surf > 0.f) {  // otherwise the node is split at the median, with no bins
+            const int m = t.m.z - t.m.y, P = min(planes, m);
+            const int ax = major_axis(t.lo.x, t.lo.y, t.lo.z, t.hi.x, t.hi.y, t.hi.z);
+            const float blo = comp(t.lo, ax), q = __fdiv_rn(__fsub_rn(comp(t.hi, ax), blo), (float)(P + 1));
+            const uint32_t p = idx[j];
+            const float4 l = plo[p], h = phi[p];
+            const int b = bin_of(centre(comp(l, ax), comp(h, ax)), blo, q, P);
+            binpos[j] = (uint16_t)b;
+            if (local >= 0) {
+                atomicAdd(&s_cnt[b], 1u);
+                atomicMin(&s_lo[0][b], ordered(l.x));
+                atomicMin(&s_lo[1][b], ordered(l.y));
+                atomicMin(&s_lo[2][b], ordered(l.z));
+                atomicMax(&s_hi[0][b], ordered(h.x));
+                atomicMax(&s_hi[1][b], ordered(h.y));
+                atomicMax(&s_hi[2][b], ordered(h.z));
+            } else {
+                sah_bin *B = bins + (size_t)t.m.y + k + b;
+                atomicAdd(&B->cnt, 1u);
+                atomicMin(&B->lo[0], ordered(l.x));
+                atomicMin(&B->lo[1], ordered(l.y));
+                atomicMin(&B->lo[2], ordered(l.z));
+                atomicMax(&B->hi[0], ordered(h.x));
+                atomicMax(&B->hi[1], ordered(h.y));
+                atomicMax(&B->hi[2], ordered(h.z));
+            }
+        }
+    }
+    __syncthreads();
+    if (local >= 0) {
+        const sah_task t = tasks[local];
+        const int P = min(planes, t.m.z - t.m.y);
+        sah_bin *B = bins + (size_t)t.m.y + local;
+        for (int b = threadIdx.x; b <= P; b += blockDim.x) {
+            if (s_cnt[b] == 0u) continue;
+            atomicAdd(&B[b].cnt, s_cnt[b]);
+            atomicMin(&B[b].lo[0], s_lo[0][b]);
+            atomicMin(&B[b].lo[1], s_lo[1][b]);
+            atomicMin(&B[b].lo[2], s_lo[2][b]);
+            atomicMax(&B[b].hi[0], s_hi[0][b]);
+            atomicMax(&B[b].hi[1], s_hi[1][b]);
+            atomicMax(&B[b].hi[2], s_hi[2][b]);
+        }
+    }
 }
 
 struct box_acc {
