@@ -974,9 +974,9 @@ def run_gputree(args):
 
 
 def run_profile_case(paths: int, tracer: str | None = None):
-    """One tuned step, then one plain step (no graphs; 1,048,576 paths unless asked otherwise):
-    a case whose launches ncu can capture one by one. `tracer` replaces the tuned form's tracer
-    (the tuning table's launch parameters stay)."""
+    """One tuned step, then one plain step on the same tree in the speculative order (no graphs;
+    1,048,576 paths unless asked otherwise): a case whose launches ncu can capture one by one.
+    `tracer` replaces the tuned form's tracer (the tuning table's launch parameters stay)."""
     import torch
     import __graft_entry__ as ge
     global N_PATHS
@@ -987,12 +987,13 @@ def run_profile_case(paths: int, tracer: str | None = None):
     if tracer:
         tuning = dict(tuning, tracer=tracer)
     step = Step(api, wl, 0, tuning)
+    step.rt_tt.select("speculative-while-while")  # the plain form's fastest order on GB300
     step.p_fused.use_graph = 0
     step.p_plain.use_graph = 0
     step.tuned()
-    step.plain()
+    step.plain_tuned_tree()
     step.rt.check(step.sp)
-    step.rt_plain.check(step.sp)
+    step.rt_tt.check(step.sp)
     print(json.dumps({"profile_case": "ok", "paths": N_PATHS, "rays": rays_in_results(step)}))
 
 
