@@ -470,24 +470,47 @@ __device__ __forceinline__ void spec_node(trav_t &s, const dev_scene &sc, const 
     bool hl, hr;
     int32_t cl, cr;
     node_test<ANY, PLAIN>(sc.nodes + 4 * (size_t)s.cur, s, r, hl, hr, dl, dr, cl, cr);
+    if (ANY) {
+        if (hl && hr) {
+            const bool left_first = dl < dr;
+            if (s.sp >= cap) {
+                atomicOr(err, ERR_STACK_OVERFLOW);
+                s.done = true;
+                return;
+            }
+            stk[s.sp * stride] = left_first ? cr : cl;
+            ++s.sp;
+            s.cur = left_first ? cl : cr;
+        } else if (hl || hr) {
+            s.cur = hl ? cl : cr;
+        } else if (s.sp == 0) {
+            s.more = false;
+        } else {
+            --s.sp;
+            s.cur = stk[s.sp * stride];
+        }
+        return;
+    }
+    // Closest hit: the same choices with one selection of the near and far child and the pop as
+    // a predicated load instead of three branches (on GB300 0.8 % off the fused path loop; the
+    // any-hit kernels compiled this way ran 3 % slower, so they keep the branches above).
+    // Near child: the left one if only it is entered, or both are and it is nearer (ties right).
+    const bool left_first = hl && (!hr || dl < dr);
+    const int32_t nearc = left_first ? cl : cr, farc = left_first ? cr : cl;
     if (hl && hr) {
-        const bool left_first = dl < dr;
         if (s.sp >= cap) {
             atomicOr(err, ERR_STACK_OVERFLOW);
             s.done = true;
             return;
         }
-        stk[s.sp * stride] = left_first ? cr : cl;
+        stk[s.sp * stride] = farc;
         ++s.sp;
-        s.cur = left_first ? cl : cr;
-    } else if (hl || hr) {
-        s.cur = hl ? cl : cr;
-    } else if (s.sp == 0) {
-        s.more = false;
-    } else {
-        --s.sp;
-        s.cur = stk[s.sp * stride];
     }
+    const bool pop = !hl && !hr && s.sp > 0;
+    s.sp -= pop ? 1 : 0;
+    const int32_t popped = pop ? stk[s.sp * stride] : nearc;
+    s.more = s.more && (hl || hr || pop);  // no child entered and nothing stacked: the search ends
+    s.cur = (hl || hr) ? nearc : popped;
 }
 
 // Visit of a 4-wide node: four slab tests, the hit children ordered by entry distance (a
