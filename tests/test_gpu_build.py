@@ -140,6 +140,39 @@ def test_gpu_tree_nan_vertices(gpu_tracer, wl, orc, builder):
     gpu_tracer.select("while-while")
 
 
+def test_gpu_trees_are_deterministic(api, wl, builder):
+    """The same scene built twice, and built as one scene of a set whose scenes are built
+    concurrently on several host threads, gives the same tree: every closest hit bit for bit."""
+    import torch
+    sc = wl.soup(91, 40000, sigma=0.5)
+    lo, hi = sc.bounds()
+    rays = wl.shell_rays(92, lo, hi, 30000)
+    v, t = _dev(sc.vpos, np.float32), _dev(sc.tris, np.uint32)
+    got = []
+    for _ in range(2):
+        rt = api.BatchRayTracer(0)
+        rt.set_device_builder(builder)
+        rt.build_device(v, t, max_tris=2)
+        rt.select("while-while")
+        got.append(_trace(rt, rays, False))
+        rt.close()
+    assert (got[0].view(np.uint32) == got[1].view(np.uint32)).all()
+    others = [wl.soup(93 + i, 5000 + 3000 * i, sigma=0.5) for i in range(6)]
+    scenes = [(_dev(o.vpos, np.float32), _dev(o.tris, np.uint32)) for o in others[:3]] + [(v, t)] + \
+             [(_dev(o.vpos, np.float32), _dev(o.tris, np.uint32)) for o in others[3:]]
+    rt = api.BatchRayTracer(0)
+    rt.set_device_builder(builder)
+    rt.build_scenes_device(scenes, max_tris=2)
+    rt.select("persistent-while-while")
+    d = _dev(rays, np.float32)
+    out = torch.zeros((rays.shape[0], 4), device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    rt.trace_multi([(3, d, out)], any_hit=False, stream=stream)
+    rt.check(stream, timeout_ms=60000)
+    assert (out.cpu().numpy().view(np.uint32) == got[0].view(np.uint32)).all()
+    rt.close()
+
+
 def test_gpu_tree_errors(gpu_tracer, api):
     import torch
     v = _dev(np.zeros((3, 4)), np.float32)
