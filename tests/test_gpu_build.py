@@ -1,6 +1,6 @@
 """GPU BVH construction (grt_build_device, grt_build_scenes_device): trees built on the GPU
-from device arrays, with both tree builders (PLOC clustering and the Morton radix tree), traced
-by every tracer, against the oracle on the reference's tree.
+from device arrays, with each tree builder (top-down SAH, PLOC clustering and the Morton radix
+tree), traced by every tracer, against the oracle on the reference's tree.
 Closest hits may differ from the reference only as near-ties (another tree visits triangles in
 another order); any-hit answers are equal. Also: degenerate inputs, errors, and the statistics
 of the trees."""
