@@ -1,13 +1,14 @@
 // C-ABI of the GPU builder (include/grt.h): grt_build_device for the context's scene and
-// grt_build_scenes_device for a scene set. The kernels are in gpu_build.cu; this file owns the
-// allocations, the read-back of each tree's depth and stack bound, and the checks the host
-// builder makes (indices in range, depth within the traversal stacks).
+// grt_build_scenes_device for a scene set. The kernels are in gpu_build.cu and gpu_build_sah.cu;
+// this file owns the allocations, the host threads of a scene-set build, the read-back of each
+// tree's depth and stack bound, and the checks the host builder makes (indices in range, depth
+// within the traversal stacks).
 #include <algorithm>
 #include <array>
 #include <atomic>
 #include <chrono>
-#include <thread>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "ctx.hpp"
