@@ -82,8 +82,8 @@ cudaError_t enqueue_pathtrace(grt_ctx *c, const grt_pt_params &p, const pt_param
         e = launch_compact_hits(prim_hits, n_primary, hit_list, n_list, at<uint32_t>(c, L.compact), st);
     if (e != cudaSuccess) return e;
     if (p.mode == GRT_PT_FUSED)
-        return launch_fused(scene_for(c), ps, pp, (const float4 *)prim_rays, prim_hits, hit_list, n_list, n_paths, results,
-                            bounce_hits, lp, c->d_err, c->d_counter, at<float4>(c, L.starts), st);
+        return launch_fused(scene_for(c), ps, pp, (const float4 *)prim_rays, prim_hits, n_primary, hit_list, n_list,
+                            n_paths, results, bounce_hits, lp, c->d_err, c->d_counter, at<float4>(c, L.starts), st);
     uint32_t *queue[2] = {at<uint32_t>(c, L.queue0), at<uint32_t>(c, L.queue1)};
     float4 *rays[2] = {at<float4>(c, L.rays0), at<float4>(c, L.rays1)};
     grt_hit *hits = at<grt_hit>(c, L.hits);

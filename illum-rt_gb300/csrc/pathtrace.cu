@@ -12,6 +12,7 @@
 //     a warp's lanes are still busy.
 // Both produce the same per-path results: the math is shared (pt_math.cuh) and each path's
 // random stream depends only on its index.
+#include <algorithm>
 #include <mutex>
 
 #include "pathtrace.hpp"
@@ -377,23 +378,50 @@ __global__ void k_wf_shade(pt_scene ps, pt_params_dev pp, const uint32_t *__rest
 
 // ---- fused persistent form ----------------------------------------------------------------
 
-// First bounce ray and generator state of every path, one thread per path, launched just before
-// the fused kernel: a lane that takes a path then reads 32 coalesced bytes instead of following
-// four dependent loads (hit list -> primary ray and hit -> triangle -> vertices) while its warp
-// waits (on GB300 this took 2.3 % off the fused launch, the extra kernel included).
+// First bounce ray and generator state of every path, launched just before the fused kernel: a
+// lane that takes a path then reads 32 coalesced bytes instead of following four dependent
+// loads (hit list -> primary ray and hit -> triangle -> vertices) while its warp waits (on
+// GB300 this took 2.3 % off the fused launch, the extra kernel included). The paths of one
+// primary hit (p = i + |H| m) share its origin and normal, so a thread takes hit-list entry i and
+// up to kStartsPerThread of its paths: one chain of dependent loads for all of them.
 // starts[2p] = (origin, low word of the PCG32 state after the two direction draws),
 // starts[2p + 1] = (direction, high word); t_min = eps, t_max = FLT_MAX for every first ray.
+constexpr uint32_t kStartsPerThread = 4;
+
 __global__ void k_pt_starts(pt_scene ps, pt_params_dev pp, const float4 *__restrict__ prim_rays,
                             const grt_hit *__restrict__ prim_hits, const uint32_t *__restrict__ hit_list,
                             const uint32_t *__restrict__ n_list, uint32_t n_paths, float4 *starts) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t nl = *n_list;
-    if (p >= n_paths || nl == 0) return;
-    path_t st;
-    float4 ro, rd;
-    path_start(ps, pp, p, prim_rays, prim_hits, hit_list, nl, st, ro, rd);
-    starts[2 * (size_t)p] = make_float4(ro.x, ro.y, ro.z, __uint_as_float((uint32_t)st.rng.state));
-    starts[2 * (size_t)p + 1] = make_float4(rd.x, rd.y, rd.z, __uint_as_float((uint32_t)(st.rng.state >> 32)));
+    if (nl == 0) return;
+    // thread t: entry li = t mod |H| and its paths li + |H| (kStartsPerThread g + k), g = t / |H|
+    const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    const uint64_t g = t / nl;
+    const uint32_t li = (uint32_t)(t - g * nl);
+    const uint64_t p0 = li + (uint64_t)nl * g * kStartsPerThread;
+    if (p0 >= n_paths) return;
+    const uint32_t i = __ldg(hit_list + li);
+    const float4 a = __ldg(prim_rays + 2 * (size_t)i), b = __ldg(prim_rays + 2 * (size_t)i + 1);
+    const float4 h = __ldg(reinterpret_cast<const float4 *>(prim_hits) + i);
+    const pm::f3 o = {a.x, a.y, a.z}, d = {b.x, b.y, b.z};
+    uint32_t m;
+    const pm::f3 n = tri_normal(ps, __float_as_uint(h.w), d, m);
+    const pm::f3 org = pm::offset_hit_point(o, d, h.x, n, pp.eps);
+    for (uint32_t k = 0; k < kStartsPerThread; ++k) {
+        const uint64_t p = p0 + (uint64_t)nl * k;
+        if (p >= n_paths) break;
+        pm::pcg32 rng;
+        rng.set_sequence((uint64_t)pp.seed + p);  // as path_start
+        const float u0 = rng.uniform(), u1 = rng.uniform();
+        const pm::f3 dir = pm::align(pm::cosine_sample_hemisphere(u0, u1), n);
+        starts[2 * p] = make_float4(org.x, org.y, org.z, __uint_as_float((uint32_t)rng.state));
+        starts[2 * p + 1] = make_float4(dir.x, dir.y, dir.z, __uint_as_float((uint32_t)(rng.state >> 32)));
+    }
+}
+
+// Threads k_pt_starts needs at most for n_paths paths over |H| <= min(n_primary, n_paths) used
+// entries: |H| ceil(ceil(n_paths / |H|) / K) <= n_paths / K + 2 |H|.
+inline uint64_t starts_threads(uint32_t n_paths, uint32_t n_primary) {
+    return (uint64_t)n_paths / kStartsPerThread + 2 * (uint64_t)std::min(n_primary, n_paths) + 1;
 }
 
 // Each warp alternates between two phases (a lane takes a new path's first ray from `starts`).
@@ -540,14 +568,16 @@ fused_fn_t fused_kernel(int order, bool alpha, int fp) {
 
 template <int ORDER>
 cudaError_t fused_launch(const dev_scene &sc, const pt_scene &ps, const pt_params_dev &pp, const float4 *prim_rays,
-                         const grt_hit *prim_hits, const uint32_t *hit_list, const uint32_t *n_list, uint32_t n_paths,
+                         const grt_hit *prim_hits, uint32_t n_primary, const uint32_t *hit_list,
+                         const uint32_t *n_list, uint32_t n_paths,
                          grt_path_result *results, grt_hit *bounce_hits, const launch_params &lp, unsigned *err,
                          unsigned *counter, float4 *starts, cudaStream_t st) {
     const size_t smem = (size_t)(lp.stack_entries * sizeof(int) + kPathSlotBytes) * lp.block_threads;
     const fused_fn_t kern = fused_kernel_of<ORDER>(sc.alpha != nullptr, fast_path_of(lp.spec));
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
-    k_pt_starts<<<(n_paths + 255) / 256, 256, 0, st>>>(ps, pp, prim_rays, prim_hits, hit_list, n_list, n_paths, starts);
+    k_pt_starts<<<(unsigned)((starts_threads(n_paths, n_primary) + 255) / 256), 256, 0, st>>>(
+        ps, pp, prim_rays, prim_hits, hit_list, n_list, n_paths, starts);
     kern<<<lp.grid_blocks, lp.block_threads, smem, st>>>(sc, ps, pp, prim_rays, prim_hits, hit_list, n_list, n_paths,
                                                          results, bounce_hits, err, counter, lp.refill_threshold,
                                                          lp.refill_period, lp.stack_entries, lp.spec, starts);
@@ -602,7 +632,8 @@ cudaError_t launch_wavefront_shade(const pt_scene &ps, const pt_params_dev &pp, 
 size_t wavefront_state_bytes() { return sizeof(wf_state); }
 
 cudaError_t launch_fused(const dev_scene &sc, const pt_scene &ps, const pt_params_dev &pp, const float4 *prim_rays,
-                         const grt_hit *prim_hits, const uint32_t *hit_list, const uint32_t *n_list, uint32_t n_paths,
+                         const grt_hit *prim_hits, uint32_t n_primary, const uint32_t *hit_list,
+                         const uint32_t *n_list, uint32_t n_paths,
                          grt_path_result *results, grt_hit *bounce_hits, const launch_params &lp, unsigned *err,
                          unsigned *counter, float4 *starts, cudaStream_t st) {
     if (n_paths == 0) return cudaSuccess;
@@ -611,8 +642,8 @@ cudaError_t launch_fused(const dev_scene &sc, const pt_scene &ps, const pt_param
              : lp.order == SPECULATIVE      ? fused_launch<SPECULATIVE>
              : lp.order == WIDE_SPECULATIVE ? fused_launch<WIDE_SPECULATIVE>
                                             : fused_launch<IF_IF>;
-    return f(sc, ps, pp, prim_rays, prim_hits, hit_list, n_list, n_paths, results, bounce_hits, lp, err, counter, starts,
-             st);
+    return f(sc, ps, pp, prim_rays, prim_hits, n_primary, hit_list, n_list, n_paths, results, bounce_hits, lp, err,
+             counter, starts, st);
 }
 
 cudaError_t prepare_pt_kernels() {

@@ -39,7 +39,8 @@ cudaError_t launch_wavefront_shade(const pt_scene &ps, const pt_params_dev &pp, 
                                    grt_hit *bounce_hits, cudaStream_t st);
 
 cudaError_t launch_fused(const dev_scene &sc, const pt_scene &ps, const pt_params_dev &pp, const float4 *prim_rays,
-                         const grt_hit *prim_hits, const uint32_t *hit_list, const uint32_t *n_list, uint32_t n_paths,
+                         const grt_hit *prim_hits, uint32_t n_primary, const uint32_t *hit_list,
+                         const uint32_t *n_list, uint32_t n_paths,
                          grt_path_result *results, grt_hit *bounce_hits, const launch_params &lp, unsigned *err,
                          unsigned *counter, float4 *starts, cudaStream_t st);
 int fused_blocks_per_sm(int block_threads, int stack_entries, int order, bool alpha, const spec_cfg &spec);
