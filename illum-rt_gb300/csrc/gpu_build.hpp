@@ -1,5 +1,6 @@
-// BVH construction on the GPU (linear BVH with SAH leaf collapse), written in the device layout
-// of bvh_builder.hpp: 64-byte binary nodes, 48-byte triangle records and 128-byte 4-wide nodes.
+// BVH construction on the GPU (top-down binned SAH, PLOC clustering or linear BVH, each with SAH
+// leaf collapse), written in the device layout of bvh_builder.hpp: 64-byte binary nodes, 48-byte
+// triangle records and 128-byte 4-wide nodes.
 #pragma once
 #include <cuda_runtime.h>
 
