@@ -1,8 +1,9 @@
 // C-ABI of the GPU builder (include/grt.h): grt_build_device for the context's scene and
 // grt_build_scenes_device for a scene set. The kernels are in gpu_build.cu and gpu_build_sah.cu;
-// this file owns the allocations, the host threads of a scene-set build, the read-back of each
+// this file owns the allocations, the host threads of a scene-set build and, with the SAH
+// method, the grouping of its scenes whose trees are built together, the read-back of each
 // tree's depth and stack bound, and the checks the host builder makes (indices in range, depth
-// within the traversal stacks).
+// within the traversal stacks, a well-formed tree).
 #include <algorithm>
 #include <array>
 #include <atomic>
@@ -27,14 +28,16 @@ struct build_temps {
     void *scratch = nullptr;
     int32_t *wide_index = nullptr;
     int32_t *info = nullptr;
+    void *set = nullptr;  // a scene set's arrays for the SAH trees
     ~build_temps() {
-        for (void *p : {scratch, (void *)wide_index, (void *)info})
+        for (void *p : {scratch, (void *)wide_index, (void *)info, set})
             if (p) cudaFree(p);
     }
 };
 
 grt_status check_info(grt_ctx *c, const int32_t *info, const std::string &what) {
     if (info[GB_ERR] & GB_ERR_INDEX) return fail(c, GRT_ERR_INVALID_ARG, what + "a triangle index is beyond the vertex count");
+    if (info[GB_ERR] & GB_ERR_TREE) return fail(c, GRT_ERR_TRAVERSAL, what + "the GPU builder made a malformed tree");
     if ((info[GB_ERR] & GB_ERR_DEPTH) || info[GB_DEPTH] > kStackLarge)
         return fail(c, GRT_ERR_BVH_TOO_DEEP,
                     what + "BVH depth " + std::to_string(info[GB_DEPTH]) +
@@ -275,54 +278,111 @@ grt_status grt_build_scenes_device(grt_ctx *c, const grt_mesh *meshes, uint32_t 
     build_temps tmp;
     int32_t *wide_pool = nullptr;
     const int method = builder_method(c->device_builder);
-    const size_t scratch = gpu_build_scratch_bytes(most, method);
+    // With the SAH method the trees of a group of scenes are built together (gpu_build.cu's
+    // scene-set phases): groups of consecutive scenes of at most kSahSetMaxTris triangles.
+    const bool batched = method == GB_METHOD_SAH;
+    std::vector<uint32_t> group_at{0};
+    size_t set_bytes = 0;
+    if (batched) {
+        uint64_t in_group = 0;
+        for (uint32_t i = 0; i < count; ++i) {
+            if (in_group + meshes[i].nt > kSahSetMaxTris && i > group_at.back()) {
+                set_bytes = std::max(set_bytes, sah_set_carve(nullptr, (uint32_t)in_group, i - group_at.back()).total);
+                group_at.push_back(i);
+                in_group = 0;
+            }
+            in_group += meshes[i].nt;
+        }
+        set_bytes = std::max(set_bytes, sah_set_carve(nullptr, (uint32_t)in_group, count - group_at.back()).total);
+    }
+    group_at.push_back(count);
+    const size_t scratch = gpu_build_scratch_bytes(most, batched ? GB_METHOD_LBVH : method);
     cudaError_t e = cudaMalloc(&c->ms.d_nodes, tot[0]);
     if (e == cudaSuccess) e = cudaMalloc(&c->ms.d_recs, tot[1]);
     if (e == cudaSuccess) e = cudaMalloc((void **)&wide_pool, tot[2]);
-    if (e == cudaSuccess) e = cudaMalloc(&tmp.info, (size_t)count * 8 * 4);
+    // every scene's info, then the error word of the set trees
+    if (e == cudaSuccess) e = cudaMalloc(&tmp.info, ((size_t)count + 1) * 8 * 4);
+    if (e == cudaSuccess) e = cudaMemsetAsync(tmp.info + 8 * (size_t)count, 0, 8 * 4, st);
+    if (e == cudaSuccess && batched) e = cudaMalloc(&tmp.set, set_bytes);
     tmp.wide_index = wide_pool;
-    // The scenes are built by up to kBuildWorkers host threads, each on a stream of its own with
+    // Per-scene passes run on up to kBuildWorkers host threads, each on a stream of its own with
     // scratch of its own: a build is a chain of short launches (and, for the SAH and PLOC
-    // builders, read-backs), so one scene at a time leaves most of the GPU idle. The worker
-    // streams start after earlier work on `st`, and `st` waits for all of them.
+    // builders, read-backs), so one scene at a time leaves most of the GPU idle.
     const int workers = (int)std::min<uint32_t>(count, kBuildWorkers);
     std::vector<cudaStream_t> wst(workers, nullptr);
     std::vector<void *> wscratch(workers, nullptr);
     std::vector<cudaEvent_t> wdone(workers, nullptr);
     cudaEvent_t ready = nullptr;
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ready, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventRecord(ready, st);
     for (int w = 0; w < workers && e == cudaSuccess; ++w) {
         e = cudaStreamCreateWithFlags(&wst[w], cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&wdone[w], cudaEventDisableTiming);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(wst[w], ready, 0);
         if (e == cudaSuccess) e = cudaMalloc(&wscratch[w], scratch);
     }
-    if (e == cudaSuccess) {
-        std::atomic<uint32_t> next{0};
+    // fn(w, i) for the scenes [i0, i1) on the worker threads; the worker streams start after the
+    // work already on `st`, and `st` waits for all of them
+    auto on_workers = [&](uint32_t i0, uint32_t i1, auto fn) -> cudaError_t {
+        cudaError_t r = cudaEventRecord(ready, st);
+        for (int w = 0; w < workers && r == cudaSuccess; ++w) r = cudaStreamWaitEvent(wst[w], ready, 0);
+        if (r != cudaSuccess) return r;
+        std::atomic<uint32_t> next{i0};
         std::vector<cudaError_t> werr(workers, cudaSuccess);
         std::vector<std::thread> pool;
         for (int w = 0; w < workers; ++w)
             pool.emplace_back([&, w] {
                 werr[w] = cudaSetDevice(c->device);
-                for (uint32_t i; werr[w] == cudaSuccess && (i = next++) < count;) {
-                    const grt_mesh &m = meshes[i];
-                    werr[w] = gpu_build_binary((const float4 *)m.vpos4, m.nv, (const uint4 *)m.tris4, m.nt,
-                                               (int)max_tris, wscratch[w], scratch,
-                                               (float4 *)((char *)c->ms.d_nodes + off[i][0]),
-                                               (float4 *)((char *)c->ms.d_recs + off[i][1]),
-                                               (int32_t *)((char *)wide_pool + off[i][2]), nullptr,
-                                               tmp.info + 8 * (size_t)i, method, c->device_planes, wst[w]);
-                }
+                for (uint32_t i; werr[w] == cudaSuccess && (i = next++) < i1;) werr[w] = fn(w, i);
                 if (werr[w] == cudaSuccess) werr[w] = cudaEventRecord(wdone[w], wst[w]);
             });
         for (auto &t : pool) t.join();
         for (int w = 0; w < workers; ++w) {
-            if (e == cudaSuccess) e = werr[w];
-            if (e == cudaSuccess) e = cudaStreamWaitEvent(st, wdone[w], 0);
+            if (r == cudaSuccess) r = werr[w];
+            if (r == cudaSuccess) r = cudaStreamWaitEvent(st, wdone[w], 0);
         }
+        return r;
+    };
+    auto nodes_of = [&](uint32_t i) { return (float4 *)((char *)c->ms.d_nodes + off[i][0]); };
+    auto recs_of = [&](uint32_t i) { return (float4 *)((char *)c->ms.d_recs + off[i][1]); };
+    auto wide_of = [&](uint32_t i) { return (int32_t *)((char *)wide_pool + off[i][2]); };
+    // one scene on its own (`how`: the builder)
+    auto alone = [&](int how) {
+        return [&, how](int w, uint32_t i) {
+            const grt_mesh &m = meshes[i];
+            return gpu_build_binary((const float4 *)m.vpos4, m.nv, (const uint4 *)m.tris4, m.nt, (int)max_tris,
+                                    wscratch[w], scratch, nodes_of(i), recs_of(i), wide_of(i), nullptr,
+                                    tmp.info + 8 * (size_t)i, how, c->device_planes, wst[w]);
+        };
+    };
+    if (e == cudaSuccess && !batched) e = on_workers(0, count, alone(method));
+    for (size_t g = 0; batched && e == cudaSuccess && g + 1 < group_at.size(); ++g) {
+        const uint32_t i0 = group_at[g], i1 = group_at[g + 1];
+        std::vector<sah_set_scene> table(i1 - i0);
+        uint32_t n_g = 0;
+        for (uint32_t i = i0; i < i1; ++i) {
+            table[i - i0] = sah_set_scene{n_g, meshes[i].nt};
+            n_g += meshes[i].nt;
+        }
+        if (n_g < 2) {  // no scene to split (one triangle at most): the radix-tree path is the same
+            e = on_workers(i0, i1, alone(GB_METHOD_LBVH));
+            continue;
+        }
+        const sah_set S = sah_set_carve(tmp.set, n_g, i1 - i0);
+        for (uint32_t i = i0; i < i1 && e == cudaSuccess; ++i) {
+            const grt_mesh &m = meshes[i];
+            e = sah_set_prims(S, i - i0, table[i - i0].first, (const float4 *)m.vpos4, m.nv, (const uint4 *)m.tris4,
+                              m.nt, tmp.info + 8 * (size_t)i, st);
+        }
+        const uint32_t *order = nullptr;
+        if (e == cudaSuccess) e = sah_set_trees(S, table.data(), c->device_planes, &order, tmp.info + 8 * (size_t)count, st);
+        if (e == cudaSuccess)
+            e = on_workers(i0, i1, [&](int w, uint32_t i) {
+                const grt_mesh &m = meshes[i];
+                return sah_set_finish(S, order, table[i - i0].first, (const float4 *)m.vpos4, m.nv,
+                                      (const uint4 *)m.tris4, m.nt, (int)max_tris, wscratch[w], scratch, nodes_of(i),
+                                      recs_of(i), wide_of(i), tmp.info + 8 * (size_t)i, wst[w]);
+            });
     }
-    std::vector<int32_t> info((size_t)count * 8, 0);
+    std::vector<int32_t> info(((size_t)count + 1) * 8, 0);
     if (e == cudaSuccess) e = cudaMemcpyAsync(info.data(), tmp.info, info.size() * 4, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     for (int w = 0; w < workers; ++w) {  // every worker stream has finished, or the call fails anyway
@@ -350,6 +410,10 @@ grt_status grt_build_scenes_device(grt_ctx *c, const grt_mesh *meshes, uint32_t 
         max_bound4 = std::max(max_bound4, (uint32_t)f[GB_BOUND4]);
         off4[i] = tot4;
         tot4 += a256((size_t)std::max(f[GB_WIDE_NODES], 1) * 128);
+    }
+    if (info[8 * (size_t)count + GB_ERR] & GB_ERR_TREE) {  // the trees built for the whole set
+        grt_free_multi(c);
+        return fail(c, GRT_ERR_TRAVERSAL, "the GPU builder made a malformed tree");
     }
     e = cudaMalloc(&c->ms.d_nodes4, tot4);
     for (uint32_t i = 0; i < count && e == cudaSuccess; ++i)

@@ -917,6 +917,51 @@ cudaError_t ploc_tree(const arena &A, int n, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+// The passes after the tree, for every method: boxes and leaf collapse bottom-up, the
+// depth-first layout, the triangle records and the 4-wide indices. `A` holds the boxes and the
+// tree (children, range, parent links) and the scratch; its visit counts are zero and its
+// collapse flags one on entry.
+cudaError_t build_tail(const arena &A, const float4 *vpos, uint32_t nv, const uint4 *tris, uint32_t nt, int max_leaf,
+                       bool sah, const uint32_t *order, float4 *nodes, float4 *records, int32_t *wide_index,
+                       int32_t *links, int32_t *info, cudaStream_t st) {
+    const unsigned nb = blocks_for(nt);
+    size_t cb = A.cub_bytes;
+    cudaError_t e = cudaSuccess;
+    k_bottom_up<<<nb, kThreads, 0, st>>>(A.lo, A.hi, order, (int)nt, max_leaf, sah ? 1 : 0, A.children, A.range,
+                                         A.parent_inner, A.parent_leaf, A.slots, A.visits, A.collapsed, nodes,
+                                         info);
+    if (nt > 1) {
+        // depth-first layout; the bottom-up pass's slots and the sort's key and value arrays are
+        // free now and hold the new nodes, positions, parents and flags
+        float4 *tmp_nodes = (float4 *)A.slots;
+        int32_t *reach = A.flag, *icount = A.excl, *pos = (int32_t *)A.keys_a, *new_parent = (int32_t *)A.vals_a;
+        uint8_t *new_collapsed = (uint8_t *)A.keys_b;
+        e = cudaMemsetAsync(A.visits, 0, (size_t)nt * 4, st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(new_collapsed, 1, (size_t)nt, st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(new_parent, 0xff, (size_t)nt * 4, st);
+        if (e != cudaSuccess) return e;
+        k_reach<<<nb, kThreads, 0, st>>>((int)nt, A.collapsed, A.parent_inner, reach, info);
+        k_icount<<<nb, kThreads, 0, st>>>((int)nt, nodes, A.parent_inner, reach, A.visits, icount, info);
+        k_dfs_pos<<<nb, kThreads, 0, st>>>((int)nt, nodes, A.parent_inner, reach, icount, pos, info);
+        k_relayout<<<nb, kThreads, 0, st>>>((int)nt, nodes, A.parent_inner, reach, pos, tmp_nodes, new_parent,
+                                            new_collapsed);
+        e = cudaMemcpyAsync(nodes, tmp_nodes, (size_t)(nt - 1) * 64, cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(A.parent_inner, new_parent, (size_t)nt * 4, cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(A.collapsed, new_collapsed, (size_t)nt, cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) return e;
+    }
+    k_records<<<nb, kThreads, 0, st>>>(vpos, tris, order, nt, nv, records);
+    if (nt > 1) {
+        k_wide_flags<<<nb, kThreads, 0, st>>>((int)nt, A.collapsed, A.parent_inner, nodes, A.flag, links, info);
+        cb = A.cub_bytes;
+        e = cub::DeviceScan::ExclusiveSum(A.cub, cb, A.flag, A.excl, (int)nt, st);
+        if (e != cudaSuccess) return e;
+        k_wide_index<<<nb, kThreads, 0, st>>>((int)nt, A.flag, A.excl, wide_index, info);
+    }
+    return cudaGetLastError();
+}
+
 }  // namespace
 
 cudaError_t gpu_build_binary(const float4 *vpos, uint32_t nv, const uint4 *tris, uint32_t nt, int max_leaf,
@@ -959,39 +1004,86 @@ cudaError_t gpu_build_binary(const float4 *vpos, uint32_t nv, const uint4 *tris,
         k_radix_tree<<<blocks_for(nt - 1), kThreads, 0, st>>>(A.keys_b, (int)nt, A.children, A.range,
                                                               A.parent_inner, A.parent_leaf);
     }
-    k_bottom_up<<<nb, kThreads, 0, st>>>(A.lo, A.hi, order, (int)nt, max_leaf, sah ? 1 : 0, A.children, A.range,
-                                         A.parent_inner, A.parent_leaf, A.slots, A.visits, A.collapsed, nodes,
-                                         info);
-    if (nt > 1) {
-        // depth-first layout; the bottom-up pass's slots and the sort's key and value arrays are
-        // free now and hold the new nodes, positions, parents and flags
-        float4 *tmp_nodes = (float4 *)A.slots;
-        int32_t *reach = A.flag, *icount = A.excl, *pos = (int32_t *)A.keys_a, *new_parent = (int32_t *)A.vals_a;
-        uint8_t *new_collapsed = (uint8_t *)A.keys_b;
-        e = cudaMemsetAsync(A.visits, 0, (size_t)nt * 4, st);
-        if (e == cudaSuccess) e = cudaMemsetAsync(new_collapsed, 1, (size_t)nt, st);
-        if (e == cudaSuccess) e = cudaMemsetAsync(new_parent, 0xff, (size_t)nt * 4, st);
-        if (e != cudaSuccess) return e;
-        k_reach<<<nb, kThreads, 0, st>>>((int)nt, A.collapsed, A.parent_inner, reach, info);
-        k_icount<<<nb, kThreads, 0, st>>>((int)nt, nodes, A.parent_inner, reach, A.visits, icount, info);
-        k_dfs_pos<<<nb, kThreads, 0, st>>>((int)nt, nodes, A.parent_inner, reach, icount, pos, info);
-        k_relayout<<<nb, kThreads, 0, st>>>((int)nt, nodes, A.parent_inner, reach, pos, tmp_nodes, new_parent,
-                                            new_collapsed);
-        e = cudaMemcpyAsync(nodes, tmp_nodes, (size_t)(nt - 1) * 64, cudaMemcpyDeviceToDevice, st);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(A.parent_inner, new_parent, (size_t)nt * 4, cudaMemcpyDeviceToDevice, st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(A.collapsed, new_collapsed, (size_t)nt, cudaMemcpyDeviceToDevice, st);
-        if (e != cudaSuccess) return e;
-    }
-    k_records<<<nb, kThreads, 0, st>>>(vpos, tris, order, nt, nv, records);
-    if (nt > 1) {
-        k_wide_flags<<<nb, kThreads, 0, st>>>((int)nt, A.collapsed, A.parent_inner, nodes, A.flag, links, info);
-        cb = A.cub_bytes;
-        e = cub::DeviceScan::ExclusiveSum(A.cub, cb, A.flag, A.excl, (int)nt, st);
-        if (e != cudaSuccess) return e;
-        k_wide_index<<<nb, kThreads, 0, st>>>((int)nt, A.flag, A.excl, wide_index, info);
-    }
+    return build_tail(A, vpos, nv, tris, nt, max_leaf, sah, order, nodes, records, wide_index, links, info, st);
+}
+
+sah_set sah_set_carve(void *base, uint32_t n_total, uint32_t count) {
+    sah_set S{};
+    char *p = (char *)base;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        void *r = p ? p + off : nullptr;
+        off += up256(bytes);
+        return r;
+    };
+    const size_t m = n_total > 0 ? n_total : 1, c = count > 0 ? count : 1;
+    S.lo = (float4 *)take(m * 16);
+    S.hi = (float4 *)take(m * 16);
+    S.cbounds = (uint32_t *)take(c * 16 * 4);
+    S.children = (int2 *)take(m * 8);
+    S.range = (int2 *)take(m * 8);
+    S.parent_inner = (int32_t *)take(m * 4);
+    S.parent_leaf = (int32_t *)take(m * 4);
+    S.flag = (int32_t *)take(m * 4);
+    S.excl = (int32_t *)take(m * 4);
+    S.scenes = (sah_set_scene *)take(c * sizeof(sah_set_scene));
+    S.sah = take(sah_scratch_bytes((uint32_t)m));
+    S.cub_bytes = cub_bytes_for((uint32_t)m);
+    S.cub = take(S.cub_bytes);
+    S.total = off;
+    S.n = n_total;
+    S.count = count;
+    return S;
+}
+
+cudaError_t sah_set_prims(const sah_set &S, uint32_t i, uint32_t first, const float4 *vpos, uint32_t nv,
+                          const uint4 *tris, uint32_t nt, int32_t *info, cudaStream_t st) {
+    if (i >= S.count || (uint64_t)first + nt > S.n) return cudaErrorInvalidValue;
+    uint32_t *cb = S.cbounds + 16 * (size_t)i;
+    k_init_info<<<1, 32, 0, st>>>(info, cb);
+    if (nt) k_prims<<<blocks_for(nt), kThreads, 0, st>>>(vpos, nv, tris, nt, S.lo + first, S.hi + first, cb, info);
     return cudaGetLastError();
+}
+
+cudaError_t sah_set_trees(const sah_set &S, const sah_set_scene *scenes_host, int planes, const uint32_t **order,
+                          int32_t *set_info, cudaStream_t st) {
+    if (S.n < 2 || S.count == 0 || planes < 1 || planes > kMaxSahPlanes) return cudaErrorInvalidValue;
+    uint64_t at = 0;  // the scenes tile the positions in order
+    for (uint32_t i = 0; i < S.count; ++i) {
+        if (scenes_host[i].first != at) return cudaErrorInvalidValue;
+        at += scenes_host[i].n;
+    }
+    if (at != S.n) return cudaErrorInvalidValue;
+    cudaError_t e =
+        cudaMemcpyAsync(S.scenes, scenes_host, S.count * sizeof(sah_set_scene), cudaMemcpyHostToDevice, st);
+    // parents start at -1, so a position the tree misses is caught instead of read as an index
+    if (e == cudaSuccess) e = cudaMemsetAsync(S.parent_inner, 0xff, (size_t)S.n * 4, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(S.parent_leaf, 0xff, (size_t)S.n * 4, st);
+    if (e != cudaSuccess) return e;
+    return sah_tree_set(S.sah, S.n, S.scenes, S.count, planes, S.lo, S.hi, S.cbounds, S.children, S.range,
+                        S.parent_inner, S.parent_leaf, S.flag, S.excl, S.cub, S.cub_bytes, order, set_info, st);
+}
+
+cudaError_t sah_set_finish(const sah_set &S, const uint32_t *order, uint32_t first, const float4 *vpos,
+                           uint32_t nv, const uint4 *tris, uint32_t nt, int max_leaf, void *scratch,
+                           size_t scratch_bytes, float4 *nodes, float4 *records, int32_t *wide_index, int32_t *info,
+                           cudaStream_t st) {
+    if ((uint64_t)first + nt > S.n) return cudaErrorInvalidValue;
+    arena A = carve(scratch, nt, GB_METHOD_LBVH);
+    if (A.total > scratch_bytes) return cudaErrorInvalidValue;
+    if (nt == 0) return cudaSuccess;
+    // the boxes and the tree are the scene's slices of the set's arrays, the rest is `scratch`
+    A.lo = S.lo + first;
+    A.hi = S.hi + first;
+    A.children = S.children + first;
+    A.range = S.range + first;
+    A.parent_inner = S.parent_inner + first;
+    A.parent_leaf = S.parent_leaf + first;
+    cudaError_t e = cudaMemsetAsync(A.visits, 0, (size_t)nt * 4, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(A.collapsed, 1, (size_t)nt, st);
+    if (e != cudaSuccess) return e;
+    return build_tail(A, vpos, nv, tris, nt, max_leaf, nt > 1, order + first, nodes, records, wide_index, nullptr,
+                      info, st);
 }
 
 cudaError_t gpu_build_wide(const float4 *nodes, const int32_t *wide_index, uint32_t nt, float4 *nodes4,

@@ -55,6 +55,52 @@ cudaError_t sah_tree(void *scratch, uint32_t n, int planes, const float4 *plo, c
                      int32_t *parent_leaf, int32_t *flag, int32_t *excl, void *cub_tmp, size_t cub_bytes,
                      const uint32_t **order, int32_t *info, cudaStream_t st);
 
+// Scene sets with the SAH method: the large-node levels of every scene's tree in one chain of
+// launches over the set's primitives. Scene i holds the positions [first, first + n) of the
+// set's arrays (plo / phi, the tree arrays, the order) and its inner nodes are numbered from
+// first; `cbounds` holds 16 words per scene, the primitive pass's bounds. On return every array
+// is in each scene's own numbering (positions, inner nodes and primitives from 0), so the
+// slices at first are what sah_tree gives for the scene alone. `scenes` is on the device.
+struct sah_set_scene {
+    uint32_t first, n;
+};
+cudaError_t sah_tree_set(void *scratch, uint32_t n, const sah_set_scene *scenes, uint32_t count, int planes,
+                         const float4 *plo, const float4 *phi, const uint32_t *cbounds, int2 *children,
+                         int2 *range, int32_t *parent_inner, int32_t *parent_leaf, int32_t *flag, int32_t *excl,
+                         void *cub_tmp, size_t cub_bytes, const uint32_t **order, int32_t *info, cudaStream_t st);
+
+// A scene set's build with the SAH method in three phases (gpu_build.cu), over the arrays of
+// one allocation: primitive boxes, the tree arrays and the SAH scratch for all primitives of
+// the set, the primitive pass's bounds of every scene and the scene table.
+constexpr uint32_t kSahSetMaxTris = 1u << 25;  // most primitives of one set (larger: several sets)
+struct sah_set {
+    float4 *lo, *hi;
+    uint32_t *cbounds;  // 16 words per scene
+    int2 *children, *range;
+    int32_t *parent_inner, *parent_leaf, *flag, *excl;
+    sah_set_scene *scenes;
+    void *sah, *cub;
+    size_t cub_bytes, total;
+    uint32_t n, count;
+};
+sah_set sah_set_carve(void *base, uint32_t n_total, uint32_t count);  // base null: sizes only
+// Phase 1, scene i of the set (stream-ordered): its info and bounds initialised, the boxes of
+// its nt primitives written at positions first .. first + nt - 1 of the set's box arrays.
+cudaError_t sah_set_prims(const sah_set &S, uint32_t i, uint32_t first, const float4 *vpos, uint32_t nv,
+                          const uint4 *tris, uint32_t nt, int32_t *info, cudaStream_t st);
+// Phase 2, every scene (after phase 1 of all of them; n_total >= 2): the scene table (host,
+// scenes in position order) copied to the device, the parent links cleared, the trees built;
+// *order receives the primitive order, `set_info` (int32[8], device) the GB_ERR bits of the
+// trees of all scenes (OR-ed in).
+cudaError_t sah_set_trees(const sah_set &S, const sah_set_scene *scenes_host, int planes, const uint32_t **order,
+                          int32_t *set_info, cudaStream_t st);
+// Phase 3, scene i (after phase 2): from its tree to the binary nodes, records and 4-wide
+// indices, with `scratch` of gpu_build_scratch_bytes(nt, GB_METHOD_LBVH) bytes.
+cudaError_t sah_set_finish(const sah_set &S, const uint32_t *order, uint32_t first, const float4 *vpos,
+                           uint32_t nv, const uint4 *tris, uint32_t nt, int max_leaf, void *scratch,
+                           size_t scratch_bytes, float4 *nodes, float4 *records, int32_t *wide_index, int32_t *info,
+                           cudaStream_t st);
+
 // A pinned host word for the builders' read-backs, one per host thread (a copy into pageable
 // memory goes through a staging buffer that serialises the threads of a scene-set build).
 int32_t *readback_word();

@@ -132,6 +132,79 @@ __global__ void k_sah_root(const uint32_t *bounds, int n, sah_task *large, int *
     }
 }
 
+// The roots of a scene set (one warp): the scenes of more than kSmall primitives into the large
+// list in scene order, so that the list is sorted by first position like every later level's,
+// the scenes of 2 .. kSmall primitives into the small list. Scene i's primitives are the
+// positions [first, first + n) and its inner nodes are numbered from first.
+__global__ void k_sah_roots(const sah_set_scene *__restrict__ scenes, int count, const uint32_t *__restrict__ cbounds,
+                            sah_task *large, int *n_large, sah_task *small, int *n_small) {
+    const int lane = threadIdx.x & 31;
+    if (threadIdx.x >= 32) return;
+    const unsigned below = (1u << lane) - 1u;
+    int nlarge = 0, nsmall = 0;
+    for (int c0 = 0; c0 < count; c0 += 32) {
+        const int i = c0 + lane;
+        sah_task t{};
+        int n = 0;
+        if (i < count) {
+            const sah_set_scene sc = scenes[i];
+            const uint32_t *b = cbounds + 16 * (size_t)i + 6;  // the box bounds of the primitive pass
+            n = (int)sc.n;
+            t.lo = make_float4(unordered(b[0]), unordered(b[1]), unordered(b[2]), 0.f);
+            t.hi = make_float4(unordered(b[3]), unordered(b[4]), unordered(b[5]), 0.f);
+            t.m = make_int4((int)sc.first, (int)sc.first, (int)(sc.first + sc.n), 0);
+        }
+        const bool is_large = n > kSmall, is_small = n >= 2 && n <= kSmall;
+        const unsigned lm = __ballot_sync(kFull, is_large), sm = __ballot_sync(kFull, is_small);
+        if (is_large) large[nlarge + __popc(lm & below)] = t;
+        if (is_small) small[nsmall + __popc(sm & below)] = t;
+        nlarge += __popc(lm);
+        nsmall += __popc(sm);
+    }
+    if (lane == 0) {
+        *n_large = nlarge;
+        *n_small = nsmall;
+    }
+}
+
+// Scene i of a set whose position j lies in [first, first + n): the last scene whose first
+// position is at most j (an empty scene shares its first position with the scene after it).
+__device__ __forceinline__ int scene_of_pos(const sah_set_scene *scenes, int count, uint32_t j) {
+    int lo = 0, hi = count - 1, k = 0;
+    while (lo <= hi) {
+        const int mid = (lo + hi) >> 1;
+        if (scenes[mid].first <= j) {
+            k = mid;
+            lo = mid + 1;
+        } else {
+            hi = mid - 1;
+        }
+    }
+    return k;
+}
+
+// A scene set's tree arrays in every scene's own numbering: positions, inner nodes and
+// primitives of scene i less its first position (leaf references are complemented positions).
+// Slot first + n - 1 of a scene holds no inner node; converting what it holds does no harm.
+__global__ void __launch_bounds__(kT) k_sah_localize(const sah_set_scene *__restrict__ scenes, int count, int n,
+                                                     int2 *children, int2 *range, int32_t *parent_inner,
+                                                     int32_t *parent_leaf, uint32_t *order) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const uint32_t f = scenes[scene_of_pos(scenes, count, (uint32_t)j)].first;
+    // in unsigned arithmetic, so that an unused slot's contents cannot overflow
+    auto less = [f](int v) { return (int)((uint32_t)v - f); };
+    auto ref = [f](int v) { return v >= 0 ? (int)((uint32_t)v - f) : (int)~((uint32_t)~v - f); };
+    order[j] -= f;
+    const int pl = parent_leaf[j];
+    if (pl >= 0) parent_leaf[j] = less(pl);
+    const int pi = parent_inner[j];
+    if (pi >= 0) parent_inner[j] = less(pi);
+    const int2 c = children[j], r = range[j];
+    children[j] = make_int2(ref(c.x), ref(c.y));
+    range[j] = make_int2(less(r.x), less(r.y));
+}
+
 // The node of position j among the level's large nodes (sorted by first position), or -1.
 __device__ __forceinline__ int task_of_pos(const sah_task *tasks, int cnt, int j) {
     int lo = 0, hi = cnt - 1, k = -1;
@@ -736,23 +809,16 @@ sah_arena sah_carve(void *base, uint32_t n) {
     return A;
 }
 
-}  // namespace
-
-size_t sah_scratch_bytes(uint32_t n) { return sah_carve(nullptr, n).total; }
-
-cudaError_t sah_tree(void *scratch, uint32_t n, int planes, const float4 *plo, const float4 *phi,
-                     const uint32_t *bounds, int2 *children, int2 *range, int32_t *parent_inner,
-                     int32_t *parent_leaf, int32_t *flag, int32_t *excl, void *cub_tmp, size_t cub_bytes,
-                     const uint32_t **order, int32_t *info, cudaStream_t st) {
-    if (n < 2 || planes < 1 || planes > kMaxSahPlanes) return cudaErrorInvalidValue;
-    const sah_arena A = sah_carve(scratch, n);
+// The levels of large nodes, from the list the root kernel made, then the warp-per-node phase;
+// *order receives the primitive order.
+cudaError_t sah_levels(const sah_arena &A, uint32_t n, int planes, const float4 *plo, const float4 *phi,
+                       int2 *children, int2 *range, int32_t *parent_inner, int32_t *parent_leaf, int32_t *flag,
+                       int32_t *excl, void *cub_tmp, size_t cub_bytes, const uint32_t **order, int32_t *info,
+                       cudaStream_t st) {
     const unsigned nb = (n + kT - 1) / kT;
     int *n_large[2] = {A.counters, A.counters + 1}, *n_small = A.counters + 2;
     sah_task *tasks[2] = {A.tasks_a, A.tasks_b};
     uint32_t *idx[2] = {A.idx_a, A.idx_b};
-    k_sah_clear<<<(unsigned)((A.nbins + kT - 1) / kT), kT, 0, st>>>(A.bins, A.nbins);
-    k_iota<<<nb, kT, 0, st>>>(A.idx_a, n);
-    k_sah_root<<<1, 32, 0, st>>>(bounds, (int)n, A.tasks_a, n_large[0], A.small, n_small);
     cudaError_t e = cudaGetLastError();
     int cur = 0;
     // every round takes at least one primitive off each large node, so n rounds always finish
@@ -790,6 +856,40 @@ cudaError_t sah_tree(void *scratch, uint32_t n, int planes, const float4 *plo, c
     k_sah_small<<<(unsigned)((n / 2 + 1 + kSmallWarps - 1) / kSmallWarps), 32 * kSmallWarps, 0, st>>>(
         A.small, n_small, idx[cur], plo, phi, planes, children, range, parent_inner, parent_leaf, info);
     *order = idx[cur];
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+size_t sah_scratch_bytes(uint32_t n) { return sah_carve(nullptr, n).total; }
+
+cudaError_t sah_tree(void *scratch, uint32_t n, int planes, const float4 *plo, const float4 *phi,
+                     const uint32_t *bounds, int2 *children, int2 *range, int32_t *parent_inner,
+                     int32_t *parent_leaf, int32_t *flag, int32_t *excl, void *cub_tmp, size_t cub_bytes,
+                     const uint32_t **order, int32_t *info, cudaStream_t st) {
+    if (n < 2 || planes < 1 || planes > kMaxSahPlanes) return cudaErrorInvalidValue;
+    const sah_arena A = sah_carve(scratch, n);
+    k_sah_clear<<<(unsigned)((A.nbins + kT - 1) / kT), kT, 0, st>>>(A.bins, A.nbins);
+    k_iota<<<(n + kT - 1) / kT, kT, 0, st>>>(A.idx_a, n);
+    k_sah_root<<<1, 32, 0, st>>>(bounds, (int)n, A.tasks_a, A.counters, A.small, A.counters + 2);
+    return sah_levels(A, n, planes, plo, phi, children, range, parent_inner, parent_leaf, flag, excl, cub_tmp,
+                      cub_bytes, order, info, st);
+}
+
+cudaError_t sah_tree_set(void *scratch, uint32_t n, const sah_set_scene *scenes, uint32_t count, int planes,
+                         const float4 *plo, const float4 *phi, const uint32_t *cbounds, int2 *children,
+                         int2 *range, int32_t *parent_inner, int32_t *parent_leaf, int32_t *flag, int32_t *excl,
+                         void *cub_tmp, size_t cub_bytes, const uint32_t **order, int32_t *info, cudaStream_t st) {
+    if (n < 2 || count == 0 || planes < 1 || planes > kMaxSahPlanes) return cudaErrorInvalidValue;
+    const sah_arena A = sah_carve(scratch, n);
+    k_sah_clear<<<(unsigned)((A.nbins + kT - 1) / kT), kT, 0, st>>>(A.bins, A.nbins);
+    k_iota<<<(n + kT - 1) / kT, kT, 0, st>>>(A.idx_a, n);
+    k_sah_roots<<<1, 32, 0, st>>>(scenes, (int)count, cbounds, A.tasks_a, A.counters, A.small, A.counters + 2);
+    cudaError_t e = sah_levels(A, n, planes, plo, phi, children, range, parent_inner, parent_leaf, flag, excl,
+                               cub_tmp, cub_bytes, order, info, st);
+    if (e != cudaSuccess) return e;
+    k_sah_localize<<<(n + kT - 1) / kT, kT, 0, st>>>(scenes, (int)count, (int)n, children, range, parent_inner,
+                                                     parent_leaf, const_cast<uint32_t *>(*order));
     return cudaGetLastError();
 }
 

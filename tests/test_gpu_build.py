@@ -173,6 +173,55 @@ def test_gpu_trees_are_deterministic(api, wl, builder):
     rt.close()
 
 
+def test_sah_scene_set_trees_equal_single_builds(api, wl):
+    """With the SAH method the trees of a scene set are built together, one chain of launches
+    for the large nodes of every scene, and each scene still gets the tree it gets alone: scenes
+    of 0 and 1 triangles, of 2 to 32 (the warp-per-node phase only), just above that, one with a
+    NaN vertex, and larger soups. Same statistics, every closest hit bit for bit, the same
+    any-hit answers."""
+    import torch
+    sizes = [5000, 0, 1, 2, 3, 31, 32, 33, 64, 257, 40000, 0, 1, 1000, 70000]
+    meshes, rays = [], []
+    for i, n in enumerate(sizes):
+        if n == 0:
+            v, t = np.zeros((3, 4), np.float32), np.zeros((0, 4), np.uint32)
+            lo, hi = np.zeros(3, np.float32), np.ones(3, np.float32)
+        else:
+            sc = wl.soup(400 + i, n, sigma=0.5)
+            lo, hi = sc.bounds()
+            v, t = sc.vpos.copy(), sc.tris
+        if n == 257:
+            v[5, 1] = np.nan  # a triangle that no ray hits
+        meshes.append((_dev(v, np.float32), _dev(t, np.uint32)))
+        rays.append(wl.shell_rays(500 + i, lo, hi, 3000))
+    single = []
+    rt = api.BatchRayTracer(0)
+    rt.select("while-while")
+    for (v, t), r in zip(meshes, rays):
+        st = rt.build_device(v, t, max_tris=2)
+        single.append((st, _trace(rt, r, False), _occluded(_trace(rt, r, True))))
+    rt.close()
+    rt = api.BatchRayTracer(0)
+    stats = rt.build_scenes_device(meshes, max_tris=2)
+    rt.select("persistent-while-while")
+    stream = torch.cuda.current_stream().cuda_stream
+    d = [_dev(r, np.float32) for r in rays]
+    for i, (st, _, _) in enumerate(single):
+        assert (stats[i]["inner_nodes"], stats[i]["depth"], stats[i]["tri_records"]) == \
+            (st["inner_nodes"], st["depth"], st["tri_records"]), i
+    for any_hit in (False, True):
+        outs = [torch.zeros((r.shape[0], 4), device="cuda") for r in rays]
+        rt.trace_multi([(i, d[i], outs[i]) for i in range(len(rays))], any_hit=any_hit, stream=stream)
+        rt.check(stream, timeout_ms=60000)
+        for i, o in enumerate(outs):
+            got = o.cpu().numpy()
+            if any_hit:
+                assert (_occluded(got) == single[i][2]).all(), i
+            else:
+                assert (got.view(np.uint32) == single[i][1].view(np.uint32)).all(), i
+    rt.close()
+
+
 def test_gpu_tree_errors(gpu_tracer, api):
     import torch
     v = _dev(np.zeros((3, 4)), np.float32)
