@@ -367,11 +367,11 @@ grt_status grt_build_scenes_device(grt_ctx *c, const grt_mesh *meshes, uint32_t 
             continue;
         }
         const sah_set S = sah_set_carve(tmp.set, n_g, i1 - i0);
-        for (uint32_t i = i0; i < i1 && e == cudaSuccess; ++i) {
+        e = on_workers(i0, i1, [&](int w, uint32_t i) {
             const grt_mesh &m = meshes[i];
-            e = sah_set_prims(S, i - i0, table[i - i0].first, (const float4 *)m.vpos4, m.nv, (const uint4 *)m.tris4,
-                              m.nt, tmp.info + 8 * (size_t)i, st);
-        }
+            return sah_set_prims(S, i - i0, table[i - i0].first, (const float4 *)m.vpos4, m.nv,
+                                 (const uint4 *)m.tris4, m.nt, tmp.info + 8 * (size_t)i, wst[w]);
+        });
         const uint32_t *order = nullptr;
         if (e == cudaSuccess) e = sah_set_trees(S, table.data(), c->device_planes, &order, tmp.info + 8 * (size_t)count, st);
         if (e == cudaSuccess)

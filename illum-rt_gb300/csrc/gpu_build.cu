@@ -59,10 +59,17 @@ __device__ __forceinline__ float half_area(float4 lo, float4 hi) {
     return dx * dy + dy * dz + dz * dx;
 }
 
-// 1. triangle boxes and the bounds of their centres
+// the bound word w of the 12 (centre min, centre max, box min, box max): a minimum?
+__device__ __forceinline__ bool bound_is_min(unsigned w) { return w < 3 || (w >= 6 && w < 9); }
+
+// 1. triangle boxes and the bounds of their centres (combined per warp, then per block, so that
+// one block adds to the 12 shared bound words once)
 __global__ void __launch_bounds__(kThreads) k_prims(const float4 *__restrict__ vpos, uint32_t nv,
                                                     const uint4 *__restrict__ tris, uint32_t nt, float4 *lo_out,
                                                     float4 *hi_out, uint32_t *cbounds, int32_t *info) {
+    __shared__ uint32_t s_bounds[12];
+    if (threadIdx.x < 12) s_bounds[threadIdx.x] = bound_is_min(threadIdx.x) ? 0xffffffffu : 0u;
+    __syncthreads();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     float cmin[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, cmax[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
     float bmin[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, bmax[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
@@ -108,10 +115,19 @@ __global__ void __launch_bounds__(kThreads) k_prims(const float4 *__restrict__ v
     if ((threadIdx.x & 31u) == 0 && cmin[0] <= cmax[0]) {
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-            atomicMin(cbounds + a, ordered(cmin[a]));
-            atomicMax(cbounds + 3 + a, ordered(cmax[a]));
-            atomicMin(cbounds + 6 + a, ordered(bmin[a]));
-            atomicMax(cbounds + 9 + a, ordered(bmax[a]));
+            atomicMin(s_bounds + a, ordered(cmin[a]));
+            atomicMax(s_bounds + 3 + a, ordered(cmax[a]));
+            atomicMin(s_bounds + 6 + a, ordered(bmin[a]));
+            atomicMax(s_bounds + 9 + a, ordered(bmax[a]));
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 12) {
+        const uint32_t v = s_bounds[threadIdx.x];
+        if (bound_is_min(threadIdx.x)) {
+            if (v != 0xffffffffu) atomicMin(cbounds + threadIdx.x, v);
+        } else if (v != 0u) {
+            atomicMax(cbounds + threadIdx.x, v);
         }
     }
 }
@@ -746,7 +762,7 @@ __global__ void __launch_bounds__(kThreads) k_wide_nodes(const float4 *__restric
 __global__ void k_init_info(int32_t *info, uint32_t *cbounds) {
     if (threadIdx.x < 8) info[threadIdx.x] = threadIdx.x == GB_FINITE ? 1 : 0;
     const unsigned t = threadIdx.x;
-    if (t < 12) cbounds[t] = (t < 3 || (t >= 6 && t < 9)) ? 0xffffffffu : 0u;
+    if (t < 12) cbounds[t] = bound_is_min(t) ? 0xffffffffu : 0u;
 }
 
 inline size_t up256(size_t b) { return (b + 255) & ~(size_t)255; }
