@@ -476,7 +476,10 @@ grt_status grt_build_scenes_device(grt_ctx *ctx, const grt_mesh *meshes, uint32_
  *   GRT_DEVICE_BUILD_LBVH: the radix tree of the Morton codes (Karras 2012), built in one pass:
  *     the fastest build (for scenes rebuilt every frame), trees that trace a few per cent slower.
  * GRT_DEVICE_BUILD_DEFAULT is GRT_DEVICE_BUILD_SAH. grt_build_scenes_device builds the scenes of
- * a set concurrently (up to 8 host threads, each with a stream of its own). */
+ * a set concurrently (up to 8 host threads, each with a stream of its own); with the SAH method
+ * the trees of all its scenes are built together, level by level over all their triangles,
+ * each scene's tree the one it gets alone. A builder that made a malformed tree (an internal
+ * fault, never an input's) fails the build with GRT_ERR_TRAVERSAL. */
 enum { GRT_DEVICE_BUILD_DEFAULT = 0, GRT_DEVICE_BUILD_LBVH = 1, GRT_DEVICE_BUILD_PLOC = 2, GRT_DEVICE_BUILD_SAH = 3 };
 grt_status grt_set_device_builder(grt_ctx *ctx, int method);
 /* Candidate planes per node of GRT_DEVICE_BUILD_SAH (1..256, default 256; as many as a node has
