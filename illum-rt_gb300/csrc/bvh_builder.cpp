@@ -16,8 +16,11 @@
 #include <cfloat>
 #include <cmath>
 #include <cstring>
+#include <exception>
 #include <functional>
 #include <future>
+#include <mutex>
+#include <system_error>
 #include <thread>
 
 namespace grt {
@@ -151,13 +154,32 @@ struct builder {
         if (chunks == 1) {
             work(0);
         } else {
+            // the threads that start share the chunks (the calling thread takes them all if none
+            // starts); an exception in one, such as memory running out, is raised after the join
             std::vector<std::thread> th;
             std::atomic<int> next{0};
-            for (int t = 0; t < threads; ++t)
-                th.emplace_back([&] {
+            std::exception_ptr failed;
+            std::mutex failed_mutex;
+            auto run = [&] {
+                try {
                     for (int c; (c = next++) < chunks;) work(c);
-                });
+                } catch (...) {
+                    std::lock_guard<std::mutex> lock(failed_mutex);
+                    if (!failed) failed = std::current_exception();
+                    next = chunks;
+                }
+            };
+            th.reserve(threads);
+            for (int t = 0; t < threads; ++t) {
+                try {
+                    th.emplace_back(run);
+                } catch (const std::system_error &) {
+                    break;
+                }
+            }
+            if (th.empty()) run();
             for (auto &t : th) t.join();
+            if (failed) std::rethrow_exception(failed);
         }
         for (auto &ex : extra)
             for (auto &pr : ex) {

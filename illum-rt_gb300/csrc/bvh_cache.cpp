@@ -109,6 +109,11 @@ bool load_tree(const std::string &path, const hasher &h, uint32_t nv, uint32_t n
               hd.key_a == h.a && hd.key_b == h.b && hd.nv == nv && hd.nt == nt && hd.split == o.split &&
               hd.max_tris == o.max_tris && hd.planes == o.planes && hd.esc == (o.esc ? 1 : 0) &&
               hd.n_nodes < (1ull << 32) && hd.n_index < (1ull << 32);
+    if (ok) {  // the file holds exactly what the header announces (nothing is allocated for a lie)
+        const long want = (long)(sizeof(hd) + hd.n_nodes * sizeof(ref_node) + hd.n_index * 4);
+        ok = std::fseek(f, 0, SEEK_END) == 0 && std::ftell(f) == want &&
+             std::fseek(f, (long)sizeof(hd), SEEK_SET) == 0;
+    }
     if (ok) {
         out.root = hd.root;
         out.nodes.resize(hd.n_nodes);
@@ -257,15 +262,17 @@ const char *leaf_stats(const ref_tree &t, grt_leaf_stats *s) {
 extern "C" {
 
 grt_status grt_set_bvh_cache(grt_ctx *c, const char *dir) {
-    if (!c) return GRT_ERR_INVALID_ARG;
-    c->cache_dir = dir ? dir : "";
-    while (c->cache_dir.size() > 1 && c->cache_dir.back() == '/') c->cache_dir.pop_back();
-    if (!c->cache_dir.empty() && access(c->cache_dir.c_str(), W_OK) != 0) {
-        const std::string d = c->cache_dir;
-        c->cache_dir.clear();
-        return fail(c, GRT_ERR_INVALID_ARG, "BVH cache directory '" + d + "' is not writable");
-    }
-    return GRT_OK;
+    return guarded(c, [&]() -> grt_status {
+        if (!c) return GRT_ERR_INVALID_ARG;
+        c->cache_dir = dir ? dir : "";
+        while (c->cache_dir.size() > 1 && c->cache_dir.back() == '/') c->cache_dir.pop_back();
+        if (!c->cache_dir.empty() && access(c->cache_dir.c_str(), W_OK) != 0) {
+            const std::string d = c->cache_dir;
+            c->cache_dir.clear();
+            return fail(c, GRT_ERR_INVALID_ARG, "BVH cache directory '" + d + "' is not writable");
+        }
+        return GRT_OK;
+    });
 }
 
 grt_status grt_bvh_cache_stats(const grt_ctx *c, uint64_t *hits, uint64_t *misses) {
@@ -276,28 +283,36 @@ grt_status grt_bvh_cache_stats(const grt_ctx *c, uint64_t *hits, uint64_t *misse
 }
 
 grt_status grt_export_bvh_obj(grt_ctx *c, int max_depth, const char *path) {
-    if (!c || !path) return GRT_ERR_INVALID_ARG;
-    if (!c->built) return fail(c, GRT_ERR_NOT_BUILT, "no scene has been built");
-    if (c->gpu_tree) return fail(c, GRT_ERR_INVALID_ARG, "a BVH built on the GPU or refitted has no reference tree to export");
-    return write_obj(c->tree, max_depth, path) ? GRT_OK : fail(c, GRT_ERR_INVALID_ARG, std::string("cannot write ") + path);
+    return guarded(c, [&]() -> grt_status {
+        if (!c || !path) return GRT_ERR_INVALID_ARG;
+        if (!c->built) return fail(c, GRT_ERR_NOT_BUILT, "no scene has been built");
+        if (c->gpu_tree) return fail(c, GRT_ERR_INVALID_ARG, "a BVH built on the GPU or refitted has no reference tree to export");
+        return write_obj(c->tree, max_depth, path) ? GRT_OK : fail(c, GRT_ERR_INVALID_ARG, std::string("cannot write ") + path);
+    });
 }
 
 grt_status grt_bvh_leaf_stats(grt_ctx *c, grt_leaf_stats *s) {
-    if (!c || !s) return GRT_ERR_INVALID_ARG;
-    if (!c->built) return fail(c, GRT_ERR_NOT_BUILT, "no scene has been built");
-    if (c->gpu_tree) return fail(c, GRT_ERR_INVALID_ARG, "a BVH built on the GPU or refitted has no reference tree");
-    const char *e = leaf_stats(c->tree, s);
-    return e ? fail(c, GRT_ERR_INVALID_ARG, e) : GRT_OK;
+    return guarded(c, [&]() -> grt_status {
+        if (!c || !s) return GRT_ERR_INVALID_ARG;
+        if (!c->built) return fail(c, GRT_ERR_NOT_BUILT, "no scene has been built");
+        if (c->gpu_tree) return fail(c, GRT_ERR_INVALID_ARG, "a BVH built on the GPU or refitted has no reference tree");
+        const char *e = leaf_stats(c->tree, s);
+        return e ? fail(c, GRT_ERR_INVALID_ARG, e) : GRT_OK;
+    });
 }
 
 grt_status grt_host_bvh_export_obj(const grt_host_bvh *h, int max_depth, const char *path) {
-    if (!h || !path) return GRT_ERR_INVALID_ARG;
-    return write_obj(host_tree(h), max_depth, path) ? GRT_OK : GRT_ERR_INVALID_ARG;
+    return guarded(nullptr, [&]() -> grt_status {
+        if (!h || !path) return GRT_ERR_INVALID_ARG;
+        return write_obj(host_tree(h), max_depth, path) ? GRT_OK : GRT_ERR_INVALID_ARG;
+    });
 }
 
 grt_status grt_host_bvh_leaf_stats(const grt_host_bvh *h, grt_leaf_stats *s) {
-    if (!h || !s) return GRT_ERR_INVALID_ARG;
-    return leaf_stats(host_tree(h), s) ? GRT_ERR_INVALID_ARG : GRT_OK;
+    return guarded(nullptr, [&]() -> grt_status {
+        if (!h || !s) return GRT_ERR_INVALID_ARG;
+        return leaf_stats(host_tree(h), s) ? GRT_ERR_INVALID_ARG : GRT_OK;
+    });
 }
 
 }  // extern "C"

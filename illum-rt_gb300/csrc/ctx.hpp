@@ -6,6 +6,7 @@
 #include <atomic>
 #include <chrono>
 #include <cstring>
+#include <exception>
 #include <string>
 #include <vector>
 
@@ -139,6 +140,27 @@ struct timed_call {
 inline grt_status fail(grt_ctx *c, grt_status s, const std::string &msg) {
     if (c) c->err = msg;
     return s;
+}
+
+// The body of a C-ABI entry point, run so that no C++ exception leaves the library: host memory
+// or a host thread that could not be had (std::bad_alloc, std::system_error, std::length_error)
+// becomes GRT_ERR_OOM, with the reason in grt_last_error where there is a context.
+template <class F> grt_status guarded(grt_ctx *c, F &&body) noexcept {
+    const char *why = "unknown exception";
+    try {
+        return body();
+    } catch (const std::exception &e) {
+        why = e.what();
+    } catch (...) {
+    }
+    if (c) {
+        try {
+            c->err = std::string("host resources exhausted: ") + why;
+        } catch (...) {
+            c->err.clear();
+        }
+    }
+    return GRT_ERR_OOM;
 }
 
 inline grt_status cuda_fail(grt_ctx *c, cudaError_t e, const char *what) {

@@ -55,14 +55,22 @@ def test_cache_hit_gives_the_same_tree(api, wl, tmp_path):
     assert all(np.array_equal(a, b) for a, b in zip(first[:2], third[:2]))
     rt.build(sc.vpos, sc.tris)
     assert rt.cache_stats() == (2, 3)
+    # a header that announces more nodes than the file holds (its node count at byte 56) costs a
+    # build, and nothing of the announced size is allocated
+    data = bytearray(path.read_bytes())
+    data[56:64] = (1 << 24).to_bytes(8, "little")
+    path.write_bytes(bytes(data))
+    rt.build(sc.vpos, sc.tris)
+    assert rt.cache_stats() == (2, 4)
+    assert all(np.array_equal(a, b) for a, b in zip(first[:2], rt.export_bvh()[:2]))
     # a changed vertex is another scene
     v = sc.vpos.copy()
     v[7, 2] += 0.01
     rt.build(v, sc.tris)
-    assert rt.cache_stats() == (2, 4)
+    assert rt.cache_stats() == (2, 5)
     rt.set_bvh_cache(None)
     rt.build(sc.vpos, sc.tris)
-    assert rt.cache_stats() == (2, 4)
+    assert rt.cache_stats() == (2, 5)
     with pytest.raises(api.GRTError):
         rt.set_bvh_cache(str(tmp_path / "does-not-exist"))
     rt.close()
