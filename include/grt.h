@@ -22,8 +22,9 @@
  * platform's encoding (rt/cpu/wavefront.cpp:60-70): occluded rays get ref = 0xFFFFFFFF and
  * t = 4294967296.0f; the others t = FLT_MAX, ref = 0; beta and gamma are not written.
  *
- * Errors are status codes, never exceptions, and the library never resets the device
- * (the reference's check_cuda_error calls cudaDeviceReset, rt/cuda/cuda-helpers.cpp:5-12).
+ * Errors are status codes, never exceptions (host memory or a host thread that cannot be had
+ * is GRT_ERR_OOM), and the library never resets the device (the reference's check_cuda_error
+ * calls cudaDeviceReset, rt/cuda/cuda-helpers.cpp:5-12).
  * All launches are stream-ordered and asynchronous; grt_check() synchronises the stream and
  * reports errors that kernels flagged (stack overflow, step limit). A context is not
  * thread-safe; use one context per host thread.
