@@ -1,5 +1,6 @@
 """Host logic of bench.py that the benchmark line depends on: the tuned tree options read from
-the tuning table, and the figures read from the committed ncu summary of the fused kernel."""
+the tuning table, the figures read from the committed ncu summary of the fused kernel, and the
+timing loop of the CPU baseline."""
 import json
 import os
 import sys
@@ -104,3 +105,27 @@ def test_classify_paths_first_differing_bounce():
     bh_g[30, 0, 3] = np.uint32(1).view(np.float32)
     r = bench.classify_paths(res_g, bh_g, res_o, bh_o)
     assert r["differing"] == 2 and r["not_near_ties"] == 1
+
+
+def test_cpu_baseline_repeats_until_enough_work():
+    """One untimed warm-up step, then steps until both the time and the repetition minimum are
+    reached; the rate is the median of the repetitions."""
+
+    class FakeStep:
+        calls = 0
+
+        def run(self):
+            self.calls += 1
+            return 1_000_000 * self.calls, 0.5
+
+        def cores(self):
+            return 7
+
+    f = FakeStep()
+    rate, reps, n, t, cores = bench.cpu_baseline(f, min_seconds=1.2, min_reps=2)
+    assert f.calls == 4 and reps == 3 and t == 1.5 and cores == 7
+    assert n == (2 + 3 + 4) * 1_000_000
+    assert rate == 6.0  # median of 4, 6 and 8 Mrays/s
+    f = FakeStep()
+    rate, reps, n, t, cores = bench.cpu_baseline(f, min_seconds=0.1, min_reps=5)
+    assert f.calls == 6 and reps == 5 and rate == 8.0  # median of 4, 6, 8, 10, 12
